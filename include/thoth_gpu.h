@@ -1,0 +1,225 @@
+/*
+ * thoth_gpu.h — C ABI of the GB300 Monte-Carlo engine behind Thoth's
+ * `!mcl_pricer` (allow_gpu: true).
+ *
+ * Plain C: POD structs, pointers and sizes only, so a C++23 host, a ctypes
+ * binding or any other FFI can call it. Every entry point returns an int
+ * status (THOTH_GPU_OK or a negative THOTH_GPU_E_* code); no exception or
+ * C++ type crosses this boundary. All result memory is caller-owned.
+ *
+ * Reference interface this replaces (GValas/Thoth):
+ *   pricer/src/tasks/mcl_gpu.hpp:16-48   namespace gpu { Available, DeviceInfo,
+ *                                        PriceEuropeanGbm }
+ *   pricer/src/tasks/pricer_mcl_gpu_gate.cpp:82-126
+ *                                        BookIsGpuSupported / PriceContract
+ *   pricer/src/tasks/pricer_mcl.cpp:623-644, 677-709
+ *                                        the CPU path loop (Tree_Run) and the
+ *                                        indicator read-out (Tree_Read) that a
+ *                                        whole-book call replaces
+ *
+ * Threading: every entry point may be called from any host thread (the
+ * reference server prices on a per-request std::thread, run_server.cpp:110-116).
+ * Calls are serialised by an internal mutex; the device arena and stream are
+ * created lazily on the first call and reused.
+ */
+#ifndef THOTH_GPU_H
+#define THOTH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define THOTH_GPU_OK 0
+#define THOTH_GPU_E_INVALID (-1)     /* bad descriptor / argument            */
+#define THOTH_GPU_E_NODEVICE (-2)    /* no usable CUDA device                */
+#define THOTH_GPU_E_CUDA (-3)        /* a CUDA runtime call failed           */
+#define THOTH_GPU_E_UNSUPPORTED (-4) /* book outside the GPU gate            */
+#define THOTH_GPU_E_CANCELLED (-5)   /* thoth_gpu_request_cancel() honoured  */
+#define THOTH_GPU_E_NOMEM (-6)       /* device arena could not grow          */
+#define THOTH_GPU_E_TOO_LARGE (-7)   /* size above a documented maximum      */
+
+/* ---- enumerations ------------------------------------------------------ */
+/* diffusion models (reference: marketdata/single.cpp:65-153) */
+#define THOTH_MODEL_GBM 0    /* SpotDiffusionNode, constant vol            */
+#define THOTH_MODEL_HESTON 1 /* HestonVarianceNode (QE) + HestonSpotNode   */
+#define THOTH_MODEL_LSV 2    /* Heston + LocalVolatilityNode leverage      */
+
+/* payoffs (reference: nodes/vanilla_flow_node.cpp, barrier_flow_node.cpp,
+ * variance_flow_node.cpp, absolute_basket_node.cpp) */
+#define THOTH_PRODUCT_VANILLA 0
+#define THOTH_PRODUCT_BARRIER 1
+#define THOTH_PRODUCT_VARIANCE 2
+#define THOTH_PRODUCT_BASKET 3 /* vanilla on sum_i w_i S_i */
+
+#define THOTH_CALL 0
+#define THOTH_PUT 1
+
+/* pathwise Greeks mask (ThothBookDesc.greeks) */
+#define THOTH_GREEK_DELTA 1 /* d premium / d S0 of the product's asset        */
+#define THOTH_GREEK_VEGA 2  /* d premium / d sigma (GBM assets), per 1.0 vol  */
+
+/* largest supported sizes (checked; larger books return THOTH_GPU_E_TOO_LARGE) */
+#define THOTH_MAX_ASSETS 8
+#define THOTH_MAX_SOBOL_DIMS 4097 /* reference SobolGenerator::MaxDimension()  */
+#define THOTH_MAX_DATES 8192
+#define THOTH_MAX_PRODUCTS 4096
+
+/* ---- book descriptor ---------------------------------------------------- */
+typedef struct ThothAsset
+{
+    int32_t model;      /* THOTH_MODEL_*                                          */
+    int32_t lev_points; /* LSV: points per leverage layer (else 0)                */
+    double spot;        /* S(0)                                                   */
+    /* [n_dates] cumulative carry r - q - repo to each date: the DriftNode value;
+     * a step's log-drift is carry[i]*t[i] - carry[i-1]*t[i-1]
+     * (spot_diffusion_node.cpp:45-46, heston_spot_node.cpp:54-55)              */
+    const double* carry;
+    double vol; /* GBM: constant sigma                                           */
+    /* Heston / LSV base (heston_variance_node.cpp:8-14, heston_spot_node.cpp:8-14) */
+    double v0, kappa, theta, xi, rho;
+    /* LSV leverage layers, one per diffusion date: grid point k of layer i sits at
+     * log-spot (lev_offset[i] + k) * lev_ln_step[i]; read at S_{i-1} by clamped
+     * linear interpolation (local_volatility_node.cpp:19-47).                  */
+    const double* lev_ln_step; /* [n_dates]                                      */
+    const int64_t* lev_offset; /* [n_dates]                                      */
+    const double* lev_values;  /* [n_dates * lev_points]                         */
+} ThothAsset;
+
+typedef struct ThothProduct
+{
+    int32_t kind;        /* THOTH_PRODUCT_*                                        */
+    int32_t option_type; /* THOTH_CALL / THOTH_PUT (vanilla, barrier, basket)     */
+    int32_t asset;       /* underlying asset index (not used by baskets)          */
+    int32_t maturity;    /* flow date index                                       */
+    double strike;
+    /* discounting: df = exp(-t[maturity] * zero_rate) (contract_node.cpp:16-51)  */
+    double zero_rate;
+    double fx; /* contract -> book currency factor (book_node.cpp:16-31)       */
+    /* quanto: the payoff reads S_i * exp(-quanto * t[i]) with
+     * quanto = sigma_S * sigma_FX * rho (quanto_adjustment_node.cpp:20-42); 0 = none */
+    double quanto;
+    /* barrier (barrier_flow_node.cpp:23-56); level already BGK-shifted if the
+     * contract is continuously monitored (contracts/barrier.cpp:151-165)        */
+    int32_t barrier_up, barrier_in;
+    double barrier_level;
+    int32_t n_monitor;
+    const int32_t* monitor; /* sorted date indices                               */
+    /* variance swap (variance_flow_node.cpp:13-60)                              */
+    double notional, strike_variance, total_year_fraction, past_variance;
+    int32_t n_obs;
+    const int32_t* obs; /* sorted observation indices; NULL = every date 1..maturity */
+    /* basket (absolute_basket_node.cpp:15-26): level = sum_k weights[k] * S_{components[k]} */
+    int32_t n_components;
+    const int32_t* components;
+    const double* weights;
+} ThothProduct;
+
+typedef struct ThothBookDesc
+{
+    int32_t n_dates;     /* diffusion dates including today (index 0)              */
+    const int32_t* days; /* [n_dates] calendar days from today, or NULL             */
+    const double* t;     /* [n_dates] ACT/365 year fractions, t[0] = 0              */
+    int32_t n_assets;
+    const ThothAsset* assets;
+    /* [n_assets*n_assets] row-major lower-triangular Cholesky factor L over the
+     * assets' white noises; asset u's GBM Brownian is driven by sum_v L[u][v] n_v
+     * (pricer_mcl.cpp:246-314). NULL = independent noises.                      */
+    const double* cholesky;
+    int32_t n_products;
+    const ThothProduct* products;
+    int64_t paths;      /* number of Monte-Carlo paths (> 1)                       */
+    int64_t sobol_skip; /* leading Sobol points skipped (mcl_configuration sobol_skip) */
+    int32_t use_sobol;  /* 1: Sobol + Brownian bridge; 0: counter-based pseudo-random */
+    int32_t greeks;     /* THOTH_GREEK_* mask                                       */
+    uint64_t seed;      /* pseudo-random stream (use_sobol = 0, and Sobol dims > 4097) */
+} ThothBookDesc;
+
+/* Per-product and book results. Arrays are caller-owned, n_products long;
+ * delta / vega arrays may be NULL when not requested. trust = standard error
+ * sqrt((S2 - S1^2/n)/(n-1)/n) (monte_carlo_node.cpp:35-40). */
+typedef struct ThothBookResult
+{
+    double book_premium;
+    double book_trust;
+    double* premium;
+    double* trust;
+    double* delta;
+    double* delta_trust;
+    double* vega;
+    double* vega_trust;
+    double device_ms; /* device time of the pricing kernels (CUDA events)         */
+} ThothBookResult;
+
+/* Reference gpu::GbmResult (mcl_gpu.hpp:34-38). */
+typedef struct ThothGbmResult
+{
+    double premium;
+    double trust;
+} ThothGbmResult;
+
+/* ---- entry points ------------------------------------------------------ */
+
+/* 1 iff a CUDA device of compute capability 10.3 is usable.
+ * Replaces gpu::Available() (mcl_gpu.cpp via mcl_gpu.cu:77-82). */
+int thoth_gpu_available(void);
+
+/* One-line device description into buf (NUL-terminated, truncated to n).
+ * Replaces gpu::DeviceInfo() (mcl_gpu.cu:84-98). */
+int thoth_gpu_device_info(char* buf, size_t n);
+
+/* European vanilla under GBM in the forward measure:
+ *   F_T = forward * exp(-vol^2 T / 2 + vol sqrt(T) Z),  premium = df * mean(payoff)
+ * Z is the first Sobol dimension (point 0 skipped) through the inverse normal,
+ * so the result is deterministic and `seed` only selects the pseudo-random
+ * stream when paths exceed 2^32 - 1. Replaces gpu::PriceEuropeanGbm
+ * (mcl_gpu.hpp:40-46, mcl_gpu.cu:100-154). */
+int thoth_gpu_price_european_gbm(double forward, double strike, double t, double vol, double df,
+                                 int is_call, int64_t paths, uint64_t seed, ThothGbmResult* out);
+
+/* Price a whole book in one sweep: every product on shared paths, FP64 sums
+ * and sums of squares, pathwise Greeks on request. Replaces the reference's
+ * per-contract GPU loop (pricer_mcl_gpu_gate.cpp:109-126) and, for the GPU
+ * gate's widened model x payoff set, the CPU Tree_Run/Tree_Read
+ * (pricer_mcl.cpp:598-709). */
+int thoth_gpu_price_book(const ThothBookDesc* book, ThothBookResult* out);
+
+/* Price n_books independent books (ragged path and step counts) in one
+ * persistent launch, replayed from a CUDA graph when the same shapes repeat.
+ * No reference counterpart beyond repeated PriceBook calls (pricer_mcl.cpp:197-240). */
+int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBookResult* out);
+
+/* Sobol integer coordinates x[d] (before the 2^-32 scaling) of points
+ * skip+1 .. skip+n_points of the Joe-Kuo sequence, row-major [point][dim].
+ * Same numbers as SobolGenerator::Next after Skip(skip)
+ * (sobol_generator.cpp:80-121). Test hook for bit-exact parity. */
+int thoth_gpu_sobol_points(int32_t dims, int64_t skip, int64_t n_points, uint32_t* out);
+
+/* Normalised Brownian-bridge increments n[f][i] = dW_i / sqrt(dt_i), i = 1..N,
+ * of paths skip+1 .. skip+n_paths, FP32, layout [path][factor][N].
+ * Same construction as PathGenerator::NextPath (path_generator.cpp:126-198).
+ * t: [n_dates] year fractions. Test hook. */
+int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factors, int64_t skip,
+                                int64_t n_paths, float* out);
+
+/* Inverse standard-normal CDF in FP32 of the uniforms x * 2^-32, x given as
+ * uint32 Sobol coordinates. Test hook for the device quantile. */
+int thoth_gpu_normal_quantiles(const uint32_t* x, int64_t n, float* out);
+
+/* Cooperative cancellation (reference: helpers/cancellation.hpp:9-15): a
+ * running thoth_gpu_price_* call polls a host-mapped word between launches and
+ * returns THOTH_GPU_E_CANCELLED. The flag is cleared by thoth_gpu_clear_cancel. */
+int thoth_gpu_request_cancel(void);
+int thoth_gpu_clear_cancel(void);
+
+/* Text of the last error on this thread (never NULL). */
+const char* thoth_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* THOTH_GPU_H */

@@ -1,0 +1,149 @@
+"""TEST INFRASTRUCTURE: Python handles on the parity oracles.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package. It loads
+  * oracle/_build/liboracle_port.so  — the C restatement (thoth_oracle.c),
+  * oracle/_ref/libref_oracle.so     — the reference's own node graph
+    (present only where the reference checkout was available to build it).
+"""
+import ctypes as C
+import os
+import pathlib
+import subprocess
+
+import numpy as np
+
+from thoth_gb300 import abi
+
+HERE = pathlib.Path(__file__).resolve().parent
+ROOT = HERE.parent
+JK_TABLE = ROOT / "thoth_gb300" / "data" / "joe_kuo_6_21201.bin"
+PORT_SO = HERE / "_build" / "liboracle_port.so"
+REF_SO = HERE / "_ref" / "libref_oracle.so"
+
+_port = None
+_ref = None
+
+
+def build(ref=None):
+    """Compile the port (and the reference build when its sources exist)."""
+    targets = ["port"]
+    refroot = pathlib.Path(ref or os.environ.get("THOTH_REFERENCE", "/root/reference"))
+    if (refroot / "pricer" / "src").is_dir():
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "REF=%s" % refroot] + targets, check=True)
+
+
+def port():
+    global _port
+    if _port is None:
+        if not PORT_SO.exists():
+            build()
+        lib = C.CDLL(str(PORT_SO))
+        lib.oracle_load_direction_numbers.argtypes = [C.c_char_p]
+        lib.oracle_sobol_points.argtypes = [C.c_int, C.c_int64, C.c_int64, C.POINTER(C.c_uint32)]
+        lib.oracle_normal_cdf_inv.argtypes = [C.c_double]
+        lib.oracle_normal_cdf_inv.restype = C.c_double
+        lib.oracle_normal_cdf_inv_n.argtypes = [C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
+        lib.oracle_bridge_increments.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int64,
+                                                 C.c_int64, C.c_uint64, C.POINTER(C.c_double)]
+        lib.oracle_price_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBookResult), C.c_int,
+                                          C.POINTER(C.c_double), C.c_int64]
+        for f in ("oracle_bs_price",):
+            getattr(lib, f).argtypes = [C.c_double] * 5 + [C.c_int]
+            getattr(lib, f).restype = C.c_double
+        lib.oracle_bs_delta.argtypes = [C.c_double] * 6 + [C.c_int]
+        lib.oracle_bs_delta.restype = C.c_double
+        lib.oracle_bs_vega.argtypes = [C.c_double] * 6
+        lib.oracle_bs_vega.restype = C.c_double
+        lib.oracle_heston_price.argtypes = [C.c_double] * 10 + [C.c_int]
+        lib.oracle_heston_price.restype = C.c_double
+        rc = lib.oracle_load_direction_numbers(str(JK_TABLE).encode())
+        if rc != 0:
+            raise RuntimeError("cannot load %s (%d)" % (JK_TABLE, rc))
+        _port = lib
+    return _port
+
+
+def ref_available():
+    return REF_SO.exists()
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        lib = C.CDLL(str(REF_SO))
+        lib.ref_sobol_points.argtypes = [C.c_int, C.c_int64, C.c_int64, C.POINTER(C.c_uint32)]
+        lib.ref_normal_cdf_inv.argtypes = [C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]
+        lib.ref_bridge_increments.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int64, C.c_int64,
+                                              C.c_uint64, C.POINTER(C.c_double)]
+        lib.ref_price_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBookResult),
+                                       C.POINTER(C.c_double), C.c_int64]
+        _ref = lib
+    return _ref
+
+
+def _u32(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def sobol_points(dims, skip, n, which="port"):
+    out = np.zeros((n, dims), dtype=np.uint32)
+    lib = port() if which == "port" else ref()
+    f = lib.oracle_sobol_points if which == "port" else lib.ref_sobol_points
+    d = f(dims, skip, n, _u32(out))
+    return out[:, :d]
+
+
+def normal_cdf_inv(p, which="port"):
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros_like(p)
+    if which == "port":
+        port().oracle_normal_cdf_inv_n(_d(p), p.size, _d(out))
+    else:
+        ref().ref_normal_cdf_inv(_d(p), p.size, _d(out))
+    return out
+
+
+def bridge_increments(t, factors, skip, n_paths, seed=0, which="port"):
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    N = len(t) - 1
+    out = np.zeros((n_paths, factors, N))
+    f = port().oracle_bridge_increments if which == "port" else ref().ref_bridge_increments
+    f(_d(t), len(t), factors, skip, n_paths, seed, _d(out))
+    return out
+
+
+def price_book(book, which="port", threads=1, n_per_path=0):
+    """Returns dict(book_premium, book_trust, premium, trust, per_path)."""
+    d = book.desc()
+    r, arrs = book.result()
+    per = np.zeros((max(n_per_path, 1), len(book.products)))
+    if which == "port":
+        rc = port().oracle_price_book(C.byref(d), C.byref(r), threads, _d(per) if n_per_path else None, n_per_path)
+    else:
+        rc = ref().ref_price_book(C.byref(d), C.byref(r), _d(per) if n_per_path else None, n_per_path)
+    if rc != 0:
+        raise RuntimeError("%s price_book failed: %d" % (which, rc))
+    return dict(book_premium=r.book_premium, book_trust=r.book_trust, premium=arrs["premium"].copy(),
+                trust=arrs["trust"].copy(), per_path=per[:n_per_path].copy() if n_per_path else None)
+
+
+def bs_price(F, K, T, vol, df, is_call=True):
+    return port().oracle_bs_price(F, K, T, vol, df, int(is_call))
+
+
+def bs_delta(S, K, T, vol, r, q, is_call=True):
+    return port().oracle_bs_delta(S, K, T, vol, r, q, int(is_call))
+
+
+def bs_vega(S, K, T, vol, r, q):
+    return port().oracle_bs_vega(S, K, T, vol, r, q)
+
+
+def heston_price(S, K, T, r, q, v0, kappa, theta, xi, rho, is_call=True):
+    return port().oracle_heston_price(S, K, T, r, q, v0, kappa, theta, xi, rho, int(is_call))

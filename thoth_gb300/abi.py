@@ -1,0 +1,270 @@
+"""ctypes mirror of include/thoth_gpu.h and a builder for book descriptors.
+
+The structs below must stay field-for-field identical to the C header; the
+library exports ``thoth_gpu_abi_sizes`` so tests can check the layouts.
+"""
+import ctypes as C
+
+import numpy as np
+
+THOTH_GPU_OK = 0
+THOTH_GPU_E_INVALID = -1
+THOTH_GPU_E_NODEVICE = -2
+THOTH_GPU_E_CUDA = -3
+THOTH_GPU_E_UNSUPPORTED = -4
+THOTH_GPU_E_CANCELLED = -5
+THOTH_GPU_E_NOMEM = -6
+THOTH_GPU_E_TOO_LARGE = -7
+
+MODEL_GBM, MODEL_HESTON, MODEL_LSV = 0, 1, 2
+VANILLA, BARRIER, VARIANCE, BASKET = 0, 1, 2, 3
+CALL, PUT = 0, 1
+GREEK_DELTA, GREEK_VEGA = 1, 2
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+
+
+class ThothAsset(C.Structure):
+    _fields_ = [
+        ("model", C.c_int32),
+        ("lev_points", C.c_int32),
+        ("spot", C.c_double),
+        ("carry", _dp),
+        ("vol", C.c_double),
+        ("v0", C.c_double),
+        ("kappa", C.c_double),
+        ("theta", C.c_double),
+        ("xi", C.c_double),
+        ("rho", C.c_double),
+        ("lev_ln_step", _dp),
+        ("lev_offset", _i64p),
+        ("lev_values", _dp),
+    ]
+
+
+class ThothProduct(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("option_type", C.c_int32),
+        ("asset", C.c_int32),
+        ("maturity", C.c_int32),
+        ("strike", C.c_double),
+        ("zero_rate", C.c_double),
+        ("fx", C.c_double),
+        ("quanto", C.c_double),
+        ("barrier_up", C.c_int32),
+        ("barrier_in", C.c_int32),
+        ("barrier_level", C.c_double),
+        ("n_monitor", C.c_int32),
+        ("monitor", _ip),
+        ("notional", C.c_double),
+        ("strike_variance", C.c_double),
+        ("total_year_fraction", C.c_double),
+        ("past_variance", C.c_double),
+        ("n_obs", C.c_int32),
+        ("obs", _ip),
+        ("n_components", C.c_int32),
+        ("components", _ip),
+        ("weights", _dp),
+    ]
+
+
+class ThothBookDesc(C.Structure):
+    _fields_ = [
+        ("n_dates", C.c_int32),
+        ("days", _ip),
+        ("t", _dp),
+        ("n_assets", C.c_int32),
+        ("assets", C.POINTER(ThothAsset)),
+        ("cholesky", _dp),
+        ("n_products", C.c_int32),
+        ("products", C.POINTER(ThothProduct)),
+        ("paths", C.c_int64),
+        ("sobol_skip", C.c_int64),
+        ("use_sobol", C.c_int32),
+        ("greeks", C.c_int32),
+        ("seed", C.c_uint64),
+    ]
+
+
+class ThothBookResult(C.Structure):
+    _fields_ = [
+        ("book_premium", C.c_double),
+        ("book_trust", C.c_double),
+        ("premium", _dp),
+        ("trust", _dp),
+        ("delta", _dp),
+        ("delta_trust", _dp),
+        ("vega", _dp),
+        ("vega_trust", _dp),
+        ("device_ms", C.c_double),
+    ]
+
+
+class ThothGbmResult(C.Structure):
+    _fields_ = [("premium", C.c_double), ("trust", C.c_double)]
+
+
+def _ptr(arr, ctype):
+    return arr.ctypes.data_as(C.POINTER(ctype))
+
+
+class Book:
+    """Owns the numpy buffers behind one ThothBookDesc (keeps them alive).
+
+    Assets and products are plain dicts; ``desc()`` materialises the C view.
+    Dates are calendar days from today (ACT/365) unless ``times`` is given.
+    """
+
+    def __init__(self, days=None, times=None, paths=1 << 14, sobol_skip=0, use_sobol=True, seed=0, greeks=0):
+        if days is not None:
+            self.days = np.ascontiguousarray(days, dtype=np.int32)
+            self.t = (self.days - self.days[0]).astype(np.float64) / 365.0
+        else:
+            self.days = None
+            self.t = np.ascontiguousarray(times, dtype=np.float64)
+        self.n_dates = len(self.t)
+        self.assets = []
+        self.products = []
+        self.cholesky = None
+        self.paths = int(paths)
+        self.sobol_skip = int(sobol_skip)
+        self.use_sobol = bool(use_sobol)
+        self.seed = int(seed)
+        self.greeks = int(greeks)
+        self._keep = []
+
+    # -- assets ---------------------------------------------------------
+    def _carry(self, carry):
+        if np.isscalar(carry):
+            return np.full(self.n_dates, float(carry))
+        return np.ascontiguousarray(carry, dtype=np.float64)
+
+    def add_gbm(self, spot, vol, carry):
+        self.assets.append(dict(model=MODEL_GBM, spot=spot, vol=vol, carry=self._carry(carry)))
+        return len(self.assets) - 1
+
+    def add_heston(self, spot, v0, kappa, theta, xi, rho, carry, leverage=None):
+        a = dict(model=MODEL_HESTON, spot=spot, v0=v0, kappa=kappa, theta=theta, xi=xi, rho=rho,
+                 carry=self._carry(carry))
+        if leverage is not None:
+            ln_step, offset, values = leverage
+            a["model"] = MODEL_LSV
+            a["lev_ln_step"] = np.ascontiguousarray(ln_step, dtype=np.float64)
+            a["lev_offset"] = np.ascontiguousarray(offset, dtype=np.int64)
+            a["lev_values"] = np.ascontiguousarray(values, dtype=np.float64)
+            assert a["lev_values"].shape[0] == self.n_dates
+        self.assets.append(a)
+        return len(self.assets) - 1
+
+    # -- products -------------------------------------------------------
+    def add_vanilla(self, asset, strike, maturity, option_type=CALL, zero_rate=0.0, fx=1.0, quanto=0.0):
+        self.products.append(dict(kind=VANILLA, asset=asset, strike=strike, maturity=maturity,
+                                  option_type=option_type, zero_rate=zero_rate, fx=fx, quanto=quanto))
+        return len(self.products) - 1
+
+    def add_barrier(self, asset, strike, maturity, level, up, knock_in, monitor, option_type=CALL,
+                    zero_rate=0.0, fx=1.0, quanto=0.0):
+        self.products.append(dict(kind=BARRIER, asset=asset, strike=strike, maturity=maturity,
+                                  option_type=option_type, zero_rate=zero_rate, fx=fx, quanto=quanto,
+                                  barrier_level=level, barrier_up=int(up), barrier_in=int(knock_in),
+                                  monitor=np.ascontiguousarray(monitor, dtype=np.int32)))
+        return len(self.products) - 1
+
+    def add_variance(self, asset, maturity, strike_variance, notional=1.0, zero_rate=0.0, fx=1.0,
+                     total_year_fraction=0.0, past_variance=0.0, obs=None, quanto=0.0):
+        p = dict(kind=VARIANCE, asset=asset, strike=0.0, maturity=maturity, option_type=CALL,
+                 zero_rate=zero_rate, fx=fx, quanto=quanto, strike_variance=strike_variance,
+                 notional=notional, total_year_fraction=total_year_fraction, past_variance=past_variance)
+        if obs is not None:
+            p["obs"] = np.ascontiguousarray(obs, dtype=np.int32)
+        self.products.append(p)
+        return len(self.products) - 1
+
+    def add_basket(self, components, weights, strike, maturity, option_type=CALL, zero_rate=0.0, fx=1.0,
+                   quanto=0.0):
+        self.products.append(dict(kind=BASKET, asset=-1, strike=strike, maturity=maturity,
+                                  option_type=option_type, zero_rate=zero_rate, fx=fx, quanto=quanto,
+                                  components=np.ascontiguousarray(components, dtype=np.int32),
+                                  weights=np.ascontiguousarray(weights, dtype=np.float64)))
+        return len(self.products) - 1
+
+    def set_cholesky(self, L):
+        self.cholesky = np.ascontiguousarray(L, dtype=np.float64)
+
+    # -- C view ---------------------------------------------------------
+    def desc(self):
+        keep = []
+        na, npr = len(self.assets), len(self.products)
+        A = (ThothAsset * max(na, 1))()
+        for i, a in enumerate(self.assets):
+            A[i].model = a["model"]
+            A[i].spot = a["spot"]
+            A[i].carry = _ptr(a["carry"], C.c_double)
+            A[i].vol = a.get("vol", 0.0)
+            for k in ("v0", "kappa", "theta", "xi", "rho"):
+                setattr(A[i], k, a.get(k, 0.0))
+            if a["model"] == MODEL_LSV:
+                A[i].lev_points = a["lev_values"].shape[1]
+                A[i].lev_ln_step = _ptr(a["lev_ln_step"], C.c_double)
+                A[i].lev_offset = _ptr(a["lev_offset"], C.c_int64)
+                A[i].lev_values = _ptr(a["lev_values"], C.c_double)
+        P = (ThothProduct * max(npr, 1))()
+        for i, p in enumerate(self.products):
+            P[i].kind = p["kind"]
+            P[i].option_type = p["option_type"]
+            P[i].asset = p["asset"]
+            P[i].maturity = p["maturity"]
+            P[i].strike = p["strike"]
+            P[i].zero_rate = p["zero_rate"]
+            P[i].fx = p["fx"]
+            P[i].quanto = p["quanto"]
+            if p["kind"] == BARRIER:
+                P[i].barrier_up = p["barrier_up"]
+                P[i].barrier_in = p["barrier_in"]
+                P[i].barrier_level = p["barrier_level"]
+                P[i].n_monitor = len(p["monitor"])
+                P[i].monitor = _ptr(p["monitor"], C.c_int32)
+            if p["kind"] == VARIANCE:
+                P[i].notional = p["notional"]
+                P[i].strike_variance = p["strike_variance"]
+                P[i].total_year_fraction = p["total_year_fraction"]
+                P[i].past_variance = p["past_variance"]
+                if "obs" in p:
+                    P[i].n_obs = len(p["obs"])
+                    P[i].obs = _ptr(p["obs"], C.c_int32)
+            if p["kind"] == BASKET:
+                P[i].n_components = len(p["components"])
+                P[i].components = _ptr(p["components"], C.c_int32)
+                P[i].weights = _ptr(p["weights"], C.c_double)
+        d = ThothBookDesc()
+        d.n_dates = self.n_dates
+        d.days = _ptr(self.days, C.c_int32) if self.days is not None else None
+        d.t = _ptr(self.t, C.c_double)
+        d.n_assets = na
+        d.assets = A
+        d.cholesky = _ptr(self.cholesky, C.c_double) if self.cholesky is not None else None
+        d.n_products = npr
+        d.products = P
+        d.paths = self.paths
+        d.sobol_skip = self.sobol_skip
+        d.use_sobol = int(self.use_sobol)
+        d.greeks = self.greeks
+        d.seed = self.seed
+        keep += [A, P]
+        self._keep = keep
+        return d
+
+    def result(self, greeks=False):
+        """Allocate a ThothBookResult with numpy-backed arrays; returns (res, arrays)."""
+        n = len(self.products)
+        arrs = {k: np.zeros(n) for k in ("premium", "trust", "delta", "delta_trust", "vega", "vega_trust")}
+        r = ThothBookResult()
+        r.premium = _ptr(arrs["premium"], C.c_double)
+        r.trust = _ptr(arrs["trust"], C.c_double)
+        if greeks:
+            for k in ("delta", "delta_trust", "vega", "vega_trust"):
+                setattr(r, k, _ptr(arrs[k], C.c_double))
+        return r, arrs
