@@ -209,6 +209,21 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
  * uint32 Sobol coordinates. Test hook for the device quantile. */
 int thoth_gpu_normal_quantiles(const uint32_t* x, int64_t n, float* out);
 
+/* Host-only test hook (no device needed): the time-ordered Brownian-bridge
+ * program the kernels execute. first_count[2*(i-1)] / [2*(i-1)+1] = first node
+ * and node count of step i (count 0 = pop); nodes[4*k..4*k+3] = (lw, rw, sd,
+ * build step) of node k; *n_nodes and *stack_depth are set. Buffers must hold
+ * n_dates-1 steps and n_dates-1 nodes. Same schedule as
+ * PathGenerator::BuildBridgeSchedule (path_generator.cpp:49-120). */
+int thoth_gpu_bridge_program(const double* t, int32_t n_dates, int32_t* first_count, double* nodes,
+                             int32_t* n_nodes, int32_t* stack_depth);
+
+/* Host-only test hook: validate a descriptor and report the launch plan.
+ * out[0] kernel variant, [1] paths per tile, [2] shared-memory bytes per CTA,
+ * [3] observation slots, [4] path groups, [5] bridge stack depth,
+ * [6] Sobol dimensions, [7] tiles. Returns the descriptor's status code. */
+int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out);
+
 /* Cooperative cancellation (reference: helpers/cancellation.hpp:9-15): a
  * running thoth_gpu_price_* call polls a host-mapped word between launches and
  * returns THOTH_GPU_E_CANCELLED. The flag is cleared by thoth_gpu_clear_cancel. */

@@ -56,8 +56,9 @@ def port():
         lib.oracle_bs_delta.restype = C.c_double
         lib.oracle_bs_vega.argtypes = [C.c_double] * 6
         lib.oracle_bs_vega.restype = C.c_double
-        lib.oracle_heston_price.argtypes = [C.c_double] * 10 + [C.c_int]
-        lib.oracle_heston_price.restype = C.c_double
+        for f in ("oracle_heston_price", "oracle_heston_price_p12"):
+            getattr(lib, f).argtypes = [C.c_double] * 10 + [C.c_int]
+            getattr(lib, f).restype = C.c_double
         rc = lib.oracle_load_direction_numbers(str(JK_TABLE).encode())
         if rc != 0:
             raise RuntimeError("cannot load %s (%d)" % (JK_TABLE, rc))
@@ -146,4 +147,10 @@ def bs_vega(S, K, T, vol, r, q):
 
 
 def heston_price(S, K, T, r, q, v0, kappa, theta, xi, rho, is_call=True):
+    """FP64 Heston price (Lewis single integral of the little-trap characteristic function)."""
     return port().oracle_heston_price(S, K, T, r, q, v0, kappa, theta, xi, rho, int(is_call))
+
+
+def heston_price_p12(S, K, T, r, q, v0, kappa, theta, xi, rho, is_call=True):
+    """The reference's P1/P2 decomposition of the same price (second rule)."""
+    return port().oracle_heston_price_p12(S, K, T, r, q, v0, kappa, theta, xi, rho, int(is_call))

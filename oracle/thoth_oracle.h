@@ -48,13 +48,17 @@ int oracle_price_book(const ThothBookDesc* d, ThothBookResult* r, int threads, d
                       int64_t n_per_path);
 
 /* Closed forms (FP64): Black-Scholes (pricer/src/helpers/finance.cpp:64-85)
- * and the Heston characteristic-function price in the "little Heston trap"
- * form (finance.cpp:472-568), integrated by adaptive Gauss-Kronrod 7-15. */
+ * and the Heston characteristic-function price with the "little Heston trap"
+ * characteristic function (finance.cpp:472-568): the Lewis single-integral
+ * form as the primary oracle and the reference's P1/P2 form as a cross-check,
+ * both integrated by adaptive Gauss-Kronrod 7-15. */
 double oracle_bs_price(double forward, double strike, double t, double vol, double df, int is_call);
 double oracle_bs_delta(double spot, double strike, double t, double vol, double r, double q, int is_call);
 double oracle_bs_vega(double spot, double strike, double t, double vol, double r, double q);
 double oracle_heston_price(double spot, double strike, double t, double r, double q, double v0,
                            double kappa, double theta, double xi, double rho, int is_call);
+double oracle_heston_price_p12(double spot, double strike, double t, double r, double q, double v0,
+                               double kappa, double theta, double xi, double rho, int is_call);
 
 #ifdef __cplusplus
 }

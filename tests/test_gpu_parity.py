@@ -1,0 +1,203 @@
+"""GPU parity: the CUDA engine through its C ABI against the oracle.
+
+Oracles: the reference's own code (through the fixtures in tests/golden,
+generated from the reference build) and its bit-exact CPU restatement
+(oracle/thoth_oracle.c) on the same Sobol paths; FP64 closed forms.
+
+Tolerances (FP32 path arithmetic against an FP64 reference on shared paths):
+  Sobol integers          bit-exact
+  quantile                |dz| <= 5e-7 * max(1, |z|)
+  bridge increments       |dn| <= 2e-5
+  prices (shared paths)   |gpu - ref| <= 0.5 SE  and  <= 1e-4 |ref| + 1e-5
+"""
+import numpy as np
+import pytest
+
+import oracle
+from thoth_gb300 import abi, workloads as W
+from tests.golden.make_golden import books, mixed_book
+
+pytestmark = pytest.mark.gpu
+
+REL, ABS = 1e-4, 1e-5
+
+
+def assert_shared_path_parity(gpu_res, premium, trust, label=""):
+    g = np.asarray(gpu_res["premium"])
+    err = np.abs(g - premium)
+    bad = (err > 0.5 * trust + 1e-12) | (err > REL * np.abs(premium) + ABS)
+    assert not bad.any(), "%s: worst product %d gpu %.8g ref %.8g se %.3g" % (
+        label, int(np.argmax(err)), g[np.argmax(err)], premium[np.argmax(err)], trust[np.argmax(err)])
+
+
+# ---- Sobol / quantile / bridge ------------------------------------------------
+
+def test_sobol_bit_exact_vs_reference_fixtures(gpu, golden):
+    g = golden["sobol"]
+    for k in ("a", "b", "c", "d"):
+        dims, skip, n = (int(v) for v in g[k + "_args"])
+        assert np.array_equal(gpu.sobol_points(dims, skip, n), g[k]), k
+
+
+@pytest.mark.parametrize("dims,skip,n", [(1, 0, 4096), (1460, 0, 300), (4097, 999, 17), (64, 2 ** 31, 100)])
+def test_sobol_bit_exact_vs_oracle(gpu, dims, skip, n):
+    assert np.array_equal(gpu.sobol_points(dims, skip, n), oracle.sobol_points(dims, skip, n))
+
+
+def test_quantile_accuracy(gpu):
+    rng = np.random.default_rng(1)
+    x = rng.integers(1, 2 ** 32, size=1 << 20, dtype=np.uint64).astype(np.uint32)
+    specials = np.array([1, 2, 3, 1000, 2 ** 31 - 2, 2 ** 31 - 1, 2 ** 31, 2 ** 31 + 1, 2 ** 32 - 2, 2 ** 32 - 1,
+                         0x7FFFFF80, 0x80000080, 0x00100000, 0xFFF00000], dtype=np.uint32)
+    x = np.concatenate([x, specials])
+    z = gpu.normal_quantiles(x).astype(np.float64)
+    ref = oracle.normal_cdf_inv(x.astype(np.float64) / 2.0 ** 32)
+    assert np.isfinite(z).all()
+    assert np.all(np.abs(z - ref) <= 5e-7 * np.maximum(1.0, np.abs(ref)))
+    assert z[-8] == 0.0 or abs(z[-8]) < 1e-9          # u = 1/2 exactly
+    assert np.all(np.sign(z[len(x) - len(specials):]) == np.sign(ref[len(x) - len(specials):]))
+
+
+def test_bridge_increments_vs_reference_fixtures(gpu, golden):
+    g = golden["bridge"]
+    got = gpu.bridge_increments(g["t"], 2, 3, 3)
+    assert np.abs(got - g["inc"]).max() < 2e-5
+    got = gpu.bridge_increments(g["t2"], 2, 0, 2)
+    assert np.abs(got - g["inc2"]).max() < 2e-5
+
+
+@pytest.mark.parametrize("t", [np.array([0.0, 0.25]), np.array([0, 0.1, 0.15, 0.4, 0.41, 1.0, 2.0]),
+                               np.arange(0, 731) / 365.0])
+def test_bridge_increments_vs_oracle(gpu, t):
+    for F in (1, 2):
+        got = gpu.bridge_increments(t, F, 1000, 300)     # tiles straddle the skip offset
+        ref = oracle.bridge_increments(t, F, 1000, 300)
+        assert np.abs(got - ref).max() < 2e-5
+
+
+# ---- books against the reference (fixtures) and the oracle -------------------
+
+def test_books_vs_reference_fixtures(gpu, golden):
+    g = golden["books"]
+    for name, b in books().items():
+        r = gpu.price_book(b)
+        assert_shared_path_parity(r, g[name + "_premium"], g[name + "_trust"], name)
+        np.testing.assert_allclose(r["trust"], g[name + "_trust"], rtol=1e-3, atol=1e-9, err_msg=name)
+        assert abs(r["book_premium"] - g[name + "_book"][0]) <= 0.5 * g[name + "_book"][1]
+
+
+def test_config1_gbm_call(gpu):
+    b = W.gbm_call(paths=1 << 18)
+    r = gpu.price_book(b, greeks=True)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "cfg1")
+    bs = oracle.bs_price(100 * np.exp(0.02), 100, 1.0, 0.25, np.exp(-0.03))
+    assert abs(r["premium"][0] - bs) < 3 * r["trust"][0]
+    # pathwise Greeks against the closed forms (Sobol error only)
+    assert abs(r["delta"][0] - oracle.bs_delta(100, 100, 1.0, 0.25, 0.03, 0.01)) < 3 * r["delta_trust"][0] + 1e-5
+    assert abs(r["vega"][0] - oracle.bs_vega(100, 100, 1.0, 0.25, 0.03, 0.01)) < 3 * r["vega_trust"][0] + 1e-3
+
+
+def test_drop_in_price_european_gbm(gpu):
+    # gpu::PriceEuropeanGbm semantics: forward measure, df given
+    F, K, T, vol, df = 100 * np.exp(0.02), 95.0, 1.0, 0.25, np.exp(-0.03)
+    for call in (True, False):
+        p, tr = gpu.price_european_gbm(F, K, T, vol, df, call, 1 << 18)
+        bs = oracle.bs_price(F, K, T, vol, df, call)
+        assert abs(p - bs) < 3 * tr
+    assert gpu.price_european_gbm(F, K, T, vol, df, True, 0) == (0.0, 0.0)
+
+
+def test_heston_calendar_grid_shared_paths(gpu):
+    b = W.heston_grid(paths=1 << 14, calendar=True)
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "heston daily")
+
+
+def test_heston_grid_vs_characteristic_function(gpu):
+    b = W.heston_grid(paths=1 << 20)
+    r = gpu.price_book(b)
+    cf = []
+    for m in W.MONTHS:
+        for K in W.STRIKES:
+            for typ in (abi.CALL, abi.PUT):
+                cf.append(oracle.heston_price(100, K, m / 12.0, 0.03, 0.0, 0.04, 1.5, 0.04, 0.6, -0.7, typ == abi.CALL))
+    cf = np.array(cf)
+    # QE at 252 steps/yr has a small discretisation bias; Sobol error is well below the MC trust
+    assert np.all(np.abs(r["premium"] - cf) <= 4 * r["trust"] + 2e-3 * np.maximum(cf, 1.0))
+
+
+def test_lsv_book_shared_paths(gpu):
+    b = W.lsv_book(paths=1 << 12)
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "lsv")
+
+
+def test_mixed_book_shared_paths(gpu):
+    b = mixed_book(paths=1 << 13)
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "mixed")
+    assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"]
+
+
+# ---- edge cases ----------------------------------------------------------------
+
+@pytest.mark.parametrize("skip,paths", [(0, 2), (0, 255), (0, 257), (1, 1000), (255, 513), (12345, 777)])
+def test_ragged_path_ranges(gpu, skip, paths):
+    b = W.heston_grid(paths=paths, calendar=True, months=(1, 2), strikes=(95, 105))
+    b.sobol_skip = skip
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "skip %d paths %d" % (skip, paths))
+
+
+def test_maturity_zero_and_single_step(gpu):
+    b = abi.Book(days=[0, 1], paths=1000)
+    a = b.add_gbm(100.0, 0.3, 0.01)
+    b.add_vanilla(a, 90.0, 0, abi.CALL, zero_rate=0.05)    # pays intrinsic today, df = 1
+    b.add_vanilla(a, 90.0, 1, abi.CALL, zero_rate=0.05)
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert abs(r["premium"][0] - 10.0) < 1e-5 and r["trust"][0] < 1e-6
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "single step")
+
+
+def test_beyond_sobol_budget_is_statistically_consistent(gpu):
+    # 2100 daily steps x 2 factors: tail dims from the counter-based generator, not the
+    # reference's serial xoshiro stream, so only statistical agreement is expected
+    b = W.heston_grid(paths=1 << 14, calendar=True, months=(69,), strikes=(100,))
+    r = gpu.price_book(b)
+    cf = [oracle.heston_price(100, 100, 2099 / 365.0, 0.03, 0, 0.04, 1.5, 0.04, 0.6, -0.7, t == abi.CALL)
+          for t in (abi.CALL, abi.PUT)]
+    assert np.all(np.abs(r["premium"] - cf) < 5 * r["trust"] + 0.05)
+
+
+def test_pseudo_random_mode(gpu):
+    b = W.gbm_call(paths=1 << 18, greeks=False)
+    b.use_sobol = False
+    b.seed = 42
+    r = gpu.price_book(b)
+    bs = oracle.bs_price(100 * np.exp(0.02), 100, 1.0, 0.25, np.exp(-0.03))
+    assert abs(r["premium"][0] - bs) < 4 * r["trust"][0]
+    b.seed = 43
+    r2 = gpu.price_book(b)
+    assert r2["premium"][0] != r["premium"][0]
+
+
+def test_determinism_bit_identical_reruns(gpu):
+    b = W.lsv_book(paths=1 << 12)
+    r1, r2 = gpu.price_book(b), gpu.price_book(b)
+    assert np.array_equal(r1["premium"], r2["premium"]) and r1["book_premium"] == r2["book_premium"]
+
+
+def test_invalid_descriptor_is_an_error_not_a_fault(gpu):
+    b = W.gbm_call(paths=1000)
+    b.products[0]["asset"] = 3
+    with pytest.raises(gpu.ThothGpuError) as e:
+        gpu.price_book(b)
+    assert e.value.code == abi.THOTH_GPU_E_INVALID
+    assert gpu.available()                      # the context is still usable
+    assert gpu.price_book(W.gbm_call(paths=1000))["premium"][0] > 0

@@ -1,0 +1,141 @@
+"""Host-side logic of the CUDA library that needs no device: ABI layout,
+exported symbols, the time-ordered bridge program, descriptor validation and
+kernel selection."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle
+import thoth_gb300 as G
+from thoth_gb300 import abi, workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "thoth_gpu.h")
+
+
+def test_library_exports_every_declared_entry_point():
+    names = re.findall(r"^\s*(?:int|const char\*)\s+(thoth_gpu_\w+)\s*\(", open(HEADER).read(), re.M)
+    assert len(names) >= 13
+    lib = G.lib()
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_abi_layout_matches_header():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "thoth_gpu.h"
+int main(void){
+ printf("%zu %zu %zu %zu %zu\n", sizeof(ThothAsset), sizeof(ThothProduct), sizeof(ThothBookDesc), sizeof(ThothBookResult), sizeof(ThothGbmResult));
+ printf("%zu %zu %zu %zu\n", offsetof(ThothAsset, lev_values), offsetof(ThothProduct, weights), offsetof(ThothBookDesc, seed), offsetof(ThothBookResult, device_ms));
+ return 0;}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "a.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "a")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    got = [int(v) for v in out]
+    want = [C.sizeof(abi.ThothAsset), C.sizeof(abi.ThothProduct), C.sizeof(abi.ThothBookDesc),
+            C.sizeof(abi.ThothBookResult), C.sizeof(abi.ThothGbmResult),
+            abi.ThothAsset.lev_values.offset, abi.ThothProduct.weights.offset, abi.ThothBookDesc.seed.offset,
+            abi.ThothBookResult.device_ms.offset]
+    assert got == want
+
+
+def _emulate(t, F, skip, npaths):
+    """Run the kernel's time-ordered bridge program in FP64 on the oracle's normals."""
+    fc, nodes, depth = G.bridge_program(t)
+    m = len(t) - 1
+    pts = oracle.sobol_points(min(m * F, 4097), skip, npaths)
+    out = np.zeros((npaths, F, m))
+    for p in range(npaths):
+        z = oracle.normal_cdf_inv(pts[p].astype(np.float64) / 2.0 ** 32)
+        for f in range(F):
+            wprev, top, stk = 0.0, 0.0, []
+            for i in range(1, m + 1):
+                first, cnt = fc[i - 1]
+                if cnt == 0:
+                    wi, top = top, stk.pop()
+                else:
+                    for k in range(cnt):
+                        lw, rw, sd, b = nodes[first + k]
+                        wn = lw * wprev + rw * top + sd * z[int(b) * F + f]
+                        if k + 1 < cnt:
+                            stk.append(top)
+                            top = wn
+                        else:
+                            wi = wn
+                    assert len(stk) < depth
+                out[p, f, i - 1] = (wi - wprev) / np.sqrt(t[i] - t[i - 1])
+                wprev = wi
+    return out
+
+
+@pytest.mark.parametrize("t", [np.array([0.0, 1.0]), np.arange(0, 366) / 365.0, np.arange(0, 505) / 252.0,
+                               np.array([0, 0.1, 0.15, 0.4, 0.41, 1.0, 2.0]),
+                               np.concatenate([[0], np.sort(np.random.default_rng(3).random(60)) * 2])])
+def test_bridge_program_reproduces_reference_bridge(t):
+    for F in (1, 2):
+        e = _emulate(t, F, 7, 3)
+        r = oracle.bridge_increments(t, F, 7, 3)
+        # program weights are stored in FP32
+        assert np.abs(e - r).max() < 5e-6
+
+
+def test_bridge_program_stack_depth_is_logarithmic():
+    for n in (1, 2, 3, 10, 100, 730, 4096):
+        _, _, depth = G.bridge_program(np.arange(n + 1) / 365.0)
+        assert depth <= int(np.ceil(np.log2(n + 1))) + 2
+
+
+def _code(book):
+    try:
+        G.plan_summary(book)
+        return 0
+    except G.ThothGpuError as e:
+        return e.code
+
+
+def test_descriptor_validation():
+    ok = W.gbm_call(paths=1000)
+    assert _code(ok) == 0
+    b = W.gbm_call(paths=1)
+    assert _code(b) == abi.THOTH_GPU_E_INVALID               # reference: paths must be > 1
+    b = W.gbm_call(paths=1000)
+    b.sobol_skip = 2 ** 32 - 10
+    assert _code(b) == abi.THOTH_GPU_E_TOO_LARGE             # 32-bit direction numbers
+    b = W.gbm_call(paths=1000)
+    b.products[0]["maturity"] = 5
+    assert _code(b) == abi.THOTH_GPU_E_INVALID               # maturity beyond the grid
+    b = abi.Book(times=[0.0, 0.5, 0.5], paths=100)
+    b.add_gbm(100, 0.2, 0.0)
+    b.add_vanilla(0, 100, 2)
+    assert _code(b) == abi.THOTH_GPU_E_INVALID               # dates not increasing
+    b = abi.Book(days=[0, 10, 20], paths=100)
+    b.add_gbm(100, 0.2, 0.0)
+    b.add_barrier(0, 100, 2, 90, up=False, knock_in=False, monitor=[2, 1])
+    assert _code(b) == abi.THOTH_GPU_E_INVALID               # unsorted monitor list
+    b = abi.Book(days=[0, 10], paths=100)
+    for _ in range(9):
+        b.add_gbm(100, 0.2, 0.0)
+    b.add_vanilla(0, 100, 1)
+    assert _code(b) == abi.THOTH_GPU_E_TOO_LARGE             # more than THOTH_MAX_ASSETS
+
+
+def test_kernel_selection_and_sizes():
+    s = G.plan_summary(W.gbm_call())
+    assert (s["variant"], s["sobol_dims"], s["stack_depth"]) == (5, 1, 1)
+    s = G.plan_summary(W.heston_grid(paths=1 << 20))
+    assert s["variant"] == 4 and s["sobol_dims"] == 1008 and s["slots"] == 7 and s["tiles"] == 4097
+    s = G.plan_summary(W.heston_grid(paths=1000, calendar=True))
+    assert s["sobol_dims"] == 1460
+    s = G.plan_summary(W.lsv_book(paths=1000))
+    assert s["variant"] == 3 and s["sobol_dims"] == 3650 and s["smem"] <= 227 * 1024

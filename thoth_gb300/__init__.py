@@ -1,0 +1,131 @@
+"""thoth_gb300 — GB300 (sm_103a) Monte-Carlo engine behind Thoth's !mcl_pricer.
+
+Python mirror of the reference's GPU interface (pricer/src/tasks/mcl_gpu.hpp:16-48:
+``Available``, ``DeviceInfo``, ``PriceEuropeanGbm``) plus the whole-book entry
+point, all calling the C ABI of ``libthoth_gpu.so`` (include/thoth_gpu.h).
+There is no CPU fallback: without the built library every call raises.
+"""
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+from . import abi
+from .abi import Book  # noqa: F401
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libthoth_gpu.so"
+
+_lib = None
+
+
+class ThothGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("thoth_gpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libthoth_gpu.so (built by thoth_gb300.build); raise if it is missing."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ThothGpuError(abi.THOTH_GPU_E_NODEVICE,
+                                "%s is not built: run `python -m thoth_gb300.build`" % LIB_PATH)
+        L = C.CDLL(str(LIB_PATH))
+        L.thoth_gpu_available.restype = C.c_int
+        L.thoth_gpu_device_info.argtypes = [C.c_char_p, C.c_size_t]
+        L.thoth_gpu_price_european_gbm.argtypes = [C.c_double] * 5 + [C.c_int, C.c_int64, C.c_uint64,
+                                                                       C.POINTER(abi.ThothGbmResult)]
+        L.thoth_gpu_price_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBookResult)]
+        L.thoth_gpu_price_batch.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(abi.ThothBookResult)]
+        L.thoth_gpu_sobol_points.argtypes = [C.c_int32, C.c_int64, C.c_int64, C.POINTER(C.c_uint32)]
+        L.thoth_gpu_bridge_increments.argtypes = [C.POINTER(C.c_double), C.c_int32, C.c_int32, C.c_int64, C.c_int64,
+                                                  C.POINTER(C.c_float)]
+        L.thoth_gpu_normal_quantiles.argtypes = [C.POINTER(C.c_uint32), C.c_int64, C.POINTER(C.c_float)]
+        L.thoth_gpu_bridge_program.argtypes = [C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int32),
+                                               C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.thoth_gpu_plan_summary.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(C.c_int64)]
+        L.thoth_gpu_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != abi.THOTH_GPU_OK:
+        raise ThothGpuError(rc, lib().thoth_gpu_last_error().decode())
+
+
+def available():
+    """Reference gpu::Available()."""
+    return bool(lib().thoth_gpu_available())
+
+
+def device_info():
+    """Reference gpu::DeviceInfo()."""
+    buf = C.create_string_buffer(256)
+    _check(lib().thoth_gpu_device_info(buf, 256))
+    return buf.value.decode()
+
+
+def price_european_gbm(forward, strike, t, vol, df, is_call, paths, seed=0):
+    """Reference gpu::PriceEuropeanGbm -> (premium, trust)."""
+    r = abi.ThothGbmResult()
+    _check(lib().thoth_gpu_price_european_gbm(forward, strike, t, vol, df, int(bool(is_call)), int(paths), int(seed),
+                                              C.byref(r)))
+    return r.premium, r.trust
+
+
+def price_book(book, greeks=False):
+    """Price every product of ``book`` (an abi.Book) in one sweep on the GPU."""
+    d = book.desc()
+    r, arrs = book.result(greeks=greeks)
+    _check(lib().thoth_gpu_price_book(C.byref(d), C.byref(r)))
+    out = dict(book_premium=r.book_premium, book_trust=r.book_trust, device_ms=r.device_ms)
+    out.update({k: v.copy() for k, v in arrs.items()})
+    return out
+
+
+def sobol_points(dims, skip, n):
+    out = np.zeros((n, dims), dtype=np.uint32)
+    _check(lib().thoth_gpu_sobol_points(dims, skip, n, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+    return out
+
+
+def normal_quantiles(x):
+    x = np.ascontiguousarray(x, dtype=np.uint32)
+    out = np.zeros(x.shape, dtype=np.float32)
+    _check(lib().thoth_gpu_normal_quantiles(x.ctypes.data_as(C.POINTER(C.c_uint32)), x.size,
+                                            out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def bridge_increments(t, factors, skip, n_paths):
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    N = len(t) - 1
+    out = np.zeros((n_paths, factors, N), dtype=np.float32)
+    _check(lib().thoth_gpu_bridge_increments(t.ctypes.data_as(C.POINTER(C.c_double)), len(t), factors, skip, n_paths,
+                                             out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def bridge_program(t):
+    """Host-only: the time-ordered bridge program (first/count per step, nodes, stack depth)."""
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    m = len(t) - 1
+    fc = np.zeros(2 * m, dtype=np.int32)
+    nodes = np.zeros(4 * m, dtype=np.float64)
+    nn, depth = C.c_int32(), C.c_int32()
+    _check(lib().thoth_gpu_bridge_program(t.ctypes.data_as(C.POINTER(C.c_double)), len(t),
+                                          fc.ctypes.data_as(C.POINTER(C.c_int32)),
+                                          nodes.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nn), C.byref(depth)))
+    return fc.reshape(m, 2), nodes[:4 * nn.value].reshape(nn.value, 4), depth.value
+
+
+def plan_summary(book):
+    """Host-only: validate a book and return its launch plan as a dict."""
+    d = book.desc()
+    out = np.zeros(8, dtype=np.int64)
+    _check(lib().thoth_gpu_plan_summary(C.byref(d), out.ctypes.data_as(C.POINTER(C.c_int64))))
+    keys = ("variant", "tile", "smem", "slots", "groups", "stack_depth", "sobol_dims", "tiles")
+    return dict(zip(keys, (int(v) for v in out)))

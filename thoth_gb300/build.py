@@ -1,0 +1,76 @@
+"""Build the engine's shared library for sm_103a, in-tree.
+
+    python -m thoth_gb300.build        # -> thoth_gb300/_build/libthoth_gpu.so
+
+nvcc cross-compiles without a GPU. The Joe-Kuo table is embedded into the
+library from thoth_gb300/data/joe_kuo_6_21201.bin through a generated C file.
+"""
+import concurrent.futures as cf
+import os
+import pathlib
+import shutil
+import subprocess
+import sys
+
+HERE = pathlib.Path(__file__).resolve().parent
+ROOT = HERE.parent
+BUILD = HERE / "_build"
+CSRC = HERE / "csrc"
+LIB = BUILD / "libthoth_gpu.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["kernels.cu", "thoth_gpu.cu"]
+
+
+def nvcc():
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(exe):
+        raise RuntimeError("nvcc not found")
+    return exe
+
+
+def _gen_blob():
+    data = (HERE / "data" / "joe_kuo_6_21201.bin").read_bytes()
+    out = BUILD / "jk_blob.c"
+    lines = ["#include <stddef.h>", "const unsigned char thoth_jk_blob[] = {"]
+    for i in range(0, len(data), 32):
+        lines.append(",".join(str(b) for b in data[i:i + 32]) + ",")
+    lines.append("};")
+    lines.append("const size_t thoth_jk_blob_size = %d;" % len(data))
+    text = "\n".join(lines) + "\n"
+    if not out.exists() or out.read_text() != text:
+        out.write_text(text)
+    return out
+
+
+def _compile(src, verbose):
+    obj = BUILD / (pathlib.Path(src).stem + ".o")
+    cmd = [nvcc(), "-c", str(CSRC / src), "-o", str(obj), "-O3", "-lineinfo", "-std=c++17",
+           "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"), "-I", str(CSRC)] + ARCH
+    if verbose:
+        cmd += ["-Xptxas", "-v"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s" % (src, r.stderr))
+    return obj, r.stderr
+
+
+def build(verbose=False):
+    BUILD.mkdir(exist_ok=True)
+    blob = _gen_blob()
+    blob_o = BUILD / "jk_blob.o"
+    subprocess.run(["gcc", "-c", "-fPIC", "-O1", str(blob), "-o", str(blob_o)], check=True)
+    with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
+        results = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+    objs = [r[0] for r in results]
+    if verbose:
+        for _, log in results:
+            sys.stderr.write(log)
+    tmp = BUILD / (LIB.name + ".tmp")
+    cmd = [nvcc(), "-shared", "-o", str(tmp)] + [str(o) for o in objs] + [str(blob_o)] + ARCH + ["-lcudart"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

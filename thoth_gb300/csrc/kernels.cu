@@ -1,0 +1,690 @@
+// kernels.cu — sm_103a kernels of the Monte-Carlo engine (see engine.cuh).
+#include "engine.cuh"
+
+#include <cuda_runtime.h>
+
+namespace thoth {
+
+// ---------------------------------------------------------------------------
+// shared-memory carve-up (host and device compute the same sizes)
+// ---------------------------------------------------------------------------
+struct Smem {
+    uint32_t* hs;   // [sobol_dims] high Sobol part of the current tile
+    float* stk;     // [stack_depth][n_factors_active][T]
+    float* slots;   // [n_slots][T + 1]
+    float* grp;     // [n_groups][T + 1]
+    float* last;    // [n_groups][T + 1]
+    int* valid;     // [T]
+    float* part;    // [T * 6]
+    double* red;    // [2 * warps]
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+__host__ __device__ inline size_t smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots,
+                                             int n_groups)
+{
+    size_t b = 0;
+    b += align16(sizeof(uint32_t) * (size_t)sobol_dims);
+    b += align16(sizeof(float) * (size_t)stack_depth * nfa * T);
+    b += align16(sizeof(float) * (size_t)n_slots * (T + 1));
+    b += 2 * align16(sizeof(float) * (size_t)n_groups * (T + 1));
+    b += align16(sizeof(int) * (size_t)T);
+    b += align16(sizeof(float) * (size_t)T * 6);
+    b += align16(sizeof(double) * 2 * (T / 32));
+    return b;
+}
+
+__device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
+{
+    Smem s;
+    size_t o = 0;
+    s.hs = reinterpret_cast<uint32_t*>(base + o);
+    o += align16(sizeof(uint32_t) * (size_t)P.sobol_dims);
+    s.stk = reinterpret_cast<float*>(base + o);
+    o += align16(sizeof(float) * (size_t)P.stack_depth * P.n_factors_active * T);
+    s.slots = reinterpret_cast<float*>(base + o);
+    o += align16(sizeof(float) * (size_t)P.n_slots_used * (T + 1));
+    s.grp = reinterpret_cast<float*>(base + o);
+    o += align16(sizeof(float) * (size_t)P.n_groups * (T + 1));
+    s.last = reinterpret_cast<float*>(base + o);
+    o += align16(sizeof(float) * (size_t)P.n_groups * (T + 1));
+    s.valid = reinterpret_cast<int*>(base + o);
+    o += align16(sizeof(int) * (size_t)T);
+    s.part = reinterpret_cast<float*>(base + o);
+    o += align16(sizeof(float) * (size_t)T * 6);
+    s.red = reinterpret_cast<double*>(base + o);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Sobol for the current tile. Path n = m * T + t (T = 2^TB). gray(n) splits
+// into bits >= TB, shared by the whole tile (XOR of V[d][TB..] over them is
+// computed once per tile and dimension into smem), and the thread's low TB
+// bits lo = gray(t) ^ ((m & 1) << (TB - 1)), combined from V[d][0..TB-1] with
+// per-thread bit masks: x = H_d ^ XOR_j (V[d][j] & mask_j). V[d][0..7] are read
+// as two 16-byte loads with a warp-uniform address (L1 broadcast), so no
+// per-thread table gather touches memory.
+// ---------------------------------------------------------------------------
+template <int TB>
+__device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m)
+{
+    constexpr int T = 1 << TB;
+    const uint64_t g = (uint64_t)m ^ ((uint64_t)m >> 1);
+    for (int d = threadIdx.x; d < P.sobol_dims; d += T) {
+        const uint32_t* V = P.sobol_v + d * SOBOL_BITS + TB;
+        uint32_t acc = 0;
+        uint64_t gg = g;
+        for (int k = 0; gg != 0 && k < SOBOL_BITS - TB; ++k, gg >>= 1)
+            if (gg & 1u) acc ^= __ldg(V + k);
+        hs[d] = acc;
+    }
+}
+
+struct SobolLane {
+    const uint32_t* hs;
+    uint32_t mask[8]; // all-ones where bit j of the thread's low Gray bits is set
+};
+
+template <int TB>
+__device__ __forceinline__ SobolLane sobol_lane(const DevPlan& P, uint32_t* hs, int64_t m)
+{
+    SobolLane L;
+    const uint32_t t = threadIdx.x;
+    const uint32_t lo = (t ^ (t >> 1) ^ ((uint32_t)(m & 1) << (TB - 1))) & ((1u << TB) - 1);
+    L.hs = hs;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) L.mask[j] = (j < TB && ((lo >> j) & 1u)) ? 0xFFFFFFFFu : 0u;
+    return L;
+}
+
+// Gaussian for reference dimension `dim` of Sobol index n
+__device__ __forceinline__ float gauss(const DevPlan& P, const SobolLane& L, uint64_t n, int dim)
+{
+    uint32_t x;
+    if (dim < P.sobol_dims) {
+        const uint4* v = reinterpret_cast<const uint4*>(P.sobol_v + dim * SOBOL_BITS);
+        const uint4 a = __ldg(v), b = __ldg(v + 1);
+        x = L.hs[dim];
+        x ^= (a.x & L.mask[0]) ^ (a.y & L.mask[1]) ^ (a.z & L.mask[2]) ^ (a.w & L.mask[3]);
+        x ^= (b.x & L.mask[4]) ^ (b.y & L.mask[5]) ^ (b.z & L.mask[6]) ^ (b.w & L.mask[7]);
+    } else {
+        x = hash_u32(P.seed, n, (uint32_t)dim);
+    }
+    return quantile_u32(x);
+}
+
+// ---------------------------------------------------------------------------
+// One time step of the bridge for every active factor slot: fills nz[] with the
+// normalised increments n_i = (W_i - W_{i-1}) / sqrt(t_i - t_{i-1}).
+// ---------------------------------------------------------------------------
+template <int NA, int T>
+__device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, const StepRec& rec, int& sp,
+                                            const SobolLane& L, uint64_t n, float (&Wprev)[2 * NA],
+                                            float (&top)[2 * NA], float (&nz)[2 * NA])
+{
+    constexpr int FS = 2 * NA;
+    const int t = threadIdx.x;
+    const int nfa = P.n_factors_active;
+    float Wi[FS];
+#pragma unroll
+    for (int f = 0; f < FS; ++f) Wi[f] = 0.f;
+    if (rec.count == 0) {
+        const int base = (sp - 1) * nfa * T + t;
+#pragma unroll
+        for (int f = 0; f < FS; ++f) {
+            const int a = f < NA ? f : f - NA;
+            const int ci = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
+            if (a < P.n_assets && ci >= 0) {
+                Wi[f] = top[f];
+                top[f] = S.stk[base + ci * T];
+            }
+        }
+        --sp;
+    } else {
+        float lw = rec.lw, rw = rec.rw, sd = rec.sd;
+        int dim = rec.dim;
+        for (int k = 0; k < rec.count; ++k) {
+            if (k > 0) {
+                const BridgeNode nd = P.nodes[rec.first + k - 1];
+                lw = nd.lw;
+                rw = nd.rw;
+                sd = nd.sd;
+                dim = nd.bstep * P.ref_factors;
+            }
+            const bool push = k + 1 < rec.count;
+            const int base = sp * nfa * T + t;
+#pragma unroll
+            for (int f = 0; f < FS; ++f) {
+                const int a = f < NA ? f : f - NA;
+                const int ci = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
+                if (a < P.n_assets && ci >= 0) {
+                    const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
+                    const float z = gauss(P, L, n, dim + fid);
+                    const float Wn = fmaf(lw, Wprev[f], fmaf(rw, top[f], sd * z));
+                    if (push) {
+                        S.stk[base + ci * T] = top[f];
+                        top[f] = Wn;
+                    } else {
+                        Wi[f] = Wn;
+                    }
+                }
+            }
+            if (push) ++sp;
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < FS; ++f) {
+        nz[f] = (Wi[f] - Wprev[f]) * rec.isd;
+        Wprev[f] = Wi[f];
+    }
+}
+
+// leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47)
+__device__ __forceinline__ void leverage(const DevPlan& P, int a, int i, float x, float& L, float& dL)
+{
+    const int layer = __ldg(P.lev_layer + a * (P.n_steps + 1) + i);
+    const float2 mp = __ldg(P.lev_map + a * P.lev_layers_stride + layer);
+    const int npts = P.lev_points[a];
+    const float* v = P.lev_values + (a * P.lev_layers_stride + layer) * npts;
+    const float f = fmaf(x, mp.x, mp.y);
+    const int last = npts - 1;
+    if (f <= 0.f) {
+        L = __ldg(v);
+        dL = 0.f;
+    } else if (f >= (float)last) {
+        L = __ldg(v + last);
+        dL = 0.f;
+    } else {
+        const int k = (int)f;
+        const float w = f - (float)k;
+        const float v0 = __ldg(v + k), v1 = __ldg(v + k + 1);
+        L = fmaf(w, v1 - v0, v0);
+        dL = (v1 - v0) * mp.x;
+    }
+}
+
+__device__ __forceinline__ float intrinsic(const DevProduct& pr, float s)
+{
+    const float iv = pr.call ? s - pr.K : pr.K - s;
+    return fmaxf(iv, 0.f);
+}
+
+// discounted flow of product pr on tile path k (contract_node.cpp:16-51)
+__device__ __forceinline__ float payoff(const DevPlan& P, const DevProduct& pr, const float* slots, const float* grp,
+                                       int stride, int k)
+{
+    float s;
+    switch (pr.kind) {
+    case P_VARIANCE: {
+        const float sum2 = grp[pr.slot_g * stride + k];
+        return pr.notional * ((pr.past + sum2) * pr.inv_T - pr.kvar) * pr.df;
+    }
+    case P_BARRIER: {
+        const float ext = grp[pr.slot_g * stride + k];
+        const bool hit = pr.up ? (ext >= pr.level) : (ext <= pr.level);
+        const bool alive = pr.knock_in ? hit : !hit;
+        if (!alive) return 0.f;
+        s = slots[pr.slot_s * stride + k] * pr.qfac;
+        break;
+    }
+    case P_BASKET: {
+        s = 0.f;
+        for (int c = 0; c < pr.comp_n; ++c) {
+            const Comp cp = P.comps[pr.comp_first + c];
+            s = fmaf(slots[cp.slot * stride + k], cp.w, s);
+        }
+        break;
+    }
+    default:
+        s = slots[pr.slot_s * stride + k] * pr.qfac;
+    }
+    return intrinsic(pr, s) * pr.df;
+}
+
+// pathwise delta and vega of product pr on tile path k
+__device__ __forceinline__ void greeks_of(const DevPlan& P, const DevProduct& pr, const float* slots, int stride,
+                                          int k, float& d, float& g)
+{
+    d = 0.f;
+    g = 0.f;
+    const float sgn = pr.call ? 1.f : -1.f;
+    if (pr.kind == P_VANILLA) {
+        const float sT = slots[pr.slot_s * stride + k];
+        const float s = sT * pr.qfac;
+        if (intrinsic(pr, s) > 0.f) {
+            const float y = pr.slot_y >= 0 ? slots[pr.slot_y * stride + k] : 1.f;
+            d = sgn * s * pr.inv_s0 * y * pr.df;
+            if (pr.slot_w >= 0) g = sgn * s * (slots[pr.slot_w * stride + k] - pr.vol_t) * pr.df;
+        }
+    } else if (pr.kind == P_BASKET) {
+        float s = 0.f, ds = 0.f;
+        for (int c = 0; c < pr.comp_n; ++c) {
+            const Comp cp = P.comps[pr.comp_first + c];
+            const float sc = slots[cp.slot * stride + k] * cp.w;
+            s += sc;
+            const float y = cp.slot_y >= 0 ? slots[cp.slot_y * stride + k] : 1.f;
+            ds = fmaf(sc * cp.inv_s0, y, ds);
+        }
+        if (intrinsic(pr, s) > 0.f) d = sgn * ds * pr.df;
+    }
+}
+
+__device__ __forceinline__ StepRec load_rec(const DevPlan& P, int i)
+{
+    const float4* r = reinterpret_cast<const float4*>(P.recs + (i - 1));
+    const float4 a = __ldg(r), b = __ldg(r + 1);
+    StepRec s;
+    s.lw = a.x;
+    s.rw = a.y;
+    s.sd = a.z;
+    s.dim = __float_as_int(a.w);
+    s.isd = b.x;
+    s.count = __float_as_int(b.y);
+    s.first = __float_as_int(b.z);
+    s.ev = __float_as_int(b.w);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// The book kernel. Template parameters:
+//   TB      log2 paths per tile (= threads per CTA)
+//   NA      compile-time asset slots (1 = single-asset fast path)
+//   MODEL   M_GBM / M_HESTON / M_LSV for single-model books, M_MIXED otherwise
+//   UNIFORM every step has the same per-asset constants (kept in registers)
+// ---------------------------------------------------------------------------
+template <int TB, int NA, int MODEL, bool UNIFORM>
+__global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const DevPlan P)
+{
+    constexpr int T = 1 << TB;
+    constexpr int FS = 2 * NA;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Smem S = carve(smem_raw, P, T);
+    const int t = threadIdx.x;
+    const int stride = T + 1;
+    __shared__ int s_cancel;
+
+    double* acc = P.acc + (size_t)blockIdx.x * P.n_acc;
+    for (int j = t; j < P.n_acc; j += T) acc[j] = 0.0;
+
+    // uniform step constants (UNIFORM: step 1's for every step)
+    float4 u0[NA], u1[NA], u2[NA];
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+        if (UNIFORM && a < P.n_assets) {
+            const float4* cs = reinterpret_cast<const float4*>(P.steps[a].c);
+            u0[a] = __ldg(cs);
+            u1[a] = __ldg(cs + 1);
+            u2[a] = __ldg(cs + 2);
+        } else {
+            u0[a] = u1[a] = u2[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+
+    for (int64_t tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
+        const int64_t m = P.tile_first + tile;
+        const uint64_t n = (uint64_t)m * T + (uint64_t)t;
+        const bool valid = n >= (uint64_t)P.skip + 1 && n <= (uint64_t)(P.skip + P.paths);
+        __syncthreads(); // previous tile fully evaluated
+        if (t == 0) s_cancel = (P.cancel != nullptr) ? *P.cancel : 0;
+        if (P.use_sobol) tile_high_bits<TB>(P, S.hs, m);
+        __syncthreads();
+        if (s_cancel) {
+            if (t == 0) atomicExch(P.status, 1);
+            return;
+        }
+        const SobolLane L = sobol_lane<TB>(P, S.hs, m);
+
+        // ---- path state -------------------------------------------------
+        float x[NA], comp[NA], v[NA], Wb[NA], y[NA];
+        float Wprev[FS], top[FS], nz[FS];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            x[a] = 0.f;
+            comp[a] = 0.f;
+            v[a] = P.v0[a];
+            Wb[a] = 0.f;
+            y[a] = 1.f;
+        }
+#pragma unroll
+        for (int f = 0; f < FS; ++f) {
+            Wprev[f] = 0.f;
+            top[f] = 0.f;
+            nz[f] = 0.f;
+        }
+        int sp = 0;
+        for (int g = 0; g < P.n_groups; ++g) {
+            S.grp[g * stride + t] = P.grp_init[g];
+            S.last[g * stride + t] = 0.f;
+        }
+
+        // events on date index i for asset a (after the state at date i is known)
+        auto apply_events = [&](int i, int a, float xa, float step, float wa, float ya) {
+            const int2 r = P.ev_range[i * P.n_assets + a];
+            for (int e = r.x; e < r.x + r.y; ++e) {
+                const Event ev = P.events[e];
+                switch (ev.type) {
+                case EV_SNAP_S: S.slots[ev.a * stride + t] = P.s0[a] * expf(xa); break;
+                case EV_SNAP_W: S.slots[ev.a * stride + t] = wa; break;
+                case EV_SNAP_Y: S.slots[ev.a * stride + t] = ya; break;
+                case EV_GRP_MIN: {
+                    float* g = S.grp + ev.a * stride + t;
+                    *g = fminf(*g, xa - ev.p);
+                    break;
+                }
+                case EV_GRP_MAX: {
+                    float* g = S.grp + ev.a * stride + t;
+                    *g = fmaxf(*g, xa - ev.p);
+                    break;
+                }
+                case EV_GRP_SQ_STEP: {
+                    float* g = S.grp + ev.a * stride + t;
+                    const float d = step - ev.p;
+                    *g = fmaf(d, d, *g);
+                    break;
+                }
+                default: { // EV_GRP_SQ_OBS
+                    float* g = S.grp + ev.a * stride + t;
+                    float* l = S.last + ev.a * stride + t;
+                    const float d = xa - *l - ev.p;
+                    *g = fmaf(d, d, *g);
+                    *l = xa;
+                }
+                }
+            }
+        };
+#pragma unroll
+        for (int a = 0; a < NA; ++a)
+            if (a < P.n_assets) apply_events(0, a, 0.f, 0.f, 0.f, 1.f);
+
+        // ---- time loop (step records prefetched one step ahead) ------------
+        StepRec rec = load_rec(P, 1);
+        for (int i = 1; i <= P.n_steps; ++i) {
+            const StepRec cur = rec;
+            if (i < P.n_steps) rec = load_rec(P, i + 1);
+            if (P.use_sobol) {
+                bridge_step<NA, T>(P, S, cur, sp, L, n, Wprev, top, nz);
+            } else {
+#pragma unroll
+                for (int f = 0; f < FS; ++f) {
+                    const int a = f < NA ? f : f - NA;
+                    const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
+                    if (a < P.n_assets && fid >= 0)
+                        nz[f] = quantile_u32(hash_u32(P.seed, n, (uint32_t)((i - 1) * P.ref_factors + fid)));
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < NA; ++a) {
+                if (a >= P.n_assets) continue;
+                float4 c0, c1, c2;
+                if (UNIFORM) {
+                    c0 = u0[a];
+                    c1 = u1[a];
+                    c2 = u2[a];
+                } else {
+                    const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + a].c);
+                    c0 = __ldg(cs);
+                    c1 = __ldg(cs + 1);
+                    c2 = __ldg(cs + 2);
+                }
+                const int model = (MODEL == M_MIXED) ? P.model[a] : MODEL;
+                float step;
+                if (model == M_GBM) {
+                    float e = nz[a];
+                    if (MODEL == M_MIXED && P.corr) {
+                        e = 0.f;
+#pragma unroll
+                        for (int u = 0; u < NA; ++u)
+                            if (u < P.n_assets) e = fmaf(P.chol[a * MAX_ASSETS + u], nz[u], e);
+                    }
+                    step = fmaf(c0.y, e, c0.x);
+                    Wb[a] = fmaf(c0.z, e, Wb[a]);
+                } else {
+                    const float vp = v[a];
+                    const float vc = qe_step(vp, nz[NA + a], c0.x, c0.y, c0.z, c0.w);
+                    float Lv = 1.f, dL = 0.f;
+                    if (model == M_LSV) leverage(P, a, i, x[a], Lv, dL);
+                    const float s = vp + vc;
+                    if (!P.degenerate[a]) {
+                        const float B = fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * nz[a];
+                        if (model == M_LSV) {
+                            step = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
+                            y[a] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
+                        } else {
+                            step = c1.x + B - c1.w * s;
+                        }
+                    } else {
+                        const float sq = fast_sqrt(vp * c2.z) * nz[a];
+                        step = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
+                        if (model == M_LSV) y[a] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
+                    }
+                    v[a] = vc;
+                }
+                // Kahan-compensated log-spot
+                const float yy = step - comp[a];
+                const float tt = x[a] + yy;
+                comp[a] = (tt - x[a]) - yy;
+                x[a] = tt;
+                if (cur.ev) apply_events(i, a, x[a], step, Wb[a], y[a]);
+            }
+        }
+        S.valid[t] = valid ? 1 : 0;
+        __syncthreads();
+
+        // ---- product evaluation: thread per product, FP32 tile partials ----
+        const int C = P.n_products;
+        for (int pc = 0; pc < C; pc += T) {
+            const int CP = min(C - pc, T);
+            const int G = T / CP;
+            const int pl = t % CP, g = t / CP;
+            float a6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (g < G) {
+                const DevProduct pr = P.products[pc + pl];
+                for (int k = g; k < T; k += G) {
+                    if (!S.valid[k]) continue;
+                    const float f = payoff(P, pr, S.slots, S.grp, stride, k);
+                    a6[0] += f;
+                    a6[1] = fmaf(f, f, a6[1]);
+                    if (P.greeks) {
+                        float d, gg;
+                        greeks_of(P, pr, S.slots, stride, k, d, gg);
+                        a6[2] += d;
+                        a6[3] = fmaf(d, d, a6[3]);
+                        a6[4] += gg;
+                        a6[5] = fmaf(gg, gg, a6[5]);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 6; ++j) S.part[(g * CP + pl) * 6 + j] = a6[j];
+            }
+            __syncthreads();
+            if (t < CP) {
+                double s6[6] = {0, 0, 0, 0, 0, 0};
+                for (int g2 = 0; g2 < G; ++g2)
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) s6[j] += (double)S.part[(g2 * CP + t) * 6 + j];
+#pragma unroll
+                for (int j = 0; j < 6; ++j) acc[(size_t)(pc + t) * 6 + j] += s6[j];
+            }
+            __syncthreads();
+        }
+        // ---- book value per path (book_node.cpp:16-31) ---------------------
+        float b = 0.f;
+        if (valid)
+            for (int p = 0; p < C; ++p) {
+                const DevProduct pr = P.products[p];
+                b = fmaf(payoff(P, pr, S.slots, S.grp, stride, t), pr.fx, b);
+            }
+        double b1 = b, b2 = (double)b * b;
+        for (int o = 16; o > 0; o >>= 1) {
+            b1 += __shfl_xor_sync(0xffffffffu, b1, o);
+            b2 += __shfl_xor_sync(0xffffffffu, b2, o);
+        }
+        if ((t & 31) == 0) {
+            S.red[2 * (t >> 5)] = b1;
+            S.red[2 * (t >> 5) + 1] = b2;
+        }
+        __syncthreads();
+        if (t == 0) {
+            double s1 = 0, s2 = 0;
+            for (int w = 0; w < T / 32; ++w) {
+                s1 += S.red[2 * w];
+                s2 += S.red[2 * w + 1];
+            }
+            acc[(size_t)C * 6] += s1;
+            acc[(size_t)C * 6 + 1] += s2;
+        }
+    }
+}
+
+// fixed-order FP64 reduction of the per-CTA rows
+__global__ void reduce_rows(const double* __restrict__ acc, int rows, int n_acc, double* __restrict__ out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_acc) return;
+    double s = 0.0;
+    for (int r = 0; r < rows; ++r) s += acc[(size_t)r * n_acc + j];
+    out[j] = s;
+}
+
+// ---- test hooks -----------------------------------------------------------
+__global__ void sobol_points_kernel(const uint32_t* __restrict__ V, int dims, int64_t skip, int64_t n_points,
+                                    uint32_t* __restrict__ out)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n_points * dims) return;
+    const int64_t p = idx / dims;
+    const int d = (int)(idx % dims);
+    const uint64_t nn = (uint64_t)(skip + 1 + p);
+    const uint64_t g = nn ^ (nn >> 1);
+    uint32_t x = 0;
+    for (int k = 0; k < SOBOL_BITS; ++k)
+        if ((g >> k) & 1u) x ^= __ldg(V + (size_t)d * SOBOL_BITS + k);
+    out[idx] = x;
+}
+
+__global__ void quantile_kernel(const uint32_t* __restrict__ x, int64_t n, float* __restrict__ out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = quantile_u32(x[i]);
+}
+
+// writes the bridge increments of every valid path: out[path][factor][N]
+template <int TB>
+__global__ void __launch_bounds__(1 << TB) bridge_kernel(const DevPlan P, float* __restrict__ out)
+{
+    constexpr int T = 1 << TB;
+    constexpr int NA = 1; // factor slots 0..1 carry reference factors 0..1
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Smem S = carve(smem_raw, P, T);
+    const int t = threadIdx.x;
+    for (int64_t tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
+        const int64_t m = P.tile_first + tile;
+        const uint64_t n = (uint64_t)m * T + (uint64_t)t;
+        const bool valid = n >= (uint64_t)P.skip + 1 && n <= (uint64_t)(P.skip + P.paths);
+        __syncthreads();
+        tile_high_bits<TB>(P, S.hs, m);
+        __syncthreads();
+        const SobolLane L = sobol_lane<TB>(P, S.hs, m);
+        float Wprev[2] = {0.f, 0.f}, top[2] = {0.f, 0.f}, nz[2];
+        int sp = 0;
+        const int64_t path = (int64_t)n - P.skip - 1;
+        for (int i = 1; i <= P.n_steps; ++i) {
+            const StepRec rec = load_rec(P, i);
+            bridge_step<NA, T>(P, S, rec, sp, L, n, Wprev, top, nz);
+            if (valid) {
+                for (int f = 0; f < P.n_factors_active; ++f)
+                    out[((size_t)path * P.n_factors_active + f) * P.n_steps + (i - 1)] = nz[f];
+            }
+        }
+    }
+}
+
+// ---- launch wrappers --------------------------------------------------------
+template <int TB, int NA, int MODEL, bool UNIFORM>
+static cudaError_t launch_book_t(const DevPlan& P, int grid, size_t smem, cudaStream_t st)
+{
+    auto k = book_kernel<TB, NA, MODEL, UNIFORM>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, 1 << TB, smem, st>>>(P);
+    return cudaGetLastError();
+}
+
+// variants: 0 GBM, 1 Heston, 2 LSV (single asset, per-step constants),
+//           3 mixed multi-asset, 4 Heston with uniform steps, 5 GBM with uniform steps
+cudaError_t launch_book(const DevPlan& P, int variant, int grid, size_t smem, cudaStream_t st)
+{
+    switch (variant) {
+    case 0: return launch_book_t<8, 1, M_GBM, false>(P, grid, smem, st);
+    case 1: return launch_book_t<8, 1, M_HESTON, false>(P, grid, smem, st);
+    case 2: return launch_book_t<8, 1, M_LSV, false>(P, grid, smem, st);
+    case 3: return launch_book_t<7, MAX_ASSETS, M_MIXED, false>(P, grid, smem, st);
+    case 4: return launch_book_t<8, 1, M_HESTON, true>(P, grid, smem, st);
+    case 5: return launch_book_t<8, 1, M_GBM, true>(P, grid, smem, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+int book_variant_tile_bits(int variant) { return variant == 3 ? 7 : 8; }
+
+template <int TB, int NA, int MODEL, bool UNIFORM>
+static int occ_t(size_t smem)
+{
+    auto k = book_kernel<TB, NA, MODEL, UNIFORM>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
+    int n = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 1 << TB, smem) != cudaSuccess) return 1;
+    return n < 1 ? 1 : n;
+}
+
+// resident CTAs per SM of a variant at a given dynamic shared-memory size
+int book_occupancy(int variant, size_t smem)
+{
+    switch (variant) {
+    case 0: return occ_t<8, 1, M_GBM, false>(smem);
+    case 1: return occ_t<8, 1, M_HESTON, false>(smem);
+    case 2: return occ_t<8, 1, M_LSV, false>(smem);
+    case 3: return occ_t<7, MAX_ASSETS, M_MIXED, false>(smem);
+    case 4: return occ_t<8, 1, M_HESTON, true>(smem);
+    case 5: return occ_t<8, 1, M_GBM, true>(smem);
+    default: return 1;
+    }
+}
+size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups)
+{
+    return smem_bytes(T, sobol_dims, stack_depth, nfa, n_slots, n_groups);
+}
+
+cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st)
+{
+    reduce_rows<<<(n_acc + 127) / 128, 128, 0, st>>>(acc, rows, n_acc, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64_t n_points, uint32_t* out,
+                                cudaStream_t st)
+{
+    const int64_t total = n_points * dims;
+    if (total == 0) return cudaSuccess;
+    sobol_points_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(V, dims, skip, n_points, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quantile(const uint32_t* x, int64_t n, float* out, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    quantile_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bridge(const DevPlan& P, int grid, size_t smem, float* out, cudaStream_t st)
+{
+    auto k = bridge_kernel<8>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, 256, smem, st>>>(P, out);
+    return cudaGetLastError();
+}
+
+} // namespace thoth

@@ -1,0 +1,1109 @@
+// thoth_gpu.cu — host side of the C ABI declared in include/thoth_gpu.h.
+//
+// Turns a ThothBookDesc into a flat device plan (time grid constants, the
+// time-ordered Brownian-bridge program, path events, product table), uploads it
+// in one copy into a per-process device arena, runs the persistent book kernel
+// and the fixed-order FP64 reduction, and finalises premium / trust exactly as
+// the reference's indicators do (monte_carlo_node.cpp:26-40).
+#include "thoth_gpu.h"
+#include "engine.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace thoth {
+cudaError_t launch_book(const DevPlan& P, int variant, int grid, size_t smem, cudaStream_t st);
+int book_variant_tile_bits(int variant);
+int book_occupancy(int variant, size_t smem);
+size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups);
+cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st);
+cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64_t n_points, uint32_t* out,
+                                cudaStream_t st);
+cudaError_t launch_quantile(const uint32_t* x, int64_t n, float* out, cudaStream_t st);
+cudaError_t launch_bridge(const DevPlan& P, int grid, size_t smem, float* out, cudaStream_t st);
+} // namespace thoth
+
+// Joe-Kuo table embedded at build time (generated translation unit)
+extern "C" const unsigned char thoth_jk_blob[];
+extern "C" const size_t thoth_jk_blob_size;
+
+using namespace thoth;
+
+namespace {
+
+thread_local std::string g_err = "";
+std::mutex g_mu;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                                         \
+    do {                                                                                                       \
+        cudaError_t e_ = (expr);                                                                               \
+        if (e_ != cudaSuccess)                                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? THOTH_GPU_E_NOMEM : THOTH_GPU_E_CUDA,                \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));                                   \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// per-process device state
+// ---------------------------------------------------------------------------
+struct Device {
+    bool ready = false;
+    int id = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint32_t* sobol_v = nullptr;    // [4097][32]
+    uint32_t* sobol_rows = nullptr; // [4097][32]
+    uint32_t* sobol_rows32 = nullptr; // [4097][32]
+    unsigned char* arena = nullptr;
+    size_t arena_size = 0;
+    unsigned char* pinned = nullptr; // host staging (plan upload + result download)
+    size_t pinned_size = 0;
+    int* cancel_host = nullptr;      // host-mapped cancel word
+    int* cancel_dev = nullptr;
+};
+Device g_dev;
+
+int max_dims() { return 4097; }
+
+// direction numbers V[d][32] from the embedded Joe-Kuo table (sobol_generator.cpp:22-76)
+bool build_direction_numbers(std::vector<uint32_t>& V, std::vector<uint32_t>& rows, std::vector<uint32_t>& rows32)
+{
+    const unsigned char* b = thoth_jk_blob;
+    if (thoth_jk_blob_size < 16 || std::memcmp(b, "JK621201", 8) != 0) return false;
+    uint32_t dims, nm;
+    std::memcpy(&dims, b + 8, 4);
+    std::memcpy(&nm, b + 12, 4);
+    const uint32_t* S = reinterpret_cast<const uint32_t*>(b + 16);
+    const uint32_t* A = S + dims;
+    const uint32_t* MO = A + dims;
+    const uint32_t* M = MO + dims + 1;
+    const int D = (int)dims + 1;
+    V.assign((size_t)D * 32, 0);
+    for (int i = 0; i < 32; i++) V[i] = 1u << (31 - i);
+    for (int d = 1; d < D; d++) {
+        const uint32_t s = S[d - 1], a = A[d - 1];
+        const uint32_t* m = M + MO[d - 1];
+        uint32_t* v = V.data() + (size_t)d * 32;
+        if (s >= 32) {
+            for (int i = 0; i < 32; i++) v[i] = m[i] << (31 - i);
+        } else {
+            for (uint32_t i = 0; i < s; i++) v[i] = m[i] << (31 - i);
+            for (uint32_t i = s; i < 32; i++) {
+                v[i] = v[i - s] ^ (v[i - s] >> s);
+                for (uint32_t k = 1; k < s; k++) v[i] ^= ((a >> (s - 1 - k)) & 1u) * v[i - k];
+            }
+        }
+    }
+    // low-bit tables: rows[d][k] = XOR_{j<4, bit j of k} V[d][j]; rows[d][16+k] likewise over V[d][4..7]
+    rows.assign((size_t)D * 32, 0);
+    for (int d = 0; d < D; d++)
+        for (int k = 0; k < 16; k++) {
+            uint32_t lo = 0, hi = 0;
+            for (int j = 0; j < 4; j++)
+                if ((k >> j) & 1) {
+                    lo ^= V[(size_t)d * 32 + j];
+                    hi ^= V[(size_t)d * 32 + 4 + j];
+                }
+            rows[(size_t)d * 32 + k] = lo;
+            rows[(size_t)d * 32 + 16 + k] = hi;
+        }
+    // 5-bit tables: rows32[d][k] = XOR_{j<5, bit j of k} V[d][j]
+    rows32.assign((size_t)D * 32, 0);
+    for (int d = 0; d < D; d++)
+        for (int k = 0; k < 32; k++) {
+            uint32_t x = 0;
+            for (int j = 0; j < 5; j++)
+                if ((k >> j) & 1) x ^= V[(size_t)d * 32 + j];
+            rows32[(size_t)d * 32 + k] = x;
+        }
+    return true;
+}
+
+int ensure_device()
+{
+    if (g_dev.ready) {
+        CUDA_TRY(cudaSetDevice(g_dev.id));
+        return THOTH_GPU_OK;
+    }
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(THOTH_GPU_E_NODEVICE, "no CUDA device");
+    cudaDeviceProp p;
+    CUDA_TRY(cudaGetDeviceProperties(&p, 0));
+    if (!(p.major == 10 && p.minor == 3))
+        return fail(THOTH_GPU_E_NODEVICE, std::string("device ") + p.name + " is not sm_103 (built for sm_103a only)");
+    g_dev.id = 0;
+    CUDA_TRY(cudaSetDevice(0));
+    g_dev.sms = p.multiProcessorCount;
+    CUDA_TRY(cudaStreamCreateWithFlags(&g_dev.stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&g_dev.ev0));
+    CUDA_TRY(cudaEventCreate(&g_dev.ev1));
+    std::vector<uint32_t> V, rows, rows32;
+    if (!build_direction_numbers(V, rows, rows32)) return fail(THOTH_GPU_E_INVALID, "embedded Joe-Kuo table is corrupt");
+    CUDA_TRY(cudaMalloc(&g_dev.sobol_v, V.size() * 4));
+    CUDA_TRY(cudaMalloc(&g_dev.sobol_rows, rows.size() * 4));
+    CUDA_TRY(cudaMalloc(&g_dev.sobol_rows32, rows32.size() * 4));
+    CUDA_TRY(cudaMemcpy(g_dev.sobol_v, V.data(), V.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(g_dev.sobol_rows, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(g_dev.sobol_rows32, rows32.data(), rows32.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaHostAlloc(&g_dev.cancel_host, sizeof(int), cudaHostAllocMapped));
+    *g_dev.cancel_host = 0;
+    CUDA_TRY(cudaHostGetDevicePointer(&g_dev.cancel_dev, g_dev.cancel_host, 0));
+    g_dev.ready = true;
+    return THOTH_GPU_OK;
+}
+
+int ensure_arena(size_t bytes)
+{
+    if (bytes <= g_dev.arena_size) return THOTH_GPU_OK;
+    if (g_dev.arena) cudaFree(g_dev.arena);
+    g_dev.arena = nullptr;
+    g_dev.arena_size = 0;
+    const size_t sz = std::max(bytes, (size_t)1 << 22) * 5 / 4;
+    CUDA_TRY(cudaMalloc(&g_dev.arena, sz));
+    g_dev.arena_size = sz;
+    return THOTH_GPU_OK;
+}
+
+int ensure_pinned(size_t bytes)
+{
+    if (bytes <= g_dev.pinned_size) return THOTH_GPU_OK;
+    if (g_dev.pinned) cudaFreeHost(g_dev.pinned);
+    g_dev.pinned = nullptr;
+    g_dev.pinned_size = 0;
+    const size_t sz = std::max(bytes, (size_t)1 << 20) * 5 / 4;
+    CUDA_TRY(cudaHostAlloc(&g_dev.pinned, sz, cudaHostAllocDefault));
+    g_dev.pinned_size = sz;
+    return THOTH_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// packing helper: 16-byte aligned sections of one upload blob
+// ---------------------------------------------------------------------------
+struct Blob {
+    std::vector<unsigned char> bytes;
+    template <class T>
+    size_t put(const std::vector<T>& v)
+    {
+        const size_t off = (bytes.size() + 15) & ~size_t(15);
+        bytes.resize(off + v.size() * sizeof(T) + 16);
+        if (!v.empty()) std::memcpy(bytes.data() + off, v.data(), v.size() * sizeof(T));
+        bytes.resize(off + v.size() * sizeof(T));
+        return off;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Brownian bridge: the reference schedule (path_generator.cpp:49-120) and its
+// time-ordered program. Processing dates 1..m in order, date i is either a
+// pending right anchor (pop) or the end of a chain of nodes whose left anchor
+// is date i-1; every node but the last in a chain is pushed.
+// ---------------------------------------------------------------------------
+struct BridgeProgram {
+    std::vector<StepProg> prog;
+    std::vector<BridgeNode> nodes;
+    int stack_depth = 1;
+};
+
+bool build_bridge(const std::vector<double>& t, BridgeProgram& out, std::string& err)
+{
+    const int m = (int)t.size() - 1;
+    std::vector<int> bi(m), li(m), ri(m);
+    std::vector<double> lw(m), rw(m), sd(m);
+    auto bt = [&](int k) { return t[(size_t)k + 1]; };
+    std::vector<int> map(m, 0);
+    map[m - 1] = 1;
+    bi[0] = m - 1;
+    sd[0] = std::sqrt(bt(m - 1));
+    lw[0] = rw[0] = 0.0;
+    int j = 0;
+    for (int i = 1; i < m; i++) {
+        while (map[j]) j++;
+        int k = j;
+        while (!map[k]) k++;
+        int l = j + ((k - 1 - j) >> 1);
+        map[l] = i + 1;
+        bi[i] = l;
+        li[i] = j;
+        ri[i] = k;
+        if (j != 0) {
+            lw[i] = (bt(k) - bt(l)) / (bt(k) - bt(j - 1));
+            rw[i] = (bt(l) - bt(j - 1)) / (bt(k) - bt(j - 1));
+            sd[i] = std::sqrt((bt(l) - bt(j - 1)) * (bt(k) - bt(l)) / (bt(k) - bt(j - 1)));
+        } else {
+            lw[i] = (bt(k) - bt(l)) / bt(k);
+            rw[i] = bt(l) / bt(k);
+            sd[i] = std::sqrt(bt(l) * (bt(k) - bt(l)) / bt(k));
+        }
+        j = k + 1;
+        if (j >= m) j = 0;
+    }
+    // gap (left date, right date) -> build step; point date of each build step
+    std::map<std::pair<int, int>, int> gap;
+    std::vector<int> point(m);
+    for (int i = 0; i < m; i++) {
+        point[i] = bi[i] + 1;
+        if (i > 0) gap[{li[i], ri[i] + 1}] = i;
+    }
+    auto node_of = [&](int s) {
+        BridgeNode n;
+        n.lw = (float)lw[s];
+        n.rw = (float)rw[s];
+        n.sd = (float)sd[s];
+        n.bstep = s;
+        return n;
+    };
+    std::vector<int> stack; // pending dates
+    out.prog.assign(m, StepProg{0, 0});
+    out.nodes.clear();
+    int depth = 0;
+    for (int i = 1; i <= m; i++) {
+        StepProg sp{(int)out.nodes.size(), 0};
+        if (i == 1) {
+            out.nodes.push_back(node_of(0));
+            sp.count = 1;
+            if (m == 1) {
+                out.prog[0] = sp;
+                continue;
+            }
+            stack.push_back(m);
+        }
+        if (stack.back() == i) {
+            if (sp.count != 0) {
+                err = "bridge program: unexpected pop after push";
+                return false;
+            }
+            stack.pop_back();
+            out.prog[i - 1] = sp;
+            continue;
+        }
+        for (;;) {
+            const int b = stack.back();
+            auto it = gap.find({i - 1, b});
+            if (it == gap.end()) {
+                err = "bridge program: no node for gap";
+                return false;
+            }
+            out.nodes.push_back(node_of(it->second));
+            sp.count++;
+            if (point[it->second] == i) break;
+            stack.push_back(point[it->second]);
+        }
+        depth = std::max(depth, (int)stack.size());
+        out.prog[i - 1] = sp;
+    }
+    out.stack_depth = depth + 1;
+    return true;
+}
+
+// per-step records: first node inline, node count, 1/sqrt(dt), event flag
+std::vector<StepRec> make_recs(const BridgeProgram& bp, const std::vector<float>& isd, const std::vector<char>& ev_flag,
+                               int ref_factors)
+{
+    const size_t N = isd.size();
+    std::vector<StepRec> recs(N);
+    for (size_t i = 0; i < N; i++) {
+        StepRec& r = recs[i];
+        std::memset(&r, 0, sizeof r);
+        r.isd = isd[i];
+        r.ev = ev_flag.empty() ? 0 : ev_flag[i];
+        if (i < bp.prog.size()) {
+            const StepProg& p = bp.prog[i];
+            r.count = p.count;
+            r.first = p.first + 1;
+            if (p.count > 0) {
+                const BridgeNode& n = bp.nodes[p.first];
+                r.lw = n.lw;
+                r.rw = n.rw;
+                r.sd = n.sd;
+                r.dim = n.bstep * ref_factors;
+            }
+        }
+    }
+    return recs;
+}
+
+// ---------------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------------
+struct Plan {
+    DevPlan dp{};
+    Blob blob;
+    // offsets of the sections inside the blob
+    size_t o_steps, o_isd, o_prog, o_nodes, o_recs, o_evr, o_ev, o_lay, o_map, o_levv, o_ginit, o_prod, o_comp;
+    int variant = 1, T = 256;
+    size_t smem = 0;
+    int n_products = 0;
+    int64_t paths = 0;
+    std::vector<int> greek_mask;
+};
+
+bool finite(double x) { return std::isfinite(x); }
+
+int build_plan(const ThothBookDesc* d, Plan& P)
+{
+    if (!d) return fail(THOTH_GPU_E_INVALID, "null descriptor");
+    const int nd = d->n_dates, N = nd - 1, NA = d->n_assets;
+    if (nd < 2 || nd > THOTH_MAX_DATES) return fail(THOTH_GPU_E_INVALID, "n_dates must be in [2, THOTH_MAX_DATES]");
+    if (!d->t) return fail(THOTH_GPU_E_INVALID, "t is null");
+    if (NA < 1 || NA > THOTH_MAX_ASSETS || !d->assets)
+        return fail(NA > THOTH_MAX_ASSETS ? THOTH_GPU_E_TOO_LARGE : THOTH_GPU_E_INVALID, "n_assets out of range");
+    if (d->n_products < 1 || d->n_products > THOTH_MAX_PRODUCTS || !d->products)
+        return fail(d->n_products > THOTH_MAX_PRODUCTS ? THOTH_GPU_E_TOO_LARGE : THOTH_GPU_E_INVALID,
+                    "n_products out of range");
+    if (d->paths <= 1) return fail(THOTH_GPU_E_INVALID, "paths must be > 1");
+    if (d->sobol_skip < 0) return fail(THOTH_GPU_E_INVALID, "sobol_skip must be >= 0");
+    if (d->use_sobol && (uint64_t)d->sobol_skip + (uint64_t)d->paths >= ((uint64_t)1 << 32))
+        return fail(THOTH_GPU_E_TOO_LARGE, "sobol_skip + paths must stay below 2^32 (32-bit direction numbers)");
+    // time lists (monte_carlo_node.cpp:100-124)
+    std::vector<double> tl(nd), dtl(nd, 0.0);
+    for (int i = 0; i < nd; i++) {
+        if (d->days) {
+            tl[i] = (double)(d->days[i] - d->days[0]) / 365.0;
+            if (i > 0) dtl[i] = (double)(d->days[i] - d->days[i - 1]) / 365.0;
+        } else {
+            tl[i] = d->t[i];
+            if (i > 0) dtl[i] = d->t[i] - d->t[i - 1];
+        }
+        if (!finite(tl[i]) || (i > 0 && !(tl[i] > tl[i - 1])))
+            return fail(THOTH_GPU_E_INVALID, "dates must be strictly increasing");
+    }
+    if (tl[0] != 0.0) return fail(THOTH_GPU_E_INVALID, "t[0] must be 0");
+
+    DevPlan& D = P.dp;
+    std::memset(&D, 0, sizeof D);
+    D.n_steps = N;
+    D.n_assets = NA;
+    D.use_sobol = d->use_sobol ? 1 : 0;
+    D.greeks = d->greeks & (THOTH_GREEK_DELTA | THOTH_GREEK_VEGA);
+    D.skip = d->sobol_skip;
+    D.paths = d->paths;
+    D.seed = d->seed;
+    // factors: spots first, then variance noises (pricer_mcl.cpp:414-432)
+    int F = NA, n_stoch = 0, n_lsv = 0;
+    bool mixed = false;
+    for (int a = 0; a < NA; a++) {
+        const ThothAsset& A = d->assets[a];
+        if (A.model < THOTH_MODEL_GBM || A.model > THOTH_MODEL_LSV) return fail(THOTH_GPU_E_INVALID, "bad model");
+        if (!A.carry) return fail(THOTH_GPU_E_INVALID, "asset carry is null");
+        if (!(A.spot > 0) || !finite(A.spot)) return fail(THOTH_GPU_E_INVALID, "spot must be > 0");
+        D.model[a] = A.model;
+        D.s0[a] = (float)A.spot;
+        D.vol[a] = (float)A.vol;
+        D.v0[a] = (float)A.v0;
+        D.fid_spot[a] = a;
+        D.cidx_spot[a] = a;
+        D.fid_var[a] = -1;
+        D.cidx_var[a] = -1;
+        if (A.model != THOTH_MODEL_GBM) {
+            D.fid_var[a] = NA + n_stoch;
+            D.cidx_var[a] = NA + n_stoch;
+            n_stoch++;
+            F++;
+            if (!(A.kappa > 0) || !(A.v0 >= 0) || !(A.theta >= 0) || !(A.xi >= 0) || !(std::fabs(A.rho) <= 1))
+                return fail(THOTH_GPU_E_INVALID, "bad Heston parameters");
+            D.degenerate[a] = (A.xi <= 1e-12) ? 1 : 0;
+        } else if (!(A.vol >= 0) || !finite(A.vol)) {
+            return fail(THOTH_GPU_E_INVALID, "bad GBM vol");
+        }
+        if (A.model == THOTH_MODEL_LSV) {
+            n_lsv++;
+            if (A.lev_points < 2 || !A.lev_ln_step || !A.lev_offset || !A.lev_values)
+                return fail(THOTH_GPU_E_INVALID, "LSV asset needs leverage layers");
+        }
+        if (a > 0 && A.model != d->assets[0].model) mixed = true;
+    }
+    D.ref_factors = F;
+    D.n_factors_active = F;
+    D.sobol_dims = d->use_sobol ? (int)std::min<long>((long)N * F, max_dims()) : 0;
+    D.corr = 0;
+    if (NA > 1 && d->cholesky) {
+        for (int u = 0; u < NA; u++)
+            for (int v = 0; v < NA; v++) {
+                const double l = d->cholesky[u * NA + v];
+                if (!finite(l)) return fail(THOTH_GPU_E_INVALID, "cholesky not finite");
+                D.chol[u * MAX_ASSETS + v] = (float)l;
+            }
+        D.corr = 1;
+    }
+    // variant (tile size fixed by it; uniform-step variants decided below)
+    if (NA == 1 && !mixed) {
+        P.variant = d->assets[0].model; // 0 GBM, 1 Heston, 2 LSV
+    } else {
+        P.variant = 3;
+    }
+    if (D.corr && P.variant != 3) P.variant = 3;
+    P.T = 1 << book_variant_tile_bits(P.variant);
+    const int T = P.T;
+    (void)mixed;
+
+    // bridge program (path-generator times: YearFraction(today, d_i) = tl)
+    BridgeProgram bp;
+    std::string err;
+    if (d->use_sobol) {
+        if (!build_bridge(tl, bp, err)) return fail(THOTH_GPU_E_INVALID, err);
+    } else {
+        bp.prog.assign(N, StepProg{0, 0});
+        bp.stack_depth = 0;
+    }
+    D.stack_depth = bp.stack_depth;
+    std::vector<float> isd(N);
+    for (int i = 1; i <= N; i++) isd[i - 1] = (float)(1.0 / std::sqrt(tl[i] - tl[i - 1]));
+
+    // per-step asset constants
+    std::vector<AssetStep> steps((size_t)N * NA);
+    for (int i = 1; i <= N; i++)
+        for (int a = 0; a < NA; a++) {
+            const ThothAsset& A = d->assets[a];
+            AssetStep& s = steps[(size_t)(i - 1) * NA + a];
+            std::memset(&s, 0, sizeof s);
+            const double dt = dtl[i];
+            const double carry_drift = A.carry[i] * tl[i] - A.carry[i - 1] * tl[i - 1];
+            if (!finite(carry_drift)) return fail(THOTH_GPU_E_INVALID, "carry not finite");
+            if (A.model == THOTH_MODEL_GBM) {
+                const double v = A.vol;
+                s.c[0] = (float)(carry_drift - v * v / 2 * dt);
+                s.c[1] = (float)(v * std::sqrt(dt));
+                s.c[2] = (float)std::sqrt(dt);
+            } else {
+                const double kappa = A.kappa, theta = A.theta, xi = A.xi, rho = A.rho, g = 0.5;
+                const double e = std::exp(-kappa * dt);
+                s.c[0] = (float)e;
+                s.c[1] = (float)(theta * (1 - e));
+                s.c[2] = (float)(xi * xi * e / kappa * (1 - e));
+                s.c[3] = (float)(theta * xi * xi / (2 * kappa) * (1 - e) * (1 - e));
+                s.c[4] = (float)carry_drift;
+                if (xi > 1e-12) {
+                    s.c[5] = (float)(-rho * kappa * theta / xi * dt);
+                    s.c[6] = (float)(g * dt * kappa * rho / xi);
+                    s.c[7] = (float)(g * dt * 0.5);
+                    s.c[8] = (float)(g * dt * (1.0 - rho * rho));
+                    s.c[9] = (float)(rho / xi);
+                }
+                s.c[10] = (float)dt;
+            }
+        }
+
+    // uniform steps: every step's constants equal step 1's (bitwise)
+    bool uniform = true;
+    for (int i = 1; i < N && uniform; i++)
+        for (int a = 0; a < NA && uniform; a++)
+            if (std::memcmp(&steps[(size_t)i * NA + a], &steps[a], sizeof(AssetStep)) != 0) uniform = false;
+    D.uniform_steps = uniform ? 1 : 0;
+    if (uniform && P.variant == 1) P.variant = 4;
+    if (uniform && P.variant == 0) P.variant = 5;
+
+    // leverage layers, deduplicated per asset
+    std::vector<int> lev_layer((size_t)NA * nd, 0);
+    std::vector<std::vector<float2>> maps(NA);
+    std::vector<std::vector<float>> vals(NA);
+    int layers_stride = 1, lev_pts_max = 2;
+    for (int a = 0; a < NA; a++) {
+        const ThothAsset& A = d->assets[a];
+        if (A.model != THOTH_MODEL_LSV) continue;
+        D.lev_points[a] = A.lev_points;
+        lev_pts_max = std::max(lev_pts_max, A.lev_points);
+        std::vector<int> rep; // representative date of each layer
+        for (int i = 0; i < nd; i++) {
+            int found = -1;
+            for (size_t r = 0; r < rep.size() && found < 0; r++) {
+                const int k = rep[r];
+                if (A.lev_ln_step[k] == A.lev_ln_step[i] && A.lev_offset[k] == A.lev_offset[i] &&
+                    std::memcmp(A.lev_values + (size_t)k * A.lev_points, A.lev_values + (size_t)i * A.lev_points,
+                                sizeof(double) * A.lev_points) == 0)
+                    found = (int)r;
+            }
+            if (found < 0) {
+                if (!(A.lev_ln_step[i] > 0)) return fail(THOTH_GPU_E_INVALID, "lev_ln_step must be > 0");
+                found = (int)rep.size();
+                rep.push_back(i);
+                const double inv = 1.0 / A.lev_ln_step[i];
+                maps[a].push_back(make_float2((float)inv, (float)(std::log(A.spot) * inv - (double)A.lev_offset[i])));
+                for (int k = 0; k < A.lev_points; k++) vals[a].push_back((float)A.lev_values[(size_t)i * A.lev_points + k]);
+            }
+            lev_layer[(size_t)a * nd + i] = found;
+        }
+        layers_stride = std::max(layers_stride, (int)rep.size());
+    }
+    std::vector<float2> lev_map((size_t)NA * layers_stride, make_float2(0.f, 0.f));
+    std::vector<float> lev_values((size_t)NA * layers_stride * lev_pts_max, 0.f);
+    for (int a = 0; a < NA; a++) {
+        for (size_t r = 0; r < maps[a].size(); r++) lev_map[(size_t)a * layers_stride + r] = maps[a][r];
+        const int np = std::max(D.lev_points[a], 1);
+        for (size_t r = 0; r < maps[a].size(); r++)
+            for (int k = 0; k < D.lev_points[a]; k++)
+                lev_values[((size_t)a * layers_stride + r) * np + k] = vals[a][r * np + k];
+    }
+    D.lev_layers_stride = layers_stride;
+
+    // products -> slots, groups, events
+    std::map<std::tuple<int, int, int>, int> slot_of; // (type, asset, date)
+    std::map<std::tuple<int, int, double, std::vector<int>>, int> group_of;
+    std::vector<float> grp_init;
+    std::vector<std::vector<Event>> ev((size_t)nd * NA);
+    auto slot = [&](int type, int a, int date) {
+        auto key = std::make_tuple(type, a, date);
+        auto it = slot_of.find(key);
+        if (it != slot_of.end()) return it->second;
+        const int s = (int)slot_of.size();
+        slot_of[key] = s;
+        Event e{type, s, 0.f, 0};
+        ev[(size_t)date * NA + a].push_back(e);
+        return s;
+    };
+    const bool want_delta = (D.greeks & THOTH_GREEK_DELTA) != 0, want_vega = (D.greeks & THOTH_GREEK_VEGA) != 0;
+    std::vector<DevProduct> prods(d->n_products);
+    std::vector<Comp> comps;
+    P.greek_mask.assign(d->n_products, 0);
+    for (int p = 0; p < d->n_products; p++) {
+        const ThothProduct& Q = d->products[p];
+        DevProduct& R = prods[p];
+        std::memset(&R, 0, sizeof R);
+        R.slot_y = R.slot_w = -1;
+        if (Q.maturity < 0 || Q.maturity > N) return fail(THOTH_GPU_E_INVALID, "maturity index out of range");
+        if (Q.option_type != THOTH_CALL && Q.option_type != THOTH_PUT) return fail(THOTH_GPU_E_INVALID, "bad option type");
+        if (!finite(Q.strike) || !finite(Q.zero_rate) || !finite(Q.fx) || !finite(Q.quanto))
+            return fail(THOTH_GPU_E_INVALID, "product parameters not finite");
+        const int mat = Q.maturity;
+        R.kind = Q.kind;
+        R.call = Q.option_type == THOTH_CALL;
+        R.K = (float)Q.strike;
+        R.df = (float)(mat == 0 ? 1.0 : std::exp(tl[0] * Q.zero_rate - tl[mat] * Q.zero_rate));
+        R.fx = (float)Q.fx;
+        R.qfac = (float)std::exp(-Q.quanto * tl[mat]);
+        const bool single = Q.kind != THOTH_PRODUCT_BASKET;
+        if (single && (Q.asset < 0 || Q.asset >= NA)) return fail(THOTH_GPU_E_INVALID, "product asset out of range");
+        const int a = single ? Q.asset : 0;
+        switch (Q.kind) {
+        case THOTH_PRODUCT_VANILLA:
+        case THOTH_PRODUCT_BARRIER: {
+            R.slot_s = slot(EV_SNAP_S, a, mat);
+            R.inv_s0 = (float)(1.0 / d->assets[a].spot);
+            if (Q.kind == THOTH_PRODUCT_VANILLA) {
+                if (want_delta) {
+                    P.greek_mask[p] |= 1;
+                    if (d->assets[a].model == THOTH_MODEL_LSV) R.slot_y = slot(EV_SNAP_Y, a, mat);
+                }
+                if (want_vega && d->assets[a].model == THOTH_MODEL_GBM) {
+                    P.greek_mask[p] |= 2;
+                    R.slot_w = slot(EV_SNAP_W, a, mat);
+                    R.vol_t = (float)(d->assets[a].vol * tl[mat]);
+                }
+            } else {
+                if (Q.n_monitor < 0 || (Q.n_monitor > 0 && !Q.monitor)) return fail(THOTH_GPU_E_INVALID, "bad monitor list");
+                std::vector<int> mon(Q.monitor, Q.monitor + Q.n_monitor);
+                for (size_t k = 0; k < mon.size(); k++)
+                    if (mon[k] < 0 || mon[k] > N || (k > 0 && mon[k] < mon[k - 1]))
+                        return fail(THOTH_GPU_E_INVALID, "monitor indices must be sorted and in range");
+                if (!(Q.barrier_level > 0)) return fail(THOTH_GPU_E_INVALID, "barrier level must be > 0");
+                const int type = Q.barrier_up ? EV_GRP_MAX : EV_GRP_MIN;
+                auto key = std::make_tuple(type, a, Q.quanto, mon);
+                auto it = group_of.find(key);
+                int g;
+                if (it == group_of.end()) {
+                    g = (int)grp_init.size();
+                    group_of[key] = g;
+                    grp_init.push_back(Q.barrier_up ? -INFINITY : INFINITY);
+                    for (int k : mon) ev[(size_t)k * NA + a].push_back(Event{type, g, (float)(Q.quanto * tl[k]), 0});
+                } else {
+                    g = it->second;
+                }
+                R.slot_g = g;
+                R.up = Q.barrier_up ? 1 : 0;
+                R.knock_in = Q.barrier_in ? 1 : 0;
+                R.level = (float)std::log(Q.barrier_level / d->assets[a].spot);
+            }
+            break;
+        }
+        case THOTH_PRODUCT_VARIANCE: {
+            std::vector<int> obs;
+            if (Q.n_obs > 0) {
+                if (!Q.obs) return fail(THOTH_GPU_E_INVALID, "bad observation list");
+                obs.assign(Q.obs, Q.obs + Q.n_obs);
+                for (size_t k = 0; k < obs.size(); k++)
+                    if (obs[k] < 0 || obs[k] > N || (k > 0 && obs[k] <= obs[k - 1]))
+                        return fail(THOTH_GPU_E_INVALID, "observation indices must be increasing and in range");
+            }
+            const int type = obs.empty() ? EV_GRP_SQ_STEP : EV_GRP_SQ_OBS;
+            std::vector<int> key_dates = obs.empty() ? std::vector<int>{mat} : obs;
+            auto key = std::make_tuple(type, a, Q.quanto, key_dates);
+            auto it = group_of.find(key);
+            int g;
+            if (it == group_of.end()) {
+                g = (int)grp_init.size();
+                group_of[key] = g;
+                grp_init.push_back(0.f);
+                if (obs.empty()) {
+                    for (int j = 1; j <= mat; j++)
+                        ev[(size_t)j * NA + a].push_back(Event{type, g, (float)(Q.quanto * (tl[j] - tl[j - 1])), 0});
+                } else {
+                    int prev = 0;
+                    for (int o : obs) {
+                        ev[(size_t)o * NA + a].push_back(Event{type, g, (float)(Q.quanto * (tl[o] - tl[prev])), 0});
+                        prev = o;
+                    }
+                }
+            } else {
+                g = it->second;
+            }
+            R.slot_g = g;
+            const double T = (Q.total_year_fraction > 0) ? Q.total_year_fraction : tl[mat];
+            R.inv_T = (float)(T > 0 ? 1.0 / T : 0.0);
+            R.past = (float)Q.past_variance;
+            R.notional = (float)Q.notional;
+            R.kvar = (float)Q.strike_variance;
+            break;
+        }
+        case THOTH_PRODUCT_BASKET: {
+            if (Q.n_components < 1 || !Q.components || !Q.weights) return fail(THOTH_GPU_E_INVALID, "basket needs components");
+            R.comp_first = (int)comps.size();
+            R.comp_n = Q.n_components;
+            for (int k = 0; k < Q.n_components; k++) {
+                const int c = Q.components[k];
+                if (c < 0 || c >= NA || !finite(Q.weights[k])) return fail(THOTH_GPU_E_INVALID, "bad basket component");
+                Comp cp;
+                cp.slot = slot(EV_SNAP_S, c, mat);
+                cp.w = (float)(Q.weights[k] * std::exp(-Q.quanto * tl[mat]));
+                cp.slot_y = (want_delta && d->assets[c].model == THOTH_MODEL_LSV) ? slot(EV_SNAP_Y, c, mat) : -1;
+                cp.inv_s0 = (float)(1.0 / d->assets[c].spot);
+                comps.push_back(cp);
+            }
+            R.qfac = 1.f;
+            if (want_delta) P.greek_mask[p] |= 1;
+            break;
+        }
+        default:
+            return fail(THOTH_GPU_E_INVALID, "bad product kind");
+        }
+        R.greek_mask = P.greek_mask[p];
+    }
+    if (comps.empty()) comps.push_back(Comp{0, 0.f, -1, 0.f});
+    if (grp_init.empty()) grp_init.push_back(0.f);
+    D.n_slots_used = std::max((int)slot_of.size(), 1);
+    D.n_groups = (int)group_of.size();
+    D.n_products = d->n_products;
+    // events, ordered per (date, asset)
+    std::vector<int2> ev_range((size_t)nd * NA);
+    std::vector<Event> events;
+    std::vector<char> ev_flag(N, 0);
+    for (size_t k = 0; k < ev.size(); k++) {
+        ev_range[k] = make_int2((int)events.size(), (int)ev[k].size());
+        events.insert(events.end(), ev[k].begin(), ev[k].end());
+        const size_t date = k / NA;
+        if (!ev[k].empty() && date >= 1) ev_flag[date - 1] = 1;
+    }
+    if (events.empty()) events.push_back(Event{0, 0, 0.f, 0});
+    const std::vector<StepRec> recs = make_recs(bp, isd, ev_flag, F);
+
+    // tiles over Sobol indices [skip + 1, skip + paths]
+    const int64_t lo = d->sobol_skip + 1, hi = d->sobol_skip + d->paths;
+    D.tile_first = lo / T;
+    D.n_tiles = hi / T - lo / T + 1;
+    P.smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, D.n_factors_active, D.n_slots_used, D.n_groups);
+    if (P.smem > 227 * 1024) return fail(THOTH_GPU_E_TOO_LARGE, "book needs more shared memory than one SM has");
+    D.n_acc = 6 * d->n_products + 2;
+    P.n_products = d->n_products;
+    P.paths = d->paths;
+
+    // pack
+    if (bp.nodes.empty()) bp.nodes.push_back(BridgeNode{0, 0, 0, 0});
+    P.o_steps = P.blob.put(steps);
+    P.o_isd = P.blob.put(isd);
+    P.o_prog = P.blob.put(bp.prog);
+    P.o_nodes = P.blob.put(bp.nodes);
+    P.o_recs = P.blob.put(recs);
+    P.o_evr = P.blob.put(ev_range);
+    P.o_ev = P.blob.put(events);
+    P.o_lay = P.blob.put(lev_layer);
+    P.o_map = P.blob.put(lev_map);
+    P.o_levv = P.blob.put(lev_values);
+    P.o_ginit = P.blob.put(grp_init);
+    P.o_prod = P.blob.put(prods);
+    P.o_comp = P.blob.put(comps);
+    return THOTH_GPU_OK;
+}
+
+void bind(Plan& P, unsigned char* base)
+{
+    DevPlan& D = P.dp;
+    D.steps = reinterpret_cast<const AssetStep*>(base + P.o_steps);
+    D.inv_sqrt_dt = reinterpret_cast<const float*>(base + P.o_isd);
+    D.prog = reinterpret_cast<const StepProg*>(base + P.o_prog);
+    D.nodes = reinterpret_cast<const BridgeNode*>(base + P.o_nodes);
+    D.recs = reinterpret_cast<const StepRec*>(base + P.o_recs);
+    D.ev_range = reinterpret_cast<const int2*>(base + P.o_evr);
+    D.events = reinterpret_cast<const Event*>(base + P.o_ev);
+    D.lev_layer = reinterpret_cast<const int*>(base + P.o_lay);
+    D.lev_map = reinterpret_cast<const float2*>(base + P.o_map);
+    D.lev_values = reinterpret_cast<const float*>(base + P.o_levv);
+    D.grp_init = reinterpret_cast<const float*>(base + P.o_ginit);
+    D.products = reinterpret_cast<const DevProduct*>(base + P.o_prod);
+    D.comps = reinterpret_cast<const Comp*>(base + P.o_comp);
+    D.sobol_v = g_dev.sobol_v;
+    D.sobol_rows = g_dev.sobol_rows;
+    D.sobol_rows32 = g_dev.sobol_rows32;
+    D.cancel = g_dev.cancel_dev;
+}
+
+int grid_for(const Plan& P)
+{
+    // persistent grid: resident CTAs per SM x SMs, capped by the tile count
+    static std::map<std::pair<int, size_t>, int> occ;
+    auto key = std::make_pair(P.variant, P.smem);
+    int per_sm = 1;
+    auto it = occ.find(key);
+    if (it != occ.end()) {
+        per_sm = it->second;
+    } else {
+        per_sm = book_occupancy(P.variant, P.smem);
+        occ[key] = per_sm;
+    }
+    const int64_t g = std::min<int64_t>((int64_t)per_sm * g_dev.sms, P.dp.n_tiles);
+    return (int)std::max<int64_t>(g, 1);
+}
+
+double trust_of(double s1, double s2, double n)
+{
+    double var = (s2 - s1 * s1 / n) / (n - 1);
+    if (var < 0) var = 0; // round-off on a constant payoff
+    return std::sqrt(var / n);
+}
+
+int price_locked(const ThothBookDesc* book, ThothBookResult* out)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
+    int rc = ensure_device();
+    if (rc) return rc;
+    Plan P;
+    rc = build_plan(book, P);
+    if (rc) return rc;
+    const int grid = grid_for(P);
+    const size_t n_acc = (size_t)P.dp.n_acc;
+    // arena: [plan blob][acc rows][out][status]
+    const size_t o_acc = (P.blob.bytes.size() + 255) & ~size_t(255);
+    const size_t o_out = o_acc + ((sizeof(double) * grid * n_acc + 255) & ~size_t(255));
+    const size_t o_st = o_out + ((sizeof(double) * n_acc + 255) & ~size_t(255));
+    rc = ensure_arena(o_st + 256);
+    if (rc) return rc;
+    rc = ensure_pinned(std::max(P.blob.bytes.size(), sizeof(double) * n_acc + sizeof(int)));
+    if (rc) return rc;
+    std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
+    cudaStream_t st = g_dev.stream;
+    CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(g_dev.arena + o_st, 0, sizeof(int), st));
+    bind(P, g_dev.arena);
+    P.dp.acc = reinterpret_cast<double*>(g_dev.arena + o_acc);
+    P.dp.status = reinterpret_cast<int*>(g_dev.arena + o_st);
+    CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+    CUDA_TRY(launch_book(P.dp, P.variant, grid, P.smem, st));
+    CUDA_TRY(launch_reduce(P.dp.acc, grid, (int)n_acc, reinterpret_cast<double*>(g_dev.arena + o_out), st));
+    CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
+    // blob upload has completed before this point in stream order; reuse the staging buffer
+    CUDA_TRY(cudaMemcpyAsync(g_dev.pinned, g_dev.arena + o_out, sizeof(double) * n_acc, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(g_dev.pinned + sizeof(double) * n_acc, g_dev.arena + o_st, sizeof(int),
+                             cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+    int status;
+    std::memcpy(&status, g_dev.pinned + sizeof(double) * n_acc, sizeof(int));
+    if (status == 1) return fail(THOTH_GPU_E_CANCELLED, "pricing cancelled");
+    const double* o = reinterpret_cast<const double*>(g_dev.pinned);
+    const double n = (double)P.paths;
+    const double nan = std::nan("");
+    for (int p = 0; p < P.n_products; p++) {
+        const double* a = o + 6 * (size_t)p;
+        if (out->premium) out->premium[p] = a[0] / n;
+        if (out->trust) out->trust[p] = trust_of(a[0], a[1], n);
+        const bool dok = (P.greek_mask[p] & 1) != 0, vok = (P.greek_mask[p] & 2) != 0;
+        if (out->delta) out->delta[p] = dok ? a[2] / n : nan;
+        if (out->delta_trust) out->delta_trust[p] = dok ? trust_of(a[2], a[3], n) : nan;
+        if (out->vega) out->vega[p] = vok ? a[4] / n : nan;
+        if (out->vega_trust) out->vega_trust[p] = vok ? trust_of(a[4], a[5], n) : nan;
+    }
+    out->book_premium = o[6 * (size_t)P.n_products] / n;
+    out->book_trust = trust_of(o[6 * (size_t)P.n_products], o[6 * (size_t)P.n_products + 1], n);
+    out->device_ms = ms;
+    return THOTH_GPU_OK;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int thoth_gpu_available(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    return ensure_device() == THOTH_GPU_OK ? 1 : 0;
+}
+
+int thoth_gpu_device_info(char* buf, size_t n)
+{
+    if (!buf || n == 0) return fail(THOTH_GPU_E_INVALID, "null buffer");
+    int count = 0;
+    std::string s;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        s = "no CUDA device found";
+    } else {
+        cudaDeviceProp p;
+        if (cudaGetDeviceProperties(&p, 0) != cudaSuccess) {
+            s = "CUDA device query failed";
+        } else {
+            s = std::string(p.name) + " (sm_" + std::to_string(p.major) + std::to_string(p.minor) + ", " +
+                std::to_string(p.multiProcessorCount) + " SMs, " +
+                std::to_string((long long)(p.totalGlobalMem >> 20)) + " MiB)";
+        }
+    }
+    std::snprintf(buf, n, "%s", s.c_str());
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_price_book(const ThothBookDesc* book, ThothBookResult* out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    return price_locked(book, out);
+}
+
+int thoth_gpu_price_european_gbm(double forward, double strike, double t, double vol, double df, int is_call,
+                                 int64_t paths, uint64_t seed, ThothGbmResult* out)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
+    if (paths <= 0) {
+        // reference behaviour for an empty run (mcl_gpu.cu:104-107)
+        out->premium = 0.0;
+        out->trust = 0.0;
+        return THOTH_GPU_OK;
+    }
+    if (!(t > 0) || !(forward > 0) || !(df > 0) || !(vol >= 0))
+        return fail(THOTH_GPU_E_INVALID, "forward, df and t must be > 0 and vol >= 0");
+    const double times[2] = {0.0, t};
+    const double carry[2] = {0.0, 0.0};
+    ThothAsset A;
+    std::memset(&A, 0, sizeof A);
+    A.model = THOTH_MODEL_GBM;
+    A.spot = forward;
+    A.carry = carry;
+    A.vol = vol;
+    ThothProduct Q;
+    std::memset(&Q, 0, sizeof Q);
+    Q.kind = THOTH_PRODUCT_VANILLA;
+    Q.option_type = is_call ? THOTH_CALL : THOTH_PUT;
+    Q.asset = 0;
+    Q.maturity = 1;
+    Q.strike = strike;
+    Q.zero_rate = -std::log(df) / t;
+    Q.fx = 1.0;
+    ThothBookDesc d;
+    std::memset(&d, 0, sizeof d);
+    d.n_dates = 2;
+    d.t = times;
+    d.n_assets = 1;
+    d.assets = &A;
+    d.n_products = 1;
+    d.products = &Q;
+    d.paths = paths < 2 ? 2 : paths;
+    d.use_sobol = (uint64_t)paths < ((uint64_t)1 << 32) ? 1 : 0;
+    d.seed = seed;
+    double prem = 0, tr = 0;
+    ThothBookResult r;
+    std::memset(&r, 0, sizeof r);
+    r.premium = &prem;
+    r.trust = &tr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    const int rc = price_locked(&d, &r);
+    if (rc) return rc;
+    out->premium = prem;
+    out->trust = tr;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_sobol_points(int32_t dims, int64_t skip, int64_t n_points, uint32_t* out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (dims < 1 || dims > max_dims() || skip < 0 || n_points < 0 || !out)
+        return fail(THOTH_GPU_E_INVALID, "bad Sobol request");
+    if ((uint64_t)skip + (uint64_t)n_points >= ((uint64_t)1 << 32)) return fail(THOTH_GPU_E_TOO_LARGE, "index >= 2^32");
+    int rc = ensure_device();
+    if (rc) return rc;
+    const size_t bytes = sizeof(uint32_t) * (size_t)dims * (size_t)n_points;
+    rc = ensure_arena(bytes + 256);
+    if (rc) return rc;
+    uint32_t* d_out = reinterpret_cast<uint32_t*>(g_dev.arena);
+    CUDA_TRY(launch_sobol_points(g_dev.sobol_v, dims, skip, n_points, d_out, g_dev.stream));
+    CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
+    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_normal_quantiles(const uint32_t* x, int64_t n, float* out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (n < 0 || (n > 0 && (!x || !out))) return fail(THOTH_GPU_E_INVALID, "bad quantile request");
+    int rc = ensure_device();
+    if (rc) return rc;
+    const size_t bx = ((sizeof(uint32_t) * (size_t)n + 255) & ~size_t(255));
+    rc = ensure_arena(bx + sizeof(float) * (size_t)n + 256);
+    if (rc) return rc;
+    uint32_t* dx = reinterpret_cast<uint32_t*>(g_dev.arena);
+    float* dy = reinterpret_cast<float*>(g_dev.arena + bx);
+    CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, g_dev.stream));
+    CUDA_TRY(launch_quantile(dx, n, dy, g_dev.stream));
+    CUDA_TRY(cudaMemcpyAsync(out, dy, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, g_dev.stream));
+    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factors, int64_t skip, int64_t n_paths,
+                                float* out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!t || n_dates < 2 || n_dates > THOTH_MAX_DATES || factors < 1 || factors > 2 || skip < 0 || n_paths < 1 || !out)
+        return fail(THOTH_GPU_E_INVALID, "bad bridge request");
+    if ((uint64_t)skip + (uint64_t)n_paths >= ((uint64_t)1 << 32)) return fail(THOTH_GPU_E_TOO_LARGE, "index >= 2^32");
+    int rc = ensure_device();
+    if (rc) return rc;
+    std::vector<double> tl(t, t + n_dates);
+    for (int i = 1; i < n_dates; i++)
+        if (!(tl[i] > tl[i - 1])) return fail(THOTH_GPU_E_INVALID, "t must be strictly increasing");
+    BridgeProgram bp;
+    std::string err;
+    if (!build_bridge(tl, bp, err)) return fail(THOTH_GPU_E_INVALID, err);
+    const int N = n_dates - 1;
+    std::vector<float> isd(N);
+    for (int i = 1; i <= N; i++) isd[i - 1] = (float)(1.0 / std::sqrt(tl[i] - tl[i - 1]));
+    Plan P;
+    DevPlan& D = P.dp;
+    std::memset(&D, 0, sizeof D);
+    D.n_steps = N;
+    D.n_assets = 1;
+    D.ref_factors = factors;
+    D.n_factors_active = factors;
+    D.sobol_dims = (int)std::min<long>((long)N * factors, max_dims());
+    D.use_sobol = 1;
+    D.stack_depth = bp.stack_depth;
+    D.skip = skip;
+    D.paths = n_paths;
+    D.fid_spot[0] = 0;
+    D.cidx_spot[0] = 0;
+    D.fid_var[0] = factors == 2 ? 1 : -1;
+    D.cidx_var[0] = factors == 2 ? 1 : -1;
+    const int T = 256;
+    D.tile_first = (skip + 1) / T;
+    D.n_tiles = (skip + n_paths) / T - (skip + 1) / T + 1;
+    P.o_isd = P.blob.put(isd);
+    P.o_prog = P.blob.put(bp.prog);
+    P.o_nodes = P.blob.put(bp.nodes);
+    P.o_recs = P.blob.put(make_recs(bp, isd, std::vector<char>(), factors));
+    const size_t smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, factors, 0, 0);
+    const size_t o_out = (P.blob.bytes.size() + 255) & ~size_t(255);
+    const size_t bytes = sizeof(float) * (size_t)n_paths * factors * N;
+    rc = ensure_arena(o_out + bytes + 256);
+    if (rc) return rc;
+    rc = ensure_pinned(P.blob.bytes.size());
+    if (rc) return rc;
+    std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
+    CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, g_dev.stream));
+    D.inv_sqrt_dt = reinterpret_cast<const float*>(g_dev.arena + P.o_isd);
+    D.prog = reinterpret_cast<const StepProg*>(g_dev.arena + P.o_prog);
+    D.nodes = reinterpret_cast<const BridgeNode*>(g_dev.arena + P.o_nodes);
+    D.recs = reinterpret_cast<const StepRec*>(g_dev.arena + P.o_recs);
+    D.sobol_v = g_dev.sobol_v;
+    D.sobol_rows = g_dev.sobol_rows;
+    D.sobol_rows32 = g_dev.sobol_rows32;
+    float* d_out = reinterpret_cast<float*>(g_dev.arena + o_out);
+    const int grid = (int)std::min<int64_t>(D.n_tiles, (int64_t)g_dev.sms * 2);
+    CUDA_TRY(launch_bridge(D, grid, smem, d_out, g_dev.stream));
+    CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
+    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBookResult* out)
+{
+    if (!books || !out || n_books < 0) return fail(THOTH_GPU_E_INVALID, "bad batch");
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (int b = 0; b < n_books; b++) {
+        const int rc = price_locked(&books[b], &out[b]);
+        if (rc) return rc;
+    }
+    return THOTH_GPU_OK;
+}
+
+// no lock: called from another thread while a pricing call holds the mutex
+int thoth_gpu_request_cancel(void)
+{
+    if (!g_dev.ready) return fail(THOTH_GPU_E_NODEVICE, "engine not initialised");
+    *(volatile int*)g_dev.cancel_host = 1;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_clear_cancel(void)
+{
+    if (g_dev.ready) *(volatile int*)g_dev.cancel_host = 0;
+    return THOTH_GPU_OK;
+}
+
+const char* thoth_gpu_last_error(void) { return g_err.c_str(); }
+
+int thoth_gpu_bridge_program(const double* t, int32_t n_dates, int32_t* first_count, double* nodes, int32_t* n_nodes,
+                             int32_t* stack_depth)
+{
+    if (!t || n_dates < 2 || n_dates > THOTH_MAX_DATES || !first_count || !nodes || !n_nodes || !stack_depth)
+        return fail(THOTH_GPU_E_INVALID, "bad bridge program request");
+    std::vector<double> tl(t, t + n_dates);
+    for (int i = 1; i < n_dates; i++)
+        if (!(tl[i] > tl[i - 1])) return fail(THOTH_GPU_E_INVALID, "t must be strictly increasing");
+    BridgeProgram bp;
+    std::string err;
+    if (!build_bridge(tl, bp, err)) return fail(THOTH_GPU_E_INVALID, err);
+    for (size_t i = 0; i < bp.prog.size(); i++) {
+        first_count[2 * i] = bp.prog[i].first;
+        first_count[2 * i + 1] = bp.prog[i].count;
+    }
+    for (size_t k = 0; k < bp.nodes.size(); k++) {
+        nodes[4 * k] = bp.nodes[k].lw;
+        nodes[4 * k + 1] = bp.nodes[k].rw;
+        nodes[4 * k + 2] = bp.nodes[k].sd;
+        nodes[4 * k + 3] = bp.nodes[k].bstep;
+    }
+    *n_nodes = (int32_t)bp.nodes.size();
+    *stack_depth = bp.stack_depth;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null output");
+    std::lock_guard<std::mutex> lk(g_mu);
+    Plan P;
+    const int rc = build_plan(book, P);
+    if (rc) return rc;
+    out[0] = P.variant;
+    out[1] = P.T;
+    out[2] = (int64_t)P.smem;
+    out[3] = P.dp.n_slots_used;
+    out[4] = P.dp.n_groups;
+    out[5] = P.dp.stack_depth;
+    out[6] = P.dp.sobol_dims;
+    out[7] = P.dp.n_tiles;
+    return THOTH_GPU_OK;
+}
+
+} // extern "C"
