@@ -1,0 +1,253 @@
+"""Benchmark: Heston vanilla grid on one GB300.
+
+Workload (the engine's headline configuration): one Heston underlying
+(kappa 1.5, theta 0.04, xi 0.6, rho -0.7, v0 0.04, S0 100, r 0.03, q 0), 9 strikes
+80..120 x 7 maturities 1,2,3,4,5,12,24 months x call/put = 126 cells priced on
+shared paths; 2^20 Sobol paths with Brownian bridge (2 dimensions per step),
+252 steps a year (504 steps to 24 months), FP32 path state, FP64 reductions.
+
+metric: path-steps per second (paths x steps / time) of the whole job.
+  value  device time of the pricing kernels with the plan resident in HBM
+         (CUDA events on the engine's stream; L2 flushed before every step)
+  e2e    the reference-facing C-ABI call thoth_gpu_price_book from host
+         descriptors: plan build, host->device copy, kernels, device->host copy
+Run: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Under torchrun each rank prices its own disjoint Sobol block (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PATHS = 1 << 20
+STEPS_PER_YEAR = 252
+FLOPS_PER_PATH_STEP = 96  # algorithmic FP32 flops of a Heston-QE + Andersen path-step (FMA = 2)
+# DRAM bytes per launch of the book kernel from the ncu capture summarised in
+# profiles/book_kernel_heston_grid.md (a 2^18-path capture; the traffic is the
+# plan, the Sobol tables and the per-CTA sums, which do not grow with paths)
+NCU_DRAM_BYTES_PER_LAUNCH = 216832
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="thoth", choices=["thoth", "reference"])
+    ap.add_argument("--cpu-sample-paths", type=int, default=1 << 18)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def workload(rank=0):
+    from thoth_gb300 import workloads as W
+    b = W.heston_grid(paths=PATHS, steps_per_year=STEPS_PER_YEAR)
+    b.sobol_skip = rank * PATHS  # disjoint Sobol block per rank
+    return b
+
+
+def config(world):
+    return {"workload": "heston_vanilla_grid", "paths": PATHS, "steps": 2 * STEPS_PER_YEAR,
+            "steps_per_year": STEPS_PER_YEAR, "cells": 126, "strikes": "80..120 step 5",
+            "maturities_months": [1, 2, 3, 4, 5, 12, 24], "sobol_dims": 1008, "brownian_bridge": True,
+            "parallelism": "dp%d" % world if world > 1 else "single",
+            "l2": "flushed (256 MiB write) before every timed step"}
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(sample_paths, threads):
+    """The oracle (CPU restatement of the reference's node graph) on a bounded sample."""
+    import oracle
+    from thoth_gb300 import workloads as W
+    b = W.heston_grid(paths=sample_paths, steps_per_year=STEPS_PER_YEAR)
+    t0 = time.perf_counter()
+    oracle.price_book(b, "port", threads=threads)
+    dt = time.perf_counter() - t0
+    n_steps = 2 * STEPS_PER_YEAR
+    return {"value": sample_paths * n_steps / dt, "unit": "path-steps/s", "cores": threads, "kind": "port",
+            "sample": "%d paths x %d steps of the same Heston grid (126 cells), %d threads, %.2f s"
+                      % (sample_paths, n_steps, threads, dt)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n_steps = 2 * STEPS_PER_YEAR
+    for _ in range(args.warmup):
+        cpu_baseline(1 << 12, threads)
+    vals = [cpu_baseline(args.cpu_sample_paths, threads) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    line = {"metric": "path-steps/sec", "value": v, "unit": "path-steps/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * PATHS * n_steps / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(1),
+            "cpu_baseline": dict(vals[-1], value=v),
+            "e2e": {"value": v, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's CPU Monte-Carlo restated bit-exactly in oracle/thoth_oracle.c, all host "
+                    "threads, each step a bounded sample of the workload; ms_per_step scaled to 2^20 paths"}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    import thoth_gb300 as G
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n_steps = 2 * STEPS_PER_YEAR
+    book = workload(rank)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    peak_fp32 = G.measure_fp32_peak()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- kernel throughput, plan resident --------------------------------
+    res = G.ResidentBook(book)
+    for _ in range(max(args.warmup, 3)):
+        res.run()
+    dev_ms = []
+    barrier()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1)          # evict L2 (129 MB) before each timed step
+            r = res.run()           # synchronous: kernels timed by CUDA events on the engine stream
+            dev_ms.append(r["device_ms"])
+        barrier()
+        wall = time.perf_counter() - t0
+    res.close()
+    ms = sum(dev_ms) / len(dev_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * PATHS * n_steps / (ms * 1e-3)
+
+    # ---- end to end through the C ABI from host descriptors ---------------
+    for _ in range(2):
+        G.price_book(book)
+    barrier()
+    e2e_ms, h2d, d2h = [], 0, 0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r = G.price_book(book)  # returns after the device->host copy of the results
+        e2e_ms.append(1e3 * (time.perf_counter() - t1))
+        h2d, d2h = r["h2d_bytes"], r["d2h_bytes"]
+    e_ms = sum(e2e_ms) / len(e2e_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e_ms = float(t.item())
+    e2e = world * PATHS * n_steps / (e_ms * 1e-3)
+
+    if rank == 0:
+        achieved = FLOPS_PER_PATH_STEP * PATHS * n_steps / (ms * 1e-3) / 1e12
+        line = {
+            "metric": "path-steps/sec", "value": value, "unit": "path-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(world),
+            "e2e": {"value": e2e, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
+                         "frac": achieved / peak_fp32, "traffic": NCU_DRAM_BYTES_PER_LAUNCH,
+                         "peak_source": "FMA microbenchmark in this run (thoth_gpu_measure_fp32_peak); "
+                                        "MEASURED_PEAKS.json records no FP32 figure",
+                         "flops_per_unit": FLOPS_PER_PATH_STEP, "unit_of_work": "path-step"},
+            "clocks": clk.summary(),
+            "wall_s_timed_region": wall,
+        }
+        line["cpu_baseline"] = cpu_baseline(args.cpu_sample_paths, os.cpu_count() or 1)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

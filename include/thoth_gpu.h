@@ -151,8 +151,15 @@ typedef struct ThothBookResult
     double* delta_trust;
     double* vega;
     double* vega_trust;
-    double device_ms; /* device time of the pricing kernels (CUDA events)         */
+    double device_ms;  /* device time of the pricing kernels (CUDA events on the engine's stream) */
+    int64_t h2d_bytes; /* bytes copied host -> device by this call                           */
+    int64_t d2h_bytes; /* bytes copied device -> host by this call                           */
 } ThothBookResult;
+
+/* A book whose plan is resident on the device: created once, priced many
+ * times (e.g. the reference's bump-and-revalue reprices share one grid and
+ * Sobol block, pricer.cpp:273-392), destroyed by the caller. */
+typedef struct ThothBookHandle ThothBookHandle;
 
 /* Reference gpu::GbmResult (mcl_gpu.hpp:34-38). */
 typedef struct ThothGbmResult
@@ -186,6 +193,20 @@ int thoth_gpu_price_european_gbm(double forward, double strike, double t, double
  * gate's widened model x payoff set, the CPU Tree_Run/Tree_Read
  * (pricer_mcl.cpp:598-709). */
 int thoth_gpu_price_book(const ThothBookDesc* book, ThothBookResult* out);
+
+/* Upload a book's plan and keep it resident. *out receives the handle. */
+int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out);
+
+/* Price a resident book (no host -> device copy of the plan). */
+int thoth_gpu_book_run(ThothBookHandle* handle, ThothBookResult* out);
+
+/* Release a resident book's device memory. */
+int thoth_gpu_book_destroy(ThothBookHandle* handle);
+
+/* Measurement hook, no reference counterpart: FP32 FMA throughput of the
+ * device from a kernel of independent FMA chains; *tflops = 2 flops per FMA
+ * over the kernel's CUDA-event time; *sm_mhz = the implied SM clock. */
+int thoth_gpu_measure_fp32_peak(double* tflops, double* ms);
 
 /* Price n_books independent books (ragged path and step counts) in one
  * persistent launch, replayed from a CUDA graph when the same shapes repeat.

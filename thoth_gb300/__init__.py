@@ -47,6 +47,10 @@ def lib():
                                                C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.thoth_gpu_plan_summary.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(C.c_int64)]
         L.thoth_gpu_last_error.restype = C.c_char_p
+        L.thoth_gpu_book_create.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(C.c_void_p)]
+        L.thoth_gpu_book_run.argtypes = [C.c_void_p, C.POINTER(abi.ThothBookResult)]
+        L.thoth_gpu_book_destroy.argtypes = [C.c_void_p]
+        L.thoth_gpu_measure_fp32_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -81,9 +85,47 @@ def price_book(book, greeks=False):
     d = book.desc()
     r, arrs = book.result(greeks=greeks)
     _check(lib().thoth_gpu_price_book(C.byref(d), C.byref(r)))
-    out = dict(book_premium=r.book_premium, book_trust=r.book_trust, device_ms=r.device_ms)
+    out = dict(book_premium=r.book_premium, book_trust=r.book_trust, device_ms=r.device_ms,
+               h2d_bytes=r.h2d_bytes, d2h_bytes=r.d2h_bytes)
     out.update({k: v.copy() for k, v in arrs.items()})
     return out
+
+
+class ResidentBook:
+    """A book whose plan stays on the device (thoth_gpu_book_create / _run / _destroy)."""
+
+    def __init__(self, book, greeks=False):
+        self.book = book
+        self.greeks = greeks
+        self._d = book.desc()
+        self.h = C.c_void_p()
+        _check(lib().thoth_gpu_book_create(C.byref(self._d), C.byref(self.h)))
+
+    def run(self):
+        r, arrs = self.book.result(greeks=self.greeks)
+        _check(lib().thoth_gpu_book_run(self.h, C.byref(r)))
+        out = dict(book_premium=r.book_premium, book_trust=r.book_trust, device_ms=r.device_ms,
+                   h2d_bytes=r.h2d_bytes, d2h_bytes=r.d2h_bytes)
+        out.update({k: v.copy() for k, v in arrs.items()})
+        return out
+
+    def close(self):
+        if self.h:
+            lib().thoth_gpu_book_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def measure_fp32_peak():
+    """FP32 FMA throughput of the device, TFLOP/s (2 flops per FMA)."""
+    tf, ms = C.c_double(), C.c_double()
+    _check(lib().thoth_gpu_measure_fp32_peak(C.byref(tf), C.byref(ms)))
+    return tf.value
 
 
 def sobol_points(dims, skip, n):

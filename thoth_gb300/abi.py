@@ -1,7 +1,8 @@
 """ctypes mirror of include/thoth_gpu.h and a builder for book descriptors.
 
-The structs below must stay field-for-field identical to the C header; the
-library exports ``thoth_gpu_abi_sizes`` so tests can check the layouts.
+The structs below must stay field-for-field identical to the C header;
+tests/test_host_logic.py compiles a C probe of the header and compares sizes
+and offsets.
 """
 import ctypes as C
 
@@ -100,6 +101,8 @@ class ThothBookResult(C.Structure):
         ("vega", _dp),
         ("vega_trust", _dp),
         ("device_ms", C.c_double),
+        ("h2d_bytes", C.c_int64),
+        ("d2h_bytes", C.c_int64),
     ]
 
 

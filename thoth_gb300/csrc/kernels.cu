@@ -600,6 +600,33 @@ __global__ void __launch_bounds__(1 << TB) bridge_kernel(const DevPlan P, float*
     }
 }
 
+// ---- FP32 peak microbenchmark: 8 independent FMA chains per thread ----------
+__global__ void __launch_bounds__(256) fma_peak_kernel(float* out, int iters, float a, float b)
+{
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            x0 = fmaf(x0, a, b);
+            x1 = fmaf(x1, a, b);
+            x2 = fmaf(x2, a, b);
+            x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b);
+            x5 = fmaf(x5, a, b);
+            x6 = fmaf(x6, a, b);
+            x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 1.2345f) out[blockIdx.x] = s; // keeps the chains alive
+}
+
+cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st)
+{
+    fma_peak_kernel<<<blocks, 256, 0, st>>>(out, iters, 0.999999f, 1e-7f);
+    return cudaGetLastError();
+}
+
 // ---- launch wrappers --------------------------------------------------------
 template <int TB, int NA, int MODEL, bool UNIFORM>
 static cudaError_t launch_book_t(const DevPlan& P, int grid, size_t smem, cudaStream_t st)

@@ -30,6 +30,7 @@ cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64
                                 cudaStream_t st);
 cudaError_t launch_quantile(const uint32_t* x, int64_t n, float* out, cudaStream_t st);
 cudaError_t launch_bridge(const DevPlan& P, int grid, size_t smem, float* out, cudaStream_t st);
+cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st);
 } // namespace thoth
 
 // Joe-Kuo table embedded at build time (generated translation unit)
@@ -783,39 +784,40 @@ double trust_of(double s1, double s2, double n)
     return std::sqrt(var / n);
 }
 
-int price_locked(const ThothBookDesc* book, ThothBookResult* out)
+// device layout of one priced book: [plan blob][acc rows][out][status]
+struct Layout {
+    size_t o_acc, o_out, o_st, total;
+};
+
+Layout layout_of(const Plan& P, int grid)
 {
-    if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
-    int rc = ensure_device();
-    if (rc) return rc;
-    Plan P;
-    rc = build_plan(book, P);
-    if (rc) return rc;
-    const int grid = grid_for(P);
+    Layout L;
     const size_t n_acc = (size_t)P.dp.n_acc;
-    // arena: [plan blob][acc rows][out][status]
-    const size_t o_acc = (P.blob.bytes.size() + 255) & ~size_t(255);
-    const size_t o_out = o_acc + ((sizeof(double) * grid * n_acc + 255) & ~size_t(255));
-    const size_t o_st = o_out + ((sizeof(double) * n_acc + 255) & ~size_t(255));
-    rc = ensure_arena(o_st + 256);
-    if (rc) return rc;
-    rc = ensure_pinned(std::max(P.blob.bytes.size(), sizeof(double) * n_acc + sizeof(int)));
-    if (rc) return rc;
-    std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
+    L.o_acc = (P.blob.bytes.size() + 255) & ~size_t(255);
+    L.o_out = L.o_acc + ((sizeof(double) * grid * n_acc + 255) & ~size_t(255));
+    L.o_st = L.o_out + ((sizeof(double) * n_acc + 255) & ~size_t(255));
+    L.total = L.o_st + 256;
+    return L;
+}
+
+// launch the book kernel and the reduction on a plan already bound to `base`,
+// copy the sums back and finalise the indicators
+int run_bound(Plan& P, unsigned char* base, const Layout& L, int grid, ThothBookResult* out)
+{
+    const size_t n_acc = (size_t)P.dp.n_acc;
     cudaStream_t st = g_dev.stream;
-    CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(g_dev.arena + o_st, 0, sizeof(int), st));
-    bind(P, g_dev.arena);
-    P.dp.acc = reinterpret_cast<double*>(g_dev.arena + o_acc);
-    P.dp.status = reinterpret_cast<int*>(g_dev.arena + o_st);
+    int rc = ensure_pinned(sizeof(double) * n_acc + sizeof(int));
+    if (rc) return rc;
+    P.dp.acc = reinterpret_cast<double*>(base + L.o_acc);
+    P.dp.status = reinterpret_cast<int*>(base + L.o_st);
+    CUDA_TRY(cudaMemsetAsync(base + L.o_st, 0, sizeof(int), st));
     CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
     CUDA_TRY(launch_book(P.dp, P.variant, grid, P.smem, st));
-    CUDA_TRY(launch_reduce(P.dp.acc, grid, (int)n_acc, reinterpret_cast<double*>(g_dev.arena + o_out), st));
+    CUDA_TRY(launch_reduce(P.dp.acc, grid, (int)n_acc, reinterpret_cast<double*>(base + L.o_out), st));
     CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
-    // blob upload has completed before this point in stream order; reuse the staging buffer
-    CUDA_TRY(cudaMemcpyAsync(g_dev.pinned, g_dev.arena + o_out, sizeof(double) * n_acc, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(g_dev.pinned + sizeof(double) * n_acc, g_dev.arena + o_st, sizeof(int),
-                             cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(g_dev.pinned, base + L.o_out, sizeof(double) * n_acc, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(g_dev.pinned + sizeof(double) * n_acc, base + L.o_st, sizeof(int), cudaMemcpyDeviceToHost,
+                             st));
     CUDA_TRY(cudaStreamSynchronize(st));
     float ms = 0;
     CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
@@ -838,15 +840,118 @@ int price_locked(const ThothBookDesc* book, ThothBookResult* out)
     out->book_premium = o[6 * (size_t)P.n_products] / n;
     out->book_trust = trust_of(o[6 * (size_t)P.n_products], o[6 * (size_t)P.n_products + 1], n);
     out->device_ms = ms;
+    out->h2d_bytes = 0;
+    out->d2h_bytes = (int64_t)(sizeof(double) * n_acc + sizeof(int));
+    return THOTH_GPU_OK;
+}
+
+int price_locked(const ThothBookDesc* book, ThothBookResult* out)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
+    int rc = ensure_device();
+    if (rc) return rc;
+    Plan P;
+    rc = build_plan(book, P);
+    if (rc) return rc;
+    const int grid = grid_for(P);
+    const Layout L = layout_of(P, grid);
+    rc = ensure_arena(L.total);
+    if (rc) return rc;
+    rc = ensure_pinned(P.blob.bytes.size());
+    if (rc) return rc;
+    std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
+    CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, g_dev.stream));
+    bind(P, g_dev.arena);
+    rc = run_bound(P, g_dev.arena, L, grid, out);
+    if (rc) return rc;
+    out->h2d_bytes = (int64_t)P.blob.bytes.size();
     return THOTH_GPU_OK;
 }
 
 } // namespace
 
+struct ThothBookHandle {
+    Plan plan;
+    int grid = 1;
+    Layout layout{};
+    unsigned char* dev = nullptr;
+};
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
+
+int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null handle pointer");
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc = ensure_device();
+    if (rc) return rc;
+    ThothBookHandle* h = new ThothBookHandle();
+    rc = build_plan(book, h->plan);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    h->grid = grid_for(h->plan);
+    h->layout = layout_of(h->plan, h->grid);
+    cudaError_t e = cudaMalloc(&h->dev, h->layout.total);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(THOTH_GPU_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    e = cudaMemcpy(h->dev, h->plan.blob.bytes.data(), h->plan.blob.bytes.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(h->dev);
+        delete h;
+        return fail(THOTH_GPU_E_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    }
+    bind(h->plan, h->dev);
+    *out = h;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_book_run(ThothBookHandle* h, ThothBookResult* out)
+{
+    if (!h || !out) return fail(THOTH_GPU_E_INVALID, "null handle or result");
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc = ensure_device();
+    if (rc) return rc;
+    return run_bound(h->plan, h->dev, h->layout, h->grid, out);
+}
+
+int thoth_gpu_book_destroy(ThothBookHandle* h)
+{
+    if (!h) return THOTH_GPU_OK;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (h->dev) cudaFree(h->dev);
+    delete h;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_measure_fp32_peak(double* tflops, double* ms_out)
+{
+    if (!tflops) return fail(THOTH_GPU_E_INVALID, "null output");
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc = ensure_device();
+    if (rc) return rc;
+    rc = ensure_arena(1 << 20);
+    if (rc) return rc;
+    const int blocks = g_dev.sms * 8, iters = 4096;
+    float* d = reinterpret_cast<float*>(g_dev.arena);
+    CUDA_TRY(launch_fma_peak(d, blocks, 64, g_dev.stream)); // warm-up
+    CUDA_TRY(cudaEventRecord(g_dev.ev0, g_dev.stream));
+    CUDA_TRY(launch_fma_peak(d, blocks, iters, g_dev.stream));
+    CUDA_TRY(cudaEventRecord(g_dev.ev1, g_dev.stream));
+    CUDA_TRY(cudaEventSynchronize(g_dev.ev1));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+    const double fmas = (double)blocks * 256 * iters * 16 * 8;
+    *tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
+    if (ms_out) *ms_out = ms;
+    return THOTH_GPU_OK;
+}
 
 int thoth_gpu_available(void)
 {
