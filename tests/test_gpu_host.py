@@ -1,0 +1,25 @@
+"""The C++ drop-in (namespace gpu over the C ABI, thoth_gb300/host) on the GPU:
+the reference's PriceEuropeanGbm call shape, a whole book, and the ERR path."""
+import math
+import os
+import subprocess
+
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+EXE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "thoth_gb300", "_build", "host_check")
+
+
+def test_cpp_dropin(gpu):
+    out = subprocess.run([EXE], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    lines = {ln.split()[0]: ln.split()[1:] for ln in out.stdout.splitlines() if ln}
+    prem, trust = (float(v) for v in lines["gbm"])
+    bs = oracle.bs_price(100 * math.exp(0.02), 100, 1.0, 0.25, math.exp(-0.03))
+    assert abs(prem - bs) < 3 * trust
+    call, put, book, book_trust = (float(v) for v in lines["book"])
+    parity = math.exp(-0.03) * (100 * math.exp(0.02) - 100)                      # df (F - K)
+    assert abs((call - put) - parity) < 3 * book_trust + 1e-3
+    assert "error" in lines and "paths must be > 1" in out.stdout
