@@ -208,6 +208,27 @@ int thoth_gpu_book_destroy(ThothBookHandle* handle);
  * over the kernel's CUDA-event time; *sm_mhz = the implied SM clock. */
 int thoth_gpu_measure_fp32_peak(double* tflops, double* ms);
 
+/* Capacity of the device array behind thoth_gpu_price_book_noalloc. */
+#define THOTH_NOALLOC_SCRATCH_BYTES (2u << 20)
+
+/* Allocation-free variant of thoth_gpu_price_book; no counterpart in the
+ * reference. For callers that must not allocate device memory: a host whose
+ * memory is budgeted and locked before pricing starts, or code running inside a
+ * framework that owns every allocation on the device. It calls no cudaMalloc,
+ * cudaFree, cudaHostAlloc or other allocating routine; the plan, the Sobol
+ * direction numbers and the FP64 partial sums all live in one statically
+ * allocated device array of THOTH_NOALLOC_SCRATCH_BYTES (2 MiB), which every
+ * GPU that loads the library holds until the process exits. Books whose plan
+ * and sums do not fit return THOTH_GPU_E_TOO_LARGE (large books use fewer CTAs
+ * before that). The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. The
+ * call is synchronous on the legacy default stream. Every call reuses the same
+ * array and leaves its contents behind; the library serialises its own calls,
+ * and work that overlaps one of these calls on the same GPU and touches the
+ * array races with it. Same inputs, outputs and results as
+ * thoth_gpu_price_book, except device_ms, which is not measured here (NaN). */
+int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out);
+
 /* Price n_books independent books (ragged path and step counts) in one
  * persistent launch, replayed from a CUDA graph when the same shapes repeat.
  * No reference counterpart beyond repeated PriceBook calls (pricer_mcl.cpp:197-240). */

@@ -870,6 +870,103 @@ int price_locked(const ThothBookDesc* book, ThothBookResult* out)
 
 } // namespace
 
+// ---------------------------------------------------------------------------
+// Allocation-free pricing (thoth_gpu_price_book_noalloc): everything the book
+// kernel reads or writes besides the caller's host buffers lives in this one
+// statically allocated device array. Host code may not use its name as a
+// device address; the address is looked up per device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[THOTH_NOALLOC_SCRATCH_BYTES];
+
+static constexpr int kMaxDevices = 64;
+static unsigned char* g_noalloc_ptr[kMaxDevices] = {};
+
+// once per device, with that device current
+static int noalloc_address(int dev, unsigned char** out)
+{
+    if (dev < 0 || dev >= kMaxDevices) return fail(THOTH_GPU_E_NODEVICE, "device index out of range");
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return fail(THOTH_GPU_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return THOTH_GPU_OK;
+}
+
+static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
+    int dev = 0, count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return fail(THOTH_GPU_E_NODEVICE, "no CUDA device");
+    CUDA_TRY(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(THOTH_GPU_E_NODEVICE, std::string("device ") + prop.name + " is not sm_103 (built for sm_103a only)");
+    unsigned char* base = nullptr;
+    int rc = noalloc_address(dev, &base);
+    if (rc) return rc;
+    Plan P;
+    rc = build_plan(book, P);
+    if (rc) return rc;
+    // direction numbers of the book's Sobol dimensions, from the embedded table
+    std::vector<uint32_t> V, rows, rows32;
+    if (!build_direction_numbers(V, rows, rows32)) return fail(THOTH_GPU_E_INVALID, "embedded Joe-Kuo table is corrupt");
+    const size_t v_bytes = sizeof(uint32_t) * 32 * (size_t)std::max(P.dp.sobol_dims, 1);
+    const size_t n_acc = (size_t)P.dp.n_acc;
+    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t o_v = up(P.blob.bytes.size());
+    const size_t o_out = o_v + up(v_bytes);
+    const size_t o_st = o_out + up(sizeof(double) * n_acc);
+    const size_t o_acc = o_st + 256;
+    const size_t row = sizeof(double) * n_acc;
+    if (o_acc + row > THOTH_NOALLOC_SCRATCH_BYTES)
+        return fail(THOTH_GPU_E_TOO_LARGE, "book needs " + std::to_string(o_acc + row) +
+                                               " bytes of device scratch; the allocation-free entry point holds " +
+                                               std::to_string((size_t)THOTH_NOALLOC_SCRATCH_BYTES));
+    // as many CTA rows of FP64 sums as the array still holds (at most the normal persistent grid)
+    const int64_t fit = (int64_t)((THOTH_NOALLOC_SCRATCH_BYTES - o_acc) / row);
+    const int64_t full = (int64_t)book_occupancy(P.variant, P.smem) * prop.multiProcessorCount;
+    const int grid = (int)std::max<int64_t>(1, std::min(std::min(full, fit), P.dp.n_tiles));
+    CUDA_TRY(cudaMemcpy(base, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(base + o_v, V.data(), v_bytes, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(base + o_st, 0, sizeof(int))); // status must start at zero; the sums are zeroed by the kernel
+    bind(P, base);
+    P.dp.sobol_v = reinterpret_cast<const uint32_t*>(base + o_v);
+    P.dp.sobol_rows = nullptr;
+    P.dp.sobol_rows32 = nullptr;
+    P.dp.cancel = nullptr;
+    P.dp.acc = reinterpret_cast<double*>(base + o_acc);
+    P.dp.status = reinterpret_cast<int*>(base + o_st);
+    CUDA_TRY(launch_book(P.dp, P.variant, grid, P.smem, 0));
+    CUDA_TRY(launch_reduce(P.dp.acc, grid, (int)n_acc, reinterpret_cast<double*>(base + o_out), 0));
+    std::vector<double> o(n_acc);
+    int status = 0;
+    CUDA_TRY(cudaMemcpy(o.data(), base + o_out, sizeof(double) * n_acc, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(&status, base + o_st, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status != 0) return fail(THOTH_GPU_E_CANCELLED, "pricing cancelled");
+    const double n = (double)P.paths;
+    const double nan = std::nan("");
+    for (int p = 0; p < P.n_products; p++) {
+        const double* a = o.data() + 6 * (size_t)p;
+        if (out->premium) out->premium[p] = a[0] / n;
+        if (out->trust) out->trust[p] = trust_of(a[0], a[1], n);
+        const bool dok = (P.greek_mask[p] & 1) != 0, vok = (P.greek_mask[p] & 2) != 0;
+        if (out->delta) out->delta[p] = dok ? a[2] / n : nan;
+        if (out->delta_trust) out->delta_trust[p] = dok ? trust_of(a[2], a[3], n) : nan;
+        if (out->vega) out->vega[p] = vok ? a[4] / n : nan;
+        if (out->vega_trust) out->vega_trust[p] = vok ? trust_of(a[4], a[5], n) : nan;
+    }
+    out->book_premium = o[6 * (size_t)P.n_products] / n;
+    out->book_trust = trust_of(o[6 * (size_t)P.n_products], o[6 * (size_t)P.n_products + 1], n);
+    out->device_ms = nan;
+    out->h2d_bytes = (int64_t)(P.blob.bytes.size() + v_bytes + sizeof(int));
+    out->d2h_bytes = (int64_t)(sizeof(double) * n_acc + sizeof(int));
+    return THOTH_GPU_OK;
+}
+
 struct ThothBookHandle {
     Plan plan;
     int grid = 1;
@@ -881,6 +978,12 @@ struct ThothBookHandle {
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
+
+int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    return price_noalloc_locked(book, out);
+}
 
 int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out)
 {
