@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="thoth", choices=["thoth", "reference"])
     ap.add_argument("--cpu-sample-paths", type=int, default=1 << 18)
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain-MC grid section")
     return ap.parse_args()
 
 
@@ -234,6 +235,21 @@ def run_gpu(args):
             "wall_s_timed_region": wall,
         }
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample_paths, os.cpu_count() or 1)
+        if not args.no_surrogate:
+            from thoth_gb300 import surrogate as S
+            info = S.benchmark()
+            line["grid_cells_per_sec"] = {
+                "target": "90th-percentile cell error <= 1e-3 vs the FP64 Heston closed form "
+                          "(relative, floor 1% of spot); 4096 parameter sets x 252 lattice cells",
+                "surrogate": info["cells_per_sec"], "plain_mc": info["plain_mc_cells_per_sec"],
+                "speedup": info["speedup"], "surrogate_inference_only": info["inference_cells_per_sec"],
+                "plain_mc_paths": info["plain_mc_paths"],
+                "error_surrogate_raw": info["error_surrogate_raw"],
+                "error_surrogate_pipeline": info["error_surrogate_pipeline"],
+                "error_plain_mc": info["error_plain_mc"],
+                "detail": {k: info[k] for k in ("inference_s", "inference_device_ms", "judge_s", "judge_sets",
+                                                "fallback_s", "fallback_cells", "failing_buckets", "label_seconds",
+                                                "train_seconds", "epochs", "final_loss", "train_labels")}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -266,6 +266,34 @@ int thoth_gpu_bridge_program(const double* t, int32_t n_dates, int32_t* first_co
  * [6] Sobol dimensions, [7] tiles. Returns the descriptor's status code. */
 int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out);
 
+/* Test hook, no reference counterpart: one tcgen05 BF16 tensor-core GEMM,
+ * D (128 x N, FP32) = A (128 x K, bf16 bits) * B (N x K, bf16 bits)^T, all
+ * row-major host arrays; N and K multiples of 16, N <= 256, K <= 256. Used to
+ * check the tensor-core building blocks of the surrogate against the CPU. */
+int thoth_gpu_tc_gemm_test(const uint16_t* a, const uint16_t* b, int32_t n, int32_t k, float* d);
+
+/* ---- learned surrogate (no reference counterpart) ------------------------
+ * A 7 -> 4 x 128 SiLU -> 1 MLP of the Heston vanilla price surface, trained
+ * and served by BF16 tcgen05 tensor-core kernels with FP32 accumulation and
+ * FP32 Adam. Inputs are the 7 features already scaled to [-1, 1] (row-major
+ * [n][7]); outputs are the normalised prices the model was trained on. */
+typedef struct ThothSurrogate ThothSurrogate;
+int thoth_gpu_surrogate_create(ThothSurrogate** out, uint64_t seed);
+int thoth_gpu_surrogate_destroy(ThothSurrogate* s);
+int thoth_gpu_surrogate_n_params(void);
+int thoth_gpu_surrogate_get_params(ThothSurrogate* s, float* params);
+int thoth_gpu_surrogate_set_params(ThothSurrogate* s, const float* params);
+/* Weighted MSE sum_i ((yhat_i - y_i) / scale_i)^2 / n, Adam with a cosine
+ * learning-rate decay over all steps; batch a multiple of 128. */
+int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
+                              int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss);
+/* Gradient of that loss over `rows` rows (multiple of 128) at the current
+ * parameters, without updating them; for checks against a CPU oracle. */
+int thoth_gpu_surrogate_gradient(ThothSurrogate* s, const float* x, const float* y, const float* scale, int32_t rows,
+                                 float* grad, double* loss);
+int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, float* y, double* device_ms);
+const char* thoth_gpu_surrogate_last_error(void);
+
 /* Cooperative cancellation (reference: helpers/cancellation.hpp:9-15): a
  * running thoth_gpu_price_* call polls a host-mapped word between launches and
  * returns THOTH_GPU_E_CANCELLED. The flag is cleared by thoth_gpu_clear_cancel. */

@@ -59,6 +59,7 @@ def port():
         for f in ("oracle_heston_price", "oracle_heston_price_p12"):
             getattr(lib, f).argtypes = [C.c_double] * 10 + [C.c_int]
             getattr(lib, f).restype = C.c_double
+        lib.oracle_heston_prices.argtypes = [C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
         rc = lib.oracle_load_direction_numbers(str(JK_TABLE).encode())
         if rc != 0:
             raise RuntimeError("cannot load %s (%d)" % (JK_TABLE, rc))
@@ -154,3 +155,13 @@ def heston_price(S, K, T, r, q, v0, kappa, theta, xi, rho, is_call=True):
 def heston_price_p12(S, K, T, r, q, v0, kappa, theta, xi, rho, is_call=True):
     """The reference's P1/P2 decomposition of the same price (second rule)."""
     return port().oracle_heston_price_p12(S, K, T, r, q, v0, kappa, theta, xi, rho, int(is_call))
+
+
+def heston_prices(S, K, T, r, q, v0, kappa, theta, xi, rho, threads=None):
+    """Vectorised FP64 Heston call prices (all arguments broadcast), on all host threads."""
+    args = np.ascontiguousarray(np.stack(np.broadcast_arrays(*(np.asarray(a, dtype=np.float64) for a in
+                                                              (S, K, T, r, q, v0, kappa, theta, xi, rho))), axis=-1)
+                                .reshape(-1, 10))
+    out = np.zeros(len(args))
+    port().oracle_heston_prices(len(args), _d(args), _d(out), int(threads or os.cpu_count() or 1))
+    return out

@@ -816,9 +816,11 @@ double oracle_heston_price(double S, double K, double T, double r, double q, dou
         LewisP h = {log(F / K), T, v0, kappa, theta, xi, rho};
         double total = lewis_adapt(0.0, 1.0, &h, 1e-16, 18);
         for (double a = 1.0; a < 1e7; a *= 2.0) {
-            const double part = lewis_adapt(a, 2.0 * a, &h, 1e-16, 18);
+            const double part = lewis_adapt(a, 2.0 * a, &h, 1e-16, 14);
             total += part;
-            if (fabs(part) < 1e-17 && a > 64) break;
+            /* the integrand decays monotonically past its oscillations: stop once a
+             * dyadic panel adds less than 1e-16 of the total (or in absolute terms) */
+            if (a > 64 && (fabs(part) < 1e-17 || fabs(part) < 1e-16 * fabs(total))) break;
         }
         call = df * (F - sqrt(F * K) / M_PI * total);
     }
@@ -834,4 +836,39 @@ double oracle_heston_price_p12(double S, double K, double T, double r, double q,
     HestonP h = {F, K, T, v0, kappa, theta, xi, rho, 1};
     const double call = df * (F * heston_prob(h, 1) - K * heston_prob(h, 2));
     return is_call ? call : call - df * (F - K);
+}
+
+/* many Heston prices at once on `threads` host threads; args[i] = (S, K, T, r, q,
+ * v0, kappa, theta, xi, rho), calls. */
+typedef struct {
+    const double* args;
+    double* out;
+    int64_t lo, hi;
+} CfJob;
+
+static void* cf_job(void* p)
+{
+    CfJob* j = (CfJob*)p;
+    for (int64_t i = j->lo; i < j->hi; i++) {
+        const double* a = j->args + 10 * i;
+        j->out[i] = oracle_heston_price(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], 1);
+    }
+    return NULL;
+}
+
+int oracle_heston_prices(int64_t n, const double* args, double* out, int threads)
+{
+    if (threads < 1) threads = 1;
+    pthread_t th[256];
+    CfJob jobs[256];
+    if (threads > 256) threads = 256;
+    for (int k = 0; k < threads; k++) {
+        jobs[k].args = args;
+        jobs[k].out = out;
+        jobs[k].lo = n * k / threads;
+        jobs[k].hi = n * (k + 1) / threads;
+        pthread_create(&th[k], NULL, cf_job, &jobs[k]);
+    }
+    for (int k = 0; k < threads; k++) pthread_join(th[k], NULL);
+    return 0;
 }

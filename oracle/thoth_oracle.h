@@ -60,6 +60,9 @@ double oracle_heston_price(double spot, double strike, double t, double r, doubl
 double oracle_heston_price_p12(double spot, double strike, double t, double r, double q, double v0,
                                double kappa, double theta, double xi, double rho, int is_call);
 
+/* batch of Heston calls, args[i] = (S, K, T, r, q, v0, kappa, theta, xi, rho), on `threads` threads */
+int oracle_heston_prices(int64_t n, const double* args, double* out, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,8 @@ def lib():
         L.thoth_gpu_book_run.argtypes = [C.c_void_p, C.POINTER(abi.ThothBookResult)]
         L.thoth_gpu_book_destroy.argtypes = [C.c_void_p]
         L.thoth_gpu_measure_fp32_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.thoth_gpu_tc_gemm_test.argtypes = [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.c_int32, C.c_int32,
+                                             C.POINTER(C.c_float)]
         _lib = L
     return _lib
 
@@ -126,6 +128,28 @@ def measure_fp32_peak():
     tf, ms = C.c_double(), C.c_double()
     _check(lib().thoth_gpu_measure_fp32_peak(C.byref(tf), C.byref(ms)))
     return tf.value
+
+
+def to_bf16_bits(x):
+    """float32 array -> bf16 bit patterns (round to nearest even)."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return u.astype(np.uint16)
+
+
+def from_bf16_bits(b):
+    return (np.asarray(b, dtype=np.uint32) << 16).view(np.float32)
+
+
+def tc_gemm_test(a, b):
+    """D = A (128 x K) @ B (N x K)^T on the tensor cores (inputs rounded to bf16)."""
+    a16, b16 = to_bf16_bits(a), to_bf16_bits(b)
+    n, k = b16.shape
+    d = np.zeros((128, n), dtype=np.float32)
+    _check(lib().thoth_gpu_tc_gemm_test(a16.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                        b16.ctypes.data_as(C.POINTER(C.c_uint16)), n, k,
+                                        d.ctypes.data_as(C.POINTER(C.c_float))))
+    return d
 
 
 def sobol_points(dims, skip, n):

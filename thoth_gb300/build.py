@@ -18,7 +18,7 @@ BUILD = HERE / "_build"
 CSRC = HERE / "csrc"
 LIB = BUILD / "libthoth_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "thoth_gpu.cu"]
+SOURCES = ["kernels.cu", "thoth_gpu.cu", "surrogate.cu", "surrogate_host.cu"]
 
 
 def nvcc():

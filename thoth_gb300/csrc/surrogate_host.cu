@@ -1,0 +1,412 @@
+// surrogate_host.cu — C ABI of the learned Heston surrogate: a 7 -> 4 x 128
+// SiLU -> 1 MLP trained and served by the tcgen05 kernels of surrogate.cu.
+// No reference counterpart: the reference has no learned pricer.
+#include "thoth_gpu.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <random>
+#include <string>
+#include <vector>
+
+namespace thoth {
+namespace mlp {
+struct TrainArgs {
+    int rows;
+    const __nv_bfloat16* x;
+    const float* y;
+    const float* inv_w2;
+    const float* params;
+    const __nv_bfloat16* wbf;
+    float* z[5];
+    __nv_bfloat16* a[5];
+    __nv_bfloat16* dz[5];
+    float* part;
+    float* loss_part;
+    int* status;
+};
+} // namespace mlp
+cudaError_t mlp_train_step(const mlp::TrainArgs& A, float* params, float* m, float* v, __nv_bfloat16* wbf, float lr,
+                           float b1, float b2, float eps, float bc1, float bc2, float* loss_out, cudaStream_t st);
+cudaError_t mlp_infer(const __nv_bfloat16* x, int n, const float* params, const __nv_bfloat16* wbf, float* y,
+                      int* status, int grid, cudaStream_t st);
+int mlp_n_params();
+int mlp_n_bf();
+} // namespace thoth
+
+using namespace thoth;
+
+namespace {
+thread_local std::string s_err;
+std::mutex s_mu;
+int sfail(int code, const std::string& m)
+{
+    s_err = m;
+    return code;
+}
+#define STRY(expr)                                                                                              \
+    do {                                                                                                        \
+        cudaError_t e_ = (expr);                                                                                \
+        if (e_ != cudaSuccess)                                                                                  \
+            return sfail(e_ == cudaErrorMemoryAllocation ? THOTH_GPU_E_NOMEM : THOTH_GPU_E_CUDA,                \
+                         std::string(#expr) + ": " + cudaGetErrorString(e_));                                    \
+    } while (0)
+
+constexpr int H = 128, KIN = 16, NF = 7;
+constexpr int OFF_W1 = 0, OFF_B1 = H * KIN, OFF_W2 = OFF_B1 + H, LAYER = H * H + H, OFF_W5 = OFF_W2 + 3 * LAYER,
+              OFF_B5 = OFF_W5 + H;
+
+__nv_bfloat16 to_bf(float f)
+{
+    return __float2bfloat16(f);
+}
+} // namespace
+
+struct ThothSurrogate {
+    int np = 0, nbf = 0;
+    float* params = nullptr; // FP32 master
+    float* m = nullptr;
+    float* v = nullptr;
+    __nv_bfloat16* wbf = nullptr;
+    int* status = nullptr;
+    cudaStream_t st = nullptr;
+    int sms = 0;
+    int64_t step = 0;
+    // training buffers (grown on demand)
+    int cap_rows = 0;
+    unsigned char* tb = nullptr;
+    mlp::TrainArgs A{};
+    float* loss = nullptr;
+    // inference buffers
+    int64_t cap_inf = 0;
+    unsigned char* ib = nullptr;
+};
+
+namespace {
+
+void host_params_to_bf(const std::vector<float>& p, std::vector<__nv_bfloat16>& w)
+{
+    w.assign((size_t)H * KIN + 3 * (size_t)H * H, to_bf(0.f));
+    for (int j = 0; j < H * KIN; j++) w[j] = to_bf(p[OFF_W1 + j]);
+    for (int l = 0; l < 3; l++)
+        for (int j = 0; j < H * H; j++) w[(size_t)H * KIN + (size_t)l * H * H + j] = to_bf(p[OFF_W2 + l * LAYER + j]);
+}
+
+int upload_params(ThothSurrogate* s, const std::vector<float>& p)
+{
+    std::vector<__nv_bfloat16> w;
+    host_params_to_bf(p, w);
+    STRY(cudaMemcpyAsync(s->params, p.data(), sizeof(float) * s->np, cudaMemcpyHostToDevice, s->st));
+    STRY(cudaMemcpyAsync(s->wbf, w.data(), sizeof(__nv_bfloat16) * w.size(), cudaMemcpyHostToDevice, s->st));
+    STRY(cudaStreamSynchronize(s->st));
+    return THOTH_GPU_OK;
+}
+
+int ensure_train(ThothSurrogate* s, int rows)
+{
+    if (rows <= s->cap_rows) return THOTH_GPU_OK;
+    if (s->tb) cudaFree(s->tb);
+    s->tb = nullptr;
+    const int tiles = rows / 128;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~size_t(255);
+        return o;
+    };
+    const size_t ox = take((size_t)rows * KIN * 2), oy = take((size_t)rows * 4), ow = take((size_t)rows * 4);
+    size_t oz[5], oa[5], od[5];
+    for (int l = 1; l <= 4; l++) {
+        oz[l] = take((size_t)rows * H * 4);
+        oa[l] = take((size_t)rows * H * 2);
+        od[l] = take((size_t)rows * H * 2);
+    }
+    const size_t op = take((size_t)tiles * s->np * 4), ol = take((size_t)tiles * 4), oloss = take(4);
+    STRY(cudaMalloc(&s->tb, off));
+    s->cap_rows = rows;
+    mlp::TrainArgs& A = s->A;
+    A.x = reinterpret_cast<const __nv_bfloat16*>(s->tb + ox);
+    A.y = reinterpret_cast<const float*>(s->tb + oy);
+    A.inv_w2 = reinterpret_cast<const float*>(s->tb + ow);
+    for (int l = 1; l <= 4; l++) {
+        A.z[l] = reinterpret_cast<float*>(s->tb + oz[l]);
+        A.a[l] = reinterpret_cast<__nv_bfloat16*>(s->tb + oa[l]);
+        A.dz[l] = reinterpret_cast<__nv_bfloat16*>(s->tb + od[l]);
+    }
+    A.z[0] = nullptr;
+    A.a[0] = nullptr;
+    A.dz[0] = nullptr;
+    A.part = reinterpret_cast<float*>(s->tb + op);
+    A.loss_part = reinterpret_cast<float*>(s->tb + ol);
+    s->loss = reinterpret_cast<float*>(s->tb + oloss);
+    A.params = s->params;
+    A.wbf = s->wbf;
+    A.status = s->status;
+    return THOTH_GPU_OK;
+}
+
+// pack rows [i0, i0 + rows) of a (possibly permuted) host dataset into pinned-free host staging
+void pack(const float* x, const float* y, const float* scale, const int64_t* idx, int64_t i0, int rows,
+          std::vector<__nv_bfloat16>& hx, std::vector<float>& hy, std::vector<float>& hw)
+{
+    hx.assign((size_t)rows * KIN, to_bf(0.f));
+    hy.resize(rows);
+    hw.resize(rows);
+    for (int r = 0; r < rows; r++) {
+        const int64_t i = idx ? idx[i0 + r] : i0 + r;
+        for (int f = 0; f < NF; f++) {
+            // each feature enters as a bf16 pair hi + lo (columns f and f + 7, tied weights),
+            // keeping about 16 significant bits of the input
+            const float v = x[i * NF + f];
+            const __nv_bfloat16 hi = to_bf(v);
+            hx[(size_t)r * KIN + f] = hi;
+            hx[(size_t)r * KIN + NF + f] = to_bf(v - __bfloat162float(hi));
+        }
+        hy[r] = y[i];
+        const double sc = scale ? scale[i] : 1.0;
+        hw[r] = (float)(1.0 / (sc * sc));
+    }
+}
+
+int upload_batch(ThothSurrogate* s, const std::vector<__nv_bfloat16>& hx, const std::vector<float>& hy,
+                 const std::vector<float>& hw)
+{
+    mlp::TrainArgs& A = s->A;
+    STRY(cudaMemcpyAsync(const_cast<__nv_bfloat16*>(A.x), hx.data(), hx.size() * 2, cudaMemcpyHostToDevice, s->st));
+    STRY(cudaMemcpyAsync(const_cast<float*>(A.y), hy.data(), hy.size() * 4, cudaMemcpyHostToDevice, s->st));
+    STRY(cudaMemcpyAsync(const_cast<float*>(A.inv_w2), hw.data(), hw.size() * 4, cudaMemcpyHostToDevice, s->st));
+    A.a[0] = const_cast<__nv_bfloat16*>(A.x);
+    return THOTH_GPU_OK;
+}
+
+int check_status(ThothSurrogate* s)
+{
+    int st = 0;
+    STRY(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    STRY(cudaStreamSynchronize(s->st));
+    if (st) return sfail(THOTH_GPU_E_CUDA, "tensor-core MMA did not complete (bounded wait expired)");
+    return THOTH_GPU_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int thoth_gpu_surrogate_create(ThothSurrogate** out, uint64_t seed)
+{
+    if (!out) return sfail(THOTH_GPU_E_INVALID, "null handle pointer");
+    std::lock_guard<std::mutex> lk(s_mu);
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return sfail(THOTH_GPU_E_NODEVICE, "no CUDA device");
+    cudaDeviceProp p;
+    STRY(cudaGetDeviceProperties(&p, 0));
+    if (!(p.major == 10 && p.minor == 3)) return sfail(THOTH_GPU_E_NODEVICE, "not an sm_103 device");
+    ThothSurrogate* s = new ThothSurrogate();
+    s->np = mlp_n_params();
+    s->nbf = mlp_n_bf();
+    s->sms = p.multiProcessorCount;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&s->params, sizeof(float) * s->np * 3);
+    if (e == cudaSuccess) e = cudaMalloc(&s->wbf, sizeof(__nv_bfloat16) * s->nbf);
+    if (e == cudaSuccess) e = cudaMalloc(&s->status, sizeof(int));
+    if (e != cudaSuccess) {
+        delete s;
+        return sfail(THOTH_GPU_E_NOMEM, std::string("surrogate allocation: ") + cudaGetErrorString(e));
+    }
+    s->m = s->params + s->np;
+    s->v = s->params + 2 * s->np;
+    // Xavier-uniform weights, zero biases; W1 only on the 7 real input columns
+    std::mt19937_64 rng(seed);
+    std::vector<float> h(s->np, 0.f);
+    auto fill = [&](int off, int rows, int cols, int fan_in, int used_cols) {
+        const double a = std::sqrt(6.0 / (fan_in + rows));
+        std::uniform_real_distribution<double> U(-a, a);
+        for (int r = 0; r < rows; r++)
+            for (int c = 0; c < cols; c++) h[off + r * cols + c] = c < used_cols ? (float)U(rng) : 0.f;
+    };
+    fill(OFF_W1, H, KIN, NF, NF);
+    for (int r = 0; r < H; r++) // tie the lo-part columns to the hi-part columns
+        for (int f = 0; f < NF; f++) h[OFF_W1 + r * KIN + NF + f] = h[OFF_W1 + r * KIN + f];
+    for (int l = 0; l < 3; l++) fill(OFF_W2 + l * LAYER, H, H, H, H);
+    fill(OFF_W5, 1, H, H, H);
+    int rc = upload_params(s, h);
+    if (rc == THOTH_GPU_OK) {
+        e = cudaMemsetAsync(s->m, 0, sizeof(float) * 2 * s->np, s->st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->status, 0, sizeof(int), s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        if (e != cudaSuccess) rc = sfail(THOTH_GPU_E_CUDA, cudaGetErrorString(e));
+    }
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_surrogate_destroy(ThothSurrogate* s)
+{
+    if (!s) return THOTH_GPU_OK;
+    std::lock_guard<std::mutex> lk(s_mu);
+    cudaFree(s->params);
+    cudaFree(s->wbf);
+    cudaFree(s->status);
+    if (s->tb) cudaFree(s->tb);
+    if (s->ib) cudaFree(s->ib);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_surrogate_n_params(void) { return mlp_n_params(); }
+
+int thoth_gpu_surrogate_get_params(ThothSurrogate* s, float* params)
+{
+    if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s_mu);
+    STRY(cudaMemcpyAsync(params, s->params, sizeof(float) * s->np, cudaMemcpyDeviceToHost, s->st));
+    STRY(cudaStreamSynchronize(s->st));
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_surrogate_set_params(ThothSurrogate* s, const float* params)
+{
+    if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s_mu);
+    std::vector<float> h(params, params + s->np);
+    return upload_params(s, h);
+}
+
+int thoth_gpu_surrogate_gradient(ThothSurrogate* s, const float* x, const float* y, const float* scale, int32_t rows,
+                                 float* grad, double* loss)
+{
+    if (!s || !x || !y || !grad || rows < 128 || rows % 128) return sfail(THOTH_GPU_E_INVALID, "rows must be a multiple of 128");
+    std::lock_guard<std::mutex> lk(s_mu);
+    int rc = ensure_train(s, rows);
+    if (rc) return rc;
+    std::vector<__nv_bfloat16> hx;
+    std::vector<float> hy, hw;
+    pack(x, y, scale, nullptr, 0, rows, hx, hy, hw);
+    rc = upload_batch(s, hx, hy, hw);
+    if (rc) return rc;
+    s->A.rows = rows;
+    // a step with lr = 0 leaves the parameters unchanged but fills the partial gradients
+    std::vector<float> keep_m(2 * (size_t)s->np);
+    STRY(cudaMemcpyAsync(keep_m.data(), s->m, sizeof(float) * 2 * s->np, cudaMemcpyDeviceToHost, s->st));
+    STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+    STRY(mlp_train_step(s->A, s->params, s->m, s->v, s->wbf, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f, s->loss, s->st));
+    rc = check_status(s);
+    if (rc) return rc;
+    const int tiles = rows / 128;
+    std::vector<float> part((size_t)tiles * s->np);
+    STRY(cudaMemcpyAsync(part.data(), s->A.part, sizeof(float) * part.size(), cudaMemcpyDeviceToHost, s->st));
+    float l = 0;
+    STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
+    STRY(cudaMemcpyAsync(s->m, keep_m.data(), sizeof(float) * 2 * s->np, cudaMemcpyHostToDevice, s->st));
+    STRY(cudaStreamSynchronize(s->st));
+    for (int j = 0; j < s->np; j++) {
+        double g = 0;
+        for (int t = 0; t < tiles; t++) g += part[(size_t)t * s->np + j];
+        grad[j] = (float)g;
+    }
+    if (loss) *loss = l / rows;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
+                              int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss)
+{
+    if (!s || !x || !y || n < 128 || epochs < 1 || batch < 128 || batch % 128 || !(lr > 0))
+        return sfail(THOTH_GPU_E_INVALID, "bad training arguments (batch must be a multiple of 128)");
+    std::lock_guard<std::mutex> lk(s_mu);
+    const int B = (int)std::min<int64_t>(batch, n / 128 * 128);
+    int rc = ensure_train(s, B);
+    if (rc) return rc;
+    std::vector<int64_t> idx(n);
+    for (int64_t i = 0; i < n; i++) idx[i] = i;
+    std::mt19937_64 rng(seed);
+    const int64_t steps_per_epoch = n / B, total = steps_per_epoch * epochs;
+    std::vector<__nv_bfloat16> hx;
+    std::vector<float> hy, hw;
+    double last = 0;
+    STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+    int64_t done = 0;
+    for (int e = 0; e < epochs; e++) {
+        std::shuffle(idx.begin(), idx.end(), rng);
+        double acc = 0;
+        for (int64_t b = 0; b < steps_per_epoch; b++, done++) {
+            pack(x, y, scale, idx.data(), b * B, B, hx, hy, hw);
+            rc = upload_batch(s, hx, hy, hw);
+            if (rc) return rc;
+            s->A.rows = B;
+            s->step++;
+            const double lr_t = lr * 0.5 * (1.0 + std::cos(M_PI * (double)done / (double)total)) + 1e-6;
+            const float bc1 = (float)(1.0 - std::pow(0.9, (double)s->step));
+            const float bc2 = (float)(1.0 - std::pow(0.999, (double)s->step));
+            const bool last_batch = (b == steps_per_epoch - 1);
+            STRY(mlp_train_step(s->A, s->params, s->m, s->v, s->wbf, (float)lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2,
+                                last_batch ? s->loss : nullptr, s->st));
+            if (last_batch) {
+                float l = 0;
+                STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
+                STRY(cudaStreamSynchronize(s->st));
+                acc = l / B;
+            }
+        }
+        last = acc;
+    }
+    rc = check_status(s);
+    if (rc) return rc;
+    if (final_loss) *final_loss = last;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, float* y, double* device_ms)
+{
+    if (!s || !x || !y || n < 1 || n > ((int64_t)1 << 30)) return sfail(THOTH_GPU_E_INVALID, "bad predict arguments");
+    std::lock_guard<std::mutex> lk(s_mu);
+    if (n > s->cap_inf) {
+        if (s->ib) cudaFree(s->ib);
+        s->ib = nullptr;
+        const int64_t cap = (n + 127) / 128 * 128;
+        STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 4) + 256));
+        s->cap_inf = cap;
+    }
+    __nv_bfloat16* dx = reinterpret_cast<__nv_bfloat16*>(s->ib);
+    float* dy = reinterpret_cast<float*>(s->ib + (size_t)s->cap_inf * KIN * 2);
+    std::vector<__nv_bfloat16> hx((size_t)n * KIN, to_bf(0.f));
+    for (int64_t i = 0; i < n; i++)
+        for (int f = 0; f < NF; f++) {
+            const float v = x[i * NF + f];
+            const __nv_bfloat16 hi = to_bf(v);
+            hx[(size_t)i * KIN + f] = hi;
+            hx[(size_t)i * KIN + NF + f] = to_bf(v - __bfloat162float(hi));
+        }
+    STRY(cudaMemcpyAsync(dx, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice, s->st));
+    STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+    cudaEvent_t e0, e1;
+    STRY(cudaEventCreate(&e0));
+    STRY(cudaEventCreate(&e1));
+    const int tiles = (int)((n + 127) / 128);
+    const int grid = std::min(tiles, s->sms);
+    STRY(cudaEventRecord(e0, s->st));
+    STRY(mlp_infer(dx, (int)n, s->params, s->wbf, dy, s->status, grid, s->st));
+    STRY(cudaEventRecord(e1, s->st));
+    STRY(cudaMemcpyAsync(y, dy, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+    STRY(cudaStreamSynchronize(s->st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (device_ms) *device_ms = ms;
+    return check_status(s);
+}
+
+const char* thoth_gpu_surrogate_last_error(void) { return s_err.c_str(); }
+
+} // extern "C"

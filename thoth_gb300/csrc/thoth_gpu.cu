@@ -31,6 +31,7 @@ cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64
 cudaError_t launch_quantile(const uint32_t* x, int64_t n, float* out, cudaStream_t st);
 cudaError_t launch_bridge(const DevPlan& P, int grid, size_t smem, float* out, cudaStream_t st);
 cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st);
+cudaError_t launch_tc_gemm_test(const void* A, const void* B, int N, int K, float* D, int* status, cudaStream_t st);
 } // namespace thoth
 
 // Joe-Kuo table embedded at build time (generated translation unit)
@@ -1030,6 +1031,32 @@ int thoth_gpu_book_destroy(ThothBookHandle* h)
     std::lock_guard<std::mutex> lk(g_mu);
     if (h->dev) cudaFree(h->dev);
     delete h;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_tc_gemm_test(const uint16_t* a, const uint16_t* b, int32_t n, int32_t k, float* d)
+{
+    if (!a || !b || !d || n < 16 || n > 256 || n % 16 || k < 16 || k > 256 || k % 16)
+        return fail(THOTH_GPU_E_INVALID, "tc gemm test: N, K must be multiples of 16 in [16, 256]");
+    std::lock_guard<std::mutex> lk(g_mu);
+    int rc = ensure_device();
+    if (rc) return rc;
+    const size_t ba = (size_t)128 * k * 2, bb = (size_t)n * k * 2, bd = (size_t)128 * n * 4;
+    const size_t oa = 0, ob = (ba + 255) & ~size_t(255), od = ob + ((bb + 255) & ~size_t(255)),
+                 os = od + ((bd + 255) & ~size_t(255));
+    rc = ensure_arena(os + 256);
+    if (rc) return rc;
+    unsigned char* base = g_dev.arena;
+    CUDA_TRY(cudaMemcpyAsync(base + oa, a, ba, cudaMemcpyHostToDevice, g_dev.stream));
+    CUDA_TRY(cudaMemcpyAsync(base + ob, b, bb, cudaMemcpyHostToDevice, g_dev.stream));
+    CUDA_TRY(cudaMemsetAsync(base + os, 0, sizeof(int), g_dev.stream));
+    CUDA_TRY(launch_tc_gemm_test(base + oa, base + ob, n, k, reinterpret_cast<float*>(base + od),
+                                 reinterpret_cast<int*>(base + os), g_dev.stream));
+    int status = 0;
+    CUDA_TRY(cudaMemcpyAsync(d, base + od, bd, cudaMemcpyDeviceToHost, g_dev.stream));
+    CUDA_TRY(cudaMemcpyAsync(&status, base + os, sizeof(int), cudaMemcpyDeviceToHost, g_dev.stream));
+    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+    if (status) return fail(THOTH_GPU_E_CUDA, "tensor-core MMA did not complete (bounded wait expired)");
     return THOTH_GPU_OK;
 }
 
