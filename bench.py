@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--impl", default="thoth", choices=["thoth", "reference"])
     ap.add_argument("--cpu-sample-paths", type=int, default=1 << 18)
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain-MC grid section")
+    ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch (256 books) section")
     return ap.parse_args()
 
 
@@ -154,6 +155,50 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ragged_batch_section(G, steps):
+    """256 ragged books (path counts log-uniform in [2^14, 2^22], 12..730 daily steps,
+    40% GBM / 40% Heston / 20% LSV) priced as one CUDA graph: untuned, after the
+    autotuner, and one book at a time for comparison."""
+    import numpy as np
+    from thoth_gb300 import workloads as W
+    books = W.ragged_books()
+    work = float(sum(b.paths * (len(b.days) - 1) for b in books))
+    G.autotune_clear()
+
+    def timed(k):
+        ms, wall = [], []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            r = G.price_batch(books)
+            wall.append(time.perf_counter() - t0)
+            ms.append(r[0]["device_ms"])
+        return float(np.mean(ms)), float(np.mean(wall)), r
+
+    G.price_batch(books)                       # capture
+    untuned_ms, untuned_wall, _ = timed(max(1, steps // 2))
+    t0 = time.perf_counter()
+    tune = G.autotune_batch(books, reps=1)
+    tune_s = time.perf_counter() - t0
+    G.price_batch(books)                       # capture with the tuned configuration
+    tuned_ms, tuned_wall, res = timed(max(2, steps // 2))
+    one_ms = 0.0
+    for b in books:
+        one_ms += G.price_book(b)["device_ms"]
+    G.autotune_clear()
+    return {
+        "workload": "256 ragged books: paths log-uniform [2^14, 2^22], steps uniform [12, 730], "
+                    "40% GBM / 40% Heston / 20% LSV, vanilla / barrier / variance",
+        "path_steps": work, "books": len(books),
+        "path_steps_per_sec": work / (tuned_ms * 1e-3),
+        "device_ms": tuned_ms, "e2e_ms": 1e3 * tuned_wall,
+        "e2e_path_steps_per_sec": work / tuned_wall,
+        "untuned_device_ms": untuned_ms, "one_book_at_a_time_device_ms": one_ms,
+        "autotune": dict(tune, seconds=tune_s),
+        "gpu_launches_per_batch": 2 * len(books),
+        "books_nonfinite": int(sum(not np.all(np.isfinite(r["premium"])) for r in res)),
+    }
+
+
 def run_gpu(args):
     import torch
     import thoth_gb300 as G
@@ -235,6 +280,8 @@ def run_gpu(args):
             "wall_s_timed_region": wall,
         }
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample_paths, os.cpu_count() or 1)
+        if not args.no_batch:
+            line["ragged_batch"] = ragged_batch_section(G, args.steps)
         if not args.no_surrogate:
             from thoth_gb300 import surrogate as S
             info = S.benchmark()

@@ -216,11 +216,12 @@ int thoth_gpu_measure_fp32_peak(double* tflops, double* ms);
  * memory is budgeted and locked before pricing starts, or code running inside a
  * framework that owns every allocation on the device. It calls no cudaMalloc,
  * cudaFree, cudaHostAlloc or other allocating routine; the plan, the Sobol
- * direction numbers and the FP64 partial sums all live in one statically
- * allocated device array of THOTH_NOALLOC_SCRATCH_BYTES (2 MiB), which every
- * GPU that loads the library holds until the process exits. Books whose plan
- * and sums do not fit return THOTH_GPU_E_TOO_LARGE (large books use fewer CTAs
- * before that). The first call on a device looks up the array's device address
+ * tables of the book's dimensions (direction numbers and the per-thread
+ * low-bit table, 1152 bytes per dimension) and the FP64 partial sums all live
+ * in one statically allocated device array of THOTH_NOALLOC_SCRATCH_BYTES
+ * (2 MiB), which every GPU that loads the library holds until the process
+ * exits. Books that do not fit return THOTH_GPU_E_TOO_LARGE (large books use
+ * fewer CTAs before that). The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture. The
  * call is synchronous on the legacy default stream. Every call reuses the same
  * array and leaves its contents behind; the library serialises its own calls,
@@ -229,10 +230,48 @@ int thoth_gpu_measure_fp32_peak(double* tflops, double* ms);
  * thoth_gpu_price_book, except device_ms, which is not measured here (NaN). */
 int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out);
 
-/* Price n_books independent books (ragged path and step counts) in one
- * persistent launch, replayed from a CUDA graph when the same shapes repeat.
+/* Price n_books independent books (ragged path and step counts) in one CUDA
+ * graph launch: all plans in one upload, each book's persistent kernel and
+ * reduction on one of several streams (largest first), all sums back in one
+ * copy. The graph is captured on the first call and replayed while the batch's
+ * shapes repeat. device_ms of every result is the whole batch's device time.
  * No reference counterpart beyond repeated PriceBook calls (pricer_mcl.cpp:197-240). */
 int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBookResult* out);
+
+/* ---- autotuner (no reference counterpart) ----------------------------------
+ * Times candidate launch configurations on the device with CUDA events and
+ * keeps the fastest for later calls in this process:
+ *  - per book shape (kernel variant, resident CTAs per SM, tiles of 2^TB paths):
+ *    the persistent grid, k x SMs for k = 1 .. resident CTAs per SM and the
+ *    "balanced" grid of each (same waves, fewest CTAs);
+ *  - per batch: the stream count (1 .. 32) and the grid policy of the batch
+ *    graph (0 full, 1 balanced, 2 half).
+ * Choices can be saved to and loaded from a small text file, which is tied to
+ * the device name and SM count it was measured on (THOTH_GPU_E_UNSUPPORTED
+ * when loaded on another device). */
+typedef struct ThothTuneResult {
+    int32_t grid;          /* chosen CTAs (book) */
+    int32_t default_grid;  /* untuned grid: resident CTAs per SM x SMs, capped by tiles */
+    int32_t candidates;    /* configurations timed */
+    int32_t streams;       /* chosen stream count (batch) */
+    int32_t policy;        /* chosen grid policy (batch) */
+    int32_t reserved;
+    double best_ms;        /* mean device time of the chosen configuration */
+    double default_ms;     /* the same for the untuned configuration */
+} ThothTuneResult;
+
+int thoth_gpu_autotune_book(const ThothBookDesc* book, int32_t reps, ThothTuneResult* out);
+int thoth_gpu_autotune_batch(const ThothBookDesc* books, int32_t n_books, int32_t reps, ThothTuneResult* out);
+int thoth_gpu_autotune_save(const char* path);
+int thoth_gpu_autotune_load(const char* path);
+/* forget every tuned choice (back to the untuned defaults) */
+int thoth_gpu_autotune_clear(void);
+
+/* Number of streams a batch graph fans out over (default 8). */
+int thoth_gpu_batch_streams(int32_t n);
+
+/* Replays of the cached batch graph since its capture (0 right after a capture). */
+int thoth_gpu_batch_graph_replays(void);
 
 /* Sobol integer coordinates x[d] (before the 2^-32 scaling) of points
  * skip+1 .. skip+n_points of the Joe-Kuo sequence, row-major [point][dim].

@@ -1,0 +1,131 @@
+"""Ragged batches and the autotuner on the GPU.
+
+The batch workload follows the ragged-book mix (40% GBM, 40% Heston, 20% LSV;
+vanilla / barrier / variance payoffs; ragged path and step counts) at reduced
+path counts, so the oracle prices every book in seconds. Every book is checked
+against the oracle on the same Sobol paths (0.5 SE and 1e-4 relative), and the
+batch graph against one-at-a-time pricing (bit-identical at equal grids).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from thoth_gb300 import abi, workloads as W
+from tests.test_gpu_parity import assert_shared_path_parity
+
+pytestmark = pytest.mark.gpu
+
+THREADS = max(1, min(16, os.cpu_count() or 1))
+
+
+def small_batch(n=32, seed=11):
+    return W.ragged_books(n_books=n, seed=seed, min_paths=1 << 9, max_paths=1 << 14, min_steps=12, max_steps=120)
+
+
+@pytest.fixture(autouse=True)
+def untuned(gpu):
+    gpu.autotune_clear()
+    yield
+    gpu.autotune_clear()
+
+
+def test_every_book_of_a_ragged_batch_vs_oracle(gpu):
+    books = small_batch()
+    res = gpu.price_batch(books)
+    assert len(res) == len(books)
+    for i, (b, r) in enumerate(zip(books, res)):
+        ref = oracle.price_book(b, threads=THREADS)
+        assert_shared_path_parity(r, ref["premium"], ref["trust"], "book %d" % i)
+        assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"] + 1e-4 * abs(ref["book_premium"])
+
+
+def test_batch_equals_one_at_a_time(gpu):
+    books = small_batch(n=20, seed=3)
+    res = gpu.price_batch(books)
+    for b, r in zip(books, res):
+        one = gpu.price_book(b)
+        np.testing.assert_array_equal(r["premium"], one["premium"])
+        np.testing.assert_array_equal(r["trust"], one["trust"])
+        assert r["book_premium"] == one["book_premium"]
+
+
+def test_graph_is_replayed_while_shapes_repeat(gpu):
+    books = small_batch(n=12, seed=5)
+    first = gpu.price_batch(books)
+    assert gpu.batch_graph_replays() == 0
+    again = gpu.price_batch(books)
+    assert gpu.batch_graph_replays() == 1
+    for a, b in zip(first, again):
+        np.testing.assert_array_equal(a["premium"], b["premium"])
+    # a changed parameter is a changed kernel argument: the graph is captured again
+    i = next(k for k, b in enumerate(books) if b.products[0]["kind"] == abi.VANILLA)
+    books[i].assets[0]["spot"] = 105.0
+    changed = gpu.price_batch(books)
+    assert gpu.batch_graph_replays() == 0
+    one = gpu.price_book(books[i])
+    np.testing.assert_array_equal(changed[i]["premium"], one["premium"])
+    assert not np.array_equal(changed[i]["premium"], first[i]["premium"])
+
+
+@pytest.mark.parametrize("streams", [1, 3, 16])
+def test_stream_count_does_not_change_results(gpu, streams):
+    books = small_batch(n=10, seed=9)
+    base = gpu.price_batch(books)
+    gpu.set_batch_streams(streams)
+    other = gpu.price_batch(books)
+    for a, b in zip(base, other):
+        np.testing.assert_array_equal(a["premium"], b["premium"])
+
+
+def test_empty_and_invalid_batches(gpu):
+    assert gpu.price_batch([]) == []
+    books = small_batch(n=4, seed=1)
+    books[2].paths = 1                       # invalid: paths must be > 1
+    with pytest.raises(gpu.ThothGpuError) as e:
+        gpu.price_batch(books)
+    assert e.value.code == abi.THOTH_GPU_E_INVALID and "book 2" in str(e.value)
+    books[2].paths = 1000
+    assert len(gpu.price_batch(books)) == 4  # the engine is still usable
+
+
+def test_autotune_book_keeps_parity(gpu):
+    b = W.heston_grid(paths=1 << 16, calendar=True, months=(1, 3, 6), strikes=(90, 100, 110))
+    t = gpu.autotune_book(b, reps=2)
+    assert t["candidates"] >= 2 and 1 <= t["grid"]
+    assert t["best_ms"] <= t["default_ms"] * (1 + 1e-9)
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b, threads=THREADS)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "tuned grid %d" % t["grid"])
+
+
+def test_autotune_batch_save_load(gpu, tmp_path):
+    books = small_batch(n=16, seed=21)
+    t = gpu.autotune_batch(books, reps=1)
+    assert t["streams"] in (1, 2, 4, 8, 16) and t["policy"] in (0, 1, 2) and t["candidates"] >= 3
+    path = tmp_path / "tune.txt"
+    gpu.autotune_save(path)
+    text = path.read_text().splitlines()
+    assert text[0] == "thoth-autotune 1" and text[2] == "batch %d %d" % (t["streams"], t["policy"])
+    tuned = gpu.price_batch(books)
+    gpu.autotune_clear()
+    gpu.autotune_load(path)
+    loaded = gpu.price_batch(books)
+    for a, b in zip(tuned, loaded):
+        np.testing.assert_array_equal(a["premium"], b["premium"])
+    # every book still matches the oracle under the tuned grids
+    for i in (0, 7, 15):
+        ref = oracle.price_book(books[i], threads=THREADS)
+        assert_shared_path_parity(loaded[i], ref["premium"], ref["trust"], "tuned book %d" % i)
+    # a file from another device is refused, a malformed one too
+    other = tmp_path / "other.txt"
+    other.write_text("thoth-autotune 1\ndevice 7 Some Other GPU\nbatch 4 0\n")
+    with pytest.raises(gpu.ThothGpuError) as e:
+        gpu.autotune_load(other)
+    assert e.value.code == abi.THOTH_GPU_E_UNSUPPORTED
+    bad = tmp_path / "bad.txt"
+    bad.write_text("thoth-autotune 1\nbatch -3 9\n")
+    with pytest.raises(gpu.ThothGpuError) as e:
+        gpu.autotune_load(bad)
+    assert e.value.code == abi.THOTH_GPU_E_INVALID

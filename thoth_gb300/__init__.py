@@ -51,6 +51,12 @@ def lib():
         L.thoth_gpu_book_run.argtypes = [C.c_void_p, C.POINTER(abi.ThothBookResult)]
         L.thoth_gpu_book_destroy.argtypes = [C.c_void_p]
         L.thoth_gpu_measure_fp32_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
+        L.thoth_gpu_autotune_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(abi.ThothTuneResult)]
+        L.thoth_gpu_autotune_batch.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.c_int32,
+                                               C.POINTER(abi.ThothTuneResult)]
+        L.thoth_gpu_autotune_save.argtypes = [C.c_char_p]
+        L.thoth_gpu_autotune_load.argtypes = [C.c_char_p]
         L.thoth_gpu_tc_gemm_test.argtypes = [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.c_int32, C.c_int32,
                                              C.POINTER(C.c_float)]
         _lib = L
@@ -91,6 +97,75 @@ def price_book(book, greeks=False):
                h2d_bytes=r.h2d_bytes, d2h_bytes=r.d2h_bytes)
     out.update({k: v.copy() for k, v in arrs.items()})
     return out
+
+
+def price_batch(books):
+    """Price independent books in one CUDA-graph launch; returns one result dict per book."""
+    n = len(books)
+    descs = (abi.ThothBookDesc * max(n, 1))()
+    results = (abi.ThothBookResult * max(n, 1))()
+    keep = []
+    for i, b in enumerate(books):
+        descs[i] = b.desc()
+        r, arrs = b.result()
+        results[i] = r
+        keep.append((b, arrs))
+    _check(lib().thoth_gpu_price_batch(descs, n, results))
+    out = []
+    for i, (b, arrs) in enumerate(keep):
+        r = results[i]
+        d = dict(book_premium=r.book_premium, book_trust=r.book_trust, device_ms=r.device_ms,
+                 h2d_bytes=r.h2d_bytes, d2h_bytes=r.d2h_bytes)
+        d.update({k: v.copy() for k, v in arrs.items()})
+        out.append(d)
+    return out
+
+
+def batch_graph_replays():
+    """Replays of the cached batch graph since its capture."""
+    return lib().thoth_gpu_batch_graph_replays()
+
+
+def set_batch_streams(n):
+    _check(lib().thoth_gpu_batch_streams(int(n)))
+
+
+def _tune_dict(r):
+    return dict(grid=r.grid, default_grid=r.default_grid, candidates=r.candidates, streams=r.streams,
+                policy=r.policy, best_ms=r.best_ms, default_ms=r.default_ms)
+
+
+def autotune_book(book, reps=3):
+    """Time the candidate persistent grids for this book's shape; later calls use the fastest."""
+    d = book.desc()
+    r = abi.ThothTuneResult()
+    _check(lib().thoth_gpu_autotune_book(C.byref(d), int(reps), C.byref(r)))
+    return _tune_dict(r)
+
+
+def autotune_batch(books, reps=1):
+    """Time stream counts and grid policies of the batch graph; later batches use the fastest."""
+    n = len(books)
+    descs = (abi.ThothBookDesc * max(n, 1))()
+    keep = []
+    for i, b in enumerate(books):
+        descs[i] = b.desc()
+        keep.append(b)
+    r = abi.ThothTuneResult()
+    _check(lib().thoth_gpu_autotune_batch(descs, n, int(reps), C.byref(r)))
+    return _tune_dict(r)
+
+
+def autotune_save(path):
+    _check(lib().thoth_gpu_autotune_save(str(path).encode()))
+
+
+def autotune_load(path):
+    _check(lib().thoth_gpu_autotune_load(str(path).encode()))
+
+
+def autotune_clear():
+    _check(lib().thoth_gpu_autotune_clear())
 
 
 class ResidentBook:

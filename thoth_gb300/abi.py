@@ -110,6 +110,12 @@ class ThothGbmResult(C.Structure):
     _fields_ = [("premium", C.c_double), ("trust", C.c_double)]
 
 
+class ThothTuneResult(C.Structure):
+    _fields_ = [("grid", C.c_int32), ("default_grid", C.c_int32), ("candidates", C.c_int32),
+                ("streams", C.c_int32), ("policy", C.c_int32), ("reserved", C.c_int32),
+                ("best_ms", C.c_double), ("default_ms", C.c_double)]
+
+
 def _ptr(arr, ctype):
     return arr.ctypes.data_as(C.POINTER(ctype))
 

@@ -27,6 +27,7 @@ namespace thoth {
 
 constexpr int MAX_ASSETS = 8;
 constexpr int SOBOL_BITS = 32;
+constexpr int SOBOL_LO_ROW = 256; // threads covered by the low-bit table (tiles of up to 2^8 paths)
 
 enum : int { M_GBM = 0, M_HESTON = 1, M_LSV = 2, M_MIXED = 3 };
 
@@ -143,8 +144,7 @@ struct DevPlan {
     const DevProduct* products;
     const Comp* comps;
     const uint32_t* sobol_v;     // [4097][32] direction numbers
-    const uint32_t* sobol_rows;  // [4097][32] low-bit tables (two 16-entry halves)
-    const uint32_t* sobol_rows32;// [4097][32] low-5-bit tables: XOR of V[d][0..4] by lane bits
+    const uint32_t* sobol_lo;    // [dims][SOBOL_LO_ROW] XOR of V[d][j] over the bits of gray(t), t < 256
     double* acc;                 // [gridDim][n_acc] per-CTA FP64 sums
     int n_acc;
     volatile int* cancel;        // host-mapped cancel word (may be null)
@@ -242,26 +242,27 @@ __device__ __forceinline__ float phi_neg(float z)
 // Andersen QE variance step in FP32 (heston_variance_node.cpp:17-57).
 // c = {e, theta (1 - e), A, B}: m = theta + (v - theta) e, s2 = A v + B.
 // psi = s2 / m^2 <= 1.5 is tested as s2 <= 1.5 m^2; the exponential branch
-// uses 1 - u = Phi(-z) and 1 - p = 2 m^2 / (s2 + m^2).
+// uses 1 - u = Phi(-z) and 1 - p = 2 m^2 / (s2 + m^2). Both branches are
+// evaluated and one is selected: the paths of a warp nearly always take both,
+// so this costs no more issue slots than divergence and schedules as one block.
+// The guards on the quadratic branch only act when it is not selected.
 __device__ __forceinline__ float qe_step(float v, float z, float e, float th1e, float A, float B)
 {
     const float m = fmaf(v, e, th1e);
     const float s2 = fmaf(v, A, B);
     const float m2 = m * m;
-    float vn;
-    if (s2 <= 1.5f * m2) {
-        const float c = __fdividef(2.0f * m2, s2);
-        const float b2 = c - 1.0f + fast_sqrt(c * (c - 1.0f));
-        const float a = __fdividef(m, 1.0f + b2);
-        const float bz = fast_sqrt(b2) + z;
-        vn = a * bz * bz;
-    } else {
-        const float num = s2 + m2;
-        const float one_m_p = __fdividef(2.0f * m2, num);
-        const float uc = phi_neg(z);
-        vn = (uc >= one_m_p) ? 0.0f : __fdividef(num, 2.0f * m) * __logf(__fdividef(one_m_p, uc));
-    }
-    return vn;
+    // quadratic branch
+    const float c = __fdividef(2.0f * m2, s2);
+    const float b2 = c - 1.0f + fast_sqrt(fmaxf(c * (c - 1.0f), 0.0f));
+    const float a = __fdividef(m, 1.0f + b2);
+    const float bz = fast_sqrt(fmaxf(b2, 0.0f)) + z;
+    const float vq = a * bz * bz;
+    // exponential branch
+    const float num = s2 + m2;
+    const float one_m_p = __fdividef(2.0f * m2, num);
+    const float uc = phi_neg(z);
+    const float ve = (uc >= one_m_p) ? 0.0f : __fdividef(num, 2.0f * m) * __logf(__fdividef(one_m_p, uc));
+    return (s2 <= 1.5f * m2) ? vq : ve;
 }
 
 } // namespace thoth

@@ -59,12 +59,12 @@ __device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
 
 // ---------------------------------------------------------------------------
 // Sobol for the current tile. Path n = m * T + t (T = 2^TB). gray(n) splits
-// into bits >= TB, shared by the whole tile (XOR of V[d][TB..] over them is
-// computed once per tile and dimension into smem), and the thread's low TB
-// bits lo = gray(t) ^ ((m & 1) << (TB - 1)), combined from V[d][0..TB-1] with
-// per-thread bit masks: x = H_d ^ XOR_j (V[d][j] & mask_j). V[d][0..7] are read
-// as two 16-byte loads with a warp-uniform address (L1 broadcast), so no
-// per-thread table gather touches memory.
+// into bits >= TB, shared by the whole tile, and the thread's low TB bits
+// gray(t) ^ ((m & 1) << (TB - 1)). The XOR of V[d][j] over the bits of gray(t)
+// depends on the thread only, so it is a fixed table lo[d][t] (t < 256, built
+// once on the host); the tile part (bits >= TB and the parity flip) is
+// computed once per tile and dimension into smem. One point coordinate is then
+// x = hs[d] ^ lo[d][t]: a shared-memory broadcast and one coalesced load.
 // ---------------------------------------------------------------------------
 template <int TB>
 __device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m)
@@ -72,29 +72,26 @@ __device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m)
     constexpr int T = 1 << TB;
     const uint64_t g = (uint64_t)m ^ ((uint64_t)m >> 1);
     for (int d = threadIdx.x; d < P.sobol_dims; d += T) {
-        const uint32_t* V = P.sobol_v + d * SOBOL_BITS + TB;
-        uint32_t acc = 0;
+        const uint32_t* V = P.sobol_v + d * SOBOL_BITS;
+        uint32_t acc = (m & 1) ? __ldg(V + TB - 1) : 0u;
         uint64_t gg = g;
         for (int k = 0; gg != 0 && k < SOBOL_BITS - TB; ++k, gg >>= 1)
-            if (gg & 1u) acc ^= __ldg(V + k);
+            if (gg & 1u) acc ^= __ldg(V + TB + k);
         hs[d] = acc;
     }
 }
 
 struct SobolLane {
-    const uint32_t* hs;
-    uint32_t mask[8]; // all-ones where bit j of the thread's low Gray bits is set
+    const uint32_t* hs; // tile part, smem
+    const uint32_t* lo; // this thread's column of the low-bit table
 };
 
 template <int TB>
-__device__ __forceinline__ SobolLane sobol_lane(const DevPlan& P, uint32_t* hs, int64_t m)
+__device__ __forceinline__ SobolLane sobol_lane(const DevPlan& P, uint32_t* hs, int64_t)
 {
     SobolLane L;
-    const uint32_t t = threadIdx.x;
-    const uint32_t lo = (t ^ (t >> 1) ^ ((uint32_t)(m & 1) << (TB - 1))) & ((1u << TB) - 1);
     L.hs = hs;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) L.mask[j] = (j < TB && ((lo >> j) & 1u)) ? 0xFFFFFFFFu : 0u;
+    L.lo = P.sobol_lo + threadIdx.x;
     return L;
 }
 
@@ -102,15 +99,10 @@ __device__ __forceinline__ SobolLane sobol_lane(const DevPlan& P, uint32_t* hs, 
 __device__ __forceinline__ float gauss(const DevPlan& P, const SobolLane& L, uint64_t n, int dim)
 {
     uint32_t x;
-    if (dim < P.sobol_dims) {
-        const uint4* v = reinterpret_cast<const uint4*>(P.sobol_v + dim * SOBOL_BITS);
-        const uint4 a = __ldg(v), b = __ldg(v + 1);
-        x = L.hs[dim];
-        x ^= (a.x & L.mask[0]) ^ (a.y & L.mask[1]) ^ (a.z & L.mask[2]) ^ (a.w & L.mask[3]);
-        x ^= (b.x & L.mask[4]) ^ (b.y & L.mask[5]) ^ (b.z & L.mask[6]) ^ (b.w & L.mask[7]);
-    } else {
+    if (dim < P.sobol_dims)
+        x = L.hs[dim] ^ __ldg(L.lo + dim * SOBOL_LO_ROW);
+    else
         x = hash_u32(P.seed, n, (uint32_t)dim);
-    }
     return quantile_u32(x);
 }
 
@@ -629,12 +621,30 @@ cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st)
 
 // ---- launch wrappers --------------------------------------------------------
 template <int TB, int NA, int MODEL, bool UNIFORM>
+static cudaError_t smem_attr_t()
+{
+    // once per variant: allow the device's opt-in maximum, so that launches of
+    // any size (and graph nodes captured earlier) stay valid whatever runs next
+    static bool done = false;
+    if (done) return cudaSuccess;
+    int dev = 0, mx = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, book_kernel<TB, NA, MODEL, UNIFORM>);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(book_kernel<TB, NA, MODEL, UNIFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 mx - (int)fa.sharedSizeBytes);
+    done = e == cudaSuccess;
+    return e;
+}
+
+template <int TB, int NA, int MODEL, bool UNIFORM>
 static cudaError_t launch_book_t(const DevPlan& P, int grid, size_t smem, cudaStream_t st)
 {
-    auto k = book_kernel<TB, NA, MODEL, UNIFORM>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = smem_attr_t<TB, NA, MODEL, UNIFORM>();
     if (e != cudaSuccess) return e;
-    k<<<grid, 1 << TB, smem, st>>>(P);
+    book_kernel<TB, NA, MODEL, UNIFORM><<<grid, 1 << TB, smem, st>>>(P);
     return cudaGetLastError();
 }
 
@@ -659,7 +669,7 @@ template <int TB, int NA, int MODEL, bool UNIFORM>
 static int occ_t(size_t smem)
 {
     auto k = book_kernel<TB, NA, MODEL, UNIFORM>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
+    if (smem_attr_t<TB, NA, MODEL, UNIFORM>() != cudaSuccess) return 1;
     int n = 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 1 << TB, smem) != cudaSuccess) return 1;
     return n < 1 ? 1 : n;

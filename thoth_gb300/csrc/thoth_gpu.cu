@@ -66,11 +66,11 @@ struct Device {
     bool ready = false;
     int id = 0;
     int sms = 0;
+    std::string name;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t* sobol_v = nullptr;    // [4097][32]
-    uint32_t* sobol_rows = nullptr; // [4097][32]
-    uint32_t* sobol_rows32 = nullptr; // [4097][32]
+    uint32_t* sobol_lo = nullptr;   // [4097][256]
     unsigned char* arena = nullptr;
     size_t arena_size = 0;
     unsigned char* pinned = nullptr; // host staging (plan upload + result download)
@@ -83,7 +83,7 @@ Device g_dev;
 int max_dims() { return 4097; }
 
 // direction numbers V[d][32] from the embedded Joe-Kuo table (sobol_generator.cpp:22-76)
-bool build_direction_numbers(std::vector<uint32_t>& V, std::vector<uint32_t>& rows, std::vector<uint32_t>& rows32)
+bool build_direction_numbers(std::vector<uint32_t>& V)
 {
     const unsigned char* b = thoth_jk_blob;
     if (thoth_jk_blob_size < 16 || std::memcmp(b, "JK621201", 8) != 0) return false;
@@ -111,29 +111,22 @@ bool build_direction_numbers(std::vector<uint32_t>& V, std::vector<uint32_t>& ro
             }
         }
     }
-    // low-bit tables: rows[d][k] = XOR_{j<4, bit j of k} V[d][j]; rows[d][16+k] likewise over V[d][4..7]
-    rows.assign((size_t)D * 32, 0);
-    for (int d = 0; d < D; d++)
-        for (int k = 0; k < 16; k++) {
-            uint32_t lo = 0, hi = 0;
-            for (int j = 0; j < 4; j++)
-                if ((k >> j) & 1) {
-                    lo ^= V[(size_t)d * 32 + j];
-                    hi ^= V[(size_t)d * 32 + 4 + j];
-                }
-            rows[(size_t)d * 32 + k] = lo;
-            rows[(size_t)d * 32 + 16 + k] = hi;
-        }
-    // 5-bit tables: rows32[d][k] = XOR_{j<5, bit j of k} V[d][j]
-    rows32.assign((size_t)D * 32, 0);
-    for (int d = 0; d < D; d++)
-        for (int k = 0; k < 32; k++) {
-            uint32_t x = 0;
-            for (int j = 0; j < 5; j++)
-                if ((k >> j) & 1) x ^= V[(size_t)d * 32 + j];
-            rows32[(size_t)d * 32 + k] = x;
-        }
     return true;
+}
+
+// low-bit table of dimensions [0, dims): lo[d][t] = XOR of V[d][j] over the set
+// bits j of gray(t) = t ^ (t >> 1), t < 256 (the thread part of a tile's points)
+void build_low_table(const std::vector<uint32_t>& V, int dims, std::vector<uint32_t>& lo)
+{
+    lo.assign((size_t)dims * SOBOL_LO_ROW, 0);
+    for (int d = 0; d < dims; d++)
+        for (int t = 0; t < SOBOL_LO_ROW; t++) {
+            const uint32_t g = (uint32_t)(t ^ (t >> 1));
+            uint32_t x = 0;
+            for (int j = 0; j < 8; j++)
+                if ((g >> j) & 1u) x ^= V[(size_t)d * 32 + j];
+            lo[(size_t)d * SOBOL_LO_ROW + t] = x;
+        }
 }
 
 int ensure_device()
@@ -151,17 +144,17 @@ int ensure_device()
     g_dev.id = 0;
     CUDA_TRY(cudaSetDevice(0));
     g_dev.sms = p.multiProcessorCount;
+    g_dev.name = p.name;
     CUDA_TRY(cudaStreamCreateWithFlags(&g_dev.stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreate(&g_dev.ev0));
     CUDA_TRY(cudaEventCreate(&g_dev.ev1));
-    std::vector<uint32_t> V, rows, rows32;
-    if (!build_direction_numbers(V, rows, rows32)) return fail(THOTH_GPU_E_INVALID, "embedded Joe-Kuo table is corrupt");
+    std::vector<uint32_t> V, lo;
+    if (!build_direction_numbers(V)) return fail(THOTH_GPU_E_INVALID, "embedded Joe-Kuo table is corrupt");
+    build_low_table(V, max_dims(), lo);
     CUDA_TRY(cudaMalloc(&g_dev.sobol_v, V.size() * 4));
-    CUDA_TRY(cudaMalloc(&g_dev.sobol_rows, rows.size() * 4));
-    CUDA_TRY(cudaMalloc(&g_dev.sobol_rows32, rows32.size() * 4));
+    CUDA_TRY(cudaMalloc(&g_dev.sobol_lo, lo.size() * 4));
     CUDA_TRY(cudaMemcpy(g_dev.sobol_v, V.data(), V.size() * 4, cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(g_dev.sobol_rows, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(g_dev.sobol_rows32, rows32.data(), rows32.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(g_dev.sobol_lo, lo.data(), lo.size() * 4, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaHostAlloc(&g_dev.cancel_host, sizeof(int), cudaHostAllocMapped));
     *g_dev.cancel_host = 0;
     CUDA_TRY(cudaHostGetDevicePointer(&g_dev.cancel_dev, g_dev.cancel_host, 0));
@@ -756,26 +749,51 @@ void bind(Plan& P, unsigned char* base)
     D.products = reinterpret_cast<const DevProduct*>(base + P.o_prod);
     D.comps = reinterpret_cast<const Comp*>(base + P.o_comp);
     D.sobol_v = g_dev.sobol_v;
-    D.sobol_rows = g_dev.sobol_rows;
-    D.sobol_rows32 = g_dev.sobol_rows32;
+    D.sobol_lo = g_dev.sobol_lo;
     D.cancel = g_dev.cancel_dev;
 }
 
-int grid_for(const Plan& P)
+// resident CTAs per SM of a plan's kernel variant (cached per variant and shared-memory size)
+int occupancy_of(const Plan& P)
 {
-    // persistent grid: resident CTAs per SM x SMs, capped by the tile count
     static std::map<std::pair<int, size_t>, int> occ;
     auto key = std::make_pair(P.variant, P.smem);
-    int per_sm = 1;
     auto it = occ.find(key);
-    if (it != occ.end()) {
-        per_sm = it->second;
-    } else {
-        per_sm = book_occupancy(P.variant, P.smem);
-        occ[key] = per_sm;
+    if (it != occ.end()) return it->second;
+    const int per_sm = book_occupancy(P.variant, P.smem);
+    occ[key] = per_sm;
+    return per_sm;
+}
+
+// grid policies of the persistent book kernel:
+//   0 full      resident CTAs per SM x SMs, capped by the tile count
+//   1 balanced  the same number of waves as `full` spread over the fewest CTAs
+//   2 half      half the resident CTAs (leaves room for concurrent books)
+int grid_policy(int64_t tiles, int64_t full, int policy)
+{
+    full = std::max<int64_t>(full, 1);
+    int64_t g = std::min(full, tiles);
+    if (policy == 1) {
+        const int64_t waves = (tiles + full - 1) / full;
+        g = (tiles + waves - 1) / waves;
+    } else if (policy == 2) {
+        g = std::min(std::max<int64_t>(full / 2, 1), tiles);
     }
-    const int64_t g = std::min<int64_t>((int64_t)per_sm * g_dev.sms, P.dp.n_tiles);
     return (int)std::max<int64_t>(g, 1);
+}
+
+// autotuned grids, keyed by (variant, resident CTAs per SM, tiles)
+using TuneKey = std::tuple<int, int, int64_t>;
+std::map<TuneKey, int> g_tuned;
+
+int grid_for(const Plan& P, int policy = 0)
+{
+    const int per_sm = occupancy_of(P);
+    if (policy == 0) {
+        auto it = g_tuned.find(TuneKey(P.variant, per_sm, P.dp.n_tiles));
+        if (it != g_tuned.end()) return (int)std::min<int64_t>(it->second, std::max<int64_t>(P.dp.n_tiles, 1));
+    }
+    return grid_policy(P.dp.n_tiles, (int64_t)per_sm * g_dev.sms, policy);
 }
 
 double trust_of(double s1, double s2, double n)
@@ -913,13 +931,16 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     rc = build_plan(book, P);
     if (rc) return rc;
     // direction numbers of the book's Sobol dimensions, from the embedded table
-    std::vector<uint32_t> V, rows, rows32;
-    if (!build_direction_numbers(V, rows, rows32)) return fail(THOTH_GPU_E_INVALID, "embedded Joe-Kuo table is corrupt");
-    const size_t v_bytes = sizeof(uint32_t) * 32 * (size_t)std::max(P.dp.sobol_dims, 1);
+    std::vector<uint32_t> V, lo;
+    if (!build_direction_numbers(V)) return fail(THOTH_GPU_E_INVALID, "embedded Joe-Kuo table is corrupt");
+    const int dims = std::max(P.dp.sobol_dims, 1);
+    const size_t v_bytes = sizeof(uint32_t) * 32 * (size_t)dims;
+    const size_t lo_bytes = sizeof(uint32_t) * SOBOL_LO_ROW * (size_t)dims;
     const size_t n_acc = (size_t)P.dp.n_acc;
     auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t o_v = up(P.blob.bytes.size());
-    const size_t o_out = o_v + up(v_bytes);
+    const size_t o_lo = o_v + up(v_bytes);
+    const size_t o_out = o_lo + up(lo_bytes);
     const size_t o_st = o_out + up(sizeof(double) * n_acc);
     const size_t o_acc = o_st + 256;
     const size_t row = sizeof(double) * n_acc;
@@ -933,11 +954,12 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     const int grid = (int)std::max<int64_t>(1, std::min(std::min(full, fit), P.dp.n_tiles));
     CUDA_TRY(cudaMemcpy(base, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(base + o_v, V.data(), v_bytes, cudaMemcpyHostToDevice));
+    build_low_table(V, dims, lo);
+    CUDA_TRY(cudaMemcpy(base + o_lo, lo.data(), lo_bytes, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemset(base + o_st, 0, sizeof(int))); // status must start at zero; the sums are zeroed by the kernel
     bind(P, base);
     P.dp.sobol_v = reinterpret_cast<const uint32_t*>(base + o_v);
-    P.dp.sobol_rows = nullptr;
-    P.dp.sobol_rows32 = nullptr;
+    P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(base + o_lo);
     P.dp.cancel = nullptr;
     P.dp.acc = reinterpret_cast<double*>(base + o_acc);
     P.dp.status = reinterpret_cast<int*>(base + o_st);
@@ -963,8 +985,385 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     out->book_premium = o[6 * (size_t)P.n_products] / n;
     out->book_trust = trust_of(o[6 * (size_t)P.n_products], o[6 * (size_t)P.n_products + 1], n);
     out->device_ms = nan;
-    out->h2d_bytes = (int64_t)(P.blob.bytes.size() + v_bytes + sizeof(int));
+    out->h2d_bytes = (int64_t)(P.blob.bytes.size() + v_bytes + lo_bytes + sizeof(int));
     out->d2h_bytes = (int64_t)(sizeof(double) * n_acc + sizeof(int));
+    return THOTH_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Ragged batches: every book's plan in one upload, each book's kernel and
+// reduction launched on one of several streams, the whole batch captured once
+// into a CUDA graph and replayed while the batch's shapes repeat, all sums back
+// in one copy.
+// ---------------------------------------------------------------------------
+struct BatchCache {
+    int streams_wanted = 8;
+    int policy = 0; // grid policy of every book in the batch (grid_policy)
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    cudaGraphExec_t exec = nullptr;
+    std::string signature;
+    unsigned char* dev = nullptr;
+    size_t dev_size = 0;
+    unsigned char* host = nullptr; // pinned
+    size_t host_size = 0;
+    int replays = 0;
+};
+static BatchCache g_batch;
+
+static int ensure_batch_streams()
+{
+    while ((int)g_batch.streams.size() < g_batch.streams_wanted) {
+        cudaStream_t s;
+        cudaEvent_t e;
+        CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        g_batch.streams.push_back(s);
+        g_batch.events.push_back(e);
+    }
+    return THOTH_GPU_OK;
+}
+
+// the batch's device work as recorded into the graph: zero the status words,
+// fork onto S streams, each book's kernel and reduction on the stream chosen by
+// a longest-processing-time schedule (books by decreasing path-steps, each onto
+// the stream with the least work so far), join
+static int record_batch(std::vector<Plan>& plans, const std::vector<int>& grid, const std::vector<size_t>& o_out,
+                        size_t o_sts, int S, cudaStream_t st)
+{
+    const int n = (int)plans.size();
+    CUDA_TRY(cudaMemsetAsync(g_batch.dev + o_sts, 0, sizeof(int) * (size_t)n, st));
+    CUDA_TRY(cudaEventRecord(g_batch.events[0], st));
+    for (int k = 0; k < S; k++) CUDA_TRY(cudaStreamWaitEvent(g_batch.streams[k], g_batch.events[0], 0));
+    std::vector<int> order(n);
+    for (int b = 0; b < n; b++) order[b] = b;
+    auto cost = [&](int b) { return (double)plans[b].paths * plans[b].dp.n_steps * std::max(1, plans[b].dp.n_assets); };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return cost(a) > cost(c); });
+    std::vector<double> load(S, 0.0);
+    for (int j = 0; j < n; j++) {
+        const int b = order[j];
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += cost(b);
+        cudaStream_t s = g_batch.streams[k];
+        CUDA_TRY(launch_book(plans[b].dp, plans[b].variant, grid[b], plans[b].smem, s));
+        CUDA_TRY(launch_reduce(plans[b].dp.acc, grid[b], plans[b].dp.n_acc,
+                               reinterpret_cast<double*>(g_batch.dev + o_out[b]), s));
+    }
+    for (int k = 0; k < S; k++) {
+        CUDA_TRY(cudaEventRecord(g_batch.events[k], g_batch.streams[k]));
+        CUDA_TRY(cudaStreamWaitEvent(st, g_batch.events[k], 0));
+    }
+    return THOTH_GPU_OK;
+}
+
+static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult* out)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    if (n == 0) return THOTH_GPU_OK;
+    rc = ensure_batch_streams();
+    if (rc) return rc;
+    const int S = std::min(g_batch.streams_wanted, n);
+    std::vector<Plan> plans(n);
+    std::vector<int> grid(n);
+    std::vector<size_t> o_blob(n), o_acc(n), o_out(n), o_st(n);
+    size_t off = 0;
+    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+    std::string sig = std::to_string(n) + ":" + std::to_string(S) + ":" + std::to_string(g_batch.policy);
+    for (int b = 0; b < n; b++) {
+        rc = build_plan(&books[b], plans[b]);
+        if (rc) return fail(rc, "book " + std::to_string(b) + ": " + g_err);
+        grid[b] = grid_for(plans[b], g_batch.policy);
+        o_blob[b] = off;
+        off += up(plans[b].blob.bytes.size());
+        o_acc[b] = off;
+        off += up(sizeof(double) * (size_t)grid[b] * plans[b].dp.n_acc);
+        sig += "|" + std::to_string(plans[b].variant) + "," + std::to_string(grid[b]) + "," +
+               std::to_string(plans[b].smem) + "," + std::to_string(plans[b].blob.bytes.size()) + "," +
+               std::to_string(plans[b].dp.n_acc) + "," + std::to_string(plans[b].dp.n_tiles);
+    }
+    // outputs and status words contiguous at the end: one device->host copy
+    const size_t o_outs = off;
+    size_t cur = o_outs;
+    for (int b = 0; b < n; b++) {
+        o_out[b] = cur;
+        cur += sizeof(double) * plans[b].dp.n_acc;
+    }
+    cur = up(cur);
+    const size_t o_sts = cur;
+    for (int b = 0; b < n; b++) o_st[b] = o_sts + sizeof(int) * (size_t)b;
+    const size_t total = o_sts + up(sizeof(int) * (size_t)n);
+    const size_t back = total - o_outs;
+    // device and pinned buffers (a new size invalidates the cached graph)
+    if (total > g_batch.dev_size) {
+        if (g_batch.exec) cudaGraphExecDestroy(g_batch.exec);
+        g_batch.exec = nullptr;
+        g_batch.signature.clear();
+        if (g_batch.dev) cudaFree(g_batch.dev);
+        g_batch.dev = nullptr;
+        CUDA_TRY(cudaMalloc(&g_batch.dev, total));
+        g_batch.dev_size = total;
+    }
+    if (std::max(o_outs, back) > g_batch.host_size) {
+        if (g_batch.host) cudaFreeHost(g_batch.host);
+        g_batch.host = nullptr;
+        CUDA_TRY(cudaHostAlloc(&g_batch.host, std::max(o_outs, back), cudaHostAllocDefault));
+        g_batch.host_size = std::max(o_outs, back);
+    }
+    for (int b = 0; b < n; b++)
+        std::memcpy(g_batch.host + o_blob[b], plans[b].blob.bytes.data(), plans[b].blob.bytes.size());
+    cudaStream_t st = g_dev.stream;
+    CUDA_TRY(cudaMemcpyAsync(g_batch.dev, g_batch.host, o_outs, cudaMemcpyHostToDevice, st));
+    for (int b = 0; b < n; b++) {
+        bind(plans[b], g_batch.dev + o_blob[b]);
+        plans[b].dp.acc = reinterpret_cast<double*>(g_batch.dev + o_acc[b]);
+        plans[b].dp.status = reinterpret_cast<int*>(g_batch.dev + o_st[b]);
+        // the kernel parameters are baked into the graph: a replay needs them byte-equal
+        sig.append(reinterpret_cast<const char*>(&plans[b].dp), sizeof(DevPlan));
+    }
+    if (g_batch.signature != sig || !g_batch.exec) {
+        if (g_batch.exec) cudaGraphExecDestroy(g_batch.exec);
+        g_batch.exec = nullptr;
+        g_batch.signature.clear();
+        // kernel attributes are set outside the capture
+        for (int b = 0; b < n; b++) occupancy_of(plans[b]);
+        CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        rc = record_batch(plans, grid, o_out, o_sts, S, st);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph); // always leave capture mode
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return rc;
+        }
+        if (ec != cudaSuccess) return fail(THOTH_GPU_E_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ec));
+        const cudaError_t e = cudaGraphInstantiate(&g_batch.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(THOTH_GPU_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        g_batch.signature = sig;
+        g_batch.replays = 0;
+    } else {
+        g_batch.replays++;
+    }
+    CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+    CUDA_TRY(cudaGraphLaunch(g_batch.exec, st));
+    CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
+    CUDA_TRY(cudaMemcpyAsync(g_batch.host, g_batch.dev + o_outs, back, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+    const double nan = std::nan("");
+    for (int b = 0; b < n; b++) {
+        const Plan& P = plans[b];
+        int status;
+        std::memcpy(&status, g_batch.host + (o_st[b] - o_outs), sizeof(int));
+        if (status == 1) return fail(THOTH_GPU_E_CANCELLED, "pricing cancelled");
+        const double* o = reinterpret_cast<const double*>(g_batch.host + (o_out[b] - o_outs));
+        const double np_ = (double)P.paths;
+        ThothBookResult* r = &out[b];
+        for (int p = 0; p < P.n_products; p++) {
+            const double* a = o + 6 * (size_t)p;
+            if (r->premium) r->premium[p] = a[0] / np_;
+            if (r->trust) r->trust[p] = trust_of(a[0], a[1], np_);
+            const bool dok = (P.greek_mask[p] & 1) != 0, vok = (P.greek_mask[p] & 2) != 0;
+            if (r->delta) r->delta[p] = dok ? a[2] / np_ : nan;
+            if (r->delta_trust) r->delta_trust[p] = dok ? trust_of(a[2], a[3], np_) : nan;
+            if (r->vega) r->vega[p] = vok ? a[4] / np_ : nan;
+            if (r->vega_trust) r->vega_trust[p] = vok ? trust_of(a[4], a[5], np_) : nan;
+        }
+        r->book_premium = o[6 * (size_t)P.n_products] / np_;
+        r->book_trust = trust_of(o[6 * (size_t)P.n_products], o[6 * (size_t)P.n_products + 1], np_);
+        r->device_ms = ms; // the whole batch's device time
+        r->h2d_bytes = b == 0 ? (int64_t)o_outs : 0;
+        r->d2h_bytes = b == 0 ? (int64_t)back : 0;
+    }
+    return THOTH_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: times candidate launch configurations on the device with CUDA
+// events and keeps the fastest. Book level: the persistent grid (k x SMs for
+// k = 1 .. resident CTAs per SM, and the balanced grid of each), stored per
+// (variant, resident CTAs per SM, tiles). Batch level: the stream count and
+// the grid policy of the batch graph.
+// ---------------------------------------------------------------------------
+static int autotune_book_locked(const ThothBookDesc* book, int reps, ThothTuneResult* out)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    Plan P;
+    rc = build_plan(book, P);
+    if (rc) return rc;
+    const int per_sm = occupancy_of(P);
+    const int64_t tiles = P.dp.n_tiles;
+    std::vector<int> cand;
+    for (int k = 1; k <= per_sm; k++) {
+        const int64_t full = (int64_t)k * g_dev.sms;
+        for (int pol = 0; pol < 2; pol++) {
+            const int g = grid_policy(tiles, full, pol);
+            if (std::find(cand.begin(), cand.end(), g) == cand.end()) cand.push_back(g);
+        }
+    }
+    const int def = grid_policy(tiles, (int64_t)per_sm * g_dev.sms, 0);
+    const int gmax = *std::max_element(cand.begin(), cand.end());
+    const Layout L = layout_of(P, gmax);
+    rc = ensure_arena(L.total);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpy(g_dev.arena, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
+    bind(P, g_dev.arena);
+    P.dp.acc = reinterpret_cast<double*>(g_dev.arena + L.o_acc);
+    P.dp.status = reinterpret_cast<int*>(g_dev.arena + L.o_st);
+    cudaStream_t st = g_dev.stream;
+    double best = 1e300, def_ms = 0;
+    int best_g = def;
+    for (int g : cand) {
+        CUDA_TRY(cudaMemsetAsync(g_dev.arena + L.o_st, 0, sizeof(int), st));
+        CUDA_TRY(launch_book(P.dp, P.variant, g, P.smem, st)); // warm-up
+        CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+        for (int r = 0; r < reps; r++) {
+            CUDA_TRY(launch_book(P.dp, P.variant, g, P.smem, st));
+            CUDA_TRY(launch_reduce(P.dp.acc, g, P.dp.n_acc, reinterpret_cast<double*>(g_dev.arena + L.o_out), st));
+        }
+        CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        int status = 0;
+        CUDA_TRY(cudaMemcpy(&status, g_dev.arena + L.o_st, sizeof(int), cudaMemcpyDeviceToHost));
+        if (status == 1) return fail(THOTH_GPU_E_CANCELLED, "autotune cancelled");
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+        const double per = ms / reps;
+        if (g == def) def_ms = per;
+        if (per < best) {
+            best = per;
+            best_g = g;
+        }
+    }
+    g_tuned[TuneKey(P.variant, per_sm, tiles)] = best_g;
+    if (out) {
+        out->grid = best_g;
+        out->default_grid = def;
+        out->candidates = (int32_t)cand.size();
+        out->streams = 0;
+        out->policy = 0;
+        out->best_ms = best;
+        out->default_ms = def_ms;
+    }
+    return THOTH_GPU_OK;
+}
+
+static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, ThothTuneResult* out)
+{
+    std::vector<ThothBookResult> res(std::max(n, 1));
+    std::memset(res.data(), 0, sizeof(ThothBookResult) * res.size());
+    const int keep_s = g_batch.streams_wanted, keep_p = g_batch.policy;
+    auto time_one = [&](int S, int pol, double* ms) {
+        g_batch.streams_wanted = S;
+        g_batch.policy = pol;
+        int rc = price_batch_locked(books, n, res.data()); // capture + warm-up
+        if (rc) return rc;
+        double sum = 0;
+        for (int r = 0; r < reps; r++) {
+            rc = price_batch_locked(books, n, res.data());
+            if (rc) return rc;
+            sum += res[0].device_ms;
+        }
+        *ms = sum / reps;
+        return THOTH_GPU_OK;
+    };
+    double best = 1e300, def_ms = 0;
+    int best_s = keep_s, best_p = 0, count = 0;
+    for (int S : {1, 2, 4, 8, 16, 32}) {
+        if (S > std::max(n, 1) && S != 1) break;
+        double ms;
+        const int rc = time_one(S, 0, &ms);
+        if (rc) {
+            g_batch.streams_wanted = keep_s;
+            g_batch.policy = keep_p;
+            return rc;
+        }
+        count++;
+        if (S == 8 || (n < 8 && S == 1)) def_ms = ms;
+        if (ms < best) {
+            best = ms;
+            best_s = S;
+        }
+    }
+    for (int pol : {1, 2}) {
+        double ms;
+        const int rc = time_one(best_s, pol, &ms);
+        if (rc) {
+            g_batch.streams_wanted = keep_s;
+            g_batch.policy = keep_p;
+            return rc;
+        }
+        count++;
+        if (ms < best) {
+            best = ms;
+            best_p = pol;
+        }
+    }
+    g_batch.streams_wanted = best_s;
+    g_batch.policy = best_p;
+    if (out) {
+        out->grid = 0;
+        out->default_grid = 0;
+        out->candidates = count;
+        out->streams = best_s;
+        out->policy = best_p;
+        out->best_ms = best;
+        out->default_ms = def_ms;
+    }
+    return THOTH_GPU_OK;
+}
+
+// autotune cache file: one line per choice, tied to the device it was measured on
+static int autotune_save_locked(const char* path)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(THOTH_GPU_E_INVALID, std::string("cannot write ") + path);
+    std::fprintf(f, "thoth-autotune 1\ndevice %d %s\n", g_dev.sms, g_dev.name.c_str());
+    std::fprintf(f, "batch %d %d\n", g_batch.streams_wanted, g_batch.policy);
+    for (const auto& kv : g_tuned)
+        std::fprintf(f, "grid %d %d %lld %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
+                     (long long)std::get<2>(kv.first), kv.second);
+    const bool ok = std::fclose(f) == 0;
+    return ok ? THOTH_GPU_OK : fail(THOTH_GPU_E_INVALID, std::string("cannot write ") + path);
+}
+
+static int autotune_load_locked(const char* path)
+{
+    int rc = ensure_device();
+    if (rc) return rc;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return fail(THOTH_GPU_E_INVALID, std::string("cannot read ") + path);
+    char line[512];
+    int version = 0, sms = -1;
+    std::string name;
+    std::map<TuneKey, int> grids;
+    int streams = g_batch.streams_wanted, policy = g_batch.policy;
+    bool bad = false;
+    while (std::fgets(line, sizeof line, f)) {
+        int a, b, g;
+        long long t;
+        char nm[400];
+        if (std::sscanf(line, "thoth-autotune %d", &a) == 1) version = a;
+        else if (std::sscanf(line, "device %d %399[^\n]", &a, nm) == 2) { sms = a; name = nm; }
+        else if (std::sscanf(line, "batch %d %d", &a, &b) == 2) { streams = a; policy = b; }
+        else if (std::sscanf(line, "grid %d %d %lld %d", &a, &b, &t, &g) == 4) {
+            if (g < 1 || t < 1) bad = true;
+            grids[TuneKey(a, b, (int64_t)t)] = g;
+        } else if (line[0] != '\n') bad = true;
+    }
+    std::fclose(f);
+    if (version != 1 || bad || streams < 1 || streams > 64 || policy < 0 || policy > 2)
+        return fail(THOTH_GPU_E_INVALID, std::string("malformed autotune file ") + path);
+    if (sms != g_dev.sms || name != g_dev.name)
+        return fail(THOTH_GPU_E_UNSUPPORTED, "autotune file was measured on another device (" + name + ")");
+    for (const auto& kv : grids) g_tuned[kv.first] = kv.second;
+    g_batch.streams_wanted = streams;
+    g_batch.policy = policy;
     return THOTH_GPU_OK;
 }
 
@@ -984,6 +1383,50 @@ int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out
 {
     std::lock_guard<std::mutex> lk(g_mu);
     return price_noalloc_locked(book, out);
+}
+
+int thoth_gpu_autotune_book(const ThothBookDesc* book, int32_t reps, ThothTuneResult* out)
+{
+    if (reps < 1 || reps > 1000) return fail(THOTH_GPU_E_INVALID, "reps must be in [1, 1000]");
+    std::lock_guard<std::mutex> lk(g_mu);
+    return autotune_book_locked(book, reps, out);
+}
+
+int thoth_gpu_autotune_batch(const ThothBookDesc* books, int32_t n_books, int32_t reps, ThothTuneResult* out)
+{
+    if (!books || n_books < 1) return fail(THOTH_GPU_E_INVALID, "bad batch");
+    if (reps < 1 || reps > 1000) return fail(THOTH_GPU_E_INVALID, "reps must be in [1, 1000]");
+    std::lock_guard<std::mutex> lk(g_mu);
+    return autotune_batch_locked(books, n_books, reps, out);
+}
+
+int thoth_gpu_autotune_save(const char* path)
+{
+    if (!path) return fail(THOTH_GPU_E_INVALID, "null path");
+    std::lock_guard<std::mutex> lk(g_mu);
+    return autotune_save_locked(path);
+}
+
+int thoth_gpu_autotune_load(const char* path)
+{
+    if (!path) return fail(THOTH_GPU_E_INVALID, "null path");
+    std::lock_guard<std::mutex> lk(g_mu);
+    return autotune_load_locked(path);
+}
+
+int thoth_gpu_autotune_clear(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_tuned.clear();
+    g_batch.streams_wanted = 8;
+    g_batch.policy = 0;
+    return THOTH_GPU_OK;
+}
+
+int thoth_gpu_batch_graph_replays(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_batch.replays;
 }
 
 int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out)
@@ -1260,8 +1703,7 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
     D.nodes = reinterpret_cast<const BridgeNode*>(g_dev.arena + P.o_nodes);
     D.recs = reinterpret_cast<const StepRec*>(g_dev.arena + P.o_recs);
     D.sobol_v = g_dev.sobol_v;
-    D.sobol_rows = g_dev.sobol_rows;
-    D.sobol_rows32 = g_dev.sobol_rows32;
+    D.sobol_lo = g_dev.sobol_lo;
     float* d_out = reinterpret_cast<float*>(g_dev.arena + o_out);
     const int grid = (int)std::min<int64_t>(D.n_tiles, (int64_t)g_dev.sms * 2);
     CUDA_TRY(launch_bridge(D, grid, smem, d_out, g_dev.stream));
@@ -1274,10 +1716,14 @@ int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBook
 {
     if (!books || !out || n_books < 0) return fail(THOTH_GPU_E_INVALID, "bad batch");
     std::lock_guard<std::mutex> lk(g_mu);
-    for (int b = 0; b < n_books; b++) {
-        const int rc = price_locked(&books[b], &out[b]);
-        if (rc) return rc;
-    }
+    return price_batch_locked(books, n_books, out);
+}
+
+int thoth_gpu_batch_streams(int32_t n)
+{
+    if (n < 1 || n > 64) return fail(THOTH_GPU_E_INVALID, "streams must be in [1, 64]");
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_batch.streams_wanted = n;
     return THOTH_GPU_OK;
 }
 
