@@ -32,7 +32,7 @@ FLOPS_PER_PATH_STEP = 96  # algorithmic FP32 flops of a Heston-QE + Andersen pat
 # DRAM bytes per launch of the book kernel from the ncu capture summarised in
 # profiles/book_kernel_heston_grid.md (a 2^18-path capture; the traffic is the
 # plan, the Sobol tables and the per-CTA sums, which do not grow with paths)
-NCU_DRAM_BYTES_PER_LAUNCH = 216832
+NCU_DRAM_BYTES_PER_LAUNCH = 1268224
 
 
 def parse():

@@ -1,10 +1,12 @@
 // engine.cuh — device side of the GB300 Monte-Carlo engine.
 //
 // One persistent kernel per book: every CTA walks tiles of 2^TB consecutive
-// Sobol indices, one path per thread, all steps of all factors in registers
-// (log-spot with Kahan compensation, variance, bridge anchors), and evaluates
-// every product of the book on the tile's paths before moving on. FP32 path
-// arithmetic; FP64 only for the per-CTA sums and the cross-CTA reduction.
+// Sobol indices (two paths per thread for single-asset books, one for mixed
+// books), all steps of all factors in registers (log-spot with Kahan
+// compensation, variance, bridge anchors; the bridge stack in shared memory),
+// and evaluates every product of the book on the tile's paths before moving
+// on. FP32 path arithmetic; FP64 only for the per-CTA sums and the cross-CTA
+// reduction.
 //
 // Reference semantics restated here (GValas/Thoth, pricer/src/...):
 //   Sobol Gray-code points          nodes/sobol_generator.cpp:22-121
@@ -144,7 +146,9 @@ struct DevPlan {
     const DevProduct* products;
     const Comp* comps;
     const uint32_t* sobol_v;     // [4097][32] direction numbers
-    const uint32_t* sobol_lo;    // [dims][SOBOL_LO_ROW] XOR of V[d][j] over the bits of gray(t), t < 256
+    const int* sobol_order;      // [n_sobol] Sobol dimensions in the order the step loop consumes them
+    const uint32_t* sobol_lo;    // [n_sobol][T] low-bit words of those dimensions, in that order
+    int n_sobol;
     double* acc;                 // [gridDim][n_acc] per-CTA FP64 sums
     int n_acc;
     volatile int* cancel;        // host-mapped cancel word (may be null)
@@ -161,41 +165,81 @@ struct DevPlan {
 // formed from the integer (q = min(x, 2^32 - x), 2u - 1 = (x - 2^31) 2^-31),
 // so the tails keep their relative accuracy.
 // ---------------------------------------------------------------------------
+// the pieces of quantile_u32: s = 2u - 1 and lg = log2(4 q (1 - q)) <= 0
+__device__ __forceinline__ void quantile_prep(uint32_t x, float& s, float& lg)
+{
+    const uint32_t qi = min(x, 0u - x);                                     // q * 2^32 in [1, 2^31]
+    s = __int2float_rn((int)(x ^ 0x80000000u)) * 4.656612873077393e-10f;    // 2u - 1
+    const float qf = __uint2float_rn(qi);
+    const float one_m_q = fmaf(qf, -2.3283064365386963e-10f, 1.0f);         // 1 - q
+    // at q = 1/2 the MUFU result is clamped (fminf drops a NaN operand)
+    lg = fminf(__log2f(qf * 9.313225746154785e-10f * one_m_q), 0.0f);
+}
+
+constexpr float QUANTILE_TAIL_LG = -9.016844005556021f; // w = -ln2 lg = 6.25
+
+// central polynomial in w - 3.125, valid for lg > QUANTILE_TAIL_LG
+__device__ __forceinline__ float quantile_central(float lg)
+{
+    const float v = fmaf(lg, -0.6931471805599453f, -3.125f);
+    float p = -7.202387403e-09f;
+    p = fmaf(p, v, -1.226470401e-08f);
+    p = fmaf(p, v, 6.170809376e-07f);
+    p = fmaf(p, v, -2.155695626e-06f);
+    p = fmaf(p, v, -1.975007828e-05f);
+    p = fmaf(p, v, 2.648245696e-04f);
+    p = fmaf(p, v, -1.047204452e-03f);
+    p = fmaf(p, v, -8.533770903e-03f);
+    p = fmaf(p, v, 3.396347351e-01f);
+    p = fmaf(p, v, 2.338620874e+00f);
+    return p;
+}
+
+// tail polynomial in sqrt(w) - 3.6479158, for lg <= QUANTILE_TAIL_LG
+__device__ __forceinline__ float quantile_tail(float lg)
+{
+    const float v = sqrtf(lg * -0.6931471805599453f) - 3.6479158f;
+    float p = 6.598971903e-06f;
+    p = fmaf(p, v, 5.795662157e-05f);
+    p = fmaf(p, v, -2.423309240e-04f);
+    p = fmaf(p, v, 3.854843299e-04f);
+    p = fmaf(p, v, -5.190533957e-04f);
+    p = fmaf(p, v, 9.818501131e-04f);
+    p = fmaf(p, v, -2.186479756e-03f);
+    p = fmaf(p, v, 3.518813816e-03f);
+    p = fmaf(p, v, 1.425832630e+00f);
+    p = fmaf(p, v, 4.927907588e+00f);
+    return p;
+}
+
 __device__ __forceinline__ float quantile_u32(uint32_t x)
 {
-    const uint32_t qi = min(x, 0u - x);                                         // q * 2^32 in [1, 2^31]
-    const float s = __int2float_rn((int)(x ^ 0x80000000u)) * 4.656612873077393e-10f; // 2u - 1
-    const float qf = __uint2float_rn(qi);
-    const float one_m_q = fmaf(qf, -2.3283064365386963e-10f, 1.0f);              // 1 - q
-    // log2(4 q (1 - q)) <= 0; at q = 1/2 the MUFU result is clamped (fminf drops a NaN operand)
-    const float lg = fminf(__log2f(qf * 9.313225746154785e-10f * one_m_q), 0.0f);
-    float p;
-    if (lg > -9.016844005556021f) { // w = -ln2 lg < 6.25
-        const float v = fmaf(lg, -0.6931471805599453f, -3.125f);
-        p = -7.202387403e-09f;
-        p = fmaf(p, v, -1.226470401e-08f);
-        p = fmaf(p, v, 6.170809376e-07f);
-        p = fmaf(p, v, -2.155695626e-06f);
-        p = fmaf(p, v, -1.975007828e-05f);
-        p = fmaf(p, v, 2.648245696e-04f);
-        p = fmaf(p, v, -1.047204452e-03f);
-        p = fmaf(p, v, -8.533770903e-03f);
-        p = fmaf(p, v, 3.396347351e-01f);
-        p = fmaf(p, v, 2.338620874e+00f);
-    } else {
-        const float v = sqrtf(lg * -0.6931471805599453f) - 3.6479158f;
-        p = 6.598971903e-06f;
-        p = fmaf(p, v, 5.795662157e-05f);
-        p = fmaf(p, v, -2.423309240e-04f);
-        p = fmaf(p, v, 3.854843299e-04f);
-        p = fmaf(p, v, -5.190533957e-04f);
-        p = fmaf(p, v, 9.818501131e-04f);
-        p = fmaf(p, v, -2.186479756e-03f);
-        p = fmaf(p, v, 3.518813816e-03f);
-        p = fmaf(p, v, 1.425832630e+00f);
-        p = fmaf(p, v, 4.927907588e+00f);
-    }
+    float s, lg;
+    quantile_prep(x, s, lg);
+    const float p = lg > QUANTILE_TAIL_LG ? quantile_central(lg) : quantile_tail(lg);
     return p * s;
+}
+
+// N quantiles at once: the central polynomials as one straight-line block, the
+// rare tail afterwards (same expressions as quantile_u32, same results)
+template <int N>
+__device__ __forceinline__ void quantile_n(const uint32_t (&x)[N], float (&z)[N])
+{
+    float s[N], lg[N];
+    bool tail = false;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        quantile_prep(x[i], s[i], lg[i]);
+        z[i] = quantile_central(lg[i]);
+        tail |= !(lg[i] > QUANTILE_TAIL_LG);
+    }
+    if (tail) {
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if (!(lg[i] > QUANTILE_TAIL_LG)) z[i] = quantile_tail(lg[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) z[i] *= s[i];
 }
 
 // counter-based uint32 for dimensions beyond the Sobol budget and use_sobol = 0

@@ -61,66 +61,98 @@ __device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
 // Sobol for the current tile. Path n = m * T + t (T = 2^TB). gray(n) splits
 // into bits >= TB, shared by the whole tile, and the thread's low TB bits
 // gray(t) ^ ((m & 1) << (TB - 1)). The XOR of V[d][j] over the bits of gray(t)
-// depends on the thread only, so it is a fixed table lo[d][t] (t < 256, built
-// once on the host); the tile part (bits >= TB and the parity flip) is
-// computed once per tile and dimension into smem. One point coordinate is then
-// x = hs[d] ^ lo[d][t]: a shared-memory broadcast and one coalesced load.
+// depends on the thread only: a fixed word lo[d][t]. Every Sobol dimension is
+// used once per path, in an order fixed by the bridge program, so the book's
+// low words are laid out in that order (sobol_lo[j][t], j the j-th dimension
+// consumed) and the tile part likewise (hs[j], computed once per tile). The
+// step loop then reads both sequentially: x = hs[j] ^ lo[j][t], with the
+// coalesced load of entry j + 2 in flight while entry j is used.
 // ---------------------------------------------------------------------------
 template <int TB>
 __device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m)
 {
-    constexpr int T = 1 << TB;
     const uint64_t g = (uint64_t)m ^ ((uint64_t)m >> 1);
-    for (int d = threadIdx.x; d < P.sobol_dims; d += T) {
-        const uint32_t* V = P.sobol_v + d * SOBOL_BITS;
+    for (int j = threadIdx.x; j < P.n_sobol; j += blockDim.x) {
+        const uint32_t* V = P.sobol_v + __ldg(P.sobol_order + j) * SOBOL_BITS;
         uint32_t acc = (m & 1) ? __ldg(V + TB - 1) : 0u;
         uint64_t gg = g;
         for (int k = 0; gg != 0 && k < SOBOL_BITS - TB; ++k, gg >>= 1)
             if (gg & 1u) acc ^= __ldg(V + TB + k);
-        hs[d] = acc;
+        hs[j] = acc;
     }
 }
 
+template <int T, int PP>
 struct SobolLane {
-    const uint32_t* hs; // tile part, smem
-    const uint32_t* lo; // this thread's column of the low-bit table
+    const uint32_t* hs;    // tile parts in consumption order, smem
+    const uint32_t* lo;    // column threadIdx.x of the book's low words
+    int j;                 // next entry
+    uint32_t cur[PP], nxt[PP]; // low words of entries j and j + 1, per path of the thread
 };
 
-template <int TB>
-__device__ __forceinline__ SobolLane sobol_lane(const DevPlan& P, uint32_t* hs, int64_t)
+// path p of a thread is tile column threadIdx.x + p * (T / PP)
+template <int TB, int PP>
+__device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, const uint32_t* hs)
 {
-    SobolLane L;
+    constexpr int T = 1 << TB, TH = T / PP;
+    SobolLane<T, PP> L;
     L.hs = hs;
     L.lo = P.sobol_lo + threadIdx.x;
+    L.j = 0;
+#pragma unroll
+    for (int p = 0; p < PP; ++p) {
+        L.cur[p] = P.n_sobol > 0 ? __ldg(L.lo + p * TH) : 0u;
+        L.nxt[p] = P.n_sobol > 1 ? __ldg(L.lo + T + p * TH) : 0u;
+    }
     return L;
 }
 
-// Gaussian for reference dimension `dim` of Sobol index n
-__device__ __forceinline__ float gauss(const DevPlan& P, const SobolLane& L, uint64_t n, int dim)
+// Gaussians of reference dimension `dim` for the thread's PP paths (Sobol
+// indices n[p]); a Sobol dimension is the lane's next entry
+template <int T, int PP>
+__device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, const uint64_t (&n)[PP], int dim,
+                                      float (&z)[PP])
 {
-    uint32_t x;
-    if (dim < P.sobol_dims)
-        x = L.hs[dim] ^ __ldg(L.lo + dim * SOBOL_LO_ROW);
-    else
-        x = hash_u32(P.seed, n, (uint32_t)dim);
-    return quantile_u32(x);
+    constexpr int TH = T / PP;
+    uint32_t x[PP];
+    if (dim < P.sobol_dims) {
+        const uint32_t h = L.hs[L.j];
+        const int jn = L.j + 2;
+        const bool more = jn < P.n_sobol;
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+            x[p] = h ^ L.cur[p];
+            L.cur[p] = L.nxt[p];
+            L.nxt[p] = more ? __ldg(L.lo + jn * T + p * TH) : 0u;
+        }
+        ++L.j;
+    } else {
+#pragma unroll
+        for (int p = 0; p < PP; ++p) x[p] = hash_u32(P.seed, n[p], (uint32_t)dim);
+    }
+    quantile_n<PP>(x, z);
 }
 
 // ---------------------------------------------------------------------------
-// One time step of the bridge for every active factor slot: fills nz[] with the
-// normalised increments n_i = (W_i - W_{i-1}) / sqrt(t_i - t_{i-1}).
+// One time step of the bridge for every active factor slot of the thread's PP
+// paths: fills nz[][] with the normalised increments
+// n_i = (W_i - W_{i-1}) / sqrt(t_i - t_{i-1}). Stack entry of path column k:
+// stk[(level * nfa + factor) * T + k].
 // ---------------------------------------------------------------------------
-template <int NA, int T>
+template <int NA, int T, int PP>
 __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, const StepRec& rec, int& sp,
-                                            const SobolLane& L, uint64_t n, float (&Wprev)[2 * NA],
-                                            float (&top)[2 * NA], float (&nz)[2 * NA])
+                                            SobolLane<T, PP>& L, const uint64_t (&n)[PP],
+                                            float (&Wprev)[PP][2 * NA], float (&top)[PP][2 * NA],
+                                            float (&nz)[PP][2 * NA])
 {
-    constexpr int FS = 2 * NA;
+    constexpr int FS = 2 * NA, TH = T / PP;
     const int t = threadIdx.x;
     const int nfa = P.n_factors_active;
-    float Wi[FS];
+    float Wi[PP][FS];
 #pragma unroll
-    for (int f = 0; f < FS; ++f) Wi[f] = 0.f;
+    for (int p = 0; p < PP; ++p)
+#pragma unroll
+        for (int f = 0; f < FS; ++f) Wi[p][f] = 0.f;
     if (rec.count == 0) {
         const int base = (sp - 1) * nfa * T + t;
 #pragma unroll
@@ -128,8 +160,11 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
             const int a = f < NA ? f : f - NA;
             const int ci = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
             if (a < P.n_assets && ci >= 0) {
-                Wi[f] = top[f];
-                top[f] = S.stk[base + ci * T];
+#pragma unroll
+                for (int p = 0; p < PP; ++p) {
+                    Wi[p][f] = top[p][f];
+                    top[p][f] = S.stk[base + ci * T + p * TH];
+                }
             }
         }
         --sp;
@@ -152,13 +187,17 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
                 const int ci = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
                 if (a < P.n_assets && ci >= 0) {
                     const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
-                    const float z = gauss(P, L, n, dim + fid);
-                    const float Wn = fmaf(lw, Wprev[f], fmaf(rw, top[f], sd * z));
-                    if (push) {
-                        S.stk[base + ci * T] = top[f];
-                        top[f] = Wn;
-                    } else {
-                        Wi[f] = Wn;
+                    float z[PP];
+                    gauss(P, L, n, dim + fid, z);
+#pragma unroll
+                    for (int p = 0; p < PP; ++p) {
+                        const float Wn = fmaf(lw, Wprev[p][f], fmaf(rw, top[p][f], sd * z[p]));
+                        if (push) {
+                            S.stk[base + ci * T + p * TH] = top[p][f];
+                            top[p][f] = Wn;
+                        } else {
+                            Wi[p][f] = Wn;
+                        }
                     }
                 }
             }
@@ -166,10 +205,12 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
         }
     }
 #pragma unroll
-    for (int f = 0; f < FS; ++f) {
-        nz[f] = (Wi[f] - Wprev[f]) * rec.isd;
-        Wprev[f] = Wi[f];
-    }
+    for (int p = 0; p < PP; ++p)
+#pragma unroll
+        for (int f = 0; f < FS; ++f) {
+            nz[p][f] = (Wi[p][f] - Wprev[p][f]) * rec.isd;
+            Wprev[p][f] = Wi[p][f];
+        }
 }
 
 // leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47)
@@ -285,10 +326,11 @@ __device__ __forceinline__ StepRec load_rec(const DevPlan& P, int i)
 //   MODEL   M_GBM / M_HESTON / M_LSV for single-model books, M_MIXED otherwise
 //   UNIFORM every step has the same per-asset constants (kept in registers)
 // ---------------------------------------------------------------------------
-template <int TB, int NA, int MODEL, bool UNIFORM>
-__global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const DevPlan P)
+template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
+__global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? (PP == 2 ? 6 : 3) : 1) book_kernel(const DevPlan P)
 {
-    constexpr int T = 1 << TB;
+    constexpr int T = 1 << TB;  // paths per tile
+    constexpr int TH = T / PP;  // threads per CTA; path p of thread t is tile column t + p * TH
     constexpr int FS = 2 * NA;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Smem S = carve(smem_raw, P, T);
@@ -297,7 +339,7 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
     __shared__ int s_cancel;
 
     double* acc = P.acc + (size_t)blockIdx.x * P.n_acc;
-    for (int j = t; j < P.n_acc; j += T) acc[j] = 0.0;
+    for (int j = t; j < P.n_acc; j += TH) acc[j] = 0.0;
 
     // uniform step constants (UNIFORM: step 1's for every step)
     float4 u0[NA], u1[NA], u2[NA];
@@ -315,8 +357,13 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
 
     for (int64_t tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
         const int64_t m = P.tile_first + tile;
-        const uint64_t n = (uint64_t)m * T + (uint64_t)t;
-        const bool valid = n >= (uint64_t)P.skip + 1 && n <= (uint64_t)(P.skip + P.paths);
+        uint64_t n[PP];
+        bool valid[PP];
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+            n[p] = (uint64_t)m * T + (uint64_t)(t + p * TH);
+            valid[p] = n[p] >= (uint64_t)P.skip + 1 && n[p] <= (uint64_t)(P.skip + P.paths);
+        }
         __syncthreads(); // previous tile fully evaluated
         if (t == 0) s_cancel = (P.cancel != nullptr) ? *P.cancel : 0;
         if (P.use_sobol) tile_high_bits<TB>(P, S.hs, m);
@@ -325,59 +372,64 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
             if (t == 0) atomicExch(P.status, 1);
             return;
         }
-        const SobolLane L = sobol_lane<TB>(P, S.hs, m);
+        SobolLane<T, PP> L = sobol_lane<TB, PP>(P, S.hs);
 
         // ---- path state -------------------------------------------------
-        float x[NA], comp[NA], v[NA], Wb[NA], y[NA];
-        float Wprev[FS], top[FS], nz[FS];
+        float x[PP][NA], comp[PP][NA], v[PP][NA], Wb[PP][NA], y[PP][NA];
+        float Wprev[PP][FS], top[PP][FS], nz[PP][FS];
 #pragma unroll
-        for (int a = 0; a < NA; ++a) {
-            x[a] = 0.f;
-            comp[a] = 0.f;
-            v[a] = P.v0[a];
-            Wb[a] = 0.f;
-            y[a] = 1.f;
-        }
+        for (int p = 0; p < PP; ++p) {
 #pragma unroll
-        for (int f = 0; f < FS; ++f) {
-            Wprev[f] = 0.f;
-            top[f] = 0.f;
-            nz[f] = 0.f;
+            for (int a = 0; a < NA; ++a) {
+                x[p][a] = 0.f;
+                comp[p][a] = 0.f;
+                v[p][a] = P.v0[a];
+                Wb[p][a] = 0.f;
+                y[p][a] = 1.f;
+            }
+#pragma unroll
+            for (int f = 0; f < FS; ++f) {
+                Wprev[p][f] = 0.f;
+                top[p][f] = 0.f;
+                nz[p][f] = 0.f;
+            }
         }
         int sp = 0;
-        for (int g = 0; g < P.n_groups; ++g) {
-            S.grp[g * stride + t] = P.grp_init[g];
-            S.last[g * stride + t] = 0.f;
-        }
+        for (int g = 0; g < P.n_groups; ++g)
+#pragma unroll
+            for (int p = 0; p < PP; ++p) {
+                S.grp[g * stride + t + p * TH] = P.grp_init[g];
+                S.last[g * stride + t + p * TH] = 0.f;
+            }
 
-        // events on date index i for asset a (after the state at date i is known)
-        auto apply_events = [&](int i, int a, float xa, float step, float wa, float ya) {
+        // events on date index i for asset a of tile column k (after the state at date i is known)
+        auto apply_events = [&](int i, int a, int k, float xa, float step, float wa, float ya) {
             const int2 r = P.ev_range[i * P.n_assets + a];
             for (int e = r.x; e < r.x + r.y; ++e) {
                 const Event ev = P.events[e];
                 switch (ev.type) {
-                case EV_SNAP_S: S.slots[ev.a * stride + t] = P.s0[a] * expf(xa); break;
-                case EV_SNAP_W: S.slots[ev.a * stride + t] = wa; break;
-                case EV_SNAP_Y: S.slots[ev.a * stride + t] = ya; break;
+                case EV_SNAP_S: S.slots[ev.a * stride + k] = P.s0[a] * expf(xa); break;
+                case EV_SNAP_W: S.slots[ev.a * stride + k] = wa; break;
+                case EV_SNAP_Y: S.slots[ev.a * stride + k] = ya; break;
                 case EV_GRP_MIN: {
-                    float* g = S.grp + ev.a * stride + t;
+                    float* g = S.grp + ev.a * stride + k;
                     *g = fminf(*g, xa - ev.p);
                     break;
                 }
                 case EV_GRP_MAX: {
-                    float* g = S.grp + ev.a * stride + t;
+                    float* g = S.grp + ev.a * stride + k;
                     *g = fmaxf(*g, xa - ev.p);
                     break;
                 }
                 case EV_GRP_SQ_STEP: {
-                    float* g = S.grp + ev.a * stride + t;
+                    float* g = S.grp + ev.a * stride + k;
                     const float d = step - ev.p;
                     *g = fmaf(d, d, *g);
                     break;
                 }
                 default: { // EV_GRP_SQ_OBS
-                    float* g = S.grp + ev.a * stride + t;
-                    float* l = S.last + ev.a * stride + t;
+                    float* g = S.grp + ev.a * stride + k;
+                    float* l = S.last + ev.a * stride + k;
                     const float d = xa - *l - ev.p;
                     *g = fmaf(d, d, *g);
                     *l = xa;
@@ -387,7 +439,9 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
         };
 #pragma unroll
         for (int a = 0; a < NA; ++a)
-            if (a < P.n_assets) apply_events(0, a, 0.f, 0.f, 0.f, 1.f);
+            if (a < P.n_assets)
+#pragma unroll
+                for (int p = 0; p < PP; ++p) apply_events(0, a, t + p * TH, 0.f, 0.f, 0.f, 1.f);
 
         // ---- time loop (step records prefetched one step ahead) ------------
         StepRec rec = load_rec(P, 1);
@@ -395,14 +449,17 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
             const StepRec cur = rec;
             if (i < P.n_steps) rec = load_rec(P, i + 1);
             if (P.use_sobol) {
-                bridge_step<NA, T>(P, S, cur, sp, L, n, Wprev, top, nz);
+                bridge_step<NA, T, PP>(P, S, cur, sp, L, n, Wprev, top, nz);
             } else {
 #pragma unroll
                 for (int f = 0; f < FS; ++f) {
                     const int a = f < NA ? f : f - NA;
                     const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
                     if (a < P.n_assets && fid >= 0)
-                        nz[f] = quantile_u32(hash_u32(P.seed, n, (uint32_t)((i - 1) * P.ref_factors + fid)));
+#pragma unroll
+                        for (int p = 0; p < PP; ++p)
+                            nz[p][f] =
+                                quantile_u32(hash_u32(P.seed, n[p], (uint32_t)((i - 1) * P.ref_factors + fid)));
                 }
             }
 #pragma unroll
@@ -420,54 +477,59 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
                     c2 = __ldg(cs + 2);
                 }
                 const int model = (MODEL == M_MIXED) ? P.model[a] : MODEL;
-                float step;
-                if (model == M_GBM) {
-                    float e = nz[a];
-                    if (MODEL == M_MIXED && P.corr) {
-                        e = 0.f;
 #pragma unroll
-                        for (int u = 0; u < NA; ++u)
-                            if (u < P.n_assets) e = fmaf(P.chol[a * MAX_ASSETS + u], nz[u], e);
-                    }
-                    step = fmaf(c0.y, e, c0.x);
-                    Wb[a] = fmaf(c0.z, e, Wb[a]);
-                } else {
-                    const float vp = v[a];
-                    const float vc = qe_step(vp, nz[NA + a], c0.x, c0.y, c0.z, c0.w);
-                    float Lv = 1.f, dL = 0.f;
-                    if (model == M_LSV) leverage(P, a, i, x[a], Lv, dL);
-                    const float s = vp + vc;
-                    if (!P.degenerate[a]) {
-                        const float B = fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * nz[a];
-                        if (model == M_LSV) {
-                            step = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
-                            y[a] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
-                        } else {
-                            step = c1.x + B - c1.w * s;
+                for (int p = 0; p < PP; ++p) {
+                    float step;
+                    if (model == M_GBM) {
+                        float e = nz[p][a];
+                        if (MODEL == M_MIXED && P.corr) {
+                            e = 0.f;
+#pragma unroll
+                            for (int u = 0; u < NA; ++u)
+                                if (u < P.n_assets) e = fmaf(P.chol[a * MAX_ASSETS + u], nz[p][u], e);
                         }
+                        step = fmaf(c0.y, e, c0.x);
+                        Wb[p][a] = fmaf(c0.z, e, Wb[p][a]);
                     } else {
-                        const float sq = fast_sqrt(vp * c2.z) * nz[a];
-                        step = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
-                        if (model == M_LSV) y[a] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
+                        const float vp = v[p][a];
+                        const float vc = qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
+                        float Lv = 1.f, dL = 0.f;
+                        if (model == M_LSV) leverage(P, a, i, x[p][a], Lv, dL);
+                        const float s = vp + vc;
+                        if (!P.degenerate[a]) {
+                            const float B =
+                                fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * nz[p][a];
+                            if (model == M_LSV) {
+                                step = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
+                                y[p][a] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
+                            } else {
+                                step = c1.x + B - c1.w * s;
+                            }
+                        } else {
+                            const float sq = fast_sqrt(vp * c2.z) * nz[p][a];
+                            step = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
+                            if (model == M_LSV) y[p][a] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
+                        }
+                        v[p][a] = vc;
                     }
-                    v[a] = vc;
+                    // Kahan-compensated log-spot
+                    const float yy = step - comp[p][a];
+                    const float tt = x[p][a] + yy;
+                    comp[p][a] = (tt - x[p][a]) - yy;
+                    x[p][a] = tt;
+                    if (cur.ev) apply_events(i, a, t + p * TH, x[p][a], step, Wb[p][a], y[p][a]);
                 }
-                // Kahan-compensated log-spot
-                const float yy = step - comp[a];
-                const float tt = x[a] + yy;
-                comp[a] = (tt - x[a]) - yy;
-                x[a] = tt;
-                if (cur.ev) apply_events(i, a, x[a], step, Wb[a], y[a]);
             }
         }
-        S.valid[t] = valid ? 1 : 0;
+#pragma unroll
+        for (int p = 0; p < PP; ++p) S.valid[t + p * TH] = valid[p] ? 1 : 0;
         __syncthreads();
 
         // ---- product evaluation: thread per product, FP32 tile partials ----
         const int C = P.n_products;
-        for (int pc = 0; pc < C; pc += T) {
-            const int CP = min(C - pc, T);
-            const int G = T / CP;
+        for (int pc = 0; pc < C; pc += TH) {
+            const int CP = min(C - pc, TH);
+            const int G = TH / CP;
             const int pl = t % CP, g = t / CP;
             float a6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (g < G) {
@@ -501,13 +563,18 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
             __syncthreads();
         }
         // ---- book value per path (book_node.cpp:16-31) ---------------------
-        float b = 0.f;
-        if (valid)
-            for (int p = 0; p < C; ++p) {
-                const DevProduct pr = P.products[p];
-                b = fmaf(payoff(P, pr, S.slots, S.grp, stride, t), pr.fx, b);
-            }
-        double b1 = b, b2 = (double)b * b;
+        double b1 = 0.0, b2 = 0.0;
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+            float b = 0.f;
+            if (valid[p])
+                for (int q = 0; q < C; ++q) {
+                    const DevProduct pr = P.products[q];
+                    b = fmaf(payoff(P, pr, S.slots, S.grp, stride, t + p * TH), pr.fx, b);
+                }
+            b1 += b;
+            b2 += (double)b * b;
+        }
         for (int o = 16; o > 0; o >>= 1) {
             b1 += __shfl_xor_sync(0xffffffffu, b1, o);
             b2 += __shfl_xor_sync(0xffffffffu, b2, o);
@@ -519,7 +586,7 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
         __syncthreads();
         if (t == 0) {
             double s1 = 0, s2 = 0;
-            for (int w = 0; w < T / 32; ++w) {
+            for (int w = 0; w < TH / 32; ++w) {
                 s1 += S.red[2 * w];
                 s2 += S.red[2 * w + 1];
             }
@@ -530,13 +597,44 @@ __global__ void __launch_bounds__(1 << TB, NA == 1 ? 3 : 1) book_kernel(const De
 }
 
 // fixed-order FP64 reduction of the per-CTA rows
-__global__ void reduce_rows(const double* __restrict__ acc, int rows, int n_acc, double* __restrict__ out)
+// (32 columns per CTA; row group g of REDUCE_GROUPS sums rows g, g + GROUPS, ...
+// in order, then the group sums are added in group order: the same order on
+// every run, whatever the scheduling)
+constexpr int REDUCE_GROUPS = 16;
+__global__ void __launch_bounds__(32 * REDUCE_GROUPS)
+    reduce_rows(const double* __restrict__ acc, int rows, int n_acc, double* __restrict__ out)
 {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n_acc) return;
+    __shared__ double part[REDUCE_GROUPS][33];
+    const int c = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + c;
     double s = 0.0;
-    for (int r = 0; r < rows; ++r) s += acc[(size_t)r * n_acc + j];
-    out[j] = s;
+    if (j < n_acc)
+        for (int r = g; r < rows; r += REDUCE_GROUPS) s += acc[(size_t)r * n_acc + j];
+    part[g][c] = s;
+    __syncthreads();
+    if (g == 0 && j < n_acc) {
+        double t = 0.0;
+        for (int k = 0; k < REDUCE_GROUPS; ++k) t += part[k][c];
+        out[j] = t;
+    }
+}
+
+// the book's low Sobol words in consumption order: out[j][t] = lo_all[order[j]][t]
+__global__ void gather_low_kernel(const uint32_t* __restrict__ lo_all, const int* __restrict__ order, int n, int T,
+                                  uint32_t* __restrict__ out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n * T) return;
+    const int j = (int)(i / T), t = (int)(i % T);
+    out[i] = __ldg(lo_all + (size_t)__ldg(order + j) * SOBOL_LO_ROW + t);
+}
+
+cudaError_t launch_gather_low(const uint32_t* lo_all, const int* order, int n, int T, uint32_t* out, cudaStream_t st)
+{
+    const int64_t total = (int64_t)n * T;
+    if (total == 0) return cudaSuccess;
+    gather_low_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(lo_all, order, n, T, out);
+    return cudaGetLastError();
 }
 
 // ---- test hooks -----------------------------------------------------------
@@ -572,21 +670,21 @@ __global__ void __launch_bounds__(1 << TB) bridge_kernel(const DevPlan P, float*
     const int t = threadIdx.x;
     for (int64_t tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
         const int64_t m = P.tile_first + tile;
-        const uint64_t n = (uint64_t)m * T + (uint64_t)t;
-        const bool valid = n >= (uint64_t)P.skip + 1 && n <= (uint64_t)(P.skip + P.paths);
+        const uint64_t n[1] = {(uint64_t)m * T + (uint64_t)t};
+        const bool valid = n[0] >= (uint64_t)P.skip + 1 && n[0] <= (uint64_t)(P.skip + P.paths);
         __syncthreads();
         tile_high_bits<TB>(P, S.hs, m);
         __syncthreads();
-        const SobolLane L = sobol_lane<TB>(P, S.hs, m);
-        float Wprev[2] = {0.f, 0.f}, top[2] = {0.f, 0.f}, nz[2];
+        SobolLane<T, 1> L = sobol_lane<TB, 1>(P, S.hs);
+        float Wprev[1][2] = {{0.f, 0.f}}, top[1][2] = {{0.f, 0.f}}, nz[1][2];
         int sp = 0;
-        const int64_t path = (int64_t)n - P.skip - 1;
+        const int64_t path = (int64_t)n[0] - P.skip - 1;
         for (int i = 1; i <= P.n_steps; ++i) {
             const StepRec rec = load_rec(P, i);
-            bridge_step<NA, T>(P, S, rec, sp, L, n, Wprev, top, nz);
+            bridge_step<NA, T, 1>(P, S, rec, sp, L, n, Wprev, top, nz);
             if (valid) {
                 for (int f = 0; f < P.n_factors_active; ++f)
-                    out[((size_t)path * P.n_factors_active + f) * P.n_steps + (i - 1)] = nz[f];
+                    out[((size_t)path * P.n_factors_active + f) * P.n_steps + (i - 1)] = nz[0][f];
             }
         }
     }
@@ -620,7 +718,10 @@ cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st)
 }
 
 // ---- launch wrappers --------------------------------------------------------
-template <int TB, int NA, int MODEL, bool UNIFORM>
+// paths per thread of the single-asset variants (the mixed variant keeps one)
+constexpr int PP1 = 2;
+
+template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
 static cudaError_t smem_attr_t()
 {
     // once per variant: allow the device's opt-in maximum, so that launches of
@@ -631,20 +732,20 @@ static cudaError_t smem_attr_t()
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa;
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, book_kernel<TB, NA, MODEL, UNIFORM>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, book_kernel<TB, NA, MODEL, UNIFORM, PP>);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(book_kernel<TB, NA, MODEL, UNIFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(book_kernel<TB, NA, MODEL, UNIFORM, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  mx - (int)fa.sharedSizeBytes);
     done = e == cudaSuccess;
     return e;
 }
 
-template <int TB, int NA, int MODEL, bool UNIFORM>
+template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
 static cudaError_t launch_book_t(const DevPlan& P, int grid, size_t smem, cudaStream_t st)
 {
-    cudaError_t e = smem_attr_t<TB, NA, MODEL, UNIFORM>();
+    cudaError_t e = smem_attr_t<TB, NA, MODEL, UNIFORM, PP>();
     if (e != cudaSuccess) return e;
-    book_kernel<TB, NA, MODEL, UNIFORM><<<grid, 1 << TB, smem, st>>>(P);
+    book_kernel<TB, NA, MODEL, UNIFORM, PP><<<grid, (1 << TB) / PP, smem, st>>>(P);
     return cudaGetLastError();
 }
 
@@ -653,25 +754,25 @@ static cudaError_t launch_book_t(const DevPlan& P, int grid, size_t smem, cudaSt
 cudaError_t launch_book(const DevPlan& P, int variant, int grid, size_t smem, cudaStream_t st)
 {
     switch (variant) {
-    case 0: return launch_book_t<8, 1, M_GBM, false>(P, grid, smem, st);
-    case 1: return launch_book_t<8, 1, M_HESTON, false>(P, grid, smem, st);
-    case 2: return launch_book_t<8, 1, M_LSV, false>(P, grid, smem, st);
-    case 3: return launch_book_t<7, MAX_ASSETS, M_MIXED, false>(P, grid, smem, st);
-    case 4: return launch_book_t<8, 1, M_HESTON, true>(P, grid, smem, st);
-    case 5: return launch_book_t<8, 1, M_GBM, true>(P, grid, smem, st);
+    case 0: return launch_book_t<8, 1, M_GBM, false, PP1>(P, grid, smem, st);
+    case 1: return launch_book_t<8, 1, M_HESTON, false, PP1>(P, grid, smem, st);
+    case 2: return launch_book_t<8, 1, M_LSV, false, PP1>(P, grid, smem, st);
+    case 3: return launch_book_t<7, MAX_ASSETS, M_MIXED, false, 1>(P, grid, smem, st);
+    case 4: return launch_book_t<8, 1, M_HESTON, true, PP1>(P, grid, smem, st);
+    case 5: return launch_book_t<8, 1, M_GBM, true, PP1>(P, grid, smem, st);
     default: return cudaErrorInvalidValue;
     }
 }
 
 int book_variant_tile_bits(int variant) { return variant == 3 ? 7 : 8; }
 
-template <int TB, int NA, int MODEL, bool UNIFORM>
+template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
 static int occ_t(size_t smem)
 {
-    auto k = book_kernel<TB, NA, MODEL, UNIFORM>;
-    if (smem_attr_t<TB, NA, MODEL, UNIFORM>() != cudaSuccess) return 1;
+    auto k = book_kernel<TB, NA, MODEL, UNIFORM, PP>;
+    if (smem_attr_t<TB, NA, MODEL, UNIFORM, PP>() != cudaSuccess) return 1;
     int n = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 1 << TB, smem) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, (1 << TB) / PP, smem) != cudaSuccess) return 1;
     return n < 1 ? 1 : n;
 }
 
@@ -679,12 +780,12 @@ static int occ_t(size_t smem)
 int book_occupancy(int variant, size_t smem)
 {
     switch (variant) {
-    case 0: return occ_t<8, 1, M_GBM, false>(smem);
-    case 1: return occ_t<8, 1, M_HESTON, false>(smem);
-    case 2: return occ_t<8, 1, M_LSV, false>(smem);
-    case 3: return occ_t<7, MAX_ASSETS, M_MIXED, false>(smem);
-    case 4: return occ_t<8, 1, M_HESTON, true>(smem);
-    case 5: return occ_t<8, 1, M_GBM, true>(smem);
+    case 0: return occ_t<8, 1, M_GBM, false, PP1>(smem);
+    case 1: return occ_t<8, 1, M_HESTON, false, PP1>(smem);
+    case 2: return occ_t<8, 1, M_LSV, false, PP1>(smem);
+    case 3: return occ_t<7, MAX_ASSETS, M_MIXED, false, 1>(smem);
+    case 4: return occ_t<8, 1, M_HESTON, true, PP1>(smem);
+    case 5: return occ_t<8, 1, M_GBM, true, PP1>(smem);
     default: return 1;
     }
 }
@@ -695,7 +796,7 @@ size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_sl
 
 cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st)
 {
-    reduce_rows<<<(n_acc + 127) / 128, 128, 0, st>>>(acc, rows, n_acc, out);
+    reduce_rows<<<(n_acc + 31) / 32, 32 * REDUCE_GROUPS, 0, st>>>(acc, rows, n_acc, out);
     return cudaGetLastError();
 }
 

@@ -30,6 +30,7 @@ cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64
                                 cudaStream_t st);
 cudaError_t launch_quantile(const uint32_t* x, int64_t n, float* out, cudaStream_t st);
 cudaError_t launch_bridge(const DevPlan& P, int grid, size_t smem, float* out, cudaStream_t st);
+cudaError_t launch_gather_low(const uint32_t* lo_all, const int* order, int n, int T, uint32_t* out, cudaStream_t st);
 cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_tc_gemm_test(const void* A, const void* B, int N, int K, float* D, int* status, cudaStream_t st);
 } // namespace thoth
@@ -332,6 +333,24 @@ std::vector<StepRec> make_recs(const BridgeProgram& bp, const std::vector<float>
     return recs;
 }
 
+// Sobol dimensions in the order the step loop consumes them: per step, per node
+// of its chain, the active spot factors, then the active variance factors
+// (the factor loop of bridge_step), dimensions beyond the Sobol budget left out
+std::vector<int> sobol_order(const BridgeProgram& bp, const DevPlan& D)
+{
+    std::vector<int> order;
+    if (!D.use_sobol) return order;
+    for (const StepProg& sp : bp.prog)
+        for (int k = 0; k < sp.count; k++) {
+            const int d0 = bp.nodes[sp.first + k].bstep * D.ref_factors;
+            for (int a = 0; a < D.n_assets; a++)
+                if (D.cidx_spot[a] >= 0 && d0 + D.fid_spot[a] < D.sobol_dims) order.push_back(d0 + D.fid_spot[a]);
+            for (int a = 0; a < D.n_assets; a++)
+                if (D.cidx_var[a] >= 0 && d0 + D.fid_var[a] < D.sobol_dims) order.push_back(d0 + D.fid_var[a]);
+        }
+    return order;
+}
+
 // ---------------------------------------------------------------------------
 // plan
 // ---------------------------------------------------------------------------
@@ -339,7 +358,7 @@ struct Plan {
     DevPlan dp{};
     Blob blob;
     // offsets of the sections inside the blob
-    size_t o_steps, o_isd, o_prog, o_nodes, o_recs, o_evr, o_ev, o_lay, o_map, o_levv, o_ginit, o_prod, o_comp;
+    size_t o_steps, o_isd, o_prog, o_nodes, o_recs, o_evr, o_ev, o_lay, o_map, o_levv, o_ginit, o_prod, o_comp, o_sord;
     int variant = 1, T = 256;
     size_t smem = 0;
     int n_products = 0;
@@ -703,6 +722,9 @@ int build_plan(const ThothBookDesc* d, Plan& P)
     }
     if (events.empty()) events.push_back(Event{0, 0, 0.f, 0});
     const std::vector<StepRec> recs = make_recs(bp, isd, ev_flag, F);
+    std::vector<int> order = sobol_order(bp, D);
+    D.n_sobol = (int)order.size();
+    if (order.empty()) order.push_back(0);
 
     // tiles over Sobol indices [skip + 1, skip + paths]
     const int64_t lo = d->sobol_skip + 1, hi = d->sobol_skip + d->paths;
@@ -729,6 +751,7 @@ int build_plan(const ThothBookDesc* d, Plan& P)
     P.o_ginit = P.blob.put(grp_init);
     P.o_prod = P.blob.put(prods);
     P.o_comp = P.blob.put(comps);
+    P.o_sord = P.blob.put(order);
     return THOTH_GPU_OK;
 }
 
@@ -748,8 +771,9 @@ void bind(Plan& P, unsigned char* base)
     D.grp_init = reinterpret_cast<const float*>(base + P.o_ginit);
     D.products = reinterpret_cast<const DevProduct*>(base + P.o_prod);
     D.comps = reinterpret_cast<const Comp*>(base + P.o_comp);
+    D.sobol_order = reinterpret_cast<const int*>(base + P.o_sord);
     D.sobol_v = g_dev.sobol_v;
-    D.sobol_lo = g_dev.sobol_lo;
+    D.sobol_lo = nullptr; // the book's own table: placed by the caller (low_bytes)
     D.cancel = g_dev.cancel_dev;
 }
 
@@ -803,16 +827,26 @@ double trust_of(double s1, double s2, double n)
     return std::sqrt(var / n);
 }
 
-// device layout of one priced book: [plan blob][acc rows][out][status]
+// bytes of a book's low Sobol words in consumption order ([n_sobol][T])
+size_t low_bytes(const Plan& P) { return sizeof(uint32_t) * (size_t)P.dp.n_sobol * P.T; }
+
+// the book's low words from the device-wide table (one small gather kernel)
+cudaError_t gather_low(const Plan& P, cudaStream_t st)
+{
+    return launch_gather_low(g_dev.sobol_lo, P.dp.sobol_order, P.dp.n_sobol, P.T, const_cast<uint32_t*>(P.dp.sobol_lo), st);
+}
+
+// device layout of one priced book: [plan blob][low Sobol words][acc rows][out][status]
 struct Layout {
-    size_t o_acc, o_out, o_st, total;
+    size_t o_lo, o_acc, o_out, o_st, total;
 };
 
 Layout layout_of(const Plan& P, int grid)
 {
     Layout L;
     const size_t n_acc = (size_t)P.dp.n_acc;
-    L.o_acc = (P.blob.bytes.size() + 255) & ~size_t(255);
+    L.o_lo = (P.blob.bytes.size() + 255) & ~size_t(255);
+    L.o_acc = L.o_lo + ((low_bytes(P) + 255) & ~size_t(255));
     L.o_out = L.o_acc + ((sizeof(double) * grid * n_acc + 255) & ~size_t(255));
     L.o_st = L.o_out + ((sizeof(double) * n_acc + 255) & ~size_t(255));
     L.total = L.o_st + 256;
@@ -821,16 +855,18 @@ Layout layout_of(const Plan& P, int grid)
 
 // launch the book kernel and the reduction on a plan already bound to `base`,
 // copy the sums back and finalise the indicators
-int run_bound(Plan& P, unsigned char* base, const Layout& L, int grid, ThothBookResult* out)
+int run_bound(Plan& P, unsigned char* base, const Layout& L, int grid, ThothBookResult* out, bool gather)
 {
     const size_t n_acc = (size_t)P.dp.n_acc;
     cudaStream_t st = g_dev.stream;
     int rc = ensure_pinned(sizeof(double) * n_acc + sizeof(int));
     if (rc) return rc;
+    P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(base + L.o_lo);
     P.dp.acc = reinterpret_cast<double*>(base + L.o_acc);
     P.dp.status = reinterpret_cast<int*>(base + L.o_st);
     CUDA_TRY(cudaMemsetAsync(base + L.o_st, 0, sizeof(int), st));
     CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+    if (gather) CUDA_TRY(gather_low(P, st));
     CUDA_TRY(launch_book(P.dp, P.variant, grid, P.smem, st));
     CUDA_TRY(launch_reduce(P.dp.acc, grid, (int)n_acc, reinterpret_cast<double*>(base + L.o_out), st));
     CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
@@ -881,7 +917,7 @@ int price_locked(const ThothBookDesc* book, ThothBookResult* out)
     std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
     CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, g_dev.stream));
     bind(P, g_dev.arena);
-    rc = run_bound(P, g_dev.arena, L, grid, out);
+    rc = run_bound(P, g_dev.arena, L, grid, out, true);
     if (rc) return rc;
     out->h2d_bytes = (int64_t)P.blob.bytes.size();
     return THOTH_GPU_OK;
@@ -935,7 +971,7 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     if (!build_direction_numbers(V)) return fail(THOTH_GPU_E_INVALID, "embedded Joe-Kuo table is corrupt");
     const int dims = std::max(P.dp.sobol_dims, 1);
     const size_t v_bytes = sizeof(uint32_t) * 32 * (size_t)dims;
-    const size_t lo_bytes = sizeof(uint32_t) * SOBOL_LO_ROW * (size_t)dims;
+    const size_t lo_bytes = std::max(low_bytes(P), sizeof(uint32_t));
     const size_t n_acc = (size_t)P.dp.n_acc;
     auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t o_v = up(P.blob.bytes.size());
@@ -954,7 +990,16 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     const int grid = (int)std::max<int64_t>(1, std::min(std::min(full, fit), P.dp.n_tiles));
     CUDA_TRY(cudaMemcpy(base, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(base + o_v, V.data(), v_bytes, cudaMemcpyHostToDevice));
-    build_low_table(V, dims, lo);
+    {
+        // the book's low words in consumption order, built here rather than gathered
+        std::vector<uint32_t> all;
+        build_low_table(V, dims, all);
+        const int* order = reinterpret_cast<const int*>(P.blob.bytes.data() + P.o_sord);
+        lo.assign(lo_bytes / sizeof(uint32_t), 0u);
+        for (int j = 0; j < P.dp.n_sobol; j++)
+            std::memcpy(lo.data() + (size_t)j * P.T, all.data() + (size_t)order[j] * SOBOL_LO_ROW,
+                        sizeof(uint32_t) * P.T);
+    }
     CUDA_TRY(cudaMemcpy(base + o_lo, lo.data(), lo_bytes, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemset(base + o_st, 0, sizeof(int))); // status must start at zero; the sums are zeroed by the kernel
     bind(P, base);
@@ -1045,6 +1090,7 @@ static int record_batch(std::vector<Plan>& plans, const std::vector<int>& grid, 
         const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
         load[k] += cost(b);
         cudaStream_t s = g_batch.streams[k];
+        CUDA_TRY(gather_low(plans[b], s));
         CUDA_TRY(launch_book(plans[b].dp, plans[b].variant, grid[b], plans[b].smem, s));
         CUDA_TRY(launch_reduce(plans[b].dp.acc, grid[b], plans[b].dp.n_acc,
                                reinterpret_cast<double*>(g_batch.dev + o_out[b]), s));
@@ -1066,7 +1112,7 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
     const int S = std::min(g_batch.streams_wanted, n);
     std::vector<Plan> plans(n);
     std::vector<int> grid(n);
-    std::vector<size_t> o_blob(n), o_acc(n), o_out(n), o_st(n);
+    std::vector<size_t> o_blob(n), o_lo(n), o_acc(n), o_out(n), o_st(n);
     size_t off = 0;
     auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
     std::string sig = std::to_string(n) + ":" + std::to_string(S) + ":" + std::to_string(g_batch.policy);
@@ -1076,6 +1122,8 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
         grid[b] = grid_for(plans[b], g_batch.policy);
         o_blob[b] = off;
         off += up(plans[b].blob.bytes.size());
+        o_lo[b] = off;
+        off += up(low_bytes(plans[b]));
         o_acc[b] = off;
         off += up(sizeof(double) * (size_t)grid[b] * plans[b].dp.n_acc);
         sig += "|" + std::to_string(plans[b].variant) + "," + std::to_string(grid[b]) + "," +
@@ -1116,6 +1164,7 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
     CUDA_TRY(cudaMemcpyAsync(g_batch.dev, g_batch.host, o_outs, cudaMemcpyHostToDevice, st));
     for (int b = 0; b < n; b++) {
         bind(plans[b], g_batch.dev + o_blob[b]);
+        plans[b].dp.sobol_lo = reinterpret_cast<const uint32_t*>(g_batch.dev + o_lo[b]);
         plans[b].dp.acc = reinterpret_cast<double*>(g_batch.dev + o_acc[b]);
         plans[b].dp.status = reinterpret_cast<int*>(g_batch.dev + o_st[b]);
         // the kernel parameters are baked into the graph: a replay needs them byte-equal
@@ -1211,6 +1260,8 @@ static int autotune_book_locked(const ThothBookDesc* book, int reps, ThothTuneRe
     if (rc) return rc;
     CUDA_TRY(cudaMemcpy(g_dev.arena, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
     bind(P, g_dev.arena);
+    P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + L.o_lo);
+    CUDA_TRY(gather_low(P, g_dev.stream));
     P.dp.acc = reinterpret_cast<double*>(g_dev.arena + L.o_acc);
     P.dp.status = reinterpret_cast<int*>(g_dev.arena + L.o_st);
     cudaStream_t st = g_dev.stream;
@@ -1455,6 +1506,14 @@ int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out)
         return fail(THOTH_GPU_E_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
     }
     bind(h->plan, h->dev);
+    h->plan.dp.sobol_lo = reinterpret_cast<const uint32_t*>(h->dev + h->layout.o_lo);
+    e = gather_low(h->plan, g_dev.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g_dev.stream);
+    if (e != cudaSuccess) {
+        cudaFree(h->dev);
+        delete h;
+        return fail(THOTH_GPU_E_CUDA, std::string("gather: ") + cudaGetErrorString(e));
+    }
     *out = h;
     return THOTH_GPU_OK;
 }
@@ -1465,7 +1524,7 @@ int thoth_gpu_book_run(ThothBookHandle* h, ThothBookResult* out)
     std::lock_guard<std::mutex> lk(g_mu);
     int rc = ensure_device();
     if (rc) return rc;
-    return run_bound(h->plan, h->dev, h->layout, h->grid, out);
+    return run_bound(h->plan, h->dev, h->layout, h->grid, out, false);
 }
 
 int thoth_gpu_book_destroy(ThothBookHandle* h)
@@ -1689,8 +1748,13 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
     P.o_prog = P.blob.put(bp.prog);
     P.o_nodes = P.blob.put(bp.nodes);
     P.o_recs = P.blob.put(make_recs(bp, isd, std::vector<char>(), factors));
+    std::vector<int> order = sobol_order(bp, D);
+    D.n_sobol = (int)order.size();
+    P.o_sord = P.blob.put(order);
+    P.T = T;
     const size_t smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, factors, 0, 0);
-    const size_t o_out = (P.blob.bytes.size() + 255) & ~size_t(255);
+    const size_t o_lo = (P.blob.bytes.size() + 255) & ~size_t(255);
+    const size_t o_out = o_lo + ((low_bytes(P) + 255) & ~size_t(255));
     const size_t bytes = sizeof(float) * (size_t)n_paths * factors * N;
     rc = ensure_arena(o_out + bytes + 256);
     if (rc) return rc;
@@ -1703,8 +1767,10 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
     D.nodes = reinterpret_cast<const BridgeNode*>(g_dev.arena + P.o_nodes);
     D.recs = reinterpret_cast<const StepRec*>(g_dev.arena + P.o_recs);
     D.sobol_v = g_dev.sobol_v;
-    D.sobol_lo = g_dev.sobol_lo;
+    D.sobol_order = reinterpret_cast<const int*>(g_dev.arena + P.o_sord);
+    D.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + o_lo);
     float* d_out = reinterpret_cast<float*>(g_dev.arena + o_out);
+    CUDA_TRY(gather_low(P, g_dev.stream));
     const int grid = (int)std::min<int64_t>(D.n_tiles, (int64_t)g_dev.sms * 2);
     CUDA_TRY(launch_bridge(D, grid, smem, d_out, g_dev.stream));
     CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
