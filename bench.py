@@ -193,8 +193,10 @@ def ragged_batch_section(G, steps):
         "device_ms": tuned_ms, "e2e_ms": 1e3 * tuned_wall,
         "e2e_path_steps_per_sec": work / tuned_wall,
         "untuned_device_ms": untuned_ms, "one_book_at_a_time_device_ms": one_ms,
-        "autotune": dict(tune, seconds=tune_s),
-        "gpu_launches_per_batch": 2 * len(books),
+        "autotune": dict(tune, seconds=tune_s,
+                         note="stream count, one launch shape for the single-asset books "
+                              "(-1: each book's default) and grid policy, timed on the batch graph"),
+        "gpu_launches_per_batch": 3 * len(books),  # gather, book kernel, reduction per book
         "books_nonfinite": int(sum(not np.all(np.isfinite(r["premium"])) for r in res)),
     }
 

@@ -241,21 +241,27 @@ int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBook
 /* ---- autotuner (no reference counterpart) ----------------------------------
  * Times candidate launch configurations on the device with CUDA events and
  * keeps the fastest for later calls in this process:
- *  - per book shape (kernel variant, resident CTAs per SM, tiles of 2^TB paths):
- *    the persistent grid, k x SMs for k = 1 .. resident CTAs per SM and the
- *    "balanced" grid of each (same waves, fewest CTAs);
- *  - per batch: the stream count (1 .. 32) and the grid policy of the batch
- *    graph (0 full, 1 balanced, 2 half).
+ *  - per book size, keyed by (kernel variant, ceil(log2 paths), ceil(log2
+ *    steps)): the launch shape of single-asset books (paths per tile 256 or
+ *    128, paths per thread 1 or 2, so 64 to 256 threads per CTA), and the
+ *    persistent grid (k x SMs for k = 1 .. resident CTAs per SM, and the
+ *    "balanced" grid of each: same waves, fewest CTAs);
+ *  - per batch: the stream count (1 .. 32), one launch shape for every
+ *    single-asset book of the batch (or each book's own), and the grid policy
+ *    of the batch graph (0 full, 1 balanced, 2 half).
  * Choices can be saved to and loaded from a small text file, which is tied to
  * the device name and SM count it was measured on (THOTH_GPU_E_UNSUPPORTED
- * when loaded on another device). */
+ * when loaded on another device). Step chunking has no knob here: every step
+ * of a path runs in registers in one pass. */
 typedef struct ThothTuneResult {
     int32_t grid;          /* chosen CTAs (book) */
-    int32_t default_grid;  /* untuned grid: resident CTAs per SM x SMs, capped by tiles */
+    int32_t default_grid;  /* untuned grid: default shape, resident CTAs per SM x SMs, capped by tiles */
     int32_t candidates;    /* configurations timed */
     int32_t streams;       /* chosen stream count (batch) */
-    int32_t policy;        /* chosen grid policy (batch) */
-    int32_t reserved;
+    int32_t policy;        /* chosen grid policy */
+    int32_t shape;         /* chosen launch shape (book; -1 for a batch) */
+    int32_t threads;       /* threads per CTA of the chosen shape */
+    int32_t tile_paths;    /* paths per tile of the chosen shape */
     double best_ms;        /* mean device time of the chosen configuration */
     double default_ms;     /* the same for the untuned configuration */
 } ThothTuneResult;
@@ -302,7 +308,8 @@ int thoth_gpu_bridge_program(const double* t, int32_t n_dates, int32_t* first_co
 /* Host-only test hook: validate a descriptor and report the launch plan.
  * out[0] kernel variant, [1] paths per tile, [2] shared-memory bytes per CTA,
  * [3] observation slots, [4] path groups, [5] bridge stack depth,
- * [6] Sobol dimensions, [7] tiles. Returns the descriptor's status code. */
+ * [6] Sobol dimensions, [7] tiles, [8] launch shape, [9] threads per CTA
+ * (out holds 10 values). Returns the descriptor's status code. */
 int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out);
 
 /* Test hook, no reference counterpart: one tcgen05 BF16 tensor-core GEMM,

@@ -90,24 +90,62 @@ def test_empty_and_invalid_batches(gpu):
     assert len(gpu.price_batch(books)) == 4  # the engine is still usable
 
 
-def test_autotune_book_keeps_parity(gpu):
-    b = W.heston_grid(paths=1 << 16, calendar=True, months=(1, 3, 6), strikes=(90, 100, 110))
+@pytest.mark.parametrize("make", [
+    lambda: W.heston_grid(paths=1 << 16, calendar=True, months=(1, 3, 6), strikes=(90, 100, 110)),
+    lambda: W.gbm_call(paths=1 << 15)])
+def test_autotune_book_keeps_parity(gpu, make, tmp_path):
+    b = make()
     t = gpu.autotune_book(b, reps=2)
-    assert t["candidates"] >= 2 and 1 <= t["grid"]
+    # every launch shape (paths per thread x tile size) and grid was timed; the default is among them
+    assert t["candidates"] >= 8 and 1 <= t["grid"]
+    assert t["shape"] in (0, 1, 2, 3) and t["threads"] in (64, 128, 256) and t["tile_paths"] in (128, 256)
     assert t["best_ms"] <= t["default_ms"] * (1 + 1e-9)
-    r = gpu.price_book(b)
+    plan = gpu.plan_summary(b)
+    assert plan["shape"] == t["shape"] and plan["threads"] == t["threads"] and plan["tile"] == t["tile_paths"]
+    r = gpu.price_book(b, greeks=b.greeks != 0)
     ref = oracle.price_book(b, threads=THREADS)
-    assert_shared_path_parity(r, ref["premium"], ref["trust"], "tuned grid %d" % t["grid"])
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "tuned shape %d grid %d" % (t["shape"], t["grid"]))
+    # the choice survives a save / clear / load round trip
+    path = tmp_path / "tune.txt"
+    gpu.autotune_save(path)
+    assert any(line.startswith("book ") for line in path.read_text().splitlines())
+    gpu.autotune_clear()
+    assert gpu.plan_summary(b)["shape"] == 0
+    gpu.autotune_load(path)
+    assert gpu.plan_summary(b)["shape"] == t["shape"]
+    again = gpu.price_book(b, greeks=b.greeks != 0)
+    np.testing.assert_array_equal(again["premium"], r["premium"])
+
+
+@pytest.mark.parametrize("shape_paths", [(1 << 13) + 77, 1 << 15])
+def test_every_launch_shape_matches_the_oracle(gpu, shape_paths, tmp_path):
+    """Force each launch shape through an autotune file and check parity on shared paths."""
+    import math
+    b = W.heston_grid(paths=shape_paths, calendar=True, months=(1, 2), strikes=(90, 100, 110))
+    n = b.desc().n_dates - 1
+    key = "book 1 %d %d" % (math.ceil(math.log2(shape_paths)), math.ceil(math.log2(n)))
+    base = tmp_path / "base.txt"
+    gpu.autotune_save(base)                 # header lines of this device, nothing tuned
+    ref = oracle.price_book(b, threads=THREADS)
+    for shape in range(4):
+        f = tmp_path / ("s%d.txt" % shape)
+        f.write_text(base.read_text() + "%s %d 0 0\n" % (key, shape))
+        gpu.autotune_clear()
+        gpu.autotune_load(f)
+        assert gpu.plan_summary(b)["shape"] == shape
+        r = gpu.price_book(b)
+        assert_shared_path_parity(r, ref["premium"], ref["trust"], "shape %d" % shape)
 
 
 def test_autotune_batch_save_load(gpu, tmp_path):
     books = small_batch(n=16, seed=21)
     t = gpu.autotune_batch(books, reps=1)
-    assert t["streams"] in (1, 2, 4, 8, 16) and t["policy"] in (0, 1, 2) and t["candidates"] >= 3
+    assert t["streams"] in (1, 2, 4, 8, 16) and t["policy"] in (0, 1, 2) and t["shape"] in (-1, 0, 1, 2, 3)
+    assert t["candidates"] >= 10
     path = tmp_path / "tune.txt"
     gpu.autotune_save(path)
     text = path.read_text().splitlines()
-    assert text[0] == "thoth-autotune 1" and text[2] == "batch %d %d" % (t["streams"], t["policy"])
+    assert text[0] == "thoth-autotune 1" and text[2] == "batch %d %d %d" % (t["streams"], t["policy"], t["shape"])
     tuned = gpu.price_batch(books)
     gpu.autotune_clear()
     gpu.autotune_load(path)

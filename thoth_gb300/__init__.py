@@ -132,7 +132,8 @@ def set_batch_streams(n):
 
 def _tune_dict(r):
     return dict(grid=r.grid, default_grid=r.default_grid, candidates=r.candidates, streams=r.streams,
-                policy=r.policy, best_ms=r.best_ms, default_ms=r.default_ms)
+                policy=r.policy, shape=r.shape, threads=r.threads, tile_paths=r.tile_paths, best_ms=r.best_ms,
+                default_ms=r.default_ms)
 
 
 def autotune_book(book, reps=3):
@@ -266,7 +267,7 @@ def bridge_program(t):
 def plan_summary(book):
     """Host-only: validate a book and return its launch plan as a dict."""
     d = book.desc()
-    out = np.zeros(8, dtype=np.int64)
+    out = np.zeros(10, dtype=np.int64)
     _check(lib().thoth_gpu_plan_summary(C.byref(d), out.ctypes.data_as(C.POINTER(C.c_int64))))
-    keys = ("variant", "tile", "smem", "slots", "groups", "stack_depth", "sobol_dims", "tiles")
+    keys = ("variant", "tile", "smem", "slots", "groups", "stack_depth", "sobol_dims", "tiles", "shape", "threads")
     return dict(zip(keys, (int(v) for v in out)))

@@ -327,7 +327,7 @@ __device__ __forceinline__ StepRec load_rec(const DevPlan& P, int i)
 //   UNIFORM every step has the same per-asset constants (kept in registers)
 // ---------------------------------------------------------------------------
 template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-__global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? (PP == 2 ? 6 : 3) : 1) book_kernel(const DevPlan P)
+__global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / PP) : 1) book_kernel(const DevPlan P)
 {
     constexpr int T = 1 << TB;  // paths per tile
     constexpr int TH = T / PP;  // threads per CTA; path p of thread t is tile column t + p * TH
@@ -718,8 +718,18 @@ cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st)
 }
 
 // ---- launch wrappers --------------------------------------------------------
-// paths per thread of the single-asset variants (the mixed variant keeps one)
-constexpr int PP1 = 2;
+// Launch shapes. Single-asset variants come in four: (log2 paths per tile,
+// paths per thread) = (8, 2), (8, 1), (7, 1), (7, 2), i.e. 128, 256, 128 and 64
+// threads per CTA, each bounded to 768 resident threads per SM worth of
+// registers; the autotuner picks one per book size. The mixed variant has one:
+// (7, 1).
+constexpr int N_SHAPES = 4;
+constexpr int SHAPE_TB[N_SHAPES] = {8, 8, 7, 7};
+constexpr int SHAPE_PP[N_SHAPES] = {2, 1, 1, 2};
+
+int book_shape_count(int variant) { return variant == 3 ? 1 : N_SHAPES; }
+int book_shape_tile_bits(int variant, int shape) { return variant == 3 ? 7 : SHAPE_TB[shape]; }
+int book_shape_threads(int variant, int shape) { return variant == 3 ? 128 : (1 << SHAPE_TB[shape]) / SHAPE_PP[shape]; }
 
 template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
 static cudaError_t smem_attr_t()
@@ -749,23 +759,6 @@ static cudaError_t launch_book_t(const DevPlan& P, int grid, size_t smem, cudaSt
     return cudaGetLastError();
 }
 
-// variants: 0 GBM, 1 Heston, 2 LSV (single asset, per-step constants),
-//           3 mixed multi-asset, 4 Heston with uniform steps, 5 GBM with uniform steps
-cudaError_t launch_book(const DevPlan& P, int variant, int grid, size_t smem, cudaStream_t st)
-{
-    switch (variant) {
-    case 0: return launch_book_t<8, 1, M_GBM, false, PP1>(P, grid, smem, st);
-    case 1: return launch_book_t<8, 1, M_HESTON, false, PP1>(P, grid, smem, st);
-    case 2: return launch_book_t<8, 1, M_LSV, false, PP1>(P, grid, smem, st);
-    case 3: return launch_book_t<7, MAX_ASSETS, M_MIXED, false, 1>(P, grid, smem, st);
-    case 4: return launch_book_t<8, 1, M_HESTON, true, PP1>(P, grid, smem, st);
-    case 5: return launch_book_t<8, 1, M_GBM, true, PP1>(P, grid, smem, st);
-    default: return cudaErrorInvalidValue;
-    }
-}
-
-int book_variant_tile_bits(int variant) { return variant == 3 ? 7 : 8; }
-
 template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
 static int occ_t(size_t smem)
 {
@@ -776,19 +769,64 @@ static int occ_t(size_t smem)
     return n < 1 ? 1 : n;
 }
 
-// resident CTAs per SM of a variant at a given dynamic shared-memory size
-int book_occupancy(int variant, size_t smem)
+// one single-asset model in each of the four shapes: launch (grid > 0) or occupancy (grid == 0)
+template <int MODEL, bool UNIFORM>
+static int single_t(const DevPlan* P, int shape, int grid, size_t smem, cudaStream_t st, cudaError_t* err)
 {
-    switch (variant) {
-    case 0: return occ_t<8, 1, M_GBM, false, PP1>(smem);
-    case 1: return occ_t<8, 1, M_HESTON, false, PP1>(smem);
-    case 2: return occ_t<8, 1, M_LSV, false, PP1>(smem);
-    case 3: return occ_t<7, MAX_ASSETS, M_MIXED, false, 1>(smem);
-    case 4: return occ_t<8, 1, M_HESTON, true, PP1>(smem);
-    case 5: return occ_t<8, 1, M_GBM, true, PP1>(smem);
-    default: return 1;
+    switch (shape) {
+    case 0:
+        if (grid) *err = launch_book_t<8, 1, MODEL, UNIFORM, 2>(*P, grid, smem, st);
+        return grid ? 0 : occ_t<8, 1, MODEL, UNIFORM, 2>(smem);
+    case 1:
+        if (grid) *err = launch_book_t<8, 1, MODEL, UNIFORM, 1>(*P, grid, smem, st);
+        return grid ? 0 : occ_t<8, 1, MODEL, UNIFORM, 1>(smem);
+    case 2:
+        if (grid) *err = launch_book_t<7, 1, MODEL, UNIFORM, 1>(*P, grid, smem, st);
+        return grid ? 0 : occ_t<7, 1, MODEL, UNIFORM, 1>(smem);
+    default:
+        if (grid) *err = launch_book_t<7, 1, MODEL, UNIFORM, 2>(*P, grid, smem, st);
+        return grid ? 0 : occ_t<7, 1, MODEL, UNIFORM, 2>(smem);
     }
 }
+
+static int dispatch(const DevPlan* P, int variant, int shape, int grid, size_t smem, cudaStream_t st, cudaError_t* err)
+{
+    *err = cudaSuccess;
+    if (variant != 3 && (shape < 0 || shape >= N_SHAPES)) {
+        *err = cudaErrorInvalidValue;
+        return 1;
+    }
+    switch (variant) {
+    case 0: return single_t<M_GBM, false>(P, shape, grid, smem, st, err);
+    case 1: return single_t<M_HESTON, false>(P, shape, grid, smem, st, err);
+    case 2: return single_t<M_LSV, false>(P, shape, grid, smem, st, err);
+    case 3:
+        if (grid) *err = launch_book_t<7, MAX_ASSETS, M_MIXED, false, 1>(*P, grid, smem, st);
+        return grid ? 0 : occ_t<7, MAX_ASSETS, M_MIXED, false, 1>(smem);
+    case 4: return single_t<M_HESTON, true>(P, shape, grid, smem, st, err);
+    case 5: return single_t<M_GBM, true>(P, shape, grid, smem, st, err);
+    default: *err = cudaErrorInvalidValue; return 1;
+    }
+}
+
+// variants: 0 GBM, 1 Heston, 2 LSV (single asset, per-step constants),
+//           3 mixed multi-asset, 4 Heston with uniform steps, 5 GBM with uniform steps
+cudaError_t launch_book(const DevPlan& P, int variant, int shape, int grid, size_t smem, cudaStream_t st)
+{
+    if (grid < 1) return cudaErrorInvalidValue;
+    cudaError_t e;
+    dispatch(&P, variant, shape, grid, smem, st, &e);
+    return e;
+}
+
+// resident CTAs per SM of a variant and shape at a given dynamic shared-memory size
+int book_occupancy(int variant, int shape, size_t smem)
+{
+    cudaError_t e;
+    const int n = dispatch(nullptr, variant, shape, 0, smem, 0, &e);
+    return e == cudaSuccess ? n : 1;
+}
+
 size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups)
 {
     return smem_bytes(T, sobol_dims, stack_depth, nfa, n_slots, n_groups);

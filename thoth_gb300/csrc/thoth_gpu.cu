@@ -21,9 +21,11 @@
 #include <vector>
 
 namespace thoth {
-cudaError_t launch_book(const DevPlan& P, int variant, int grid, size_t smem, cudaStream_t st);
-int book_variant_tile_bits(int variant);
-int book_occupancy(int variant, size_t smem);
+cudaError_t launch_book(const DevPlan& P, int variant, int shape, int grid, size_t smem, cudaStream_t st);
+int book_shape_count(int variant);
+int book_shape_tile_bits(int variant, int shape);
+int book_shape_threads(int variant, int shape);
+int book_occupancy(int variant, int shape, size_t smem);
 size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups);
 cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st);
 cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64_t n_points, uint32_t* out,
@@ -352,6 +354,26 @@ std::vector<int> sobol_order(const BridgeProgram& bp, const DevPlan& D)
 }
 
 // ---------------------------------------------------------------------------
+// autotuned launch choices, keyed by book size: (kernel variant before the
+// uniform-step promotion, ceil(log2 paths), ceil(log2 steps)) -> (launch shape,
+// CTAs per SM, grid policy); filled by the autotuner or an autotune file
+// ---------------------------------------------------------------------------
+using TuneKey = std::tuple<int, int, int>;
+struct TuneChoice {
+    int shape = 0, per_sm = 0, policy = 0;
+};
+std::map<TuneKey, TuneChoice> g_tuned;
+
+int ceil_log2(int64_t x)
+{
+    int k = 0;
+    while (((int64_t)1 << k) < x && k < 62) k++;
+    return k;
+}
+
+TuneKey tune_key(int base_variant, int64_t paths, int steps) { return TuneKey(base_variant, ceil_log2(paths), ceil_log2(steps)); }
+
+// ---------------------------------------------------------------------------
 // plan
 // ---------------------------------------------------------------------------
 struct Plan {
@@ -359,7 +381,7 @@ struct Plan {
     Blob blob;
     // offsets of the sections inside the blob
     size_t o_steps, o_isd, o_prog, o_nodes, o_recs, o_evr, o_ev, o_lay, o_map, o_levv, o_ginit, o_prod, o_comp, o_sord;
-    int variant = 1, T = 256;
+    int variant = 1, base_variant = 1, shape = 0, T = 256;
     size_t smem = 0;
     int n_products = 0;
     int64_t paths = 0;
@@ -368,7 +390,8 @@ struct Plan {
 
 bool finite(double x) { return std::isfinite(x); }
 
-int build_plan(const ThothBookDesc* d, Plan& P)
+// shape < 0: the autotuned shape for the book's size, else the default (0)
+int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
 {
     if (!d) return fail(THOTH_GPU_E_INVALID, "null descriptor");
     const int nd = d->n_dates, N = nd - 1, NA = d->n_assets;
@@ -461,7 +484,14 @@ int build_plan(const ThothBookDesc* d, Plan& P)
         P.variant = 3;
     }
     if (D.corr && P.variant != 3) P.variant = 3;
-    P.T = 1 << book_variant_tile_bits(P.variant);
+    P.base_variant = P.variant;
+    if (shape < 0) {
+        auto it = g_tuned.find(tune_key(P.variant, d->paths, N));
+        shape = it != g_tuned.end() ? it->second.shape : 0;
+    }
+    if (shape >= book_shape_count(P.variant)) shape = 0;
+    P.shape = shape;
+    P.T = 1 << book_shape_tile_bits(P.variant, shape);
     const int T = P.T;
     (void)mixed;
 
@@ -777,14 +807,14 @@ void bind(Plan& P, unsigned char* base)
     D.cancel = g_dev.cancel_dev;
 }
 
-// resident CTAs per SM of a plan's kernel variant (cached per variant and shared-memory size)
+// resident CTAs per SM of a plan's kernel (cached per variant, shape and shared-memory size)
 int occupancy_of(const Plan& P)
 {
-    static std::map<std::pair<int, size_t>, int> occ;
-    auto key = std::make_pair(P.variant, P.smem);
+    static std::map<std::tuple<int, int, size_t>, int> occ;
+    auto key = std::make_tuple(P.variant, P.shape, P.smem);
     auto it = occ.find(key);
     if (it != occ.end()) return it->second;
-    const int per_sm = book_occupancy(P.variant, P.smem);
+    const int per_sm = book_occupancy(P.variant, P.shape, P.smem);
     occ[key] = per_sm;
     return per_sm;
 }
@@ -806,16 +836,17 @@ int grid_policy(int64_t tiles, int64_t full, int policy)
     return (int)std::max<int64_t>(g, 1);
 }
 
-// autotuned grids, keyed by (variant, resident CTAs per SM, tiles)
-using TuneKey = std::tuple<int, int, int64_t>;
-std::map<TuneKey, int> g_tuned;
-
+// persistent grid of a plan: the autotuned choice for the book's size when the
+// plan runs in the tuned shape and no other policy is asked for, else `policy`
 int grid_for(const Plan& P, int policy = 0)
 {
     const int per_sm = occupancy_of(P);
     if (policy == 0) {
-        auto it = g_tuned.find(TuneKey(P.variant, per_sm, P.dp.n_tiles));
-        if (it != g_tuned.end()) return (int)std::min<int64_t>(it->second, std::max<int64_t>(P.dp.n_tiles, 1));
+        auto it = g_tuned.find(tune_key(P.base_variant, P.paths, P.dp.n_steps));
+        if (it != g_tuned.end() && it->second.shape == P.shape) {
+            const int k = it->second.per_sm > 0 ? std::min(it->second.per_sm, per_sm) : per_sm;
+            return grid_policy(P.dp.n_tiles, (int64_t)k * g_dev.sms, it->second.policy);
+        }
     }
     return grid_policy(P.dp.n_tiles, (int64_t)per_sm * g_dev.sms, policy);
 }
@@ -867,7 +898,7 @@ int run_bound(Plan& P, unsigned char* base, const Layout& L, int grid, ThothBook
     CUDA_TRY(cudaMemsetAsync(base + L.o_st, 0, sizeof(int), st));
     CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
     if (gather) CUDA_TRY(gather_low(P, st));
-    CUDA_TRY(launch_book(P.dp, P.variant, grid, P.smem, st));
+    CUDA_TRY(launch_book(P.dp, P.variant, P.shape, grid, P.smem, st));
     CUDA_TRY(launch_reduce(P.dp.acc, grid, (int)n_acc, reinterpret_cast<double*>(base + L.o_out), st));
     CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
     CUDA_TRY(cudaMemcpyAsync(g_dev.pinned, base + L.o_out, sizeof(double) * n_acc, cudaMemcpyDeviceToHost, st));
@@ -986,7 +1017,7 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
                                                std::to_string((size_t)THOTH_NOALLOC_SCRATCH_BYTES));
     // as many CTA rows of FP64 sums as the array still holds (at most the normal persistent grid)
     const int64_t fit = (int64_t)((THOTH_NOALLOC_SCRATCH_BYTES - o_acc) / row);
-    const int64_t full = (int64_t)book_occupancy(P.variant, P.smem) * prop.multiProcessorCount;
+    const int64_t full = (int64_t)book_occupancy(P.variant, P.shape, P.smem) * prop.multiProcessorCount;
     const int grid = (int)std::max<int64_t>(1, std::min(std::min(full, fit), P.dp.n_tiles));
     CUDA_TRY(cudaMemcpy(base, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(base + o_v, V.data(), v_bytes, cudaMemcpyHostToDevice));
@@ -1008,7 +1039,7 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     P.dp.cancel = nullptr;
     P.dp.acc = reinterpret_cast<double*>(base + o_acc);
     P.dp.status = reinterpret_cast<int*>(base + o_st);
-    CUDA_TRY(launch_book(P.dp, P.variant, grid, P.smem, 0));
+    CUDA_TRY(launch_book(P.dp, P.variant, P.shape, grid, P.smem, 0));
     CUDA_TRY(launch_reduce(P.dp.acc, grid, (int)n_acc, reinterpret_cast<double*>(base + o_out), 0));
     std::vector<double> o(n_acc);
     int status = 0;
@@ -1044,6 +1075,7 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
 struct BatchCache {
     int streams_wanted = 8;
     int policy = 0; // grid policy of every book in the batch (grid_policy)
+    int shape = -1; // launch shape of every single-asset book (-1: each book's tuned or default shape)
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
     cudaGraphExec_t exec = nullptr;
@@ -1091,7 +1123,7 @@ static int record_batch(std::vector<Plan>& plans, const std::vector<int>& grid, 
         load[k] += cost(b);
         cudaStream_t s = g_batch.streams[k];
         CUDA_TRY(gather_low(plans[b], s));
-        CUDA_TRY(launch_book(plans[b].dp, plans[b].variant, grid[b], plans[b].smem, s));
+        CUDA_TRY(launch_book(plans[b].dp, plans[b].variant, plans[b].shape, grid[b], plans[b].smem, s));
         CUDA_TRY(launch_reduce(plans[b].dp.acc, grid[b], plans[b].dp.n_acc,
                                reinterpret_cast<double*>(g_batch.dev + o_out[b]), s));
     }
@@ -1115,9 +1147,10 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
     std::vector<size_t> o_blob(n), o_lo(n), o_acc(n), o_out(n), o_st(n);
     size_t off = 0;
     auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
-    std::string sig = std::to_string(n) + ":" + std::to_string(S) + ":" + std::to_string(g_batch.policy);
+    std::string sig = std::to_string(n) + ":" + std::to_string(S) + ":" + std::to_string(g_batch.policy) + ":" +
+                      std::to_string(g_batch.shape);
     for (int b = 0; b < n; b++) {
-        rc = build_plan(&books[b], plans[b]);
+        rc = build_plan(&books[b], plans[b], g_batch.shape);
         if (rc) return fail(rc, "book " + std::to_string(b) + ": " + g_err);
         grid[b] = grid_for(plans[b], g_batch.policy);
         o_blob[b] = off;
@@ -1126,7 +1159,8 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
         off += up(low_bytes(plans[b]));
         o_acc[b] = off;
         off += up(sizeof(double) * (size_t)grid[b] * plans[b].dp.n_acc);
-        sig += "|" + std::to_string(plans[b].variant) + "," + std::to_string(grid[b]) + "," +
+        sig += "|" + std::to_string(plans[b].variant) + "," + std::to_string(plans[b].shape) + "," +
+               std::to_string(grid[b]) + "," +
                std::to_string(plans[b].smem) + "," + std::to_string(plans[b].blob.bytes.size()) + "," +
                std::to_string(plans[b].dp.n_acc) + "," + std::to_string(plans[b].dp.n_tiles);
     }
@@ -1240,62 +1274,85 @@ static int autotune_book_locked(const ThothBookDesc* book, int reps, ThothTuneRe
 {
     int rc = ensure_device();
     if (rc) return rc;
-    Plan P;
-    rc = build_plan(book, P);
-    if (rc) return rc;
-    const int per_sm = occupancy_of(P);
-    const int64_t tiles = P.dp.n_tiles;
-    std::vector<int> cand;
-    for (int k = 1; k <= per_sm; k++) {
-        const int64_t full = (int64_t)k * g_dev.sms;
-        for (int pol = 0; pol < 2; pol++) {
-            const int g = grid_policy(tiles, full, pol);
-            if (std::find(cand.begin(), cand.end(), g) == cand.end()) cand.push_back(g);
-        }
-    }
-    const int def = grid_policy(tiles, (int64_t)per_sm * g_dev.sms, 0);
-    const int gmax = *std::max_element(cand.begin(), cand.end());
-    const Layout L = layout_of(P, gmax);
-    rc = ensure_arena(L.total);
-    if (rc) return rc;
-    CUDA_TRY(cudaMemcpy(g_dev.arena, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
-    bind(P, g_dev.arena);
-    P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + L.o_lo);
-    CUDA_TRY(gather_low(P, g_dev.stream));
-    P.dp.acc = reinterpret_cast<double*>(g_dev.arena + L.o_acc);
-    P.dp.status = reinterpret_cast<int*>(g_dev.arena + L.o_st);
     cudaStream_t st = g_dev.stream;
     double best = 1e300, def_ms = 0;
-    int best_g = def;
-    for (int g : cand) {
-        CUDA_TRY(cudaMemsetAsync(g_dev.arena + L.o_st, 0, sizeof(int), st));
-        CUDA_TRY(launch_book(P.dp, P.variant, g, P.smem, st)); // warm-up
-        CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
-        for (int r = 0; r < reps; r++) {
-            CUDA_TRY(launch_book(P.dp, P.variant, g, P.smem, st));
-            CUDA_TRY(launch_reduce(P.dp.acc, g, P.dp.n_acc, reinterpret_cast<double*>(g_dev.arena + L.o_out), st));
-        }
-        CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
-        CUDA_TRY(cudaStreamSynchronize(st));
-        int status = 0;
-        CUDA_TRY(cudaMemcpy(&status, g_dev.arena + L.o_st, sizeof(int), cudaMemcpyDeviceToHost));
-        if (status == 1) return fail(THOTH_GPU_E_CANCELLED, "autotune cancelled");
-        float ms = 0;
-        CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
-        const double per = ms / reps;
-        if (g == def) def_ms = per;
-        if (per < best) {
-            best = per;
-            best_g = g;
+    int best_g = 1, def_g = 1, count = 0;
+    TuneChoice choice;
+    TuneKey key;
+    Plan best_plan;
+    for (int shape = 0;; shape++) {
+        Plan P;
+        rc = build_plan(book, P, shape);
+        if (rc) return rc;
+        if (shape >= book_shape_count(P.variant)) break;
+        key = tune_key(P.base_variant, P.paths, P.dp.n_steps);
+        const int per_sm = occupancy_of(P);
+        const int64_t tiles = P.dp.n_tiles;
+        // candidates: k x SMs for k = 1 .. resident CTAs per SM, and the balanced grid of each
+        std::vector<std::pair<int, int>> cand; // (k, policy)
+        std::vector<int> grids;
+        for (int k = 1; k <= per_sm; k++)
+            for (int pol = 0; pol < 2; pol++) {
+                const int g = grid_policy(tiles, (int64_t)k * g_dev.sms, pol);
+                if (std::find(grids.begin(), grids.end(), g) == grids.end()) {
+                    grids.push_back(g);
+                    cand.push_back({k, pol});
+                }
+            }
+        const int gmax = *std::max_element(grids.begin(), grids.end());
+        const Layout L = layout_of(P, gmax);
+        rc = ensure_arena(L.total);
+        if (rc) return rc;
+        CUDA_TRY(cudaMemcpy(g_dev.arena, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
+        bind(P, g_dev.arena);
+        P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + L.o_lo);
+        CUDA_TRY(gather_low(P, st));
+        P.dp.acc = reinterpret_cast<double*>(g_dev.arena + L.o_acc);
+        P.dp.status = reinterpret_cast<int*>(g_dev.arena + L.o_st);
+        for (size_t c = 0; c < grids.size(); c++) {
+            const int g = grids[c];
+            CUDA_TRY(cudaMemsetAsync(g_dev.arena + L.o_st, 0, sizeof(int), st));
+            CUDA_TRY(launch_book(P.dp, P.variant, P.shape, g, P.smem, st)); // warm-up
+            CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+            for (int r = 0; r < reps; r++) {
+                CUDA_TRY(launch_book(P.dp, P.variant, P.shape, g, P.smem, st));
+                CUDA_TRY(launch_reduce(P.dp.acc, g, P.dp.n_acc, reinterpret_cast<double*>(g_dev.arena + L.o_out), st));
+            }
+            CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            int status = 0;
+            CUDA_TRY(cudaMemcpy(&status, g_dev.arena + L.o_st, sizeof(int), cudaMemcpyDeviceToHost));
+            if (status == 1) return fail(THOTH_GPU_E_CANCELLED, "autotune cancelled");
+            float ms = 0;
+            CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+            const double per = ms / reps;
+            count++;
+            if (shape == 0 && g == grid_policy(tiles, (int64_t)per_sm * g_dev.sms, 0)) { // the untuned launch
+                def_ms = per;
+                def_g = g;
+            }
+            if (per < best) {
+                best = per;
+                best_g = g;
+                choice.shape = shape;
+                choice.per_sm = cand[c].first;
+                choice.policy = cand[c].second;
+                best_plan.variant = P.variant;
+                best_plan.shape = P.shape;
+                best_plan.T = P.T;
+            }
         }
     }
-    g_tuned[TuneKey(P.variant, per_sm, tiles)] = best_g;
+    g_tuned[key] = choice;
     if (out) {
         out->grid = best_g;
-        out->default_grid = def;
-        out->candidates = (int32_t)cand.size();
+        out->default_grid = def_g;
+        out->candidates = count;
         out->streams = 0;
-        out->policy = 0;
+        out->policy = choice.policy;
+        out->shape = choice.shape;
+        out->threads = book_shape_threads(best_plan.variant, best_plan.shape);
+        out->tile_paths = best_plan.T;
         out->best_ms = best;
         out->default_ms = def_ms;
     }
@@ -1306,10 +1363,11 @@ static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, Th
 {
     std::vector<ThothBookResult> res(std::max(n, 1));
     std::memset(res.data(), 0, sizeof(ThothBookResult) * res.size());
-    const int keep_s = g_batch.streams_wanted, keep_p = g_batch.policy;
-    auto time_one = [&](int S, int pol, double* ms) {
+    const int keep_s = g_batch.streams_wanted, keep_p = g_batch.policy, keep_h = g_batch.shape;
+    auto time_one = [&](int S, int pol, int shape, double* ms) {
         g_batch.streams_wanted = S;
         g_batch.policy = pol;
+        g_batch.shape = shape;
         int rc = price_batch_locked(books, n, res.data()); // capture + warm-up
         if (rc) return rc;
         double sum = 0;
@@ -1322,16 +1380,19 @@ static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, Th
         return THOTH_GPU_OK;
     };
     double best = 1e300, def_ms = 0;
-    int best_s = keep_s, best_p = 0, count = 0;
+    int best_s = keep_s, best_p = 0, best_h = -1, count = 0;
+    auto restore = [&](int rc) {
+        g_batch.streams_wanted = keep_s;
+        g_batch.policy = keep_p;
+        g_batch.shape = keep_h;
+        return rc;
+    };
+    // 1. stream count, with each book's own shape and the full grid
     for (int S : {1, 2, 4, 8, 16, 32}) {
         if (S > std::max(n, 1) && S != 1) break;
         double ms;
-        const int rc = time_one(S, 0, &ms);
-        if (rc) {
-            g_batch.streams_wanted = keep_s;
-            g_batch.policy = keep_p;
-            return rc;
-        }
+        const int rc = time_one(S, 0, -1, &ms);
+        if (rc) return restore(rc);
         count++;
         if (S == 8 || (n < 8 && S == 1)) def_ms = ms;
         if (ms < best) {
@@ -1339,14 +1400,22 @@ static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, Th
             best_s = S;
         }
     }
+    // 2. one launch shape for every single-asset book
+    for (int h = 0; h < 4; h++) {
+        double ms;
+        const int rc = time_one(best_s, 0, h, &ms);
+        if (rc) return restore(rc);
+        count++;
+        if (ms < best) {
+            best = ms;
+            best_h = h;
+        }
+    }
+    // 3. grid policy
     for (int pol : {1, 2}) {
         double ms;
-        const int rc = time_one(best_s, pol, &ms);
-        if (rc) {
-            g_batch.streams_wanted = keep_s;
-            g_batch.policy = keep_p;
-            return rc;
-        }
+        const int rc = time_one(best_s, pol, best_h, &ms);
+        if (rc) return restore(rc);
         count++;
         if (ms < best) {
             best = ms;
@@ -1355,12 +1424,16 @@ static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, Th
     }
     g_batch.streams_wanted = best_s;
     g_batch.policy = best_p;
+    g_batch.shape = best_h;
     if (out) {
         out->grid = 0;
         out->default_grid = 0;
         out->candidates = count;
         out->streams = best_s;
         out->policy = best_p;
+        out->shape = best_h;
+        out->threads = 0;
+        out->tile_paths = 0;
         out->best_ms = best;
         out->default_ms = def_ms;
     }
@@ -1375,10 +1448,10 @@ static int autotune_save_locked(const char* path)
     FILE* f = std::fopen(path, "w");
     if (!f) return fail(THOTH_GPU_E_INVALID, std::string("cannot write ") + path);
     std::fprintf(f, "thoth-autotune 1\ndevice %d %s\n", g_dev.sms, g_dev.name.c_str());
-    std::fprintf(f, "batch %d %d\n", g_batch.streams_wanted, g_batch.policy);
+    std::fprintf(f, "batch %d %d %d\n", g_batch.streams_wanted, g_batch.policy, g_batch.shape);
     for (const auto& kv : g_tuned)
-        std::fprintf(f, "grid %d %d %lld %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
-                     (long long)std::get<2>(kv.first), kv.second);
+        std::fprintf(f, "book %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
+                     kv.second.shape, kv.second.per_sm, kv.second.policy);
     const bool ok = std::fclose(f) == 0;
     return ok ? THOTH_GPU_OK : fail(THOTH_GPU_E_INVALID, std::string("cannot write ") + path);
 }
@@ -1392,29 +1465,34 @@ static int autotune_load_locked(const char* path)
     char line[512];
     int version = 0, sms = -1;
     std::string name;
-    std::map<TuneKey, int> grids;
-    int streams = g_batch.streams_wanted, policy = g_batch.policy;
+    std::map<TuneKey, TuneChoice> books;
+    int streams = g_batch.streams_wanted, policy = g_batch.policy, bshape = g_batch.shape;
     bool bad = false;
     while (std::fgets(line, sizeof line, f)) {
-        int a, b, g;
-        long long t;
+        int a, b, c, e, g, h;
         char nm[400];
         if (std::sscanf(line, "thoth-autotune %d", &a) == 1) version = a;
         else if (std::sscanf(line, "device %d %399[^\n]", &a, nm) == 2) { sms = a; name = nm; }
-        else if (std::sscanf(line, "batch %d %d", &a, &b) == 2) { streams = a; policy = b; }
-        else if (std::sscanf(line, "grid %d %d %lld %d", &a, &b, &t, &g) == 4) {
-            if (g < 1 || t < 1) bad = true;
-            grids[TuneKey(a, b, (int64_t)t)] = g;
+        else if (std::sscanf(line, "batch %d %d %d", &a, &b, &c) == 3) { streams = a; policy = b; bshape = c; }
+        else if (std::sscanf(line, "batch %d %d", &a, &b) == 2) { streams = a; policy = b; bshape = -1; }
+        else if (std::sscanf(line, "book %d %d %d %d %d %d", &a, &b, &c, &e, &g, &h) == 6) {
+            if (a < 0 || a > 5 || e < 0 || e >= book_shape_count(a) || g < 0 || h < 0 || h > 1) bad = true;
+            TuneChoice ch;
+            ch.shape = e;
+            ch.per_sm = g;
+            ch.policy = h;
+            books[TuneKey(a, b, c)] = ch;
         } else if (line[0] != '\n') bad = true;
     }
     std::fclose(f);
-    if (version != 1 || bad || streams < 1 || streams > 64 || policy < 0 || policy > 2)
+    if (version != 1 || bad || streams < 1 || streams > 64 || policy < 0 || policy > 2 || bshape < -1 || bshape > 3)
         return fail(THOTH_GPU_E_INVALID, std::string("malformed autotune file ") + path);
     if (sms != g_dev.sms || name != g_dev.name)
         return fail(THOTH_GPU_E_UNSUPPORTED, "autotune file was measured on another device (" + name + ")");
-    for (const auto& kv : grids) g_tuned[kv.first] = kv.second;
+    for (const auto& kv : books) g_tuned[kv.first] = kv.second;
     g_batch.streams_wanted = streams;
     g_batch.policy = policy;
+    g_batch.shape = bshape;
     return THOTH_GPU_OK;
 }
 
@@ -1471,6 +1549,7 @@ int thoth_gpu_autotune_clear(void)
     g_tuned.clear();
     g_batch.streams_wanted = 8;
     g_batch.policy = 0;
+    g_batch.shape = -1;
     return THOTH_GPU_OK;
 }
 
@@ -1850,6 +1929,8 @@ int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out)
     out[5] = P.dp.stack_depth;
     out[6] = P.dp.sobol_dims;
     out[7] = P.dp.n_tiles;
+    out[8] = P.shape;
+    out[9] = book_shape_threads(P.variant, P.shape);
     return THOTH_GPU_OK;
 }
 
