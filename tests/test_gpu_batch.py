@@ -117,13 +117,18 @@ def test_autotune_book_keeps_parity(gpu, make, tmp_path):
     np.testing.assert_array_equal(again["premium"], r["premium"])
 
 
-@pytest.mark.parametrize("shape_paths", [(1 << 13) + 77, 1 << 15])
-def test_every_launch_shape_matches_the_oracle(gpu, shape_paths, tmp_path):
-    """Force each launch shape through an autotune file and check parity on shared paths."""
+@pytest.mark.parametrize("variant,shape_paths", [(1, (1 << 13) + 77), (1, 1 << 15), (6, (1 << 12) + 5)])
+def test_every_launch_shape_matches_the_oracle(gpu, variant, shape_paths, tmp_path):
+    """Force each launch shape through an autotune file and check parity on shared paths:
+    variant 1 a Heston calendar grid, variant 6 the multi-asset LSV book (assets in turn)."""
     import math
-    b = W.heston_grid(paths=shape_paths, calendar=True, months=(1, 2), strikes=(90, 100, 110))
+    if variant == 1:
+        b = W.heston_grid(paths=shape_paths, calendar=True, months=(1, 2), strikes=(90, 100, 110))
+    else:
+        b = W.lsv_book(paths=shape_paths)
+    assert gpu.plan_summary(b)["variant"] in (variant, 4)
     n = b.desc().n_dates - 1
-    key = "book 1 %d %d" % (math.ceil(math.log2(shape_paths)), math.ceil(math.log2(n)))
+    key = "book %d %d %d" % (variant, math.ceil(math.log2(shape_paths)), math.ceil(math.log2(n)))
     base = tmp_path / "base.txt"
     gpu.autotune_save(base)                 # header lines of this device, nothing tuned
     ref = oracle.price_book(b, threads=THREADS)

@@ -143,6 +143,33 @@ def test_mixed_book_shared_paths(gpu):
     assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"]
 
 
+def test_independent_assets_in_turn_shared_paths(gpu):
+    """Variant 6: an uncorrelated GBM, a Heston and an LSV name priced one asset per
+    pass (the reference correlates no Heston/LSV spots), with a basket across all
+    three, a barrier, a discretely observed variance swap and pathwise delta."""
+    days = np.arange(0, 91)
+    b = abi.Book(days=days, paths=(1 << 13) + 31, greeks=abi.GREEK_DELTA | abi.GREEK_VEGA)
+    g = b.add_gbm(80.0, 0.3, 0.01)
+    h = b.add_heston(120.0, 0.05, 2.0, 0.05, 0.5, -0.6, 0.02)
+    ln_step = (np.log(250.0) - np.log(30.0)) / 49
+    offset = int(np.floor(np.log(30.0) / ln_step))
+    vals = 0.8 + 0.4 * np.random.default_rng(2).random((len(days), 50))
+    lv = b.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.0,
+                      leverage=(np.full(len(days), ln_step), np.full(len(days), offset, dtype=np.int64), vals))
+    b.add_vanilla(g, 80.0, 90, abi.CALL, zero_rate=0.02)
+    b.add_vanilla(h, 110.0, 60, abi.PUT, zero_rate=0.02)
+    b.add_vanilla(lv, 100.0, 90, abi.CALL, zero_rate=0.02)
+    b.add_barrier(lv, 100.0, 90, 85.0, up=False, knock_in=False, monitor=np.arange(1, 91), zero_rate=0.02)
+    b.add_variance(h, 90, strike_variance=0.05, notional=10.0, zero_rate=0.02, obs=np.arange(5, 91, 5))
+    b.add_basket([g, h, lv], [0.3, 0.3, 0.4], 100.0, 90, zero_rate=0.02)
+    assert gpu.plan_summary(b)["variant"] == 6
+    r = gpu.price_book(b, greeks=True)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "assets in turn")
+    assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"] + 1e-4 * abs(ref["book_premium"])
+    assert np.isfinite(r["delta"][[0, 1, 2, 5]]).all()
+
+
 # ---- edge cases ----------------------------------------------------------------
 
 @pytest.mark.parametrize("skip,paths", [(0, 2), (0, 255), (0, 257), (1, 1000), (255, 513), (12345, 777)])

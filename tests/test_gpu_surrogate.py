@@ -100,7 +100,12 @@ def test_price_grid_pipeline_small(gpu):
     m = S.Surrogate(seed=2)
     m.train(*S.train_targets(X, Y), epochs=60, batch=1024, lr=5e-3)
     ev = S.sobol_params(8, 64)
-    price, info = S.price_grid(m, ev, mc_paths=1 << 14, judge_frac=0.25, judge_paths=1 << 16)
-    assert price.shape == (8 * 252,) and np.isfinite(price).all()
-    assert info["judge_sets"] == 2 and info["cells"] == 8 * 252
+    fails = {}
+    for policy in S.POLICIES:
+        price, info = S.price_grid(m, ev, mc_paths=1 << 14, judge_frac=0.25, judge_paths=1 << 16, policy=policy)
+        assert price.shape == (8 * 252,) and np.isfinite(price).all()
+        assert info["judge_sets"] == 2 and info["cells"] == 8 * 252 and info["policy"] == policy
+        fails[policy] = info["failing_buckets"]
+    # the grid policy never takes over more buckets than the per-bucket one
+    assert fails["grid"] <= fails["bucket"]
     m.close()

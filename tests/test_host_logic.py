@@ -137,5 +137,54 @@ def test_kernel_selection_and_sizes():
     assert s["variant"] == 4 and s["sobol_dims"] == 1008 and s["slots"] == 7 and s["tiles"] == 4097
     s = G.plan_summary(W.heston_grid(paths=1000, calendar=True))
     assert s["sobol_dims"] == 1460
+    # LSV names only: the reference correlates no Heston/LSV spots, so the assets run in turn
     s = G.plan_summary(W.lsv_book(paths=1000))
-    assert s["variant"] == 3 and s["sobol_dims"] == 3650 and s["smem"] <= 227 * 1024
+    assert s["variant"] == 6 and s["sobol_dims"] == 3650 and s["smem"] <= 227 * 1024
+    # correlated GBM names need every asset's noise at once: the mixed kernel
+    from tests.golden.make_golden import mixed_book
+    s = G.plan_summary(mixed_book(paths=1000))
+    assert s["variant"] == 3 and s["tile"] == 128 and s["threads"] == 128
+    b = abi.Book(days=np.arange(0, 31), paths=1000)      # uncorrelated GBM + Heston: in turn
+    b.add_gbm(100, 0.2, 0.0)
+    b.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.0)
+    b.add_vanilla(0, 100, 30)
+    b.add_vanilla(1, 100, 30)
+    assert G.plan_summary(b)["variant"] == 6
+
+
+def test_surrogate_fallback_policies():
+    """The MC judge's bucket choice (host logic, no GPU)."""
+    from thoth_gb300 import surrogate as S
+    rng = np.random.default_rng(3)
+    tol = 1e-3
+    jerr = rng.uniform(0, 0.6e-3, size=(40, 12))
+    jerr[:, 3] = rng.uniform(1.5e-3, 4e-3, size=40)     # one bad bucket
+    jerr[:, 7] = rng.uniform(0.8e-3, 1.2e-3, size=40)   # one marginal bucket
+    bucket = S.choose_fallback(jerr, tol, "bucket")
+    assert bucket[3] and bucket[7] and bucket.sum() == 2
+    grid = S.choose_fallback(jerr, tol, "grid", margin=0.9)
+    assert grid[3] and grid.sum() <= bucket.sum()
+    e = jerr.copy()
+    e[:, grid] = 0.5 * tol
+    assert np.quantile(e, 0.9) <= 0.9 * tol
+    good = rng.uniform(0, 0.5e-3, size=(40, 12))
+    assert not S.choose_fallback(good, tol, "grid").any() and not S.choose_fallback(good, tol, "bucket").any()
+    with pytest.raises(ValueError):
+        S.choose_fallback(good, tol, "nope")
+
+
+def test_surrogate_grid_policy_prefers_short_horizons():
+    """An MC fallback book runs to its longest maturity: with the errors at short
+    maturities the grid policy stays within them."""
+    from thoth_gb300 import surrogate as S
+    rng = np.random.default_rng(5)
+    tol = 1e-3
+    n_T, n_lm = 4, 5
+    jerr = rng.uniform(0, 0.7e-3, size=(40, n_T * n_lm))
+    jerr[:, 0:n_lm] = rng.uniform(1.2e-3, 3e-3, size=(40, n_lm))     # maturity 0 is bad
+    jerr[:, 3 * n_lm + 2] = rng.uniform(0.9e-3, 1.05e-3, size=40)    # a mild long-maturity bucket
+    bad = S.choose_fallback(jerr, tol, "grid", margin=0.9, n_T=n_T).reshape(n_T, n_lm)
+    assert bad[0].any() and not bad[1:].any()
+    e = jerr.copy()
+    e[:, bad.ravel()] = 0.5 * tol
+    assert np.quantile(e, 0.9) <= 0.9 * tol

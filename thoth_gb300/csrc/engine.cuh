@@ -31,7 +31,10 @@ constexpr int MAX_ASSETS = 8;
 constexpr int SOBOL_BITS = 32;
 constexpr int SOBOL_LO_ROW = 256; // threads covered by the low-bit table (tiles of up to 2^8 paths)
 
-enum : int { M_GBM = 0, M_HESTON = 1, M_LSV = 2, M_MIXED = 3 };
+// M_SEQ: a multi-asset book whose assets are independent path by path (no
+// correlated GBM name; the reference correlates only GBM spots), simulated one
+// asset after the other with the single-asset state and a two-factor bridge
+enum : int { M_GBM = 0, M_HESTON = 1, M_LSV = 2, M_MIXED = 3, M_SEQ = 4 };
 
 // per-step, per-asset constants (12 floats, three 16-byte loads)
 //  GBM:    c[0] = carry_drift - sigma^2 dt / 2, c[1] = sigma sqrt(dt) (Brownian scale), c[2] = sqrt(dt)
@@ -74,7 +77,7 @@ enum : int {
     EV_GRP_MIN = 3,    // grp = min(grp, x - p)
     EV_GRP_MAX = 4,    // grp = max(grp, x - p)
     EV_GRP_SQ_STEP = 5,// grp += (step - p)^2   (continuous variance observation)
-    EV_GRP_SQ_OBS = 6, // grp += (x - last - p)^2, last = x  (discrete observation)
+    EV_GRP_SQ_OBS = 6, // grp += (x - last - p)^2, last = x  (discrete observation; pad = row of last)
 };
 struct Event {
     int type, a; // a = slot or group
@@ -106,7 +109,9 @@ struct Comp {
 struct DevPlan {
     // sizes
     int n_steps, n_assets, n_slots_used, n_groups;
-    int n_factors_active; // stacked factors
+    int n_last;           // discretely observed variance groups (rows of the previous observation)
+    int n_factors_active; // active factors of the book
+    int stack_factors;    // factors held in the bridge stack (n_factors_active, or 2 when assets run one by one)
     int sobol_dims;       // dims served by Sobol (<= 4097)
     int ref_factors;      // F in the reference dimension layout dim = bstep * F + f
     int use_sobol;

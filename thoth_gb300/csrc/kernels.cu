@@ -9,11 +9,11 @@ namespace thoth {
 // shared-memory carve-up (host and device compute the same sizes)
 // ---------------------------------------------------------------------------
 struct Smem {
-    uint32_t* hs;   // [sobol_dims] high Sobol part of the current tile
-    float* stk;     // [stack_depth][n_factors_active][T]
+    uint32_t* hs;   // [min(sobol_dims, HS_CHUNK)] tile parts of the current chunk of Sobol entries
+    float* stk;     // [stack_depth][stack_factors][T]
     float* slots;   // [n_slots][T + 1]
     float* grp;     // [n_groups][T + 1]
-    float* last;    // [n_groups][T + 1]
+    float* last;    // [n_last][T + 1] previous observation of each discretely observed variance group
     int* valid;     // [T]
     float* part;    // [T * 6]
     double* red;    // [2 * warps]
@@ -21,14 +21,21 @@ struct Smem {
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+__host__ __device__ constexpr int log2i(int x) { return x <= 1 ? 0 : 1 + log2i(x / 2); }
+
+// Sobol entries whose tile parts are held in shared memory at a time
+constexpr int HS_CHUNK = 512;
+__host__ __device__ inline int hs_words(int sobol_dims) { return sobol_dims < HS_CHUNK ? sobol_dims : HS_CHUNK; }
+
 __host__ __device__ inline size_t smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots,
-                                             int n_groups)
+                                             int n_groups, int n_last)
 {
     size_t b = 0;
-    b += align16(sizeof(uint32_t) * (size_t)sobol_dims);
+    b += align16(sizeof(uint32_t) * (size_t)hs_words(sobol_dims));
     b += align16(sizeof(float) * (size_t)stack_depth * nfa * T);
     b += align16(sizeof(float) * (size_t)n_slots * (T + 1));
-    b += 2 * align16(sizeof(float) * (size_t)n_groups * (T + 1));
+    b += align16(sizeof(float) * (size_t)n_groups * (T + 1));
+    b += align16(sizeof(float) * (size_t)n_last * (T + 1));
     b += align16(sizeof(int) * (size_t)T);
     b += align16(sizeof(float) * (size_t)T * 6);
     b += align16(sizeof(double) * 2 * (T / 32));
@@ -40,15 +47,15 @@ __device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
     Smem s;
     size_t o = 0;
     s.hs = reinterpret_cast<uint32_t*>(base + o);
-    o += align16(sizeof(uint32_t) * (size_t)P.sobol_dims);
+    o += align16(sizeof(uint32_t) * (size_t)hs_words(P.sobol_dims));
     s.stk = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * (size_t)P.stack_depth * P.n_factors_active * T);
+    o += align16(sizeof(float) * (size_t)P.stack_depth * P.stack_factors * T);
     s.slots = reinterpret_cast<float*>(base + o);
     o += align16(sizeof(float) * (size_t)P.n_slots_used * (T + 1));
     s.grp = reinterpret_cast<float*>(base + o);
     o += align16(sizeof(float) * (size_t)P.n_groups * (T + 1));
     s.last = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * (size_t)P.n_groups * (T + 1));
+    o += align16(sizeof(float) * (size_t)P.n_last * (T + 1));
     s.valid = reinterpret_cast<int*>(base + o);
     o += align16(sizeof(int) * (size_t)T);
     s.part = reinterpret_cast<float*>(base + o);
@@ -64,41 +71,49 @@ __device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
 // depends on the thread only: a fixed word lo[d][t]. Every Sobol dimension is
 // used once per path, in an order fixed by the bridge program, so the book's
 // low words are laid out in that order (sobol_lo[j][t], j the j-th dimension
-// consumed) and the tile part likewise (hs[j], computed once per tile). The
-// step loop then reads both sequentially: x = hs[j] ^ lo[j][t], with the
-// coalesced load of entry j + 2 in flight while entry j is used.
+// consumed) and the tile part likewise (hs[j], computed per tile in chunks of
+// HS_CHUNK entries). The step loop then reads both sequentially:
+// x = hs[j] ^ lo[j][t], with the coalesced load of entry j + 2 in flight while
+// entry j is used. Every thread of the CTA consumes the same entries in the
+// same order, so all of them reach a chunk boundary at the same call, where
+// the next chunk is computed between two barriers.
 // ---------------------------------------------------------------------------
 template <int TB>
-__device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m)
+__device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m, int j0)
 {
     const uint64_t g = (uint64_t)m ^ ((uint64_t)m >> 1);
-    for (int j = threadIdx.x; j < P.n_sobol; j += blockDim.x) {
+    const int j1 = min(j0 + HS_CHUNK, P.n_sobol);
+    for (int j = j0 + (int)threadIdx.x; j < j1; j += blockDim.x) {
         const uint32_t* V = P.sobol_v + __ldg(P.sobol_order + j) * SOBOL_BITS;
         uint32_t acc = (m & 1) ? __ldg(V + TB - 1) : 0u;
         uint64_t gg = g;
         for (int k = 0; gg != 0 && k < SOBOL_BITS - TB; ++k, gg >>= 1)
             if (gg & 1u) acc ^= __ldg(V + TB + k);
-        hs[j] = acc;
+        hs[j - j0] = acc;
     }
 }
 
 template <int T, int PP>
 struct SobolLane {
-    const uint32_t* hs;    // tile parts in consumption order, smem
+    uint32_t* hs;          // tile parts of entries [jend - HS_CHUNK, jend), smem
     const uint32_t* lo;    // column threadIdx.x of the book's low words
-    int j;                 // next entry
+    int64_t m;             // tile index
+    int j, jend;           // next entry; end of the chunk in shared memory
     uint32_t cur[PP], nxt[PP]; // low words of entries j and j + 1, per path of the thread
 };
 
-// path p of a thread is tile column threadIdx.x + p * (T / PP)
+// path p of a thread is tile column threadIdx.x + p * (T / PP); the first chunk
+// of tile parts must already be in hs
 template <int TB, int PP>
-__device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, const uint32_t* hs)
+__device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, uint32_t* hs, int64_t m)
 {
     constexpr int T = 1 << TB, TH = T / PP;
     SobolLane<T, PP> L;
     L.hs = hs;
     L.lo = P.sobol_lo + threadIdx.x;
+    L.m = m;
     L.j = 0;
+    L.jend = HS_CHUNK;
 #pragma unroll
     for (int p = 0; p < PP; ++p) {
         L.cur[p] = P.n_sobol > 0 ? __ldg(L.lo + p * TH) : 0u;
@@ -116,7 +131,13 @@ __device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, con
     constexpr int TH = T / PP;
     uint32_t x[PP];
     if (dim < P.sobol_dims) {
-        const uint32_t h = L.hs[L.j];
+        if (L.j == L.jend) { // next chunk of tile parts (uniform across the CTA, see above)
+            __syncthreads();
+            tile_high_bits<log2i(T)>(P, L.hs, L.m, L.j);
+            __syncthreads();
+            L.jend += HS_CHUNK;
+        }
+        const uint32_t h = L.hs[L.j - (L.jend - HS_CHUNK)];
         const int jn = L.j + 2;
         const bool more = jn < P.n_sobol;
 #pragma unroll
@@ -139,15 +160,23 @@ __device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, con
 // n_i = (W_i - W_{i-1}) / sqrt(t_i - t_{i-1}). Stack entry of path column k:
 // stk[(level * nfa + factor) * T + k].
 // ---------------------------------------------------------------------------
-template <int NA, int T, int PP>
+// SEQ: one asset, a0, per pass; its spot and variance factors are stack rows 0 and 1
+template <int NA, int T, int PP, bool SEQ>
 __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, const StepRec& rec, int& sp,
                                             SobolLane<T, PP>& L, const uint64_t (&n)[PP],
                                             float (&Wprev)[PP][2 * NA], float (&top)[PP][2 * NA],
-                                            float (&nz)[PP][2 * NA])
+                                            float (&nz)[PP][2 * NA], int a0)
 {
     constexpr int FS = 2 * NA, TH = T / PP;
     const int t = threadIdx.x;
-    const int nfa = P.n_factors_active;
+    const int nfa = P.stack_factors;
+    // asset and stack row of factor slot f (stack row < 0: slot inactive)
+    auto slot = [&](int f, int& a, int& ci) {
+        const int s_ = f < NA ? f : f - NA;
+        a = SEQ ? a0 : s_;
+        const int c = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
+        ci = (a < P.n_assets && c >= 0) ? (SEQ ? (f < NA ? 0 : 1) : c) : -1;
+    };
     float Wi[PP][FS];
 #pragma unroll
     for (int p = 0; p < PP; ++p)
@@ -157,9 +186,9 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
         const int base = (sp - 1) * nfa * T + t;
 #pragma unroll
         for (int f = 0; f < FS; ++f) {
-            const int a = f < NA ? f : f - NA;
-            const int ci = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
-            if (a < P.n_assets && ci >= 0) {
+            int a, ci;
+            slot(f, a, ci);
+            if (ci >= 0) {
 #pragma unroll
                 for (int p = 0; p < PP; ++p) {
                     Wi[p][f] = top[p][f];
@@ -183,9 +212,9 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
             const int base = sp * nfa * T + t;
 #pragma unroll
             for (int f = 0; f < FS; ++f) {
-                const int a = f < NA ? f : f - NA;
-                const int ci = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
-                if (a < P.n_assets && ci >= 0) {
+                int a, ci;
+                slot(f, a, ci);
+                if (ci >= 0) {
                     const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
                     float z[PP];
                     gauss(P, L, n, dim + fid, z);
@@ -323,11 +352,12 @@ __device__ __forceinline__ StepRec load_rec(const DevPlan& P, int i)
 // The book kernel. Template parameters:
 //   TB      log2 paths per tile (= threads per CTA)
 //   NA      compile-time asset slots (1 = single-asset fast path)
-//   MODEL   M_GBM / M_HESTON / M_LSV for single-model books, M_MIXED otherwise
+//   MODEL   M_GBM / M_HESTON / M_LSV for single-model books, M_MIXED for books
+//           with correlated GBM names, M_SEQ for other multi-asset books
 //   UNIFORM every step has the same per-asset constants (kept in registers)
 // ---------------------------------------------------------------------------
 template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-__global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / PP) : 1) book_kernel(const DevPlan P)
+__global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / PP) : 3) book_kernel(const DevPlan P)
 {
     constexpr int T = 1 << TB;  // paths per tile
     constexpr int TH = T / PP;  // threads per CTA; path p of thread t is tile column t + p * TH
@@ -366,41 +396,20 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
         }
         __syncthreads(); // previous tile fully evaluated
         if (t == 0) s_cancel = (P.cancel != nullptr) ? *P.cancel : 0;
-        if (P.use_sobol) tile_high_bits<TB>(P, S.hs, m);
+        if (P.use_sobol) tile_high_bits<TB>(P, S.hs, m, 0);
         __syncthreads();
         if (s_cancel) {
             if (t == 0) atomicExch(P.status, 1);
             return;
         }
-        SobolLane<T, PP> L = sobol_lane<TB, PP>(P, S.hs);
+        SobolLane<T, PP> L = sobol_lane<TB, PP>(P, S.hs, m);
 
-        // ---- path state -------------------------------------------------
-        float x[PP][NA], comp[PP][NA], v[PP][NA], Wb[PP][NA], y[PP][NA];
-        float Wprev[PP][FS], top[PP][FS], nz[PP][FS];
-#pragma unroll
-        for (int p = 0; p < PP; ++p) {
-#pragma unroll
-            for (int a = 0; a < NA; ++a) {
-                x[p][a] = 0.f;
-                comp[p][a] = 0.f;
-                v[p][a] = P.v0[a];
-                Wb[p][a] = 0.f;
-                y[p][a] = 1.f;
-            }
-#pragma unroll
-            for (int f = 0; f < FS; ++f) {
-                Wprev[p][f] = 0.f;
-                top[p][f] = 0.f;
-                nz[p][f] = 0.f;
-            }
-        }
-        int sp = 0;
         for (int g = 0; g < P.n_groups; ++g)
 #pragma unroll
-            for (int p = 0; p < PP; ++p) {
-                S.grp[g * stride + t + p * TH] = P.grp_init[g];
-                S.last[g * stride + t + p * TH] = 0.f;
-            }
+            for (int p = 0; p < PP; ++p) S.grp[g * stride + t + p * TH] = P.grp_init[g];
+        for (int g = 0; g < P.n_last; ++g)
+#pragma unroll
+            for (int p = 0; p < PP; ++p) S.last[g * stride + t + p * TH] = 0.f;
 
         // events on date index i for asset a of tile column k (after the state at date i is known)
         auto apply_events = [&](int i, int a, int k, float xa, float step, float wa, float ya) {
@@ -429,7 +438,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                 }
                 default: { // EV_GRP_SQ_OBS
                     float* g = S.grp + ev.a * stride + k;
-                    float* l = S.last + ev.a * stride + k;
+                    float* l = S.last + ev.pad * stride + k; // pad: the group's row of last
                     const float d = xa - *l - ev.p;
                     *g = fmaf(d, d, *g);
                     *l = xa;
@@ -437,87 +446,118 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                 }
             }
         };
-#pragma unroll
-        for (int a = 0; a < NA; ++a)
-            if (a < P.n_assets)
-#pragma unroll
-                for (int p = 0; p < PP; ++p) apply_events(0, a, t + p * TH, 0.f, 0.f, 0.f, 1.f);
 
-        // ---- time loop (step records prefetched one step ahead) ------------
-        StepRec rec = load_rec(P, 1);
-        for (int i = 1; i <= P.n_steps; ++i) {
-            const StepRec cur = rec;
-            if (i < P.n_steps) rec = load_rec(P, i + 1);
-            if (P.use_sobol) {
-                bridge_step<NA, T, PP>(P, S, cur, sp, L, n, Wprev, top, nz);
-            } else {
+        // one pass per asset for M_SEQ (asset a0), one pass for every asset otherwise
+        constexpr bool SEQ = (MODEL == M_SEQ);
+        const int n_pass = SEQ ? P.n_assets : 1;
+        for (int a0 = 0; a0 < n_pass; ++a0) {
+            // ---- path state -------------------------------------------------
+            float x[PP][NA], comp[PP][NA], v[PP][NA], Wb[PP][NA], y[PP][NA];
+            float Wprev[PP][FS], top[PP][FS], nz[PP][FS];
+#pragma unroll
+            for (int p = 0; p < PP; ++p) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) {
+                    x[p][a] = 0.f;
+                    comp[p][a] = 0.f;
+                    v[p][a] = P.v0[SEQ ? a0 : a];
+                    Wb[p][a] = 0.f;
+                    y[p][a] = 1.f;
+                }
 #pragma unroll
                 for (int f = 0; f < FS; ++f) {
-                    const int a = f < NA ? f : f - NA;
-                    const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
-                    if (a < P.n_assets && fid >= 0)
-#pragma unroll
-                        for (int p = 0; p < PP; ++p)
-                            nz[p][f] =
-                                quantile_u32(hash_u32(P.seed, n[p], (uint32_t)((i - 1) * P.ref_factors + fid)));
+                    Wprev[p][f] = 0.f;
+                    top[p][f] = 0.f;
+                    nz[p][f] = 0.f;
                 }
             }
+            int sp = 0;
 #pragma unroll
             for (int a = 0; a < NA; ++a) {
-                if (a >= P.n_assets) continue;
-                float4 c0, c1, c2;
-                if (UNIFORM) {
-                    c0 = u0[a];
-                    c1 = u1[a];
-                    c2 = u2[a];
+                const int aid = SEQ ? a0 : a;
+                if (aid < P.n_assets)
+#pragma unroll
+                    for (int p = 0; p < PP; ++p) apply_events(0, aid, t + p * TH, 0.f, 0.f, 0.f, 1.f);
+            }
+
+            // ---- time loop (step records prefetched one step ahead) ------------
+            StepRec rec = load_rec(P, 1);
+            for (int i = 1; i <= P.n_steps; ++i) {
+                const StepRec cur = rec;
+                if (i < P.n_steps) rec = load_rec(P, i + 1);
+                if (P.use_sobol) {
+                    bridge_step<NA, T, PP, SEQ>(P, S, cur, sp, L, n, Wprev, top, nz, a0);
                 } else {
-                    const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + a].c);
-                    c0 = __ldg(cs);
-                    c1 = __ldg(cs + 1);
-                    c2 = __ldg(cs + 2);
-                }
-                const int model = (MODEL == M_MIXED) ? P.model[a] : MODEL;
 #pragma unroll
-                for (int p = 0; p < PP; ++p) {
-                    float step;
-                    if (model == M_GBM) {
-                        float e = nz[p][a];
-                        if (MODEL == M_MIXED && P.corr) {
-                            e = 0.f;
+                    for (int f = 0; f < FS; ++f) {
+                        const int sa = f < NA ? f : f - NA;
+                        const int aid = SEQ ? a0 : sa;
+                        const int fid = f < NA ? P.fid_spot[aid] : P.fid_var[aid];
+                        if (aid < P.n_assets && fid >= 0)
 #pragma unroll
-                            for (int u = 0; u < NA; ++u)
-                                if (u < P.n_assets) e = fmaf(P.chol[a * MAX_ASSETS + u], nz[p][u], e);
-                        }
-                        step = fmaf(c0.y, e, c0.x);
-                        Wb[p][a] = fmaf(c0.z, e, Wb[p][a]);
-                    } else {
-                        const float vp = v[p][a];
-                        const float vc = qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
-                        float Lv = 1.f, dL = 0.f;
-                        if (model == M_LSV) leverage(P, a, i, x[p][a], Lv, dL);
-                        const float s = vp + vc;
-                        if (!P.degenerate[a]) {
-                            const float B =
-                                fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * nz[p][a];
-                            if (model == M_LSV) {
-                                step = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
-                                y[p][a] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
-                            } else {
-                                step = c1.x + B - c1.w * s;
-                            }
-                        } else {
-                            const float sq = fast_sqrt(vp * c2.z) * nz[p][a];
-                            step = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
-                            if (model == M_LSV) y[p][a] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
-                        }
-                        v[p][a] = vc;
+                            for (int p = 0; p < PP; ++p)
+                                nz[p][f] = quantile_u32(
+                                    hash_u32(P.seed, n[p], (uint32_t)((i - 1) * P.ref_factors + fid)));
                     }
-                    // Kahan-compensated log-spot
-                    const float yy = step - comp[p][a];
-                    const float tt = x[p][a] + yy;
-                    comp[p][a] = (tt - x[p][a]) - yy;
-                    x[p][a] = tt;
-                    if (cur.ev) apply_events(i, a, t + p * TH, x[p][a], step, Wb[p][a], y[p][a]);
+                }
+#pragma unroll
+                for (int a = 0; a < NA; ++a) {
+                    const int aid = SEQ ? a0 : a; // asset id; a is the register slot
+                    if (aid >= P.n_assets) continue;
+                    float4 c0, c1, c2;
+                    if (UNIFORM) {
+                        c0 = u0[a];
+                        c1 = u1[a];
+                        c2 = u2[a];
+                    } else {
+                        const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + aid].c);
+                        c0 = __ldg(cs);
+                        c1 = __ldg(cs + 1);
+                        c2 = __ldg(cs + 2);
+                    }
+                    const int model = (MODEL == M_MIXED || SEQ) ? P.model[aid] : MODEL;
+#pragma unroll
+                    for (int p = 0; p < PP; ++p) {
+                        float step;
+                        if (model == M_GBM) {
+                            float e = nz[p][a];
+                            if (MODEL == M_MIXED && P.corr) {
+                                e = 0.f;
+#pragma unroll
+                                for (int u = 0; u < NA; ++u)
+                                    if (u < P.n_assets) e = fmaf(P.chol[a * MAX_ASSETS + u], nz[p][u], e);
+                            }
+                            step = fmaf(c0.y, e, c0.x);
+                            Wb[p][a] = fmaf(c0.z, e, Wb[p][a]);
+                        } else {
+                            const float vp = v[p][a];
+                            const float vc = qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
+                            float Lv = 1.f, dL = 0.f;
+                            if (model == M_LSV) leverage(P, aid, i, x[p][a], Lv, dL);
+                            const float s = vp + vc;
+                            if (!P.degenerate[aid]) {
+                                const float B =
+                                    fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * nz[p][a];
+                                if (model == M_LSV) {
+                                    step = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
+                                    y[p][a] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
+                                } else {
+                                    step = c1.x + B - c1.w * s;
+                                }
+                            } else {
+                                const float sq = fast_sqrt(vp * c2.z) * nz[p][a];
+                                step = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
+                                if (model == M_LSV) y[p][a] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
+                            }
+                            v[p][a] = vc;
+                        }
+                        // Kahan-compensated log-spot
+                        const float yy = step - comp[p][a];
+                        const float tt = x[p][a] + yy;
+                        comp[p][a] = (tt - x[p][a]) - yy;
+                        x[p][a] = tt;
+                        if (cur.ev) apply_events(i, aid, t + p * TH, x[p][a], step, Wb[p][a], y[p][a]);
+                    }
                 }
             }
         }
@@ -673,15 +713,15 @@ __global__ void __launch_bounds__(1 << TB) bridge_kernel(const DevPlan P, float*
         const uint64_t n[1] = {(uint64_t)m * T + (uint64_t)t};
         const bool valid = n[0] >= (uint64_t)P.skip + 1 && n[0] <= (uint64_t)(P.skip + P.paths);
         __syncthreads();
-        tile_high_bits<TB>(P, S.hs, m);
+        tile_high_bits<TB>(P, S.hs, m, 0);
         __syncthreads();
-        SobolLane<T, 1> L = sobol_lane<TB, 1>(P, S.hs);
+        SobolLane<T, 1> L = sobol_lane<TB, 1>(P, S.hs, m);
         float Wprev[1][2] = {{0.f, 0.f}}, top[1][2] = {{0.f, 0.f}}, nz[1][2];
         int sp = 0;
         const int64_t path = (int64_t)n[0] - P.skip - 1;
         for (int i = 1; i <= P.n_steps; ++i) {
             const StepRec rec = load_rec(P, i);
-            bridge_step<NA, T, 1>(P, S, rec, sp, L, n, Wprev, top, nz);
+            bridge_step<NA, T, 1, false>(P, S, rec, sp, L, n, Wprev, top, nz, 0);
             if (valid) {
                 for (int f = 0; f < P.n_factors_active; ++f)
                     out[((size_t)path * P.n_factors_active + f) * P.n_steps + (i - 1)] = nz[0][f];
@@ -805,12 +845,14 @@ static int dispatch(const DevPlan* P, int variant, int shape, int grid, size_t s
         return grid ? 0 : occ_t<7, MAX_ASSETS, M_MIXED, false, 1>(smem);
     case 4: return single_t<M_HESTON, true>(P, shape, grid, smem, st, err);
     case 5: return single_t<M_GBM, true>(P, shape, grid, smem, st, err);
+    case 6: return single_t<M_SEQ, false>(P, shape, grid, smem, st, err);
     default: *err = cudaErrorInvalidValue; return 1;
     }
 }
 
 // variants: 0 GBM, 1 Heston, 2 LSV (single asset, per-step constants),
-//           3 mixed multi-asset, 4 Heston with uniform steps, 5 GBM with uniform steps
+//           3 mixed multi-asset with correlated GBM names, 4 Heston with uniform steps,
+//           5 GBM with uniform steps, 6 multi-asset with independent assets (one pass per asset)
 cudaError_t launch_book(const DevPlan& P, int variant, int shape, int grid, size_t smem, cudaStream_t st)
 {
     if (grid < 1) return cudaErrorInvalidValue;
@@ -827,9 +869,9 @@ int book_occupancy(int variant, int shape, size_t smem)
     return e == cudaSuccess ? n : 1;
 }
 
-size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups)
+size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups, int n_last)
 {
-    return smem_bytes(T, sobol_dims, stack_depth, nfa, n_slots, n_groups);
+    return smem_bytes(T, sobol_dims, stack_depth, nfa, n_slots, n_groups, n_last);
 }
 
 cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st)

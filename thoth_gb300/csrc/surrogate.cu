@@ -404,57 +404,111 @@ __global__ void sum_kernel(const float* x, int n, float* out)
     if (threadIdx.x == 0) *out = s[0];
 }
 
-// fused inference: persistent CTAs, weights resident in smem, 4 MMA layers per
-// 128-cell tile with bias + SiLU epilogues written back as the next operand
-__global__ void __launch_bounds__(128) infer_kernel(const __nv_bfloat16* __restrict__ x, int n, const float* params,
-                                                    const __nv_bfloat16* wbf, float* __restrict__ y, int* status)
+// fused inference: persistent CTAs of two warpgroups. The weights are resident
+// in shared memory and shared by both; each warpgroup walks its own 128-cell
+// tiles with its own TMEM accumulator (128 columns each), mbarrier and named
+// barrier, so one warpgroup's bias + SiLU epilogue overlaps the other's MMAs.
+// The epilogue streams 16 accumulator columns at a time straight into the next
+// layer's A operand (K-major core-matrix layout); the last layer folds the head.
+constexpr int INFER_THREADS = 256;
+
+__device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+
+__global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat16* __restrict__ x, int n,
+                                                              const float* params, const __nv_bfloat16* wbf,
+                                                              float* __restrict__ y, int* status)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[2];
     __shared__ uint32_t tm_s;
+    __shared__ float sb[4 * H + H + 1];              // biases of layers 1..4, head weights, head bias
     unsigned char* sW1 = sm;                         // 128 x 16
     unsigned char* sW = sW1 + H * KIN * 2;           // 3 x (128 x 128)
-    unsigned char* sX = sW + 3 * H * H * 2;          // 128 x 16
-    unsigned char* sAct = sX + ROWS * KIN * 2;       // 128 x 128
-    const int t = threadIdx.x, warp = t >> 5;
-    if (warp == 0) tc::tmem_alloc(&tm_s, 128);
-    if (t == 0) tc::mbar_init(&mbar, 1);
+    const int t = threadIdx.x, warp = t >> 5, wg = t >> 7, r = t & 127;
+    unsigned char* sX = sW + 3 * H * H * 2 + wg * (ROWS * KIN * 2 + ROWS * H * 2); // this warpgroup's 128 x 16
+    unsigned char* sAct = sX + ROWS * KIN * 2;                                    // and 128 x 128
+    if (warp == 0) tc::tmem_alloc(&tm_s, 256);
+    if (t == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+    }
     stage<H>(sW1, wbf + OFF_BF_W1, KIN, KIN, H);
     for (int l = 0; l < 3; ++l) stage<H>(sW + l * H * H * 2, wbf + OFF_BF_W2 + l * H * H, H, H, H);
-    Ctx c{&mbar, 0, 0, status};
+    for (int i = t; i < 4 * H; i += INFER_THREADS) sb[i] = params[b_off(1 + i / H) + i % H];
+    for (int i = t; i < H; i += INFER_THREADS) sb[4 * H + i] = params[OFF_W5 + i];
+    if (t == 0) sb[5 * H] = params[OFF_B5];
+    tc::fence_before_sync();
     __syncthreads();
-    c.tm = tm_s;
+    tc::fence_after_sync();
+    Ctx c{&mbar[wg], tm_s + (uint32_t)(wg * 128), 0, status};
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16; // TMEM lanes of this warp
     const int tiles = (n + ROWS - 1) / ROWS;
-    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (int tile = 2 * blockIdx.x + wg; tile < tiles; tile += 2 * gridDim.x) {
         const int r0 = tile * ROWS;
-        stage<ROWS>(sX, x + (size_t)r0 * KIN, KIN, KIN, min(ROWS, n - r0));
-        float v[H];
-        bool ok = true;
-        for (int l = 1; l <= 4; ++l) {
-            const unsigned char* a = (l == 1) ? sX : sAct;
-            const unsigned char* w = (l == 1) ? sW1 : sW + (l - 2) * H * H * 2;
-            ok = run_mma(c, 0, a, ROWS, w, H, l == 1 ? KIN : H, false) && ok;
-            if (ok) load_row(c, 0, H, v);
-            else
-                for (int j = 0; j < H; ++j) v[j] = 0.f;
-            const float* b = params + b_off(l);
-            for (int j = 0; j < H; ++j) v[j] = silu(v[j] + b[j]);
-            if (l < 4) {
-                tc::fence_before_sync();
-                __syncthreads(); // every lane has read the accumulator before it is overwritten
-                put_row(sAct, t, v, H);
-            }
+        const int valid = min(ROWS, n - r0);
+        // this warpgroup stages its input tile (row r by thread r: two 16-byte chunks)
+        for (int kb = 0; kb < KIN / 8; ++kb) {
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (r < valid) v = *reinterpret_cast<const uint4*>(x + (size_t)(r0 + r) * KIN + kb * 8);
+            *reinterpret_cast<uint4*>(sX + tc::cm_offset(r, kb * 8, ROWS)) = v;
         }
-        const float* w5 = params + OFF_W5;
-        float o = params[OFF_B5];
-        for (int j = 0; j < H; ++j) o = fmaf(w5[j], v[j], o);
-        if (r0 + t < n) y[r0 + t] = o;
-        tc::fence_before_sync();
-        __syncthreads();
+        float o = sb[5 * H];
+        for (int l = 1; l <= 4; ++l) {
+            const unsigned char* A = (l == 1) ? sX : sAct;
+            const unsigned char* W = (l == 1) ? sW1 : sW + (l - 2) * H * H * 2;
+            const int K = (l == 1) ? KIN : H;
+            // operand writes of every thread of the warpgroup -> visible to the tensor core
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            wg_sync(wg);
+            tc::fence_after_sync();
+            if (r == 0) {
+                const uint32_t idesc = tc::make_idesc_bf16(ROWS, H);
+                const uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(W);
+                for (int kk = 0; kk < K / 16; ++kk) {
+                    const uint64_t ad = tc::make_desc(a0 + (uint32_t)(2 * kk) * (ROWS * 16), ROWS * 16, 128);
+                    const uint64_t bd = tc::make_desc(b0 + (uint32_t)(2 * kk) * (H * 16), H * 16, 128);
+                    tc::mma_bf16(c.tm, ad, bd, idesc, kk > 0 ? 1u : 0u);
+                }
+                tc::mma_commit(c.mbar);
+            }
+            const bool ok = tc::mbar_wait(c.mbar, c.phase);
+            c.phase ^= 1u;
+            if (!ok && (t & 31) == 0) atomicExch(c.status, 1);
+            tc::fence_after_sync();
+            const float* bias = sb + (l - 1) * H;
+            for (int c0 = 0; c0 < H; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(c.tm + lane_base + (uint32_t)c0, v);
+                if (!ok) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = silu(v[j] + bias[c0 + j]);
+                if (l < 4) {
+                    // the MMA that read sAct has completed: overwrite it in place with the next operand
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        __align__(16) __nv_bfloat16 hv[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) hv[j] = __float2bfloat16(v[h * 8 + j]);
+                        *reinterpret_cast<uint4*>(sAct + tc::cm_offset(r, c0 + h * 8, ROWS)) =
+                            *reinterpret_cast<const uint4*>(hv);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) o = fmaf(sb[4 * H + c0 + j], v[j], o);
+                }
+            }
+            // every lane has read the accumulator before the next MMA overwrites it
+            tc::fence_before_sync();
+        }
+        if (r < valid) y[r0 + r] = o;
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(c.tm, 128);
+    if (warp == 0) tc::tmem_dealloc(tm_s, 256);
 }
 
 } // namespace mlp
@@ -506,10 +560,33 @@ cudaError_t mlp_infer(const __nv_bfloat16* x, int n, const float* params, const 
                       int* status, int grid, cudaStream_t st)
 {
     using namespace mlp;
-    const size_t smem = (size_t)(H * KIN + 3 * H * H + ROWS * KIN + ROWS * H) * 2;
+    const size_t smem = (size_t)(H * KIN + 3 * H * H + 2 * (ROWS * KIN + ROWS * H)) * 2;
     cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    infer_kernel<<<grid, 128, smem, st>>>(x, n, params, wbf, y, status);
+    infer_kernel<<<grid, INFER_THREADS, smem, st>>>(x, n, params, wbf, y, status);
+    return cudaGetLastError();
+}
+
+// one training batch from the device-resident set: rows perm[first .. first + rows)
+__global__ void gather_batch_kernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ Y,
+                                    const float* __restrict__ W, const int* __restrict__ perm, int64_t first, int rows,
+                                    __nv_bfloat16* __restrict__ xb, float* __restrict__ yb, float* __restrict__ wb)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const int64_t i = __ldg(perm + first + r);
+    const uint4* src = reinterpret_cast<const uint4*>(X + i * mlp::KIN);
+    uint4* dst = reinterpret_cast<uint4*>(xb + (int64_t)r * mlp::KIN);
+    dst[0] = __ldg(src);
+    dst[1] = __ldg(src + 1);
+    yb[r] = __ldg(Y + i);
+    wb[r] = __ldg(W + i);
+}
+
+cudaError_t mlp_gather_batch(const __nv_bfloat16* X, const float* Y, const float* W, const int* perm, int64_t first,
+                             int rows, __nv_bfloat16* xb, float* yb, float* wb, cudaStream_t st)
+{
+    gather_batch_kernel<<<(rows + 127) / 128, 128, 0, st>>>(X, Y, W, perm, first, rows, xb, yb, wb);
     return cudaGetLastError();
 }
 

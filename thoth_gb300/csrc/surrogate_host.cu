@@ -35,6 +35,8 @@ cudaError_t mlp_train_step(const mlp::TrainArgs& A, float* params, float* m, flo
                            float b1, float b2, float eps, float bc1, float bc2, float* loss_out, cudaStream_t st);
 cudaError_t mlp_infer(const __nv_bfloat16* x, int n, const float* params, const __nv_bfloat16* wbf, float* y,
                       int* status, int grid, cudaStream_t st);
+cudaError_t mlp_gather_batch(const __nv_bfloat16* X, const float* Y, const float* W, const int* perm, int64_t first,
+                             int rows, __nv_bfloat16* xb, float* yb, float* wb, cudaStream_t st);
 int mlp_n_params();
 int mlp_n_bf();
 } // namespace thoth
@@ -85,6 +87,11 @@ struct ThothSurrogate {
     // inference buffers
     int64_t cap_inf = 0;
     unsigned char* ib = nullptr;
+    // device copy of a training set and its per-epoch permutation (grown on demand)
+    int64_t cap_ds = 0;
+    unsigned char* ds = nullptr;
+    int* perm_host = nullptr; // pinned
+    cudaEvent_t perm_copied = nullptr;
 };
 
 namespace {
@@ -258,6 +265,9 @@ int thoth_gpu_surrogate_destroy(ThothSurrogate* s)
     cudaFree(s->status);
     if (s->tb) cudaFree(s->tb);
     if (s->ib) cudaFree(s->ib);
+    if (s->ds) cudaFree(s->ds);
+    if (s->perm_host) cudaFreeHost(s->perm_host);
+    if (s->perm_copied) cudaEventDestroy(s->perm_copied);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return THOTH_GPU_OK;
@@ -327,31 +337,62 @@ int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y,
     const int B = (int)std::min<int64_t>(batch, n / 128 * 128);
     int rc = ensure_train(s, B);
     if (rc) return rc;
-    std::vector<int64_t> idx(n);
-    for (int64_t i = 0; i < n; i++) idx[i] = i;
+    if (n > ((int64_t)1 << 31) - 1) return sfail(THOTH_GPU_E_TOO_LARGE, "training set beyond 2^31 rows");
+    // the whole training set goes up once, packed (bf16 hi/lo inputs, targets, loss weights);
+    // each epoch uploads one permutation and every step gathers its rows on the device
+    if (n > s->cap_ds) {
+        if (s->ds) cudaFree(s->ds);
+        if (s->perm_host) cudaFreeHost(s->perm_host);
+        s->ds = nullptr;
+        s->perm_host = nullptr;
+        s->cap_ds = 0;
+        STRY(cudaMalloc(&s->ds, (size_t)n * (KIN * 2 + 4 + 4 + 4) + 1024));
+        STRY(cudaHostAlloc(&s->perm_host, sizeof(int) * (size_t)n, cudaHostAllocDefault));
+        if (!s->perm_copied) STRY(cudaEventCreateWithFlags(&s->perm_copied, cudaEventDisableTiming));
+        s->cap_ds = n;
+    }
+    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+    __nv_bfloat16* dX = reinterpret_cast<__nv_bfloat16*>(s->ds);
+    float* dY = reinterpret_cast<float*>(s->ds + up((size_t)n * KIN * 2));
+    float* dW = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(dY) + up((size_t)n * 4));
+    int* dP = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(dW) + up((size_t)n * 4));
+    {
+        std::vector<__nv_bfloat16> hx;
+        std::vector<float> hy, hw;
+        pack(x, y, scale, nullptr, 0, (int)n, hx, hy, hw);
+        STRY(cudaMemcpy(dX, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice));
+        STRY(cudaMemcpy(dY, hy.data(), hy.size() * 4, cudaMemcpyHostToDevice));
+        STRY(cudaMemcpy(dW, hw.data(), hw.size() * 4, cudaMemcpyHostToDevice));
+    }
+    std::vector<int> idx(n);
+    for (int64_t i = 0; i < n; i++) idx[i] = (int)i;
     std::mt19937_64 rng(seed);
     const int64_t steps_per_epoch = n / B, total = steps_per_epoch * epochs;
-    std::vector<__nv_bfloat16> hx;
-    std::vector<float> hy, hw;
+    mlp::TrainArgs& A = s->A;
     double last = 0;
     STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+    STRY(cudaEventRecord(s->perm_copied, s->st));
     int64_t done = 0;
     for (int e = 0; e < epochs; e++) {
         std::shuffle(idx.begin(), idx.end(), rng);
+        STRY(cudaEventSynchronize(s->perm_copied)); // the previous permutation has left the pinned buffer
+        std::memcpy(s->perm_host, idx.data(), sizeof(int) * (size_t)n);
+        STRY(cudaMemcpyAsync(dP, s->perm_host, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->st));
+        STRY(cudaEventRecord(s->perm_copied, s->st));
         double acc = 0;
         for (int64_t b = 0; b < steps_per_epoch; b++, done++) {
-            pack(x, y, scale, idx.data(), b * B, B, hx, hy, hw);
-            rc = upload_batch(s, hx, hy, hw);
-            if (rc) return rc;
-            s->A.rows = B;
+            STRY(mlp_gather_batch(dX, dY, dW, dP, b * B, B, const_cast<__nv_bfloat16*>(A.x), const_cast<float*>(A.y),
+                                  const_cast<float*>(A.inv_w2), s->st));
+            A.a[0] = const_cast<__nv_bfloat16*>(A.x);
+            A.rows = B;
             s->step++;
             const double lr_t = lr * 0.5 * (1.0 + std::cos(M_PI * (double)done / (double)total)) + 1e-6;
             const float bc1 = (float)(1.0 - std::pow(0.9, (double)s->step));
             const float bc2 = (float)(1.0 - std::pow(0.999, (double)s->step));
             const bool last_batch = (b == steps_per_epoch - 1);
-            STRY(mlp_train_step(s->A, s->params, s->m, s->v, s->wbf, (float)lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2,
+            STRY(mlp_train_step(A, s->params, s->m, s->v, s->wbf, (float)lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2,
                                 last_batch ? s->loss : nullptr, s->st));
-            if (last_batch) {
+            if (last_batch && e == epochs - 1) {
                 float l = 0;
                 STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
                 STRY(cudaStreamSynchronize(s->st));

@@ -26,7 +26,7 @@ int book_shape_count(int variant);
 int book_shape_tile_bits(int variant, int shape);
 int book_shape_threads(int variant, int shape);
 int book_occupancy(int variant, int shape, size_t smem);
-size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups);
+size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups, int n_last);
 cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st);
 cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64_t n_points, uint32_t* out,
                                 cudaStream_t st);
@@ -337,19 +337,24 @@ std::vector<StepRec> make_recs(const BridgeProgram& bp, const std::vector<float>
 
 // Sobol dimensions in the order the step loop consumes them: per step, per node
 // of its chain, the active spot factors, then the active variance factors
-// (the factor loop of bridge_step), dimensions beyond the Sobol budget left out
-std::vector<int> sobol_order(const BridgeProgram& bp, const DevPlan& D)
+// (the factor loop of bridge_step); with one pass per asset (per_asset), the
+// same for each asset in turn. Dimensions beyond the Sobol budget are left out.
+std::vector<int> sobol_order(const BridgeProgram& bp, const DevPlan& D, bool per_asset = false)
 {
     std::vector<int> order;
     if (!D.use_sobol) return order;
-    for (const StepProg& sp : bp.prog)
-        for (int k = 0; k < sp.count; k++) {
-            const int d0 = bp.nodes[sp.first + k].bstep * D.ref_factors;
-            for (int a = 0; a < D.n_assets; a++)
-                if (D.cidx_spot[a] >= 0 && d0 + D.fid_spot[a] < D.sobol_dims) order.push_back(d0 + D.fid_spot[a]);
-            for (int a = 0; a < D.n_assets; a++)
-                if (D.cidx_var[a] >= 0 && d0 + D.fid_var[a] < D.sobol_dims) order.push_back(d0 + D.fid_var[a]);
-        }
+    const int passes = per_asset ? D.n_assets : 1;
+    for (int pass = 0; pass < passes; pass++) {
+        const int a_lo = per_asset ? pass : 0, a_hi = per_asset ? pass + 1 : D.n_assets;
+        for (const StepProg& sp : bp.prog)
+            for (int k = 0; k < sp.count; k++) {
+                const int d0 = bp.nodes[sp.first + k].bstep * D.ref_factors;
+                for (int a = a_lo; a < a_hi; a++)
+                    if (D.cidx_spot[a] >= 0 && d0 + D.fid_spot[a] < D.sobol_dims) order.push_back(d0 + D.fid_spot[a]);
+                for (int a = a_lo; a < a_hi; a++)
+                    if (D.cidx_var[a] >= 0 && d0 + D.fid_var[a] < D.sobol_dims) order.push_back(d0 + D.fid_var[a]);
+            }
+    }
     return order;
 }
 
@@ -477,13 +482,20 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
             }
         D.corr = 1;
     }
-    // variant (tile size fixed by it; uniform-step variants decided below)
-    if (NA == 1 && !mixed) {
+    // variant (tile size fixed by it; uniform-step variants decided below). The
+    // reference correlates only GBM spots (correlated_noise_node.cpp:15-27): a
+    // multi-asset book without a correlated GBM name has independent assets and
+    // runs them one after the other (variant 6).
+    bool any_gbm = false;
+    for (int a = 0; a < NA; a++) any_gbm |= d->assets[a].model == THOTH_MODEL_GBM;
+    if (NA == 1 && !mixed && !D.corr) {
         P.variant = d->assets[0].model; // 0 GBM, 1 Heston, 2 LSV
-    } else {
+    } else if (D.corr && any_gbm) {
         P.variant = 3;
+    } else {
+        P.variant = 6;
     }
-    if (D.corr && P.variant != 3) P.variant = 3;
+    D.stack_factors = P.variant == 6 ? 2 : D.n_factors_active;
     P.base_variant = P.variant;
     if (shape < 0) {
         auto it = g_tuned.find(tune_key(P.variant, d->paths, N));
@@ -696,8 +708,9 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
                         ev[(size_t)j * NA + a].push_back(Event{type, g, (float)(Q.quanto * (tl[j] - tl[j - 1])), 0});
                 } else {
                     int prev = 0;
+                    const int row = D.n_last++;
                     for (int o : obs) {
-                        ev[(size_t)o * NA + a].push_back(Event{type, g, (float)(Q.quanto * (tl[o] - tl[prev])), 0});
+                        ev[(size_t)o * NA + a].push_back(Event{type, g, (float)(Q.quanto * (tl[o] - tl[prev])), row});
                         prev = o;
                     }
                 }
@@ -752,7 +765,7 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     }
     if (events.empty()) events.push_back(Event{0, 0, 0.f, 0});
     const std::vector<StepRec> recs = make_recs(bp, isd, ev_flag, F);
-    std::vector<int> order = sobol_order(bp, D);
+    std::vector<int> order = sobol_order(bp, D, P.variant == 6);
     D.n_sobol = (int)order.size();
     if (order.empty()) order.push_back(0);
 
@@ -760,7 +773,7 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     const int64_t lo = d->sobol_skip + 1, hi = d->sobol_skip + d->paths;
     D.tile_first = lo / T;
     D.n_tiles = hi / T - lo / T + 1;
-    P.smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, D.n_factors_active, D.n_slots_used, D.n_groups);
+    P.smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, D.stack_factors, D.n_slots_used, D.n_groups, D.n_last);
     if (P.smem > 227 * 1024) return fail(THOTH_GPU_E_TOO_LARGE, "book needs more shared memory than one SM has");
     D.n_acc = 6 * d->n_products + 2;
     P.n_products = d->n_products;
@@ -1476,7 +1489,7 @@ static int autotune_load_locked(const char* path)
         else if (std::sscanf(line, "batch %d %d %d", &a, &b, &c) == 3) { streams = a; policy = b; bshape = c; }
         else if (std::sscanf(line, "batch %d %d", &a, &b) == 2) { streams = a; policy = b; bshape = -1; }
         else if (std::sscanf(line, "book %d %d %d %d %d %d", &a, &b, &c, &e, &g, &h) == 6) {
-            if (a < 0 || a > 5 || e < 0 || e >= book_shape_count(a) || g < 0 || h < 0 || h > 1) bad = true;
+            if (a < 0 || a > 6 || e < 0 || e >= book_shape_count(a) || g < 0 || h < 0 || h > 1) bad = true;
             TuneChoice ch;
             ch.shape = e;
             ch.per_sm = g;
@@ -1811,6 +1824,7 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
     D.n_assets = 1;
     D.ref_factors = factors;
     D.n_factors_active = factors;
+    D.stack_factors = factors;
     D.sobol_dims = (int)std::min<long>((long)N * factors, max_dims());
     D.use_sobol = 1;
     D.stack_depth = bp.stack_depth;
@@ -1831,7 +1845,7 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
     D.n_sobol = (int)order.size();
     P.o_sord = P.blob.put(order);
     P.T = T;
-    const size_t smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, factors, 0, 0);
+    const size_t smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, factors, 0, 0, 0);
     const size_t o_lo = (P.blob.bytes.size() + 255) & ~size_t(255);
     const size_t o_out = o_lo + ((low_bytes(P) + 255) & ~size_t(255));
     const size_t bytes = sizeof(float) * (size_t)n_paths * factors * N;
