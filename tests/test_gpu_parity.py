@@ -170,6 +170,28 @@ def test_independent_assets_in_turn_shared_paths(gpu):
     assert np.isfinite(r["delta"][[0, 1, 2, 5]]).all()
 
 
+def test_shared_running_groups_shared_paths(gpu):
+    """Barriers on nested daily monitoring prefixes (both directions), one on a list that
+    is not a prefix (its own group), and continuous variance swaps with staggered
+    maturities, one quanto: running groups with snapshots at each product's last date."""
+    b = abi.Book(days=np.arange(0, 121), paths=(1 << 13) + 9)
+    h = b.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.01)
+    for m, lvl in ((30, 85.0), (60, 80.0), (120, 75.0), (90, 82.0)):
+        b.add_barrier(h, 100.0, m, lvl, up=False, knock_in=False, monitor=np.arange(1, m + 1), zero_rate=0.02)
+    for m, lvl in ((45, 115.0), (120, 125.0)):
+        b.add_barrier(h, 95.0, m, lvl, up=True, knock_in=True, monitor=np.arange(1, m + 1), option_type=abi.PUT,
+                      zero_rate=0.02)
+    b.add_barrier(h, 100.0, 120, 80.0, up=False, knock_in=False, monitor=np.arange(2, 121, 2), zero_rate=0.02)
+    for m in (20, 60, 120):
+        b.add_variance(h, m, strike_variance=0.04, notional=100.0, zero_rate=0.02)
+    b.add_variance(h, 90, strike_variance=0.04, notional=100.0, zero_rate=0.02, quanto=0.01)
+    plan = gpu.plan_summary(b)
+    assert plan["groups"] == 5            # down, up, the odd barrier, two variance sums
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "running groups")
+
+
 # ---- edge cases ----------------------------------------------------------------
 
 @pytest.mark.parametrize("skip,paths", [(0, 2), (0, 255), (0, 257), (1, 1000), (255, 513), (12345, 777)])

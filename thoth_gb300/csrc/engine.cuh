@@ -78,6 +78,7 @@ enum : int {
     EV_GRP_MAX = 4,    // grp = max(grp, x - p)
     EV_GRP_SQ_STEP = 5,// grp += (step - p)^2   (continuous variance observation)
     EV_GRP_SQ_OBS = 6, // grp += (x - last - p)^2, last = x  (discrete observation; pad = row of last)
+    EV_SNAP_G = 7,     // slot = grp[pad]  (a running group seen by a product that ends before it)
 };
 struct Event {
     int type, a; // a = slot or group
@@ -97,6 +98,7 @@ struct DevProduct {
     int slot_y, slot_w; // greek observables (-1: none)
     float inv_s0, vol_t;
     int greek_mask;     // bit 0 delta supported, bit 1 vega supported
+    int g_snap;         // 1: slot_g is a snapshot slot of a running group, 0: the group itself
 };
 
 struct Comp {

@@ -279,11 +279,11 @@ __device__ __forceinline__ float payoff(const DevPlan& P, const DevProduct& pr, 
     float s;
     switch (pr.kind) {
     case P_VARIANCE: {
-        const float sum2 = grp[pr.slot_g * stride + k];
+        const float sum2 = (pr.g_snap ? slots : grp)[pr.slot_g * stride + k];
         return pr.notional * ((pr.past + sum2) * pr.inv_T - pr.kvar) * pr.df;
     }
     case P_BARRIER: {
-        const float ext = grp[pr.slot_g * stride + k];
+        const float ext = (pr.g_snap ? slots : grp)[pr.slot_g * stride + k];
         const bool hit = pr.up ? (ext >= pr.level) : (ext <= pr.level);
         const bool alive = pr.knock_in ? hit : !hit;
         if (!alive) return 0.f;
@@ -436,6 +436,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                     *g = fmaf(d, d, *g);
                     break;
                 }
+                case EV_SNAP_G: S.slots[ev.a * stride + k] = S.grp[ev.pad * stride + k]; break;
                 default: { // EV_GRP_SQ_OBS
                     float* g = S.grp + ev.a * stride + k;
                     float* l = S.last + ev.pad * stride + k; // pad: the group's row of last

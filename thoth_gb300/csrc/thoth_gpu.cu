@@ -395,9 +395,31 @@ struct Plan {
 
 bool finite(double x) { return std::isfinite(x); }
 
-// shape < 0: the autotuned shape for the book's size, else the default (0)
+// Untuned shape of a single-asset-kernel plan: (8, 2), unless shared memory
+// caps the CTAs per SM so low that (8, 1), with the same tile and twice the
+// threads per CTA, keeps more threads resident. Needs a device (else 0).
+int default_shape(int variant, size_t smem)
+{
+    static std::map<std::pair<int, size_t>, int> memo;
+    auto key = std::make_pair(variant, smem);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return 0;
+    }
+    const int t0 = book_occupancy(variant, 0, smem) * book_shape_threads(variant, 0);
+    const int t1 = book_occupancy(variant, 1, smem) * book_shape_threads(variant, 1);
+    const int shape = t1 > t0 ? 1 : 0;
+    memo[key] = shape;
+    return shape;
+}
+
+// shape < 0: the autotuned shape for the book's size, else the default
 int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
 {
+    const bool untuned = shape < 0;
     if (!d) return fail(THOTH_GPU_E_INVALID, "null descriptor");
     const int nd = d->n_dates, N = nd - 1, NA = d->n_assets;
     if (nd < 2 || nd > THOTH_MAX_DATES) return fail(THOTH_GPU_E_INVALID, "n_dates must be in [2, THOTH_MAX_DATES]");
@@ -497,9 +519,11 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     }
     D.stack_factors = P.variant == 6 ? 2 : D.n_factors_active;
     P.base_variant = P.variant;
+    bool tuned = false;
     if (shape < 0) {
         auto it = g_tuned.find(tune_key(P.variant, d->paths, N));
-        shape = it != g_tuned.end() ? it->second.shape : 0;
+        tuned = it != g_tuned.end();
+        shape = tuned ? it->second.shape : 0;
     }
     if (shape >= book_shape_count(P.variant)) shape = 0;
     P.shape = shape;
@@ -611,15 +635,91 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     std::map<std::tuple<int, int, double, std::vector<int>>, int> group_of;
     std::vector<float> grp_init;
     std::vector<std::vector<Event>> ev((size_t)nd * NA);
+    int n_slots = 0;
     auto slot = [&](int type, int a, int date) {
         auto key = std::make_tuple(type, a, date);
         auto it = slot_of.find(key);
         if (it != slot_of.end()) return it->second;
-        const int s = (int)slot_of.size();
+        const int s = n_slots++;
         slot_of[key] = s;
         Event e{type, s, 0.f, 0};
         ev[(size_t)date * NA + a].push_back(e);
         return s;
+    };
+    // Running groups shared by products on nested date prefixes: barriers of one
+    // asset, direction and quanto shift whose monitor lists are prefixes of one
+    // another, and continuous variance sums of one asset and quanto shift, keep
+    // one running extreme / sum over the union of their dates; a product that
+    // ends before the union reads a snapshot taken at its last date. So a book
+    // of barriers with daily monitoring and staggered maturities updates one
+    // group per asset and step instead of one per product.
+    using RunKey = std::tuple<int, int, double>; // (event type, asset, quanto)
+    std::map<RunKey, std::vector<int>> run_dates;
+    std::vector<char> run_shared(d->n_products, 0);
+    for (int p = 0; p < d->n_products; p++) {
+        const ThothProduct& Q = d->products[p];
+        if (Q.asset < 0 || Q.asset >= NA || Q.maturity < 0 || Q.maturity > N) continue; // rejected below
+        std::vector<int> dates;
+        int type;
+        if (Q.kind == THOTH_PRODUCT_BARRIER && Q.n_monitor > 0 && Q.monitor) {
+            dates.assign(Q.monitor, Q.monitor + Q.n_monitor);
+            bool ok = true;
+            for (size_t k = 0; k < dates.size(); k++)
+                ok = ok && dates[k] >= 0 && dates[k] <= N && (k == 0 || dates[k] >= dates[k - 1]);
+            if (!ok) continue;
+            type = Q.barrier_up ? EV_GRP_MAX : EV_GRP_MIN;
+        } else if (Q.kind == THOTH_PRODUCT_VARIANCE && Q.n_obs <= 0 && Q.maturity >= 1) {
+            for (int j = 1; j <= Q.maturity; j++) dates.push_back(j);
+            type = EV_GRP_SQ_STEP;
+        } else {
+            continue;
+        }
+        std::vector<int>& U = run_dates[RunKey(type, Q.asset, Q.quanto)];
+        const size_t L = std::min(U.size(), dates.size());
+        if (!std::equal(dates.begin(), dates.begin() + L, U.begin())) continue; // not a prefix: own group
+        if (dates.size() > U.size()) U.insert(U.end(), dates.begin() + L, dates.end());
+        run_shared[p] = 1;
+    }
+    std::map<RunKey, int> run_group;
+    std::map<std::pair<int, int>, int> snap_of; // (group, date) -> slot
+    // the running group of product p (created with its update events on first use)
+    auto running = [&](const RunKey& rk, int a, float init) {
+        auto it = run_group.find(rk);
+        if (it != run_group.end()) return it->second;
+        const int g = (int)grp_init.size();
+        run_group[rk] = g;
+        grp_init.push_back(init);
+        const int type = std::get<0>(rk);
+        const double q = std::get<2>(rk);
+        int prev = 0;
+        for (int k : run_dates[rk]) {
+            const float pk = (float)(type == EV_GRP_SQ_STEP ? q * (tl[k] - tl[k - 1]) : q * tl[k]);
+            ev[(size_t)k * NA + a].push_back(Event{type, g, pk, 0});
+            prev = k;
+        }
+        (void)prev;
+        return g;
+    };
+    // a product's view of running group g at its last date: the group itself when
+    // that is the group's last date, else a snapshot slot (taken after the update)
+    auto view = [&](const RunKey& rk, int g, int a, int last, DevProduct& R) {
+        if (last >= run_dates[rk].back()) {
+            R.slot_g = g;
+            R.g_snap = 0;
+            return;
+        }
+        auto key = std::make_pair(g, last);
+        auto it = snap_of.find(key);
+        int sl;
+        if (it != snap_of.end()) {
+            sl = it->second;
+        } else {
+            sl = n_slots++;
+            snap_of[key] = sl;
+            ev[(size_t)last * NA + a].push_back(Event{EV_SNAP_G, sl, 0.f, g});
+        }
+        R.slot_g = sl;
+        R.g_snap = 1;
     };
     const bool want_delta = (D.greeks & THOTH_GREEK_DELTA) != 0, want_vega = (D.greeks & THOTH_GREEK_VEGA) != 0;
     std::vector<DevProduct> prods(d->n_products);
@@ -667,18 +767,24 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
                         return fail(THOTH_GPU_E_INVALID, "monitor indices must be sorted and in range");
                 if (!(Q.barrier_level > 0)) return fail(THOTH_GPU_E_INVALID, "barrier level must be > 0");
                 const int type = Q.barrier_up ? EV_GRP_MAX : EV_GRP_MIN;
-                auto key = std::make_tuple(type, a, Q.quanto, mon);
-                auto it = group_of.find(key);
-                int g;
-                if (it == group_of.end()) {
-                    g = (int)grp_init.size();
-                    group_of[key] = g;
-                    grp_init.push_back(Q.barrier_up ? -INFINITY : INFINITY);
-                    for (int k : mon) ev[(size_t)k * NA + a].push_back(Event{type, g, (float)(Q.quanto * tl[k]), 0});
+                if (run_shared[p]) {
+                    const RunKey rk(type, a, Q.quanto);
+                    view(rk, running(rk, a, Q.barrier_up ? -INFINITY : INFINITY), a, mon.back(), R);
                 } else {
-                    g = it->second;
+                    auto key = std::make_tuple(type, a, Q.quanto, mon);
+                    auto it = group_of.find(key);
+                    int g;
+                    if (it == group_of.end()) {
+                        g = (int)grp_init.size();
+                        group_of[key] = g;
+                        grp_init.push_back(Q.barrier_up ? -INFINITY : INFINITY);
+                        for (int k : mon)
+                            ev[(size_t)k * NA + a].push_back(Event{type, g, (float)(Q.quanto * tl[k]), 0});
+                    } else {
+                        g = it->second;
+                    }
+                    R.slot_g = g;
                 }
-                R.slot_g = g;
                 R.up = Q.barrier_up ? 1 : 0;
                 R.knock_in = Q.barrier_in ? 1 : 0;
                 R.level = (float)std::log(Q.barrier_level / d->assets[a].spot);
@@ -698,8 +804,11 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
             std::vector<int> key_dates = obs.empty() ? std::vector<int>{mat} : obs;
             auto key = std::make_tuple(type, a, Q.quanto, key_dates);
             auto it = group_of.find(key);
-            int g;
-            if (it == group_of.end()) {
+            int g = -1;
+            if (run_shared[p]) {
+                const RunKey rk(type, a, Q.quanto);
+                view(rk, running(rk, a, 0.f), a, mat, R);
+            } else if (it == group_of.end()) {
                 g = (int)grp_init.size();
                 group_of[key] = g;
                 grp_init.push_back(0.f);
@@ -717,7 +826,7 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
             } else {
                 g = it->second;
             }
-            R.slot_g = g;
+            if (!run_shared[p]) R.slot_g = g;
             const double T = (Q.total_year_fraction > 0) ? Q.total_year_fraction : tl[mat];
             R.inv_T = (float)(T > 0 ? 1.0 / T : 0.0);
             R.past = (float)Q.past_variance;
@@ -749,9 +858,9 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
         R.greek_mask = P.greek_mask[p];
     }
     if (comps.empty()) comps.push_back(Comp{0, 0.f, -1, 0.f});
+    D.n_slots_used = std::max(n_slots, 1);
+    D.n_groups = (int)grp_init.size();
     if (grp_init.empty()) grp_init.push_back(0.f);
-    D.n_slots_used = std::max((int)slot_of.size(), 1);
-    D.n_groups = (int)group_of.size();
     D.n_products = d->n_products;
     // events, ordered per (date, asset)
     std::vector<int2> ev_range((size_t)nd * NA);
@@ -795,6 +904,8 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     P.o_prod = P.blob.put(prods);
     P.o_comp = P.blob.put(comps);
     P.o_sord = P.blob.put(order);
+    // shapes 0 and 1 share the 256-path tile, so the plan above serves both
+    if (untuned && !tuned && P.variant != 3 && P.shape == 0) P.shape = default_shape(P.variant, P.smem);
     return THOTH_GPU_OK;
 }
 
