@@ -192,6 +192,30 @@ def test_shared_running_groups_shared_paths(gpu):
     assert_shared_path_parity(r, ref["premium"], ref["trust"], "running groups")
 
 
+def test_lsv_assets_with_different_leverage_grids(gpu):
+    """Two LSV names whose leverage layers have 50 and 20 points (one row stride for
+    both) and change on every date (a staged layer per step), plus a basket of both."""
+    days = np.arange(0, 61)
+    b = abi.Book(days=days, paths=(1 << 12) + 3, greeks=abi.GREEK_DELTA)
+    rng = np.random.default_rng(4)
+    assets = []
+    for spot, pts in ((100.0, 50), (60.0, 20)):
+        ln_step = (np.log(4.0 * spot) - np.log(spot / 4.0)) / (pts - 1)
+        offset = int(np.floor(np.log(spot / 4.0) / ln_step))
+        vals = 0.7 + 0.6 * rng.random((len(days), pts))
+        assets.append(b.add_heston(spot, 0.04, 1.5, 0.04, 0.5, -0.6, 0.01,
+                                   leverage=(np.full(len(days), ln_step), np.full(len(days), offset, dtype=np.int64),
+                                             vals)))
+    for a, K in zip(assets, (100.0, 60.0)):
+        b.add_vanilla(a, K, 60, abi.CALL, zero_rate=0.01)
+        b.add_vanilla(a, 0.9 * K, 30, abi.PUT, zero_rate=0.01)
+    b.add_basket(assets, [0.5, 0.5], 80.0, 60, zero_rate=0.01)
+    assert gpu.plan_summary(b)["variant"] == 6
+    r = gpu.price_book(b, greeks=True)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "two leverage grids")
+
+
 # ---- edge cases ----------------------------------------------------------------
 
 @pytest.mark.parametrize("skip,paths", [(0, 2), (0, 255), (0, 257), (1, 1000), (255, 513), (12345, 777)])

@@ -147,8 +147,9 @@ struct DevPlan {
     const Event* events;
     const int* lev_layer;        // [n_assets][n_steps + 1] layer of date i
     const float2* lev_map;       // [n_assets][layers] (1/ln_step, lnS0/ln_step - offset)
-    const float* lev_values;     // [n_assets][layers][points] (asset-major with lev_stride)
+    const float* lev_values;     // [n_assets][layers][lev_row_stride]
     int lev_layers_stride;       // layers per asset (max)
+    int lev_row_stride;          // floats per leverage layer (max points over the assets)
     const float* grp_init;       // [n_groups] +inf (min), -inf (max), 0 (sums)
     const DevProduct* products;
     const Comp* comps;

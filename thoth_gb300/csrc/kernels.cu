@@ -197,16 +197,31 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
             }
         }
         --sp;
+    } else if (rec.count == 1) {
+        // a single node ending at this date (about a quarter of the steps): no push
+#pragma unroll
+        for (int f = 0; f < FS; ++f) {
+            int a, ci;
+            slot(f, a, ci);
+            if (ci >= 0) {
+                const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
+                float z[PP];
+                gauss(P, L, n, rec.dim + fid, z);
+#pragma unroll
+                for (int p = 0; p < PP; ++p) Wi[p][f] = fmaf(rec.lw, Wprev[p][f], fmaf(rec.rw, top[p][f], rec.sd * z[p]));
+            }
+        }
     } else {
         float lw = rec.lw, rw = rec.rw, sd = rec.sd;
         int dim = rec.dim;
+        BridgeNode nd = P.nodes[rec.first]; // node 1 of the chain, loaded one node ahead
         for (int k = 0; k < rec.count; ++k) {
             if (k > 0) {
-                const BridgeNode nd = P.nodes[rec.first + k - 1];
                 lw = nd.lw;
                 rw = nd.rw;
                 sd = nd.sd;
                 dim = nd.bstep * P.ref_factors;
+                if (k + 1 < rec.count) nd = P.nodes[rec.first + k];
             }
             const bool push = k + 1 < rec.count;
             const int base = sp * nfa * T + t;
@@ -242,13 +257,15 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
         }
 }
 
-// leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47)
+// leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47). The layer of
+// a date is uniform across the CTA and its rows stay in L1 (staging the current
+// layer in shared memory measured slower)
 __device__ __forceinline__ void leverage(const DevPlan& P, int a, int i, float x, float& L, float& dL)
 {
     const int layer = __ldg(P.lev_layer + a * (P.n_steps + 1) + i);
     const float2 mp = __ldg(P.lev_map + a * P.lev_layers_stride + layer);
+    const float* v = P.lev_values + (a * P.lev_layers_stride + layer) * P.lev_row_stride;
     const int npts = P.lev_points[a];
-    const float* v = P.lev_values + (a * P.lev_layers_stride + layer) * npts;
     const float f = fmaf(x, mp.x, mp.y);
     const int last = npts - 1;
     if (f <= 0.f) {

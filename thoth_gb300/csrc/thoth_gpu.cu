@@ -626,9 +626,10 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
         const int np = std::max(D.lev_points[a], 1);
         for (size_t r = 0; r < maps[a].size(); r++)
             for (int k = 0; k < D.lev_points[a]; k++)
-                lev_values[((size_t)a * layers_stride + r) * np + k] = vals[a][r * np + k];
+                lev_values[((size_t)a * layers_stride + r) * lev_pts_max + k] = vals[a][r * np + k];
     }
     D.lev_layers_stride = layers_stride;
+    D.lev_row_stride = lev_pts_max; // one row stride for every asset, whatever its point count
 
     // products -> slots, groups, events
     std::map<std::tuple<int, int, int>, int> slot_of; // (type, asset, date)
