@@ -67,6 +67,7 @@ extern "C" {
 #define THOTH_MAX_SOBOL_DIMS 4097 /* reference SobolGenerator::MaxDimension()  */
 #define THOTH_MAX_DATES 8192
 #define THOTH_MAX_PRODUCTS 4096
+#define THOTH_MAX_LEV_POINTS 65536 /* log-strike points of one leverage layer */
 
 /* ---- book descriptor ---------------------------------------------------- */
 typedef struct ThothAsset

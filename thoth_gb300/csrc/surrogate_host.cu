@@ -10,6 +10,8 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <random>
 #include <string>
 #include <vector>
@@ -119,6 +121,7 @@ int ensure_train(ThothSurrogate* s, int rows)
     if (rows <= s->cap_rows) return THOTH_GPU_OK;
     if (s->tb) cudaFree(s->tb);
     s->tb = nullptr;
+    s->cap_rows = 0; // stays empty if the allocation fails
     const int tiles = rows / 128;
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -206,246 +209,289 @@ extern "C" {
 
 int thoth_gpu_surrogate_create(ThothSurrogate** out, uint64_t seed)
 {
-    if (!out) return sfail(THOTH_GPU_E_INVALID, "null handle pointer");
-    std::lock_guard<std::mutex> lk(s_mu);
-    int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return sfail(THOTH_GPU_E_NODEVICE, "no CUDA device");
-    cudaDeviceProp p;
-    STRY(cudaGetDeviceProperties(&p, 0));
-    if (!(p.major == 10 && p.minor == 3)) return sfail(THOTH_GPU_E_NODEVICE, "not an sm_103 device");
-    ThothSurrogate* s = new ThothSurrogate();
-    s->np = mlp_n_params();
-    s->nbf = mlp_n_bf();
-    s->sms = p.multiProcessorCount;
-    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&s->params, sizeof(float) * s->np * 3);
-    if (e == cudaSuccess) e = cudaMalloc(&s->wbf, sizeof(__nv_bfloat16) * s->nbf);
-    if (e == cudaSuccess) e = cudaMalloc(&s->status, sizeof(int));
-    if (e != cudaSuccess) {
-        delete s;
-        return sfail(THOTH_GPU_E_NOMEM, std::string("surrogate allocation: ") + cudaGetErrorString(e));
+    try {
+        if (!out) return sfail(THOTH_GPU_E_INVALID, "null handle pointer");
+        std::lock_guard<std::mutex> lk(s_mu);
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return sfail(THOTH_GPU_E_NODEVICE, "no CUDA device");
+        cudaDeviceProp p;
+        STRY(cudaGetDeviceProperties(&p, 0));
+        if (!(p.major == 10 && p.minor == 3)) return sfail(THOTH_GPU_E_NODEVICE, "not an sm_103 device");
+        ThothSurrogate* s = new ThothSurrogate();
+        s->np = mlp_n_params();
+        s->nbf = mlp_n_bf();
+        s->sms = p.multiProcessorCount;
+        cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMalloc(&s->params, sizeof(float) * s->np * 3);
+        if (e == cudaSuccess) e = cudaMalloc(&s->wbf, sizeof(__nv_bfloat16) * s->nbf);
+        if (e == cudaSuccess) e = cudaMalloc(&s->status, sizeof(int));
+        if (e != cudaSuccess) {
+            delete s;
+            return sfail(THOTH_GPU_E_NOMEM, std::string("surrogate allocation: ") + cudaGetErrorString(e));
+        }
+        s->m = s->params + s->np;
+        s->v = s->params + 2 * s->np;
+        // Xavier-uniform weights, zero biases; W1 only on the 7 real input columns
+        std::mt19937_64 rng(seed);
+        std::vector<float> h(s->np, 0.f);
+        auto fill = [&](int off, int rows, int cols, int fan_in, int used_cols) {
+            const double a = std::sqrt(6.0 / (fan_in + rows));
+            std::uniform_real_distribution<double> U(-a, a);
+            for (int r = 0; r < rows; r++)
+                for (int c = 0; c < cols; c++) h[off + r * cols + c] = c < used_cols ? (float)U(rng) : 0.f;
+        };
+        fill(OFF_W1, H, KIN, NF, NF);
+        for (int r = 0; r < H; r++) // tie the lo-part columns to the hi-part columns
+            for (int f = 0; f < NF; f++) h[OFF_W1 + r * KIN + NF + f] = h[OFF_W1 + r * KIN + f];
+        for (int l = 0; l < 3; l++) fill(OFF_W2 + l * LAYER, H, H, H, H);
+        fill(OFF_W5, 1, H, H, H);
+        int rc = upload_params(s, h);
+        if (rc == THOTH_GPU_OK) {
+            e = cudaMemsetAsync(s->m, 0, sizeof(float) * 2 * s->np, s->st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(s->status, 0, sizeof(int), s->st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+            if (e != cudaSuccess) rc = sfail(THOTH_GPU_E_CUDA, cudaGetErrorString(e));
+        }
+        if (rc) {
+            delete s;
+            return rc;
+        }
+        *out = s;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }
-    s->m = s->params + s->np;
-    s->v = s->params + 2 * s->np;
-    // Xavier-uniform weights, zero biases; W1 only on the 7 real input columns
-    std::mt19937_64 rng(seed);
-    std::vector<float> h(s->np, 0.f);
-    auto fill = [&](int off, int rows, int cols, int fan_in, int used_cols) {
-        const double a = std::sqrt(6.0 / (fan_in + rows));
-        std::uniform_real_distribution<double> U(-a, a);
-        for (int r = 0; r < rows; r++)
-            for (int c = 0; c < cols; c++) h[off + r * cols + c] = c < used_cols ? (float)U(rng) : 0.f;
-    };
-    fill(OFF_W1, H, KIN, NF, NF);
-    for (int r = 0; r < H; r++) // tie the lo-part columns to the hi-part columns
-        for (int f = 0; f < NF; f++) h[OFF_W1 + r * KIN + NF + f] = h[OFF_W1 + r * KIN + f];
-    for (int l = 0; l < 3; l++) fill(OFF_W2 + l * LAYER, H, H, H, H);
-    fill(OFF_W5, 1, H, H, H);
-    int rc = upload_params(s, h);
-    if (rc == THOTH_GPU_OK) {
-        e = cudaMemsetAsync(s->m, 0, sizeof(float) * 2 * s->np, s->st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(s->status, 0, sizeof(int), s->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-        if (e != cudaSuccess) rc = sfail(THOTH_GPU_E_CUDA, cudaGetErrorString(e));
-    }
-    if (rc) {
-        delete s;
-        return rc;
-    }
-    *out = s;
-    return THOTH_GPU_OK;
 }
 
 int thoth_gpu_surrogate_destroy(ThothSurrogate* s)
 {
-    if (!s) return THOTH_GPU_OK;
-    std::lock_guard<std::mutex> lk(s_mu);
-    cudaFree(s->params);
-    cudaFree(s->wbf);
-    cudaFree(s->status);
-    if (s->tb) cudaFree(s->tb);
-    if (s->ib) cudaFree(s->ib);
-    if (s->ds) cudaFree(s->ds);
-    if (s->perm_host) cudaFreeHost(s->perm_host);
-    if (s->perm_copied) cudaEventDestroy(s->perm_copied);
-    if (s->st) cudaStreamDestroy(s->st);
-    delete s;
-    return THOTH_GPU_OK;
+    try {
+        if (!s) return THOTH_GPU_OK;
+        std::lock_guard<std::mutex> lk(s_mu);
+        cudaFree(s->params);
+        cudaFree(s->wbf);
+        cudaFree(s->status);
+        if (s->tb) cudaFree(s->tb);
+        if (s->ib) cudaFree(s->ib);
+        if (s->ds) cudaFree(s->ds);
+        if (s->perm_host) cudaFreeHost(s->perm_host);
+        if (s->perm_copied) cudaEventDestroy(s->perm_copied);
+        if (s->st) cudaStreamDestroy(s->st);
+        delete s;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_surrogate_n_params(void) { return mlp_n_params(); }
 
 int thoth_gpu_surrogate_get_params(ThothSurrogate* s, float* params)
 {
-    if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
-    std::lock_guard<std::mutex> lk(s_mu);
-    STRY(cudaMemcpyAsync(params, s->params, sizeof(float) * s->np, cudaMemcpyDeviceToHost, s->st));
-    STRY(cudaStreamSynchronize(s->st));
-    return THOTH_GPU_OK;
+    try {
+        if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaMemcpyAsync(params, s->params, sizeof(float) * s->np, cudaMemcpyDeviceToHost, s->st));
+        STRY(cudaStreamSynchronize(s->st));
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_surrogate_set_params(ThothSurrogate* s, const float* params)
 {
-    if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
-    std::lock_guard<std::mutex> lk(s_mu);
-    std::vector<float> h(params, params + s->np);
-    return upload_params(s, h);
+    try {
+        if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(s_mu);
+        std::vector<float> h(params, params + s->np);
+        return upload_params(s, h);
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_surrogate_gradient(ThothSurrogate* s, const float* x, const float* y, const float* scale, int32_t rows,
                                  float* grad, double* loss)
 {
-    if (!s || !x || !y || !grad || rows < 128 || rows % 128) return sfail(THOTH_GPU_E_INVALID, "rows must be a multiple of 128");
-    std::lock_guard<std::mutex> lk(s_mu);
-    int rc = ensure_train(s, rows);
-    if (rc) return rc;
-    std::vector<__nv_bfloat16> hx;
-    std::vector<float> hy, hw;
-    pack(x, y, scale, nullptr, 0, rows, hx, hy, hw);
-    rc = upload_batch(s, hx, hy, hw);
-    if (rc) return rc;
-    s->A.rows = rows;
-    // a step with lr = 0 leaves the parameters unchanged but fills the partial gradients
-    std::vector<float> keep_m(2 * (size_t)s->np);
-    STRY(cudaMemcpyAsync(keep_m.data(), s->m, sizeof(float) * 2 * s->np, cudaMemcpyDeviceToHost, s->st));
-    STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
-    STRY(mlp_train_step(s->A, s->params, s->m, s->v, s->wbf, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f, s->loss, s->st));
-    rc = check_status(s);
-    if (rc) return rc;
-    const int tiles = rows / 128;
-    std::vector<float> part((size_t)tiles * s->np);
-    STRY(cudaMemcpyAsync(part.data(), s->A.part, sizeof(float) * part.size(), cudaMemcpyDeviceToHost, s->st));
-    float l = 0;
-    STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
-    STRY(cudaMemcpyAsync(s->m, keep_m.data(), sizeof(float) * 2 * s->np, cudaMemcpyHostToDevice, s->st));
-    STRY(cudaStreamSynchronize(s->st));
-    for (int j = 0; j < s->np; j++) {
-        double g = 0;
-        for (int t = 0; t < tiles; t++) g += part[(size_t)t * s->np + j];
-        grad[j] = (float)g;
+    try {
+        if (!s || !x || !y || !grad || rows < 128 || rows % 128) return sfail(THOTH_GPU_E_INVALID, "rows must be a multiple of 128");
+        std::lock_guard<std::mutex> lk(s_mu);
+        int rc = ensure_train(s, rows);
+        if (rc) return rc;
+        std::vector<__nv_bfloat16> hx;
+        std::vector<float> hy, hw;
+        pack(x, y, scale, nullptr, 0, rows, hx, hy, hw);
+        rc = upload_batch(s, hx, hy, hw);
+        if (rc) return rc;
+        s->A.rows = rows;
+        // a step with lr = 0 leaves the parameters unchanged but fills the partial gradients
+        std::vector<float> keep_m(2 * (size_t)s->np);
+        STRY(cudaMemcpyAsync(keep_m.data(), s->m, sizeof(float) * 2 * s->np, cudaMemcpyDeviceToHost, s->st));
+        STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+        STRY(mlp_train_step(s->A, s->params, s->m, s->v, s->wbf, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f, s->loss, s->st));
+        rc = check_status(s);
+        if (rc) return rc;
+        const int tiles = rows / 128;
+        std::vector<float> part((size_t)tiles * s->np);
+        STRY(cudaMemcpyAsync(part.data(), s->A.part, sizeof(float) * part.size(), cudaMemcpyDeviceToHost, s->st));
+        float l = 0;
+        STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
+        STRY(cudaMemcpyAsync(s->m, keep_m.data(), sizeof(float) * 2 * s->np, cudaMemcpyHostToDevice, s->st));
+        STRY(cudaStreamSynchronize(s->st));
+        for (int j = 0; j < s->np; j++) {
+            double g = 0;
+            for (int t = 0; t < tiles; t++) g += part[(size_t)t * s->np + j];
+            grad[j] = (float)g;
+        }
+        if (loss) *loss = l / rows;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }
-    if (loss) *loss = l / rows;
-    return THOTH_GPU_OK;
 }
 
 int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
                               int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss)
 {
-    if (!s || !x || !y || n < 128 || epochs < 1 || batch < 128 || batch % 128 || !(lr > 0))
-        return sfail(THOTH_GPU_E_INVALID, "bad training arguments (batch must be a multiple of 128)");
-    std::lock_guard<std::mutex> lk(s_mu);
-    const int B = (int)std::min<int64_t>(batch, n / 128 * 128);
-    int rc = ensure_train(s, B);
-    if (rc) return rc;
-    if (n > ((int64_t)1 << 31) - 1) return sfail(THOTH_GPU_E_TOO_LARGE, "training set beyond 2^31 rows");
-    // the whole training set goes up once, packed (bf16 hi/lo inputs, targets, loss weights);
-    // each epoch uploads one permutation and every step gathers its rows on the device
-    if (n > s->cap_ds) {
-        if (s->ds) cudaFree(s->ds);
-        if (s->perm_host) cudaFreeHost(s->perm_host);
-        s->ds = nullptr;
-        s->perm_host = nullptr;
-        s->cap_ds = 0;
-        STRY(cudaMalloc(&s->ds, (size_t)n * (KIN * 2 + 4 + 4 + 4) + 1024));
-        STRY(cudaHostAlloc(&s->perm_host, sizeof(int) * (size_t)n, cudaHostAllocDefault));
-        if (!s->perm_copied) STRY(cudaEventCreateWithFlags(&s->perm_copied, cudaEventDisableTiming));
-        s->cap_ds = n;
-    }
-    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
-    __nv_bfloat16* dX = reinterpret_cast<__nv_bfloat16*>(s->ds);
-    float* dY = reinterpret_cast<float*>(s->ds + up((size_t)n * KIN * 2));
-    float* dW = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(dY) + up((size_t)n * 4));
-    int* dP = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(dW) + up((size_t)n * 4));
-    {
-        std::vector<__nv_bfloat16> hx;
-        std::vector<float> hy, hw;
-        pack(x, y, scale, nullptr, 0, (int)n, hx, hy, hw);
-        STRY(cudaMemcpy(dX, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice));
-        STRY(cudaMemcpy(dY, hy.data(), hy.size() * 4, cudaMemcpyHostToDevice));
-        STRY(cudaMemcpy(dW, hw.data(), hw.size() * 4, cudaMemcpyHostToDevice));
-    }
-    std::vector<int> idx(n);
-    for (int64_t i = 0; i < n; i++) idx[i] = (int)i;
-    std::mt19937_64 rng(seed);
-    const int64_t steps_per_epoch = n / B, total = steps_per_epoch * epochs;
-    mlp::TrainArgs& A = s->A;
-    double last = 0;
-    STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
-    STRY(cudaEventRecord(s->perm_copied, s->st));
-    int64_t done = 0;
-    for (int e = 0; e < epochs; e++) {
-        std::shuffle(idx.begin(), idx.end(), rng);
-        STRY(cudaEventSynchronize(s->perm_copied)); // the previous permutation has left the pinned buffer
-        std::memcpy(s->perm_host, idx.data(), sizeof(int) * (size_t)n);
-        STRY(cudaMemcpyAsync(dP, s->perm_host, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->st));
-        STRY(cudaEventRecord(s->perm_copied, s->st));
-        double acc = 0;
-        for (int64_t b = 0; b < steps_per_epoch; b++, done++) {
-            STRY(mlp_gather_batch(dX, dY, dW, dP, b * B, B, const_cast<__nv_bfloat16*>(A.x), const_cast<float*>(A.y),
-                                  const_cast<float*>(A.inv_w2), s->st));
-            A.a[0] = const_cast<__nv_bfloat16*>(A.x);
-            A.rows = B;
-            s->step++;
-            const double lr_t = lr * 0.5 * (1.0 + std::cos(M_PI * (double)done / (double)total)) + 1e-6;
-            const float bc1 = (float)(1.0 - std::pow(0.9, (double)s->step));
-            const float bc2 = (float)(1.0 - std::pow(0.999, (double)s->step));
-            const bool last_batch = (b == steps_per_epoch - 1);
-            STRY(mlp_train_step(A, s->params, s->m, s->v, s->wbf, (float)lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2,
-                                last_batch ? s->loss : nullptr, s->st));
-            if (last_batch && e == epochs - 1) {
-                float l = 0;
-                STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
-                STRY(cudaStreamSynchronize(s->st));
-                acc = l / B;
-            }
+    try {
+        if (!s || !x || !y || n < 128 || epochs < 1 || batch < 128 || batch % 128 || !(lr > 0))
+            return sfail(THOTH_GPU_E_INVALID, "bad training arguments (batch must be a multiple of 128)");
+        std::lock_guard<std::mutex> lk(s_mu);
+        const int B = (int)std::min<int64_t>(batch, n / 128 * 128);
+        int rc = ensure_train(s, B);
+        if (rc) return rc;
+        if (n > ((int64_t)1 << 31) - 1) return sfail(THOTH_GPU_E_TOO_LARGE, "training set beyond 2^31 rows");
+        // the whole training set goes up once, packed (bf16 hi/lo inputs, targets, loss weights);
+        // each epoch uploads one permutation and every step gathers its rows on the device
+        if (n > s->cap_ds) {
+            if (s->ds) cudaFree(s->ds);
+            if (s->perm_host) cudaFreeHost(s->perm_host);
+            s->ds = nullptr;
+            s->perm_host = nullptr;
+            s->cap_ds = 0;
+            STRY(cudaMalloc(&s->ds, (size_t)n * (KIN * 2 + 4 + 4 + 4) + 1024));
+            STRY(cudaHostAlloc(&s->perm_host, sizeof(int) * (size_t)n, cudaHostAllocDefault));
+            if (!s->perm_copied) STRY(cudaEventCreateWithFlags(&s->perm_copied, cudaEventDisableTiming));
+            s->cap_ds = n;
         }
-        last = acc;
+        auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+        __nv_bfloat16* dX = reinterpret_cast<__nv_bfloat16*>(s->ds);
+        float* dY = reinterpret_cast<float*>(s->ds + up((size_t)n * KIN * 2));
+        float* dW = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(dY) + up((size_t)n * 4));
+        int* dP = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(dW) + up((size_t)n * 4));
+        {
+            std::vector<__nv_bfloat16> hx;
+            std::vector<float> hy, hw;
+            pack(x, y, scale, nullptr, 0, (int)n, hx, hy, hw);
+            STRY(cudaMemcpy(dX, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice));
+            STRY(cudaMemcpy(dY, hy.data(), hy.size() * 4, cudaMemcpyHostToDevice));
+            STRY(cudaMemcpy(dW, hw.data(), hw.size() * 4, cudaMemcpyHostToDevice));
+        }
+        std::vector<int> idx(n);
+        for (int64_t i = 0; i < n; i++) idx[i] = (int)i;
+        std::mt19937_64 rng(seed);
+        const int64_t steps_per_epoch = n / B, total = steps_per_epoch * epochs;
+        mlp::TrainArgs& A = s->A;
+        double last = 0;
+        STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+        STRY(cudaEventRecord(s->perm_copied, s->st));
+        int64_t done = 0;
+        for (int e = 0; e < epochs; e++) {
+            std::shuffle(idx.begin(), idx.end(), rng);
+            STRY(cudaEventSynchronize(s->perm_copied)); // the previous permutation has left the pinned buffer
+            std::memcpy(s->perm_host, idx.data(), sizeof(int) * (size_t)n);
+            STRY(cudaMemcpyAsync(dP, s->perm_host, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->st));
+            STRY(cudaEventRecord(s->perm_copied, s->st));
+            double acc = 0;
+            for (int64_t b = 0; b < steps_per_epoch; b++, done++) {
+                STRY(mlp_gather_batch(dX, dY, dW, dP, b * B, B, const_cast<__nv_bfloat16*>(A.x), const_cast<float*>(A.y),
+                                      const_cast<float*>(A.inv_w2), s->st));
+                A.a[0] = const_cast<__nv_bfloat16*>(A.x);
+                A.rows = B;
+                s->step++;
+                const double lr_t = lr * 0.5 * (1.0 + std::cos(M_PI * (double)done / (double)total)) + 1e-6;
+                const float bc1 = (float)(1.0 - std::pow(0.9, (double)s->step));
+                const float bc2 = (float)(1.0 - std::pow(0.999, (double)s->step));
+                const bool last_batch = (b == steps_per_epoch - 1);
+                STRY(mlp_train_step(A, s->params, s->m, s->v, s->wbf, (float)lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2,
+                                    last_batch ? s->loss : nullptr, s->st));
+                if (last_batch && e == epochs - 1) {
+                    float l = 0;
+                    STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
+                    STRY(cudaStreamSynchronize(s->st));
+                    acc = l / B;
+                }
+            }
+            last = acc;
+        }
+        rc = check_status(s);
+        if (rc) return rc;
+        if (final_loss) *final_loss = last;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }
-    rc = check_status(s);
-    if (rc) return rc;
-    if (final_loss) *final_loss = last;
-    return THOTH_GPU_OK;
 }
 
 int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, float* y, double* device_ms)
 {
-    if (!s || !x || !y || n < 1 || n > ((int64_t)1 << 30)) return sfail(THOTH_GPU_E_INVALID, "bad predict arguments");
-    std::lock_guard<std::mutex> lk(s_mu);
-    if (n > s->cap_inf) {
-        if (s->ib) cudaFree(s->ib);
-        s->ib = nullptr;
-        const int64_t cap = (n + 127) / 128 * 128;
-        STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 4) + 256));
-        s->cap_inf = cap;
-    }
-    __nv_bfloat16* dx = reinterpret_cast<__nv_bfloat16*>(s->ib);
-    float* dy = reinterpret_cast<float*>(s->ib + (size_t)s->cap_inf * KIN * 2);
-    std::vector<__nv_bfloat16> hx((size_t)n * KIN, to_bf(0.f));
-    for (int64_t i = 0; i < n; i++)
-        for (int f = 0; f < NF; f++) {
-            const float v = x[i * NF + f];
-            const __nv_bfloat16 hi = to_bf(v);
-            hx[(size_t)i * KIN + f] = hi;
-            hx[(size_t)i * KIN + NF + f] = to_bf(v - __bfloat162float(hi));
+    try {
+        if (!s || !x || !y || n < 1 || n > ((int64_t)1 << 30)) return sfail(THOTH_GPU_E_INVALID, "bad predict arguments");
+        std::lock_guard<std::mutex> lk(s_mu);
+        if (n > s->cap_inf) {
+            if (s->ib) cudaFree(s->ib);
+            s->ib = nullptr;
+            s->cap_inf = 0;
+            const int64_t cap = (n + 127) / 128 * 128;
+            STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 4) + 256));
+            s->cap_inf = cap;
         }
-    STRY(cudaMemcpyAsync(dx, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice, s->st));
-    STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
-    cudaEvent_t e0, e1;
-    STRY(cudaEventCreate(&e0));
-    STRY(cudaEventCreate(&e1));
-    const int tiles = (int)((n + 127) / 128);
-    const int grid = std::min(tiles, s->sms);
-    STRY(cudaEventRecord(e0, s->st));
-    STRY(mlp_infer(dx, (int)n, s->params, s->wbf, dy, s->status, grid, s->st));
-    STRY(cudaEventRecord(e1, s->st));
-    STRY(cudaMemcpyAsync(y, dy, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
-    STRY(cudaStreamSynchronize(s->st));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (device_ms) *device_ms = ms;
-    return check_status(s);
+        __nv_bfloat16* dx = reinterpret_cast<__nv_bfloat16*>(s->ib);
+        float* dy = reinterpret_cast<float*>(s->ib + (size_t)s->cap_inf * KIN * 2);
+        std::vector<__nv_bfloat16> hx((size_t)n * KIN, to_bf(0.f));
+        for (int64_t i = 0; i < n; i++)
+            for (int f = 0; f < NF; f++) {
+                const float v = x[i * NF + f];
+                const __nv_bfloat16 hi = to_bf(v);
+                hx[(size_t)i * KIN + f] = hi;
+                hx[(size_t)i * KIN + NF + f] = to_bf(v - __bfloat162float(hi));
+            }
+        STRY(cudaMemcpyAsync(dx, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice, s->st));
+        STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+        cudaEvent_t e0, e1;
+        STRY(cudaEventCreate(&e0));
+        STRY(cudaEventCreate(&e1));
+        const int tiles = (int)((n + 127) / 128);
+        const int grid = std::min(tiles, s->sms);
+        STRY(cudaEventRecord(e0, s->st));
+        STRY(mlp_infer(dx, (int)n, s->params, s->wbf, dy, s->status, grid, s->st));
+        STRY(cudaEventRecord(e1, s->st));
+        STRY(cudaMemcpyAsync(y, dy, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+        STRY(cudaStreamSynchronize(s->st));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (device_ms) *device_ms = ms;
+        return check_status(s);
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 const char* thoth_gpu_surrogate_last_error(void) { return s_err.c_str(); }

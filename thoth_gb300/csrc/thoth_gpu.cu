@@ -16,6 +16,8 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -488,6 +490,8 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
             n_lsv++;
             if (A.lev_points < 2 || !A.lev_ln_step || !A.lev_offset || !A.lev_values)
                 return fail(THOTH_GPU_E_INVALID, "LSV asset needs leverage layers");
+            if (A.lev_points > THOTH_MAX_LEV_POINTS)
+                return fail(THOTH_GPU_E_TOO_LARGE, "lev_points above THOTH_MAX_LEV_POINTS");
         }
         if (a > 0 && A.model != d->assets[0].model) mixed = true;
     }
@@ -1308,12 +1312,14 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
         g_batch.signature.clear();
         if (g_batch.dev) cudaFree(g_batch.dev);
         g_batch.dev = nullptr;
+        g_batch.dev_size = 0; // stays empty if the allocation fails
         CUDA_TRY(cudaMalloc(&g_batch.dev, total));
         g_batch.dev_size = total;
     }
     if (std::max(o_outs, back) > g_batch.host_size) {
         if (g_batch.host) cudaFreeHost(g_batch.host);
         g_batch.host = nullptr;
+        g_batch.host_size = 0;
         CUDA_TRY(cudaHostAlloc(&g_batch.host, std::max(o_outs, back), cudaHostAllocDefault));
         g_batch.host_size = std::max(o_outs, back);
     }
@@ -1635,381 +1641,519 @@ extern "C" {
 
 int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    return price_noalloc_locked(book, out);
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        return price_noalloc_locked(book, out);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_autotune_book(const ThothBookDesc* book, int32_t reps, ThothTuneResult* out)
 {
-    if (reps < 1 || reps > 1000) return fail(THOTH_GPU_E_INVALID, "reps must be in [1, 1000]");
-    std::lock_guard<std::mutex> lk(g_mu);
-    return autotune_book_locked(book, reps, out);
+    try {
+        if (reps < 1 || reps > 1000) return fail(THOTH_GPU_E_INVALID, "reps must be in [1, 1000]");
+        std::lock_guard<std::mutex> lk(g_mu);
+        return autotune_book_locked(book, reps, out);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_autotune_batch(const ThothBookDesc* books, int32_t n_books, int32_t reps, ThothTuneResult* out)
 {
-    if (!books || n_books < 1) return fail(THOTH_GPU_E_INVALID, "bad batch");
-    if (reps < 1 || reps > 1000) return fail(THOTH_GPU_E_INVALID, "reps must be in [1, 1000]");
-    std::lock_guard<std::mutex> lk(g_mu);
-    return autotune_batch_locked(books, n_books, reps, out);
+    try {
+        if (!books || n_books < 1) return fail(THOTH_GPU_E_INVALID, "bad batch");
+        if (reps < 1 || reps > 1000) return fail(THOTH_GPU_E_INVALID, "reps must be in [1, 1000]");
+        std::lock_guard<std::mutex> lk(g_mu);
+        return autotune_batch_locked(books, n_books, reps, out);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_autotune_save(const char* path)
 {
-    if (!path) return fail(THOTH_GPU_E_INVALID, "null path");
-    std::lock_guard<std::mutex> lk(g_mu);
-    return autotune_save_locked(path);
+    try {
+        if (!path) return fail(THOTH_GPU_E_INVALID, "null path");
+        std::lock_guard<std::mutex> lk(g_mu);
+        return autotune_save_locked(path);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_autotune_load(const char* path)
 {
-    if (!path) return fail(THOTH_GPU_E_INVALID, "null path");
-    std::lock_guard<std::mutex> lk(g_mu);
-    return autotune_load_locked(path);
+    try {
+        if (!path) return fail(THOTH_GPU_E_INVALID, "null path");
+        std::lock_guard<std::mutex> lk(g_mu);
+        return autotune_load_locked(path);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_autotune_clear(void)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    g_tuned.clear();
-    g_batch.streams_wanted = 8;
-    g_batch.policy = 0;
-    g_batch.shape = -1;
-    return THOTH_GPU_OK;
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_tuned.clear();
+        g_batch.streams_wanted = 8;
+        g_batch.policy = 0;
+        g_batch.shape = -1;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_batch_graph_replays(void)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    return g_batch.replays;
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        return g_batch.replays;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out)
 {
-    if (!out) return fail(THOTH_GPU_E_INVALID, "null handle pointer");
-    std::lock_guard<std::mutex> lk(g_mu);
-    int rc = ensure_device();
-    if (rc) return rc;
-    ThothBookHandle* h = new ThothBookHandle();
-    rc = build_plan(book, h->plan);
-    if (rc) {
-        delete h;
-        return rc;
+    try {
+        if (!out) return fail(THOTH_GPU_E_INVALID, "null handle pointer");
+        std::lock_guard<std::mutex> lk(g_mu);
+        int rc = ensure_device();
+        if (rc) return rc;
+        ThothBookHandle* h = new ThothBookHandle();
+        rc = build_plan(book, h->plan);
+        if (rc) {
+            delete h;
+            return rc;
+        }
+        h->grid = grid_for(h->plan);
+        h->layout = layout_of(h->plan, h->grid);
+        cudaError_t e = cudaMalloc(&h->dev, h->layout.total);
+        if (e != cudaSuccess) {
+            delete h;
+            return fail(THOTH_GPU_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        e = cudaMemcpy(h->dev, h->plan.blob.bytes.data(), h->plan.blob.bytes.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(h->dev);
+            delete h;
+            return fail(THOTH_GPU_E_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+        }
+        bind(h->plan, h->dev);
+        h->plan.dp.sobol_lo = reinterpret_cast<const uint32_t*>(h->dev + h->layout.o_lo);
+        e = gather_low(h->plan, g_dev.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g_dev.stream);
+        if (e != cudaSuccess) {
+            cudaFree(h->dev);
+            delete h;
+            return fail(THOTH_GPU_E_CUDA, std::string("gather: ") + cudaGetErrorString(e));
+        }
+        *out = h;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }
-    h->grid = grid_for(h->plan);
-    h->layout = layout_of(h->plan, h->grid);
-    cudaError_t e = cudaMalloc(&h->dev, h->layout.total);
-    if (e != cudaSuccess) {
-        delete h;
-        return fail(THOTH_GPU_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    }
-    e = cudaMemcpy(h->dev, h->plan.blob.bytes.data(), h->plan.blob.bytes.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        cudaFree(h->dev);
-        delete h;
-        return fail(THOTH_GPU_E_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
-    }
-    bind(h->plan, h->dev);
-    h->plan.dp.sobol_lo = reinterpret_cast<const uint32_t*>(h->dev + h->layout.o_lo);
-    e = gather_low(h->plan, g_dev.stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(g_dev.stream);
-    if (e != cudaSuccess) {
-        cudaFree(h->dev);
-        delete h;
-        return fail(THOTH_GPU_E_CUDA, std::string("gather: ") + cudaGetErrorString(e));
-    }
-    *out = h;
-    return THOTH_GPU_OK;
 }
 
 int thoth_gpu_book_run(ThothBookHandle* h, ThothBookResult* out)
 {
-    if (!h || !out) return fail(THOTH_GPU_E_INVALID, "null handle or result");
-    std::lock_guard<std::mutex> lk(g_mu);
-    int rc = ensure_device();
-    if (rc) return rc;
-    return run_bound(h->plan, h->dev, h->layout, h->grid, out, false);
+    try {
+        if (!h || !out) return fail(THOTH_GPU_E_INVALID, "null handle or result");
+        std::lock_guard<std::mutex> lk(g_mu);
+        int rc = ensure_device();
+        if (rc) return rc;
+        return run_bound(h->plan, h->dev, h->layout, h->grid, out, false);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_book_destroy(ThothBookHandle* h)
 {
-    if (!h) return THOTH_GPU_OK;
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (h->dev) cudaFree(h->dev);
-    delete h;
-    return THOTH_GPU_OK;
+    try {
+        if (!h) return THOTH_GPU_OK;
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (h->dev) cudaFree(h->dev);
+        delete h;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_tc_gemm_test(const uint16_t* a, const uint16_t* b, int32_t n, int32_t k, float* d)
 {
-    if (!a || !b || !d || n < 16 || n > 256 || n % 16 || k < 16 || k > 256 || k % 16)
-        return fail(THOTH_GPU_E_INVALID, "tc gemm test: N, K must be multiples of 16 in [16, 256]");
-    std::lock_guard<std::mutex> lk(g_mu);
-    int rc = ensure_device();
-    if (rc) return rc;
-    const size_t ba = (size_t)128 * k * 2, bb = (size_t)n * k * 2, bd = (size_t)128 * n * 4;
-    const size_t oa = 0, ob = (ba + 255) & ~size_t(255), od = ob + ((bb + 255) & ~size_t(255)),
-                 os = od + ((bd + 255) & ~size_t(255));
-    rc = ensure_arena(os + 256);
-    if (rc) return rc;
-    unsigned char* base = g_dev.arena;
-    CUDA_TRY(cudaMemcpyAsync(base + oa, a, ba, cudaMemcpyHostToDevice, g_dev.stream));
-    CUDA_TRY(cudaMemcpyAsync(base + ob, b, bb, cudaMemcpyHostToDevice, g_dev.stream));
-    CUDA_TRY(cudaMemsetAsync(base + os, 0, sizeof(int), g_dev.stream));
-    CUDA_TRY(launch_tc_gemm_test(base + oa, base + ob, n, k, reinterpret_cast<float*>(base + od),
-                                 reinterpret_cast<int*>(base + os), g_dev.stream));
-    int status = 0;
-    CUDA_TRY(cudaMemcpyAsync(d, base + od, bd, cudaMemcpyDeviceToHost, g_dev.stream));
-    CUDA_TRY(cudaMemcpyAsync(&status, base + os, sizeof(int), cudaMemcpyDeviceToHost, g_dev.stream));
-    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
-    if (status) return fail(THOTH_GPU_E_CUDA, "tensor-core MMA did not complete (bounded wait expired)");
-    return THOTH_GPU_OK;
+    try {
+        if (!a || !b || !d || n < 16 || n > 256 || n % 16 || k < 16 || k > 256 || k % 16)
+            return fail(THOTH_GPU_E_INVALID, "tc gemm test: N, K must be multiples of 16 in [16, 256]");
+        std::lock_guard<std::mutex> lk(g_mu);
+        int rc = ensure_device();
+        if (rc) return rc;
+        const size_t ba = (size_t)128 * k * 2, bb = (size_t)n * k * 2, bd = (size_t)128 * n * 4;
+        const size_t oa = 0, ob = (ba + 255) & ~size_t(255), od = ob + ((bb + 255) & ~size_t(255)),
+                     os = od + ((bd + 255) & ~size_t(255));
+        rc = ensure_arena(os + 256);
+        if (rc) return rc;
+        unsigned char* base = g_dev.arena;
+        CUDA_TRY(cudaMemcpyAsync(base + oa, a, ba, cudaMemcpyHostToDevice, g_dev.stream));
+        CUDA_TRY(cudaMemcpyAsync(base + ob, b, bb, cudaMemcpyHostToDevice, g_dev.stream));
+        CUDA_TRY(cudaMemsetAsync(base + os, 0, sizeof(int), g_dev.stream));
+        CUDA_TRY(launch_tc_gemm_test(base + oa, base + ob, n, k, reinterpret_cast<float*>(base + od),
+                                     reinterpret_cast<int*>(base + os), g_dev.stream));
+        int status = 0;
+        CUDA_TRY(cudaMemcpyAsync(d, base + od, bd, cudaMemcpyDeviceToHost, g_dev.stream));
+        CUDA_TRY(cudaMemcpyAsync(&status, base + os, sizeof(int), cudaMemcpyDeviceToHost, g_dev.stream));
+        CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+        if (status) return fail(THOTH_GPU_E_CUDA, "tensor-core MMA did not complete (bounded wait expired)");
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_measure_fp32_peak(double* tflops, double* ms_out)
 {
-    if (!tflops) return fail(THOTH_GPU_E_INVALID, "null output");
-    std::lock_guard<std::mutex> lk(g_mu);
-    int rc = ensure_device();
-    if (rc) return rc;
-    rc = ensure_arena(1 << 20);
-    if (rc) return rc;
-    const int blocks = g_dev.sms * 8, iters = 4096;
-    float* d = reinterpret_cast<float*>(g_dev.arena);
-    CUDA_TRY(launch_fma_peak(d, blocks, 64, g_dev.stream)); // warm-up
-    CUDA_TRY(cudaEventRecord(g_dev.ev0, g_dev.stream));
-    CUDA_TRY(launch_fma_peak(d, blocks, iters, g_dev.stream));
-    CUDA_TRY(cudaEventRecord(g_dev.ev1, g_dev.stream));
-    CUDA_TRY(cudaEventSynchronize(g_dev.ev1));
-    float ms = 0;
-    CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
-    const double fmas = (double)blocks * 256 * iters * 16 * 8;
-    *tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
-    if (ms_out) *ms_out = ms;
-    return THOTH_GPU_OK;
+    try {
+        if (!tflops) return fail(THOTH_GPU_E_INVALID, "null output");
+        std::lock_guard<std::mutex> lk(g_mu);
+        int rc = ensure_device();
+        if (rc) return rc;
+        rc = ensure_arena(1 << 20);
+        if (rc) return rc;
+        const int blocks = g_dev.sms * 8, iters = 4096;
+        float* d = reinterpret_cast<float*>(g_dev.arena);
+        CUDA_TRY(launch_fma_peak(d, blocks, 64, g_dev.stream)); // warm-up
+        CUDA_TRY(cudaEventRecord(g_dev.ev0, g_dev.stream));
+        CUDA_TRY(launch_fma_peak(d, blocks, iters, g_dev.stream));
+        CUDA_TRY(cudaEventRecord(g_dev.ev1, g_dev.stream));
+        CUDA_TRY(cudaEventSynchronize(g_dev.ev1));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+        const double fmas = (double)blocks * 256 * iters * 16 * 8;
+        *tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
+        if (ms_out) *ms_out = ms;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_available(void)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    return ensure_device() == THOTH_GPU_OK ? 1 : 0;
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        return ensure_device() == THOTH_GPU_OK ? 1 : 0;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_device_info(char* buf, size_t n)
 {
-    if (!buf || n == 0) return fail(THOTH_GPU_E_INVALID, "null buffer");
-    int count = 0;
-    std::string s;
-    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
-        s = "no CUDA device found";
-    } else {
-        cudaDeviceProp p;
-        if (cudaGetDeviceProperties(&p, 0) != cudaSuccess) {
-            s = "CUDA device query failed";
+    try {
+        if (!buf || n == 0) return fail(THOTH_GPU_E_INVALID, "null buffer");
+        int count = 0;
+        std::string s;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+            s = "no CUDA device found";
         } else {
-            s = std::string(p.name) + " (sm_" + std::to_string(p.major) + std::to_string(p.minor) + ", " +
-                std::to_string(p.multiProcessorCount) + " SMs, " +
-                std::to_string((long long)(p.totalGlobalMem >> 20)) + " MiB)";
+            cudaDeviceProp p;
+            if (cudaGetDeviceProperties(&p, 0) != cudaSuccess) {
+                s = "CUDA device query failed";
+            } else {
+                s = std::string(p.name) + " (sm_" + std::to_string(p.major) + std::to_string(p.minor) + ", " +
+                    std::to_string(p.multiProcessorCount) + " SMs, " +
+                    std::to_string((long long)(p.totalGlobalMem >> 20)) + " MiB)";
+            }
         }
+        std::snprintf(buf, n, "%s", s.c_str());
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }
-    std::snprintf(buf, n, "%s", s.c_str());
-    return THOTH_GPU_OK;
 }
 
 int thoth_gpu_price_book(const ThothBookDesc* book, ThothBookResult* out)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    return price_locked(book, out);
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        return price_locked(book, out);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_price_european_gbm(double forward, double strike, double t, double vol, double df, int is_call,
                                  int64_t paths, uint64_t seed, ThothGbmResult* out)
 {
-    if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
-    if (paths <= 0) {
-        // reference behaviour for an empty run (mcl_gpu.cu:104-107)
-        out->premium = 0.0;
-        out->trust = 0.0;
+    try {
+        if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
+        if (paths <= 0) {
+            // reference behaviour for an empty run (mcl_gpu.cu:104-107)
+            out->premium = 0.0;
+            out->trust = 0.0;
+            return THOTH_GPU_OK;
+        }
+        if (!(t > 0) || !(forward > 0) || !(df > 0) || !(vol >= 0))
+            return fail(THOTH_GPU_E_INVALID, "forward, df and t must be > 0 and vol >= 0");
+        const double times[2] = {0.0, t};
+        const double carry[2] = {0.0, 0.0};
+        ThothAsset A;
+        std::memset(&A, 0, sizeof A);
+        A.model = THOTH_MODEL_GBM;
+        A.spot = forward;
+        A.carry = carry;
+        A.vol = vol;
+        ThothProduct Q;
+        std::memset(&Q, 0, sizeof Q);
+        Q.kind = THOTH_PRODUCT_VANILLA;
+        Q.option_type = is_call ? THOTH_CALL : THOTH_PUT;
+        Q.asset = 0;
+        Q.maturity = 1;
+        Q.strike = strike;
+        Q.zero_rate = -std::log(df) / t;
+        Q.fx = 1.0;
+        ThothBookDesc d;
+        std::memset(&d, 0, sizeof d);
+        d.n_dates = 2;
+        d.t = times;
+        d.n_assets = 1;
+        d.assets = &A;
+        d.n_products = 1;
+        d.products = &Q;
+        d.paths = paths < 2 ? 2 : paths;
+        d.use_sobol = (uint64_t)paths < ((uint64_t)1 << 32) ? 1 : 0;
+        d.seed = seed;
+        double prem = 0, tr = 0;
+        ThothBookResult r;
+        std::memset(&r, 0, sizeof r);
+        r.premium = &prem;
+        r.trust = &tr;
+        std::lock_guard<std::mutex> lk(g_mu);
+        const int rc = price_locked(&d, &r);
+        if (rc) return rc;
+        out->premium = prem;
+        out->trust = tr;
         return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }
-    if (!(t > 0) || !(forward > 0) || !(df > 0) || !(vol >= 0))
-        return fail(THOTH_GPU_E_INVALID, "forward, df and t must be > 0 and vol >= 0");
-    const double times[2] = {0.0, t};
-    const double carry[2] = {0.0, 0.0};
-    ThothAsset A;
-    std::memset(&A, 0, sizeof A);
-    A.model = THOTH_MODEL_GBM;
-    A.spot = forward;
-    A.carry = carry;
-    A.vol = vol;
-    ThothProduct Q;
-    std::memset(&Q, 0, sizeof Q);
-    Q.kind = THOTH_PRODUCT_VANILLA;
-    Q.option_type = is_call ? THOTH_CALL : THOTH_PUT;
-    Q.asset = 0;
-    Q.maturity = 1;
-    Q.strike = strike;
-    Q.zero_rate = -std::log(df) / t;
-    Q.fx = 1.0;
-    ThothBookDesc d;
-    std::memset(&d, 0, sizeof d);
-    d.n_dates = 2;
-    d.t = times;
-    d.n_assets = 1;
-    d.assets = &A;
-    d.n_products = 1;
-    d.products = &Q;
-    d.paths = paths < 2 ? 2 : paths;
-    d.use_sobol = (uint64_t)paths < ((uint64_t)1 << 32) ? 1 : 0;
-    d.seed = seed;
-    double prem = 0, tr = 0;
-    ThothBookResult r;
-    std::memset(&r, 0, sizeof r);
-    r.premium = &prem;
-    r.trust = &tr;
-    std::lock_guard<std::mutex> lk(g_mu);
-    const int rc = price_locked(&d, &r);
-    if (rc) return rc;
-    out->premium = prem;
-    out->trust = tr;
-    return THOTH_GPU_OK;
 }
 
 int thoth_gpu_sobol_points(int32_t dims, int64_t skip, int64_t n_points, uint32_t* out)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (dims < 1 || dims > max_dims() || skip < 0 || n_points < 0 || !out)
-        return fail(THOTH_GPU_E_INVALID, "bad Sobol request");
-    if ((uint64_t)skip + (uint64_t)n_points >= ((uint64_t)1 << 32)) return fail(THOTH_GPU_E_TOO_LARGE, "index >= 2^32");
-    int rc = ensure_device();
-    if (rc) return rc;
-    const size_t bytes = sizeof(uint32_t) * (size_t)dims * (size_t)n_points;
-    rc = ensure_arena(bytes + 256);
-    if (rc) return rc;
-    uint32_t* d_out = reinterpret_cast<uint32_t*>(g_dev.arena);
-    CUDA_TRY(launch_sobol_points(g_dev.sobol_v, dims, skip, n_points, d_out, g_dev.stream));
-    CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
-    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
-    return THOTH_GPU_OK;
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (dims < 1 || dims > max_dims() || skip < 0 || n_points < 0 || !out)
+            return fail(THOTH_GPU_E_INVALID, "bad Sobol request");
+        if ((uint64_t)skip + (uint64_t)n_points >= ((uint64_t)1 << 32)) return fail(THOTH_GPU_E_TOO_LARGE, "index >= 2^32");
+        int rc = ensure_device();
+        if (rc) return rc;
+        const size_t bytes = sizeof(uint32_t) * (size_t)dims * (size_t)n_points;
+        rc = ensure_arena(bytes + 256);
+        if (rc) return rc;
+        uint32_t* d_out = reinterpret_cast<uint32_t*>(g_dev.arena);
+        CUDA_TRY(launch_sobol_points(g_dev.sobol_v, dims, skip, n_points, d_out, g_dev.stream));
+        CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
+        CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_normal_quantiles(const uint32_t* x, int64_t n, float* out)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (n < 0 || (n > 0 && (!x || !out))) return fail(THOTH_GPU_E_INVALID, "bad quantile request");
-    int rc = ensure_device();
-    if (rc) return rc;
-    const size_t bx = ((sizeof(uint32_t) * (size_t)n + 255) & ~size_t(255));
-    rc = ensure_arena(bx + sizeof(float) * (size_t)n + 256);
-    if (rc) return rc;
-    uint32_t* dx = reinterpret_cast<uint32_t*>(g_dev.arena);
-    float* dy = reinterpret_cast<float*>(g_dev.arena + bx);
-    CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, g_dev.stream));
-    CUDA_TRY(launch_quantile(dx, n, dy, g_dev.stream));
-    CUDA_TRY(cudaMemcpyAsync(out, dy, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, g_dev.stream));
-    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
-    return THOTH_GPU_OK;
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (n < 0 || (n > 0 && (!x || !out))) return fail(THOTH_GPU_E_INVALID, "bad quantile request");
+        int rc = ensure_device();
+        if (rc) return rc;
+        const size_t bx = ((sizeof(uint32_t) * (size_t)n + 255) & ~size_t(255));
+        rc = ensure_arena(bx + sizeof(float) * (size_t)n + 256);
+        if (rc) return rc;
+        uint32_t* dx = reinterpret_cast<uint32_t*>(g_dev.arena);
+        float* dy = reinterpret_cast<float*>(g_dev.arena + bx);
+        CUDA_TRY(cudaMemcpyAsync(dx, x, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, g_dev.stream));
+        CUDA_TRY(launch_quantile(dx, n, dy, g_dev.stream));
+        CUDA_TRY(cudaMemcpyAsync(out, dy, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, g_dev.stream));
+        CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factors, int64_t skip, int64_t n_paths,
                                 float* out)
 {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!t || n_dates < 2 || n_dates > THOTH_MAX_DATES || factors < 1 || factors > 2 || skip < 0 || n_paths < 1 || !out)
-        return fail(THOTH_GPU_E_INVALID, "bad bridge request");
-    if ((uint64_t)skip + (uint64_t)n_paths >= ((uint64_t)1 << 32)) return fail(THOTH_GPU_E_TOO_LARGE, "index >= 2^32");
-    int rc = ensure_device();
-    if (rc) return rc;
-    std::vector<double> tl(t, t + n_dates);
-    for (int i = 1; i < n_dates; i++)
-        if (!(tl[i] > tl[i - 1])) return fail(THOTH_GPU_E_INVALID, "t must be strictly increasing");
-    BridgeProgram bp;
-    std::string err;
-    if (!build_bridge(tl, bp, err)) return fail(THOTH_GPU_E_INVALID, err);
-    const int N = n_dates - 1;
-    std::vector<float> isd(N);
-    for (int i = 1; i <= N; i++) isd[i - 1] = (float)(1.0 / std::sqrt(tl[i] - tl[i - 1]));
-    Plan P;
-    DevPlan& D = P.dp;
-    std::memset(&D, 0, sizeof D);
-    D.n_steps = N;
-    D.n_assets = 1;
-    D.ref_factors = factors;
-    D.n_factors_active = factors;
-    D.stack_factors = factors;
-    D.sobol_dims = (int)std::min<long>((long)N * factors, max_dims());
-    D.use_sobol = 1;
-    D.stack_depth = bp.stack_depth;
-    D.skip = skip;
-    D.paths = n_paths;
-    D.fid_spot[0] = 0;
-    D.cidx_spot[0] = 0;
-    D.fid_var[0] = factors == 2 ? 1 : -1;
-    D.cidx_var[0] = factors == 2 ? 1 : -1;
-    const int T = 256;
-    D.tile_first = (skip + 1) / T;
-    D.n_tiles = (skip + n_paths) / T - (skip + 1) / T + 1;
-    P.o_isd = P.blob.put(isd);
-    P.o_prog = P.blob.put(bp.prog);
-    P.o_nodes = P.blob.put(bp.nodes);
-    P.o_recs = P.blob.put(make_recs(bp, isd, std::vector<char>(), factors));
-    std::vector<int> order = sobol_order(bp, D);
-    D.n_sobol = (int)order.size();
-    P.o_sord = P.blob.put(order);
-    P.T = T;
-    const size_t smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, factors, 0, 0, 0);
-    const size_t o_lo = (P.blob.bytes.size() + 255) & ~size_t(255);
-    const size_t o_out = o_lo + ((low_bytes(P) + 255) & ~size_t(255));
-    const size_t bytes = sizeof(float) * (size_t)n_paths * factors * N;
-    rc = ensure_arena(o_out + bytes + 256);
-    if (rc) return rc;
-    rc = ensure_pinned(P.blob.bytes.size());
-    if (rc) return rc;
-    std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
-    CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, g_dev.stream));
-    D.inv_sqrt_dt = reinterpret_cast<const float*>(g_dev.arena + P.o_isd);
-    D.prog = reinterpret_cast<const StepProg*>(g_dev.arena + P.o_prog);
-    D.nodes = reinterpret_cast<const BridgeNode*>(g_dev.arena + P.o_nodes);
-    D.recs = reinterpret_cast<const StepRec*>(g_dev.arena + P.o_recs);
-    D.sobol_v = g_dev.sobol_v;
-    D.sobol_order = reinterpret_cast<const int*>(g_dev.arena + P.o_sord);
-    D.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + o_lo);
-    float* d_out = reinterpret_cast<float*>(g_dev.arena + o_out);
-    CUDA_TRY(gather_low(P, g_dev.stream));
-    const int grid = (int)std::min<int64_t>(D.n_tiles, (int64_t)g_dev.sms * 2);
-    CUDA_TRY(launch_bridge(D, grid, smem, d_out, g_dev.stream));
-    CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
-    CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
-    return THOTH_GPU_OK;
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!t || n_dates < 2 || n_dates > THOTH_MAX_DATES || factors < 1 || factors > 2 || skip < 0 || n_paths < 1 || !out)
+            return fail(THOTH_GPU_E_INVALID, "bad bridge request");
+        if ((uint64_t)skip + (uint64_t)n_paths >= ((uint64_t)1 << 32)) return fail(THOTH_GPU_E_TOO_LARGE, "index >= 2^32");
+        int rc = ensure_device();
+        if (rc) return rc;
+        std::vector<double> tl(t, t + n_dates);
+        for (int i = 1; i < n_dates; i++)
+            if (!(tl[i] > tl[i - 1])) return fail(THOTH_GPU_E_INVALID, "t must be strictly increasing");
+        BridgeProgram bp;
+        std::string err;
+        if (!build_bridge(tl, bp, err)) return fail(THOTH_GPU_E_INVALID, err);
+        const int N = n_dates - 1;
+        std::vector<float> isd(N);
+        for (int i = 1; i <= N; i++) isd[i - 1] = (float)(1.0 / std::sqrt(tl[i] - tl[i - 1]));
+        Plan P;
+        DevPlan& D = P.dp;
+        std::memset(&D, 0, sizeof D);
+        D.n_steps = N;
+        D.n_assets = 1;
+        D.ref_factors = factors;
+        D.n_factors_active = factors;
+        D.stack_factors = factors;
+        D.sobol_dims = (int)std::min<long>((long)N * factors, max_dims());
+        D.use_sobol = 1;
+        D.stack_depth = bp.stack_depth;
+        D.skip = skip;
+        D.paths = n_paths;
+        D.fid_spot[0] = 0;
+        D.cidx_spot[0] = 0;
+        D.fid_var[0] = factors == 2 ? 1 : -1;
+        D.cidx_var[0] = factors == 2 ? 1 : -1;
+        const int T = 256;
+        D.tile_first = (skip + 1) / T;
+        D.n_tiles = (skip + n_paths) / T - (skip + 1) / T + 1;
+        P.o_isd = P.blob.put(isd);
+        P.o_prog = P.blob.put(bp.prog);
+        P.o_nodes = P.blob.put(bp.nodes);
+        P.o_recs = P.blob.put(make_recs(bp, isd, std::vector<char>(), factors));
+        std::vector<int> order = sobol_order(bp, D);
+        D.n_sobol = (int)order.size();
+        P.o_sord = P.blob.put(order);
+        P.T = T;
+        const size_t smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, factors, 0, 0, 0);
+        const size_t o_lo = (P.blob.bytes.size() + 255) & ~size_t(255);
+        const size_t o_out = o_lo + ((low_bytes(P) + 255) & ~size_t(255));
+        const size_t bytes = sizeof(float) * (size_t)n_paths * factors * N;
+        rc = ensure_arena(o_out + bytes + 256);
+        if (rc) return rc;
+        rc = ensure_pinned(P.blob.bytes.size());
+        if (rc) return rc;
+        std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
+        CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, g_dev.stream));
+        D.inv_sqrt_dt = reinterpret_cast<const float*>(g_dev.arena + P.o_isd);
+        D.prog = reinterpret_cast<const StepProg*>(g_dev.arena + P.o_prog);
+        D.nodes = reinterpret_cast<const BridgeNode*>(g_dev.arena + P.o_nodes);
+        D.recs = reinterpret_cast<const StepRec*>(g_dev.arena + P.o_recs);
+        D.sobol_v = g_dev.sobol_v;
+        D.sobol_order = reinterpret_cast<const int*>(g_dev.arena + P.o_sord);
+        D.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + o_lo);
+        float* d_out = reinterpret_cast<float*>(g_dev.arena + o_out);
+        CUDA_TRY(gather_low(P, g_dev.stream));
+        const int grid = (int)std::min<int64_t>(D.n_tiles, (int64_t)g_dev.sms * 2);
+        CUDA_TRY(launch_bridge(D, grid, smem, d_out, g_dev.stream));
+        CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
+        CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBookResult* out)
 {
-    if (!books || !out || n_books < 0) return fail(THOTH_GPU_E_INVALID, "bad batch");
-    std::lock_guard<std::mutex> lk(g_mu);
-    return price_batch_locked(books, n_books, out);
+    try {
+        if (!books || !out || n_books < 0) return fail(THOTH_GPU_E_INVALID, "bad batch");
+        std::lock_guard<std::mutex> lk(g_mu);
+        return price_batch_locked(books, n_books, out);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_batch_streams(int32_t n)
 {
-    if (n < 1 || n > 64) return fail(THOTH_GPU_E_INVALID, "streams must be in [1, 64]");
-    std::lock_guard<std::mutex> lk(g_mu);
-    g_batch.streams_wanted = n;
-    return THOTH_GPU_OK;
+    try {
+        if (n < 1 || n > 64) return fail(THOTH_GPU_E_INVALID, "streams must be in [1, 64]");
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_batch.streams_wanted = n;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 // no lock: called from another thread while a pricing call holds the mutex
 int thoth_gpu_request_cancel(void)
 {
-    if (!g_dev.ready) return fail(THOTH_GPU_E_NODEVICE, "engine not initialised");
-    *(volatile int*)g_dev.cancel_host = 1;
-    return THOTH_GPU_OK;
+    try {
+        if (!g_dev.ready) return fail(THOTH_GPU_E_NODEVICE, "engine not initialised");
+        *(volatile int*)g_dev.cancel_host = 1;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 int thoth_gpu_clear_cancel(void)
 {
-    if (g_dev.ready) *(volatile int*)g_dev.cancel_host = 0;
-    return THOTH_GPU_OK;
+    try {
+        if (g_dev.ready) *(volatile int*)g_dev.cancel_host = 0;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 const char* thoth_gpu_last_error(void) { return g_err.c_str(); }
@@ -2017,47 +2161,59 @@ const char* thoth_gpu_last_error(void) { return g_err.c_str(); }
 int thoth_gpu_bridge_program(const double* t, int32_t n_dates, int32_t* first_count, double* nodes, int32_t* n_nodes,
                              int32_t* stack_depth)
 {
-    if (!t || n_dates < 2 || n_dates > THOTH_MAX_DATES || !first_count || !nodes || !n_nodes || !stack_depth)
-        return fail(THOTH_GPU_E_INVALID, "bad bridge program request");
-    std::vector<double> tl(t, t + n_dates);
-    for (int i = 1; i < n_dates; i++)
-        if (!(tl[i] > tl[i - 1])) return fail(THOTH_GPU_E_INVALID, "t must be strictly increasing");
-    BridgeProgram bp;
-    std::string err;
-    if (!build_bridge(tl, bp, err)) return fail(THOTH_GPU_E_INVALID, err);
-    for (size_t i = 0; i < bp.prog.size(); i++) {
-        first_count[2 * i] = bp.prog[i].first;
-        first_count[2 * i + 1] = bp.prog[i].count;
+    try {
+        if (!t || n_dates < 2 || n_dates > THOTH_MAX_DATES || !first_count || !nodes || !n_nodes || !stack_depth)
+            return fail(THOTH_GPU_E_INVALID, "bad bridge program request");
+        std::vector<double> tl(t, t + n_dates);
+        for (int i = 1; i < n_dates; i++)
+            if (!(tl[i] > tl[i - 1])) return fail(THOTH_GPU_E_INVALID, "t must be strictly increasing");
+        BridgeProgram bp;
+        std::string err;
+        if (!build_bridge(tl, bp, err)) return fail(THOTH_GPU_E_INVALID, err);
+        for (size_t i = 0; i < bp.prog.size(); i++) {
+            first_count[2 * i] = bp.prog[i].first;
+            first_count[2 * i + 1] = bp.prog[i].count;
+        }
+        for (size_t k = 0; k < bp.nodes.size(); k++) {
+            nodes[4 * k] = bp.nodes[k].lw;
+            nodes[4 * k + 1] = bp.nodes[k].rw;
+            nodes[4 * k + 2] = bp.nodes[k].sd;
+            nodes[4 * k + 3] = bp.nodes[k].bstep;
+        }
+        *n_nodes = (int32_t)bp.nodes.size();
+        *stack_depth = bp.stack_depth;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }
-    for (size_t k = 0; k < bp.nodes.size(); k++) {
-        nodes[4 * k] = bp.nodes[k].lw;
-        nodes[4 * k + 1] = bp.nodes[k].rw;
-        nodes[4 * k + 2] = bp.nodes[k].sd;
-        nodes[4 * k + 3] = bp.nodes[k].bstep;
-    }
-    *n_nodes = (int32_t)bp.nodes.size();
-    *stack_depth = bp.stack_depth;
-    return THOTH_GPU_OK;
 }
 
 int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out)
 {
-    if (!out) return fail(THOTH_GPU_E_INVALID, "null output");
-    std::lock_guard<std::mutex> lk(g_mu);
-    Plan P;
-    const int rc = build_plan(book, P);
-    if (rc) return rc;
-    out[0] = P.variant;
-    out[1] = P.T;
-    out[2] = (int64_t)P.smem;
-    out[3] = P.dp.n_slots_used;
-    out[4] = P.dp.n_groups;
-    out[5] = P.dp.stack_depth;
-    out[6] = P.dp.sobol_dims;
-    out[7] = P.dp.n_tiles;
-    out[8] = P.shape;
-    out[9] = book_shape_threads(P.variant, P.shape);
-    return THOTH_GPU_OK;
+    try {
+        if (!out) return fail(THOTH_GPU_E_INVALID, "null output");
+        std::lock_guard<std::mutex> lk(g_mu);
+        Plan P;
+        const int rc = build_plan(book, P);
+        if (rc) return rc;
+        out[0] = P.variant;
+        out[1] = P.T;
+        out[2] = (int64_t)P.smem;
+        out[3] = P.dp.n_slots_used;
+        out[4] = P.dp.n_groups;
+        out[5] = P.dp.stack_depth;
+        out[6] = P.dp.sobol_dims;
+        out[7] = P.dp.n_tiles;
+        out[8] = P.shape;
+        out[9] = book_shape_threads(P.variant, P.shape);
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
 }
 
 } // extern "C"
