@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain-MC grid section")
     ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch (256 books) section")
     ap.add_argument("--no-lsv", action="store_true", help="skip the multi-asset LSV book section")
+    ap.add_argument("--no-paths", action="store_true", help="skip the stored-paths (HBM) section")
     return ap.parse_args()
 
 
@@ -185,6 +186,38 @@ def lsv_book_section(G, flush, steps):
             "book_premium": r["book_premium"], "book_trust": r["book_trust"]}
 
 
+def paths_section(G, flush):
+    """The path-storing variant: every date's spot of every path written to HBM
+    (date-major, coalesced), 2^20 paths; GBM on 252 daily steps and the Heston grid
+    (504 steps). Rate against the measured HBM copy bandwidth."""
+    import numpy as np
+    import torch
+    from thoth_gb300 import abi, workloads as W
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    gbm = abi.Book(days=np.arange(0, 253), paths=1 << 20)
+    a = gbm.add_gbm(100.0, 0.25, 0.02)
+    gbm.add_vanilla(a, 100.0, 252, abi.CALL, zero_rate=0.03)
+    out = {}
+    for name, book in (("gbm_252", gbm), ("heston_grid_504", W.heston_grid(paths=1 << 20))):
+        G.simulate_paths(book, 0)
+        ms = []
+        for _ in range(3):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            ms.append(G.simulate_paths(book, 0)[1])
+        dev = float(np.median(ms))
+        n_dates = book.desc().n_dates
+        written = 4.0 * n_dates * book.paths
+        out[name] = {"device_ms": dev, "bytes_written": written, "gbs": written / (dev * 1e-3) / 1e9,
+                     "frac_of_measured_hbm": written / (dev * 1e-3) / 1e9 / hbm,
+                     "path_steps_per_sec": book.paths * (n_dates - 1) / (dev * 1e-3)}
+    out["note"] = ("spot of every date of every path stored to HBM by the book kernel; the kernel stays "
+                   "FP32-issue bound, so the write rate is the step rate x 4 bytes")
+    return out
+
+
 def ragged_batch_section(G, steps):
     """256 ragged books (path counts log-uniform in [2^14, 2^22], 12..730 daily steps,
     40% GBM / 40% Heston / 20% LSV) priced as one CUDA graph: untuned, after the
@@ -314,6 +347,8 @@ def run_gpu(args):
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample_paths, os.cpu_count() or 1)
         if not args.no_lsv:
             line["lsv_book"] = lsv_book_section(G, flush, args.steps)
+        if not args.no_paths:
+            line["stored_paths"] = paths_section(G, flush)
         if not args.no_batch:
             line["ragged_batch"] = ragged_batch_section(G, args.steps)
         if not args.no_surrogate:

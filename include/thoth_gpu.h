@@ -231,6 +231,15 @@ int thoth_gpu_measure_fp32_peak(double* tflops, double* ms);
  * thoth_gpu_price_book, except device_ms, which is not measured here (NaN). */
 int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out);
 
+/* Simulate the book's paths and return the spot of one asset at every date of
+ * every path: spots[date * paths + path] (caller-owned, n_dates x paths floats),
+ * path p being Sobol index sobol_skip + 1 + p. The book's products are priced on
+ * the same paths (not returned). On the device the paths are written
+ * date-major, consecutive paths by consecutive threads. *device_ms (may be
+ * null) is the kernels' device time. No reference counterpart: the
+ * reference's node graph keeps only the current path (nodes/monte_carlo_node.hpp:15-25). */
+int thoth_gpu_simulate_paths(const ThothBookDesc* book, int32_t asset, float* spots, double* device_ms);
+
 /* Price n_books independent books (ragged path and step counts) in one CUDA
  * graph launch: all plans in one upload, each book's persistent kernel and
  * reduction on one of several streams (largest first), all sums back in one

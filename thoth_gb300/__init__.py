@@ -52,6 +52,8 @@ def lib():
         L.thoth_gpu_book_destroy.argtypes = [C.c_void_p]
         L.thoth_gpu_measure_fp32_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
+        L.thoth_gpu_simulate_paths.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(C.c_float),
+                                               C.POINTER(C.c_double)]
         L.thoth_gpu_autotune_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(abi.ThothTuneResult)]
         L.thoth_gpu_autotune_batch.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.c_int32,
                                                C.POINTER(abi.ThothTuneResult)]
@@ -97,6 +99,16 @@ def price_book(book, greeks=False):
                h2d_bytes=r.h2d_bytes, d2h_bytes=r.d2h_bytes)
     out.update({k: v.copy() for k, v in arrs.items()})
     return out
+
+
+def simulate_paths(book, asset=0):
+    """Spot of `asset` at every date of every path of `book`: (float32 [n_dates][paths], device ms)."""
+    d = book.desc()
+    out = np.zeros((d.n_dates, book.paths), dtype=np.float32)
+    ms = C.c_double()
+    _check(lib().thoth_gpu_simulate_paths(C.byref(d), int(asset), out.ctypes.data_as(C.POINTER(C.c_float)),
+                                          C.byref(ms)))
+    return out, ms.value
 
 
 def price_batch(books):

@@ -159,6 +159,9 @@ struct DevPlan {
     int n_sobol;
     double* acc;                 // [gridDim][n_acc] per-CTA FP64 sums
     int n_acc;
+    float* path_out;             // [n_steps + 1][path_ld] spot of asset path_asset at every date (null: not stored)
+    int64_t path_ld;             // paths per stored date (the book's path count)
+    int path_asset;
     volatile int* cancel;        // host-mapped cancel word (may be null)
     int* status;                 // device status word
 };

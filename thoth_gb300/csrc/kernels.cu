@@ -496,6 +496,10 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                 if (aid < P.n_assets)
 #pragma unroll
                     for (int p = 0; p < PP; ++p) apply_events(0, aid, t + p * TH, 0.f, 0.f, 0.f, 1.f);
+                if (P.path_out && aid == P.path_asset)
+#pragma unroll
+                    for (int p = 0; p < PP; ++p)
+                        if (valid[p]) P.path_out[n[p] - (uint64_t)P.skip - 1] = P.s0[aid];
             }
 
             // ---- time loop (step records prefetched one step ahead) ------------
@@ -575,6 +579,9 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                         comp[p][a] = (tt - x[p][a]) - yy;
                         x[p][a] = tt;
                         if (cur.ev) apply_events(i, aid, t + p * TH, x[p][a], step, Wb[p][a], y[p][a]);
+                        // stored paths: date-major, consecutive paths on consecutive threads
+                        if (P.path_out && aid == P.path_asset && valid[p])
+                            P.path_out[(size_t)i * P.path_ld + (n[p] - (uint64_t)P.skip - 1)] = P.s0[aid] * expf(x[p][a]);
                     }
                 }
             }

@@ -82,6 +82,8 @@ struct Device {
     size_t pinned_size = 0;
     int* cancel_host = nullptr;      // host-mapped cancel word
     int* cancel_dev = nullptr;
+    float* paths = nullptr;          // stored paths of thoth_gpu_simulate_paths
+    size_t paths_size = 0;
 };
 Device g_dev;
 
@@ -176,6 +178,17 @@ int ensure_arena(size_t bytes)
     const size_t sz = std::max(bytes, (size_t)1 << 22) * 5 / 4;
     CUDA_TRY(cudaMalloc(&g_dev.arena, sz));
     g_dev.arena_size = sz;
+    return THOTH_GPU_OK;
+}
+
+int ensure_paths(size_t bytes)
+{
+    if (bytes <= g_dev.paths_size) return THOTH_GPU_OK;
+    if (g_dev.paths) cudaFree(g_dev.paths);
+    g_dev.paths = nullptr;
+    g_dev.paths_size = 0;
+    CUDA_TRY(cudaMalloc(&g_dev.paths, bytes));
+    g_dev.paths_size = bytes;
     return THOTH_GPU_OK;
 }
 
@@ -1080,6 +1093,41 @@ int price_locked(const ThothBookDesc* book, ThothBookResult* out)
     rc = run_bound(P, g_dev.arena, L, grid, out, true);
     if (rc) return rc;
     out->h2d_bytes = (int64_t)P.blob.bytes.size();
+    return THOTH_GPU_OK;
+}
+
+// the book priced as by price_locked, with the spot of one asset stored at every
+// date of every path (date-major on the device, copied to the caller's array)
+int simulate_paths_locked(const ThothBookDesc* book, int asset, float* out, double* device_ms)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null output");
+    int rc = ensure_device();
+    if (rc) return rc;
+    Plan P;
+    rc = build_plan(book, P);
+    if (rc) return rc;
+    if (asset < 0 || asset >= P.dp.n_assets) return fail(THOTH_GPU_E_INVALID, "asset out of range");
+    const size_t bytes = sizeof(float) * (size_t)(P.dp.n_steps + 1) * (size_t)P.paths;
+    const int grid = grid_for(P);
+    const Layout L = layout_of(P, grid);
+    rc = ensure_arena(L.total);
+    if (rc) return rc;
+    rc = ensure_paths(bytes);
+    if (rc) return rc;
+    rc = ensure_pinned(P.blob.bytes.size());
+    if (rc) return rc;
+    std::memcpy(g_dev.pinned, P.blob.bytes.data(), P.blob.bytes.size());
+    CUDA_TRY(cudaMemcpyAsync(g_dev.arena, g_dev.pinned, P.blob.bytes.size(), cudaMemcpyHostToDevice, g_dev.stream));
+    bind(P, g_dev.arena);
+    P.dp.path_out = g_dev.paths;
+    P.dp.path_ld = P.paths;
+    P.dp.path_asset = asset;
+    ThothBookResult sums;
+    std::memset(&sums, 0, sizeof sums);
+    rc = run_bound(P, g_dev.arena, L, grid, &sums, true);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpy(out, g_dev.paths, bytes, cudaMemcpyDeviceToHost));
+    if (device_ms) *device_ms = sums.device_ms;
     return THOTH_GPU_OK;
 }
 
@@ -2096,6 +2144,18 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
         CUDA_TRY(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, g_dev.stream));
         CUDA_TRY(cudaStreamSynchronize(g_dev.stream));
         return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_simulate_paths(const ThothBookDesc* book, int32_t asset, float* spots, double* device_ms)
+{
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        return simulate_paths_locked(book, asset, spots, device_ms);
     } catch (const std::bad_alloc&) {
         return fail(THOTH_GPU_E_NOMEM, "out of host memory");
     } catch (const std::exception& e) {
