@@ -188,3 +188,26 @@ def test_surrogate_grid_policy_prefers_short_horizons():
     e = jerr.copy()
     e[:, bad.ravel()] = 0.5 * tol
     assert np.quantile(e, 0.9) <= 0.9 * tol
+
+
+def test_running_groups_share_nested_prefixes():
+    """Planner (host only): barriers of one asset / direction / quanto shift on nested
+    monitoring prefixes, and continuous variance swaps of one asset and shift, share a
+    running group; products ending earlier read a snapshot slot."""
+    b = abi.Book(days=np.arange(0, 121), paths=1000)
+    h = b.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.01)
+    for m in (30, 60, 120, 90):
+        b.add_barrier(h, 100.0, m, 80.0, up=False, knock_in=False, monitor=np.arange(1, m + 1))
+    s = G.plan_summary(b)
+    assert s["groups"] == 1 and s["slots"] == 4 + 3            # 4 spot snapshots, 3 group snapshots
+    b.add_barrier(h, 100.0, 120, 80.0, up=False, knock_in=False, monitor=np.arange(2, 121, 2))
+    assert G.plan_summary(b)["groups"] == 2                     # not a prefix: its own group
+    b.add_barrier(h, 100.0, 60, 120.0, up=True, knock_in=True, monitor=np.arange(1, 61))
+    assert G.plan_summary(b)["groups"] == 3                     # the other direction
+    for m in (20, 60):
+        b.add_variance(h, m, strike_variance=0.04)
+    assert G.plan_summary(b)["groups"] == 4                     # one running variance sum
+    b.add_variance(h, 60, strike_variance=0.04, quanto=0.02)
+    assert G.plan_summary(b)["groups"] == 5                     # another quanto shift
+    b.add_variance(h, 60, strike_variance=0.04, obs=np.arange(5, 61, 5))
+    assert G.plan_summary(b)["groups"] == 6                     # discrete observations: own group
