@@ -240,6 +240,47 @@ int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out
  * reference's node graph keeps only the current path (nodes/monte_carlo_node.hpp:15-25). */
 int thoth_gpu_simulate_paths(const ThothBookDesc* book, int32_t asset, float* spots, double* device_ms);
 
+/* ---- bump-and-revalue Greeks on common random numbers ----------------------
+ * The reference's definitions (pricer_mcl_greeks.cpp:43-299, pricer.cpp:144-193;
+ * bump sizes pricer.hpp:20-30, constants.hpp:36), per product and for the book:
+ *   delta  sum over assets of (P(S_a * 1.01) - P) / (0.01 S_a)
+ *   gamma  sum over assets of (P(S_a * 1.1) - 2P + P(S_a * 0.9)) / (0.1 S_a)^2
+ *   vega   P(vol + 0.01) - P per vol point: GBM sigma + 0.01, Heston / LSV
+ *          v0 and theta -> (sqrt(v) + 0.01)^2 (leverage layers kept as given)
+ *   rho    (P(rates + 1bp) - P) / 1bp * 0.01: every carry and zero rate
+ *   theta  P(today + 1 day) - P (needs days; carries re-based, flat before
+ *          date 1; zero rates kept)
+ *   vega_param[k] (P(param_k + 0.01) - P) / 0.01 for k = v0, kappa, theta,
+ *          xi, rho on every Heston / LSV asset
+ * Every scenario is priced in one batch (one CUDA graph) on the same Sobol
+ * paths. Output arrays are caller-owned (n_products, vega_param 5 x
+ * n_products, any may be NULL); Greeks not requested or not available are NaN. */
+#define THOTH_BUMP_DELTA 1
+#define THOTH_BUMP_GAMMA 2
+#define THOTH_BUMP_VEGA 4
+#define THOTH_BUMP_RHO 8
+#define THOTH_BUMP_THETA 16
+#define THOTH_BUMP_PARAMS 32
+
+typedef struct ThothBumpGreeks {
+    int32_t flags;         /* in: THOTH_BUMP_* mask                                  */
+    int32_t n_scenarios;   /* out: scenarios priced, the base included               */
+    double* premium;       /* out: base premium per product                          */
+    double* delta;
+    double* gamma;
+    double* vega;
+    double* rho;
+    double* theta;
+    double* vega_param;    /* [5][n_products]                                        */
+    double book_premium, book_delta, book_gamma, book_vega, book_rho, book_theta;
+    double book_vega_param[5];
+    double device_ms;      /* the batch's device time                                */
+} ThothBumpGreeks;
+
+int thoth_gpu_bump_greeks(const ThothBookDesc* book, ThothBumpGreeks* out);
+/* the message of the last thoth_gpu_bump_greeks failure (or why theta is NaN) */
+const char* thoth_gpu_bump_greeks_last_error(void);
+
 /* Price n_books independent books (ragged path and step counts) in one CUDA
  * graph launch: all plans in one upload, each book's persistent kernel and
  * reduction on one of several streams (largest first), all sums back in one

@@ -52,6 +52,8 @@ def lib():
         L.thoth_gpu_book_destroy.argtypes = [C.c_void_p]
         L.thoth_gpu_measure_fp32_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
+        L.thoth_gpu_bump_greeks.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBumpGreeks)]
+        L.thoth_gpu_bump_greeks_last_error.restype = C.c_char_p
         L.thoth_gpu_simulate_paths.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(C.c_float),
                                                C.POINTER(C.c_double)]
         L.thoth_gpu_autotune_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(abi.ThothTuneResult)]
@@ -109,6 +111,31 @@ def simulate_paths(book, asset=0):
     _check(lib().thoth_gpu_simulate_paths(C.byref(d), int(asset), out.ctypes.data_as(C.POINTER(C.c_float)),
                                           C.byref(ms)))
     return out, ms.value
+
+
+def bump_greeks(book, flags=abi.BUMP_ALL):
+    """Bump-and-revalue Greeks on common random numbers (the reference's definitions):
+    dict of per-product arrays and book values; NaN where not requested or available."""
+    n = len(book.products)
+    d = book.desc()
+    arrs = {k: np.full(n, np.nan) for k in ("premium", "delta", "gamma", "vega", "rho", "theta")}
+    vp = np.full((5, n), np.nan)
+    g = abi.ThothBumpGreeks()
+    g.flags = int(flags)
+    for k, a in arrs.items():
+        setattr(g, k, a.ctypes.data_as(C.POINTER(C.c_double)))
+    g.vega_param = vp.ctypes.data_as(C.POINTER(C.c_double))
+    rc = lib().thoth_gpu_bump_greeks(C.byref(d), C.byref(g))
+    if rc != abi.THOTH_GPU_OK:
+        raise ThothGpuError(rc, lib().thoth_gpu_bump_greeks_last_error().decode())
+    out = dict(arrs)
+    out.update({"vega_" + p: vp[k].copy() for k, p in enumerate(abi.PARAMS)})
+    out["book"] = {k: getattr(g, "book_" + k) for k in ("premium", "delta", "gamma", "vega", "rho", "theta")}
+    out["book"].update({"vega_" + p: g.book_vega_param[k] for k, p in enumerate(abi.PARAMS)})
+    out["n_scenarios"] = g.n_scenarios
+    out["device_ms"] = g.device_ms
+    out["note"] = lib().thoth_gpu_bump_greeks_last_error().decode()
+    return out
 
 
 def price_batch(books):

@@ -116,6 +116,20 @@ class ThothTuneResult(C.Structure):
                 ("tile_paths", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double)]
 
 
+BUMP_DELTA, BUMP_GAMMA, BUMP_VEGA, BUMP_RHO, BUMP_THETA, BUMP_PARAMS = 1, 2, 4, 8, 16, 32
+BUMP_ALL = 63
+PARAMS = ("v0", "kappa", "theta", "xi", "rho")
+
+
+class ThothBumpGreeks(C.Structure):
+    _fields_ = [("flags", C.c_int32), ("n_scenarios", C.c_int32)] + \
+               [(k, C.POINTER(C.c_double)) for k in ("premium", "delta", "gamma", "vega", "rho", "theta",
+                                                     "vega_param")] + \
+               [(k, C.c_double) for k in ("book_premium", "book_delta", "book_gamma", "book_vega", "book_rho",
+                                          "book_theta")] + \
+               [("book_vega_param", C.c_double * 5), ("device_ms", C.c_double)]
+
+
 def _ptr(arr, ctype):
     return arr.ctypes.data_as(C.POINTER(ctype))
 
@@ -202,6 +216,15 @@ class Book:
 
     def set_cholesky(self, L):
         self.cholesky = np.ascontiguousarray(L, dtype=np.float64)
+
+    def copy(self):
+        """An independent copy (assets, products and arrays) without the C view."""
+        import copy as _copy
+        keep, self._keep = self._keep, []
+        try:
+            return _copy.deepcopy(self)
+        finally:
+            self._keep = keep
 
     # -- C view ---------------------------------------------------------
     def desc(self):

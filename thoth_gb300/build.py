@@ -18,7 +18,7 @@ BUILD = HERE / "_build"
 CSRC = HERE / "csrc"
 LIB = BUILD / "libthoth_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "thoth_gpu.cu", "surrogate.cu", "surrogate_host.cu"]
+SOURCES = ["kernels.cu", "thoth_gpu.cu", "surrogate.cu", "surrogate_host.cu", "greeks.cu"]
 # the path kernels flush FP32 denormals: no value on the path is subnormal, and
 # without it every MUFU approximation (rcp, rsqrt, lg2, ex2) carries a
 # denormal fix-up sequence (11 % of the Heston step's time)
