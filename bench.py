@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch (256 books) section")
     ap.add_argument("--no-lsv", action="store_true", help="skip the multi-asset LSV book section")
     ap.add_argument("--no-paths", action="store_true", help="skip the stored-paths (HBM) section")
+    ap.add_argument("--no-american", action="store_true", help="skip the American (Longstaff-Schwartz) section")
     return ap.parse_args()
 
 
@@ -218,6 +219,69 @@ def paths_section(G, flush):
     return out
 
 
+def american_section(G, flush, steps):
+    """American put by Longstaff-Schwartz on Heston paths: 2^20 paths, one year of daily
+    exercise dates (365 path rows read by the fit), and the reference tests' size (300 000
+    GBM paths, 30-day exercise grid). The fit kernel's rate in path-dates/s, the whole call
+    (simulation, fit, copies) per the C ABI, the frozen-policy Greeks, and the oracle's fit
+    on a 2^15-path sample of the same stored paths on one host core."""
+    import numpy as np
+    import torch
+    from oracle import american as am
+    from thoth_gb300 import abi
+
+    def put_book(paths, days, heston=True):
+        b = abi.Book(days=np.asarray(days), paths=paths)
+        a = b.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.03) if heston else b.add_gbm(100.0, 0.30, 0.08)
+        b.add_vanilla(a, 100.0, len(days) - 1, abi.PUT, zero_rate=0.03 if heston else 0.08)
+        return b
+
+    out = {}
+    cases = (("heston_daily_2^20", put_book(1 << 20, range(0, 366))),
+             ("gbm_30day_300000", put_book(300000, list(range(0, 361, 30)) + [365], heston=False)))
+    for name, book in cases:
+        G.price_american(book, 0)
+        ex, dev, wall = [], [], []
+        for _ in range(max(3, steps // 2)):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = G.price_american(book, 0)
+            wall.append(time.perf_counter() - t0)
+            ex.append(r["exercise_ms"])
+            dev.append(r["device_ms"])
+        rows = book.n_dates - 1
+        units = float(book.paths) * rows
+        fit_ms, e2e_ms = float(np.median(ex)), 1e3 * float(np.median(wall))
+        out[name] = {"paths": book.paths, "exercise_dates": rows, "premium": r["premium"], "trust": r["trust"],
+                     "european": r["european"], "fitted_dates": r["fitted_dates"],
+                     "fit_kernel_ms": fit_ms, "fit_path_dates_per_sec": units / (fit_ms * 1e-3),
+                     "simulate_and_fit_device_ms": float(np.median(dev)),
+                     "e2e_ms": e2e_ms, "e2e_path_dates_per_sec": units / (e2e_ms * 1e-3),
+                     "fit_read_gbs": 4.0 * units / (fit_ms * 1e-3) / 1e9}
+    book = cases[0][1]
+    t0 = time.perf_counter()
+    g = G.price_american(book, 0, flags=abi.BUMP_DELTA | abi.BUMP_GAMMA | abi.BUMP_VEGA | abi.BUMP_RHO |
+                         abi.BUMP_THETA)
+    out["heston_daily_2^20"]["greeks"] = {k: g[k] for k in ("delta", "gamma", "vega", "rho", "theta")}
+    out["heston_daily_2^20"]["greeks_wall_ms"] = 1e3 * (time.perf_counter() - t0)
+    out["heston_daily_2^20"]["greeks_device_ms"] = g["device_ms"]
+    # CPU: the oracle (numpy, exact sums, one core) on the first 2^15 stored paths
+    sample = put_book(1 << 15, range(0, 366))
+    S, _ = G.simulate_paths(sample, 0)
+    t0 = time.perf_counter()
+    o = am.fit(S, sample.t, np.full(sample.n_dates, 0.03), 100.0, False, 100.0)
+    cpu_s = time.perf_counter() - t0
+    cpu_rate = float(sample.paths) * (sample.n_dates - 1) / cpu_s
+    out["cpu_baseline"] = {"value": cpu_rate, "unit": "path-dates/s", "cores": 1, "kind": "port",
+                           "sample": "oracle.american.fit on 2^15 Heston paths x 365 daily exercise dates "
+                                     "(%.2f s)" % cpu_s,
+                           "gpu_equals_oracle_on_sample": bool(G.price_american(sample, 0)["premium"] == o["premium"])}
+    out["note"] = ("fit = one cooperative launch, one publish/reduce/release per exercise date; FP64-issue and "
+                   "latency bound (GB300 runs FP64 at 1/64 of FP32): the paths are read once (fit_read_gbs)")
+    return out
+
+
 def ragged_batch_section(G, steps):
     """256 ragged books (path counts log-uniform in [2^14, 2^22], 12..730 daily steps,
     40% GBM / 40% Heston / 20% LSV) priced as one CUDA graph: untuned, after the
@@ -349,6 +413,8 @@ def run_gpu(args):
             line["lsv_book"] = lsv_book_section(G, flush, args.steps)
         if not args.no_paths:
             line["stored_paths"] = paths_section(G, flush)
+        if not args.no_american:
+            line["american_lsm"] = american_section(G, flush, args.steps)
         if not args.no_batch:
             line["ragged_batch"] = ragged_batch_section(G, args.steps)
         if not args.no_surrogate:

@@ -281,6 +281,45 @@ int thoth_gpu_bump_greeks(const ThothBookDesc* book, ThothBumpGreeks* out);
 /* the message of the last thoth_gpu_bump_greeks failure (or why theta is NaN) */
 const char* thoth_gpu_bump_greeks_last_error(void);
 
+/* ---- American exercise by Longstaff-Schwartz --------------------------------
+ * Replaces PricerMCL::PriceAmerican (pricer_mcl_american.cpp:137-261) for one
+ * vanilla of the book: the spot paths of its asset are stored on every date up
+ * to maturity (the recorder, path_recorder.cpp), and the exercise policy is fitted
+ * once on them (FitAmericanPolicy, pricer_mcl_american.cpp:263-378): backward over
+ * dates maturity-1 .. 1, the discounted continuation of the in-the-money paths is
+ * regressed on {1, m, m^2}, m = S / strike (the spot at date 0 when the strike is
+ * not positive), at dates with at least min_itm of them, by the normal equations
+ * and Cholesky (maths.cpp:354-381, 419-470). The value is the policy applied to
+ * the same paths (ApplyAmericanPolicy, :380-447): exercise at the first date whose
+ * intrinsic value is positive and at least the fitted continuation, else at
+ * maturity, discounted at that date's zero rate; premium = max(mean, intrinsic at
+ * the spot of date 0), trust = its standard error.
+ * Greeks (flags): delta, gamma, vega and rho apply the FROZEN policy to the paths
+ * of the bumped book (spot x 1.01, x 1.1 / x 0.9, vol level + 0.01, carries and
+ * zero rates + 1bp: the bumps of thoth_gpu_bump_greeks, rho discounting at the
+ * bumped rates); theta refits on the book rolled one day (a full reprice, as the
+ * reference's theta pass). Regression and premium sums are exact (fixed point,
+ * 2^-64): results do not depend on the launch shape. */
+typedef struct ThothAmerican {
+    int32_t product;          /* in: a THOTH_PRODUCT_VANILLA of the book, quanto 0   */
+    int32_t flags;            /* in: THOTH_BUMP_DELTA|GAMMA|VEGA|RHO|THETA           */
+    int32_t min_itm;          /* in: in-the-money paths a regression needs; <= 0: 50 */
+    int32_t fitted_dates;     /* out: dates of the policy with a regression          */
+    /* in: zero rate of the premium currency at each date (n_dates) for the
+     * discounting, or NULL: the product's zero_rate at every date             */
+    const double* zero_rates;
+    double* beta;             /* out, optional [3 * n_dates]: b0 b1 b2 per date, NaN
+                                 where the date has no regression                    */
+    double premium, trust;    /* out                                                 */
+    double european;          /* out: discounted maturity payoff on the same paths   */
+    double delta, gamma, vega, rho, theta; /* out: NaN where not requested          */
+    double device_ms;         /* out: every simulation and exercise kernel           */
+    double exercise_ms;       /* out: the base fit kernel alone                      */
+} ThothAmerican;
+
+int thoth_gpu_price_american(const ThothBookDesc* book, ThothAmerican* am);
+const char* thoth_gpu_american_last_error(void);
+
 /* Price n_books independent books (ragged path and step counts) in one CUDA
  * graph launch: all plans in one upload, each book's persistent kernel and
  * reduction on one of several streams (largest first), all sums back in one

@@ -81,6 +81,12 @@ def ref():
                                               C.c_uint64, C.POINTER(C.c_double)]
         lib.ref_price_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBookResult),
                                        C.POINTER(C.c_double), C.c_int64]
+        lib.ref_least_squares.argtypes = [C.POINTER(C.c_double), C.c_int64, C.c_int, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double)]
+        lib.ref_lsm.argtypes = [C.POINTER(C.c_float), C.c_int64, C.c_int, C.POINTER(C.c_double),
+                                C.POINTER(C.c_double), C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
+                                C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                C.POINTER(C.c_double)]
         _ref = lib
     return _ref
 
@@ -133,6 +139,34 @@ def price_book(book, which="port", threads=1, n_per_path=0):
         raise RuntimeError("%s price_book failed: %d" % (which, rc))
     return dict(book_premium=r.book_premium, book_trust=r.book_trust, premium=arrs["premium"].copy(),
                 trust=arrs["trust"].copy(), per_path=per[:n_per_path].copy() if n_per_path else None)
+
+
+def ref_least_squares(X, y):
+    """The reference's LeastSquares on X [n][p], y [n]: beta, or None where it fails."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    beta = np.zeros(X.shape[1])
+    ok = ref().ref_least_squares(_d(X), X.shape[0], X.shape[1], _d(y), _d(beta))
+    return beta if ok else None
+
+
+def ref_lsm(S, tau, rates, strike, call, norm, min_itm=50, policy=None):
+    """The reference's Longstaff-Schwartz loops (sums in path order) on S [M][n] float32:
+    fit and value, or value the frozen policy (beta [M][3], has_fit [M])."""
+    S = np.ascontiguousarray(S, dtype=np.float32)
+    M, n = S.shape
+    tau = np.ascontiguousarray(tau[:M], dtype=np.float64)
+    rates = np.ascontiguousarray(rates[:M], dtype=np.float64)
+    if policy is None:
+        beta, has = np.zeros((M, 3)), np.zeros(M, dtype=np.int32)
+    else:
+        beta = np.ascontiguousarray(policy[0], dtype=np.float64)
+        has = np.ascontiguousarray(policy[1], dtype=np.int32)
+    prem, trust = C.c_double(), C.c_double()
+    ref().ref_lsm(S.ctypes.data_as(C.POINTER(C.c_float)), n, M, _d(tau), _d(rates), strike, int(call), norm,
+                  min_itm, int(policy is None), _d(beta), has.ctypes.data_as(C.POINTER(C.c_int)),
+                  C.byref(prem), C.byref(trust))
+    return dict(premium=prem.value, trust=trust.value, beta=beta, has_fit=has.astype(bool))
 
 
 def bs_price(F, K, T, vol, df, is_call=True):

@@ -20,6 +20,8 @@
 #include "sobol_generator.hpp"
 #include "distributions.hpp"
 #include "rng.hpp"
+#include "maths.hpp"
+#include "finance.hpp"
 
 #include "thoth_gpu.h"
 
@@ -441,6 +443,145 @@ int ref_price_book( const ThothBookDesc* d, ThothBookResult* r, double* per_path
         std::fprintf( stderr, "ref_price_book: %s\n", e.what() );
         return THOTH_GPU_E_INVALID;
     }
+}
+
+//! the reference's own LeastSquares (helpers/maths.cpp:419-470) on X [n][p] row-major;
+//! returns 0 where it returns an empty vector (singular normal matrix)
+int ref_least_squares( const double* X, int64_t n, int p, const double* y, double* beta )
+{
+    la_matrix* A = la_matrix_alloc( (size_t)n, (size_t)p );
+    la_vector* v = la_vector_alloc( (size_t)n );
+    for ( int64_t k = 0; k < n; k++ )
+    {
+        for ( int j = 0; j < p; j++ )
+        {
+            la_matrix_set( A, (size_t)k, (size_t)j, X[k * p + j] );
+        }
+        la_vector_set( v, (size_t)k, y[k] );
+    }
+    vector<double> b = LeastSquares( A, v );
+    la_matrix_free( A );
+    la_vector_free( v );
+    for ( size_t j = 0; j < b.size(); j++ )
+    {
+        beta[j] = b[j];
+    }
+    return b.empty() ? 0 : 1;
+}
+
+//! Longstaff-Schwartz fit and frozen apply on date-major paths S[M][n] (the engine's
+//! single-precision spots): the loops of PricerMCL::FitAmericanPolicy and
+//! ApplyAmericanPolicy (tasks/pricer_mcl_american.cpp:263-447), restated here because
+//! that file needs the whole pricer, around the reference's own LeastSquares and
+//! payoff_vanilla. Sums in path order, as the reference. fit = 0 applies beta / has_fit.
+int ref_lsm( const float* S, int64_t n, int M, const double* tau, const double* rates, double strike, int is_call,
+             double norm, int min_itm, int fit, double* beta, int* has_fit, double* premium, double* trust )
+{
+    const OptionType ty = is_call ? OptionType::Call : OptionType::Put;
+    auto intrinsic = [&]( double s ) { return payoff_vanilla( s, strike, ty, false, 0, true, 0 ); };
+    auto at = [&]( int64_t p, int t ) { return (double)S[(int64_t)t * n + p]; };
+    if ( M < 2 )
+    {
+        *premium = 0;
+        *trust = 0;
+        return 0;
+    }
+    if ( fit )
+    {
+        for ( int t = 0; t < M; t++ )
+        {
+            has_fit[t] = 0;
+            beta[3 * t] = beta[3 * t + 1] = beta[3 * t + 2] = 0;
+        }
+        vector<double> cf( (size_t)n );
+        for ( int64_t p = 0; p < n; p++ )
+        {
+            cf[p] = intrinsic( at( p, M - 1 ) );
+        }
+        for ( int t = M - 2; t >= 1; t-- )
+        {
+            double df = exp( rates[t] * tau[t] - rates[t + 1] * tau[t + 1] );
+            for ( int64_t p = 0; p < n; p++ )
+            {
+                cf[p] *= df;
+            }
+            vector<int64_t> itm;
+            for ( int64_t p = 0; p < n; p++ )
+            {
+                if ( intrinsic( at( p, t ) ) > 0 )
+                {
+                    itm.push_back( p );
+                }
+            }
+            if ( itm.size() < (size_t)min_itm )
+            {
+                continue;
+            }
+            la_matrix* X = la_matrix_alloc( itm.size(), 3 );
+            la_vector* y = la_vector_alloc( itm.size() );
+            for ( size_t k = 0; k < itm.size(); k++ )
+            {
+                double m = at( itm[k], t ) / norm;
+                la_matrix_set( X, k, 0, 1.0 );
+                la_matrix_set( X, k, 1, m );
+                la_matrix_set( X, k, 2, m * m );
+                la_vector_set( y, k, cf[itm[k]] );
+            }
+            vector<double> b = LeastSquares( X, y );
+            la_matrix_free( X );
+            la_vector_free( y );
+            if ( b.empty() )
+            {
+                continue;
+            }
+            beta[3 * t] = b[0];
+            beta[3 * t + 1] = b[1];
+            beta[3 * t + 2] = b[2];
+            has_fit[t] = 1;
+            for ( int64_t p : itm )
+            {
+                double s = at( p, t );
+                double m = s / norm;
+                double c = b[0] + b[1] * m + b[2] * m * m;
+                double iv = intrinsic( s );
+                if ( iv >= c )
+                {
+                    cf[p] = iv;
+                }
+            }
+        }
+    }
+    double sum = 0, sum2 = 0;
+    for ( int64_t p = 0; p < n; p++ )
+    {
+        double value = 0;
+        for ( int t = 1; t < M; t++ )
+        {
+            double s = at( p, t );
+            double iv = intrinsic( s );
+            if ( t == M - 1 )
+            {
+                value = iv * exp( -rates[t] * ( tau[t] - tau[0] ) );
+                break;
+            }
+            if ( iv > 0 && has_fit[t] )
+            {
+                double m = s / norm;
+                double c = beta[3 * t] + beta[3 * t + 1] * m + beta[3 * t + 2] * m * m;
+                if ( iv >= c )
+                {
+                    value = iv * exp( -rates[t] * ( tau[t] - tau[0] ) );
+                    break;
+                }
+            }
+        }
+        sum += value;
+        sum2 += value * value;
+    }
+    double mean = sum / n;
+    *trust = sqrt( ( sum2 / n - mean * mean ) / ( n - 1 ) );
+    *premium = std::max( mean, intrinsic( at( 0, 0 ) ) );
+    return 0;
 }
 
 } // extern "C"

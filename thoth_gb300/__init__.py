@@ -54,6 +54,8 @@ def lib():
         L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
         L.thoth_gpu_bump_greeks.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBumpGreeks)]
         L.thoth_gpu_bump_greeks_last_error.restype = C.c_char_p
+        L.thoth_gpu_price_american.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothAmerican)]
+        L.thoth_gpu_american_last_error.restype = C.c_char_p
         L.thoth_gpu_simulate_paths.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(C.c_float),
                                                C.POINTER(C.c_double)]
         L.thoth_gpu_autotune_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(abi.ThothTuneResult)]
@@ -135,6 +137,34 @@ def bump_greeks(book, flags=abi.BUMP_ALL):
     out["n_scenarios"] = g.n_scenarios
     out["device_ms"] = g.device_ms
     out["note"] = lib().thoth_gpu_bump_greeks_last_error().decode()
+    return out
+
+
+def price_american(book, product, flags=0, min_itm=0, zero_rates=None):
+    """American exercise of one vanilla of the book by Longstaff-Schwartz on its asset's
+    stored paths, with frozen-policy Greeks (flags: abi.BUMP_DELTA | ... | BUMP_THETA).
+    Returns premium, trust, european, the Greeks (NaN where not requested), beta
+    [n_dates, 3] (NaN where a date has no regression), fitted_dates and the device times."""
+    d = book.desc()
+    a = abi.ThothAmerican()
+    a.product = int(product)
+    a.flags = int(flags)
+    a.min_itm = int(min_itm)
+    z = None
+    if zero_rates is not None:
+        z = np.ascontiguousarray(zero_rates, dtype=np.float64)
+        if z.shape != (book.n_dates,):
+            raise ValueError("zero_rates needs one rate per date")
+        a.zero_rates = z.ctypes.data_as(C.POINTER(C.c_double))
+    beta = np.full((book.n_dates, 3), np.nan)
+    a.beta = beta.ctypes.data_as(C.POINTER(C.c_double))
+    rc = lib().thoth_gpu_price_american(C.byref(d), C.byref(a))
+    if rc != abi.THOTH_GPU_OK:
+        raise ThothGpuError(rc, lib().thoth_gpu_american_last_error().decode())
+    out = {k: getattr(a, k) for k in ("premium", "trust", "european", "delta", "gamma", "vega", "rho", "theta",
+                                      "device_ms", "exercise_ms", "fitted_dates")}
+    out["beta"] = beta
+    out["note"] = lib().thoth_gpu_american_last_error().decode()
     return out
 
 

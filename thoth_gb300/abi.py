@@ -130,6 +130,13 @@ class ThothBumpGreeks(C.Structure):
                [("book_vega_param", C.c_double * 5), ("device_ms", C.c_double)]
 
 
+class ThothAmerican(C.Structure):
+    _fields_ = [("product", C.c_int32), ("flags", C.c_int32), ("min_itm", C.c_int32), ("fitted_dates", C.c_int32),
+                ("zero_rates", C.POINTER(C.c_double)), ("beta", C.POINTER(C.c_double))] + \
+               [(k, C.c_double) for k in ("premium", "trust", "european", "delta", "gamma", "vega", "rho", "theta",
+                                          "device_ms", "exercise_ms")]
+
+
 def _ptr(arr, ctype):
     return arr.ctypes.data_as(C.POINTER(ctype))
 

@@ -1,0 +1,401 @@
+// american.cu — Longstaff-Schwartz exercise of a vanilla on its asset's stored paths, the
+// algorithm of pricer_mcl_american.cpp:263-447 (FitAmericanPolicy / ApplyAmericanPolicy)
+// with the normal-equation solve of helpers/maths.cpp:354-381 and 419-470.
+//
+// Fit: one cooperative, persistent launch walks the exercise dates backwards. At each date
+// every CTA discounts its paths' cashflows, sums the regression moments of its in-the-money
+// paths and publishes them; the last CTA to publish adds all the CTAs' sums, solves the 3x3
+// system and releases the others with a flag, and every CTA rolls its paths' cashflows back
+// through the exercise decision. The dates are sequential, so one launch with one
+// publish-and-release per date replaces one launch per date. The exercise decisions of the
+// backward pass are the frozen policy's decisions on the same paths (the same test at the
+// same dates), so the earliest exercise the pass records per path is the value the
+// reference's apply step finds: the base premium comes out of the fit without a second
+// walk over the paths.
+//
+// Apply: the frozen policy on another path set (the bumped scenarios of the Greeks), one
+// forward walk per path that stops at the first exercise.
+//
+// Sums are exact (exact.cuh), so the regressions, the decisions and the premium do not
+// depend on the grid; the arithmetic of each addend, of the solve and of the decision is
+// the reference's, operation for operation, in round-to-nearest double with no fused
+// multiply-adds (those inside the moneyness quotient give its correctly rounded value).
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the per-path work keeps FP64
+// to what the result depends on: the in-the-money test is an integer compare on the
+// spot's bits, and the quotient S / norm is one multiply and four fused multiply-adds.
+#include "american.cuh"
+
+namespace {
+
+constexpr int LSM_WARPS = LSM_THREADS / 32;
+static_assert(LSM_WARPS >= LSM_PART, "one warp per regression sum in the cross-CTA reduction");
+constexpr int LSM_QCAP = 64; // per-warp queue of in-the-money paths waiting for a full warp
+constexpr unsigned long long BARRIER_LIMIT_NS = 2000000000ull; // 2 s
+
+// max(phi (S - K), 0): payoff_vanilla with a floor at 0 (helpers/finance.cpp:9-32)
+__device__ __forceinline__ double intrinsic(double s, double k, int call)
+{
+    const double v = call ? __dsub_rn(s, k) : __dsub_rn(k, s);
+    return v < 0.0 ? 0.0 : v;
+}
+
+// intrinsic(S) > 0, decided on the single-precision bits of S (integer compare; the
+// threshold is exact, see itm_bits)
+__device__ __forceinline__ bool in_the_money(float s, const LsmArgs& A)
+{
+    const int b = __float_as_int(s);
+    return A.call ? b >= A.itm_bits : b <= A.itm_bits;
+}
+
+// S / norm rounded to nearest, from y = 1 / norm rounded to nearest. q0 = RN(S y) may be
+// more than one ulp off near a power of two; one correction step q1 = RN(q0 + RN(S - norm q0) y)
+// brings it within one ulp, and then the remainder S - norm q1 is exact and the second step
+// q1 + r y rounded once is the correctly rounded quotient (P. Markstein, IBM J. Res. Dev.
+// 34(1), 1990: y within half an ulp of 1 / norm, q1 within one ulp of S / norm).
+// Five FP64 operations in place of a full division.
+__device__ __forceinline__ double moneyness(double s, const LsmArgs& A)
+{
+    const double y = A.inv_norm, b = A.norm;
+    const double q0 = __dmul_rn(s, y);
+    const double q1 = __fma_rn(__fma_rn(-q0, b, s), y, q0);
+    return __fma_rn(__fma_rn(-q1, b, s), y, q1);
+}
+
+// b0 + b1 m + b2 m m, evaluated left to right
+__device__ __forceinline__ double continuation(double b0, double b1, double b2, double m)
+{
+    return __dadd_rn(__dadd_rn(b0, __dmul_rn(b1, m)), __dmul_rn(__dmul_rn(b2, m), m));
+}
+
+__device__ __forceinline__ void warp_sum(Fx128& a)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long lo = __shfl_xor_sync(0xffffffffu, (unsigned long long)a.lo, o);
+        const unsigned long long hi = __shfl_xor_sync(0xffffffffu, (unsigned long long)a.hi, o);
+        fx_add(a, (uint64_t)lo, (uint64_t)hi);
+    }
+}
+
+__device__ __forceinline__ unsigned long long now_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// wait until *flag >= want; false (status 2) after 2 s, or at once when another CTA
+// has failed: the caller returns, so no wait outlives the limit
+__device__ bool wait_for(const unsigned* flag, unsigned want, int* status)
+{
+    const unsigned long long t0 = now_ns();
+    while (ld_acquire(flag) < want) {
+        if (*(volatile int*)status != 0) return false;
+        if (now_ns() - t0 > BARRIER_LIMIT_NS) {
+            atomicExch(status, 2);
+            return false;
+        }
+        __nanosleep(32);
+    }
+    return true;
+}
+
+// (X^T X) beta = X^T y for X = {1, m, m^2}: Cholesky A = L L^T in place of the lower
+// triangle, forward then back substitution (maths.cpp:354-381, 419-470). False when a pivot
+// is not positive (the date keeps no regression).
+__device__ bool solve3(const Fx128* tot, double* beta)
+{
+    const double n = (double)tot[LSM_NQ].lo;
+    const double s1 = fx_to_double(tot[0]), s2 = fx_to_double(tot[1]);
+    const double s3 = fx_to_double(tot[2]), s4 = fx_to_double(tot[3]);
+    double A[3][3] = {{n, s1, s2}, {s1, s2, s3}, {s2, s3, s4}};
+    const double g[3] = {fx_to_double(tot[4]), fx_to_double(tot[5]), fx_to_double(tot[6])};
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j <= i; j++) {
+            double sum = A[i][j];
+            for (int k = 0; k < j; k++) sum = __dsub_rn(sum, __dmul_rn(A[i][k], A[j][k]));
+            if (i == j) {
+                if (sum <= 0.0) return false;
+                A[i][j] = __dsqrt_rn(sum);
+            } else {
+                A[i][j] = __ddiv_rn(sum, A[j][j]);
+            }
+        }
+    }
+    double z[3];
+    for (int i = 0; i < 3; i++) {
+        double s = g[i];
+        for (int k = 0; k < i; k++) s = __dsub_rn(s, __dmul_rn(A[i][k], z[k]));
+        z[i] = __ddiv_rn(s, A[i][i]);
+    }
+    for (int i = 2; i >= 0; i--) {
+        double s = z[i];
+        for (int k = i + 1; k < 3; k++) s = __dsub_rn(s, __dmul_rn(A[k][i], beta[k]));
+        beta[i] = __ddiv_rn(s, A[i][i]);
+    }
+    return true;
+}
+
+// one in-the-money path of the current date: its regression terms into the lane's sums,
+// its moneyness and intrinsic value into the warp's compacted list at entry o
+__device__ __forceinline__ void itm_item(int p, float sf, double y, const LsmArgs& A, Fx128* q, int64_t o, bool& bad)
+{
+    const double s = (double)sf;
+    const double iv = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
+    const double m = moneyness(s, A), m2 = __dmul_rn(m, m);
+    A.c_idx[o] = p;
+    A.c_m[o] = m;
+    A.c_iv[o] = iv;
+    fx_add_checked(q[0], m, bad);
+    fx_add_checked(q[1], m2, bad);
+    fx_add_checked(q[2], __dmul_rn(m2, m), bad);
+    fx_add_checked(q[3], __dmul_rn(m2, m2), bad);
+    fx_add_checked(q[4], y, bad);
+    fx_add_checked(q[5], __dmul_rn(m, y), bad);
+    fx_add_checked(q[6], __dmul_rn(m2, y), bad);
+}
+
+// CTA-wide exact sum of one accumulator per thread into out (thread 0 writes)
+__device__ void block_sum(Fx128 a, Fx128 (*s_w)[LSM_PART], int slot, Fx128* out)
+{
+    warp_sum(a);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_w[warp][slot] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Fx128 s = {0, 0};
+        for (int w = 0; w < LSM_WARPS; w++) fx_add(s, s_w[w][slot]);
+        *out = s;
+    }
+}
+
+__global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmArgs A)
+{
+    __shared__ Fx128 s_w[LSM_WARPS][LSM_PART];
+    __shared__ int q_idx[LSM_WARPS][LSM_QCAP];
+    __shared__ float q_s[LSM_WARPS][LSM_QCAP];
+    __shared__ double q_y[LSM_WARPS][LSM_QCAP];
+    __shared__ Fx128 s_tot[LSM_PART];
+    __shared__ double s_b[3];
+    __shared__ int s_fit, s_ok, s_last;
+    const int G = gridDim.x;
+    const int64_t T = (int64_t)G * LSM_THREADS;
+    const int64_t g0 = (int64_t)blockIdx.x * LSM_THREADS + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t gw = (int64_t)blockIdx.x * LSM_WARPS + warp; // global warp: paths gw 32 + lane + k T
+    const int64_t seg = gw * A.seg_len;
+    const unsigned below = (1u << lane) - 1u;
+    bool bad = false;
+
+    // maturity: the cashflow is the payoff, and the value if never exercised earlier
+    Fx128 eu = {0, 0};
+    {
+        const float* row = A.S + (int64_t)(A.M - 1) * A.ld;
+        const double dT = A.disc[A.M - 1];
+        for (int64_t p = g0; p < A.n; p += T) {
+            const double iv = intrinsic((double)row[p], A.strike, A.call);
+            const double v = __dmul_rn(iv, dT);
+            A.cf[p] = iv;
+            A.val[p] = v;
+            fx_add_checked(eu, v, bad);
+        }
+    }
+
+    unsigned phase = 0; // dates done
+    for (int t = A.M - 2; t >= 1; --t) {
+        const double d = A.df[t];
+        const float* row = A.S + (int64_t)t * A.ld;
+        Fx128 q[LSM_NQ];
+#pragma unroll
+        for (int i = 0; i < LSM_NQ; i++) q[i] = Fx128{0, 0};
+        // every path: discount the cashflow; the in-the-money ones queue until a full warp
+        // of them does the FP64 work (the warp's count qn and list length nout are uniform)
+        int qn = 0, nout = 0;
+        for (int64_t base = gw * 32; base < A.n; base += T) {
+            const int64_t p = base + lane;
+            bool itm = false;
+            float sf = 0.0f;
+            double y = 0.0;
+            if (p < A.n) {
+                y = __dmul_rn(A.cf[p], d);
+                A.cf[p] = y;
+                sf = row[p];
+                itm = in_the_money(sf, A);
+            }
+            const unsigned mk = __ballot_sync(0xffffffffu, itm);
+            if (itm) {
+                const int k = qn + __popc(mk & below);
+                q_idx[warp][k] = (int)p;
+                q_s[warp][k] = sf;
+                q_y[warp][k] = y;
+            }
+            qn += __popc(mk);
+            __syncwarp();
+            if (qn >= 32) {
+                qn -= 32;
+                const int k = qn + lane;
+                itm_item(q_idx[warp][k], q_s[warp][k], q_y[warp][k], A, q, seg + nout + lane, bad);
+                nout += 32;
+                __syncwarp();
+            }
+        }
+        if (lane < qn) itm_item(q_idx[warp][lane], q_s[warp][lane], q_y[warp][lane], A, q, seg + nout + lane, bad);
+        nout += qn;
+        const unsigned cnt = (unsigned)nout;
+#pragma unroll
+        for (int i = 0; i < LSM_NQ; i++) warp_sum(q[i]);
+        if (lane == 0) {
+#pragma unroll
+            for (int i = 0; i < LSM_NQ; i++) s_w[warp][i] = q[i];
+            s_w[warp][LSM_NQ] = Fx128{cnt, 0};
+        }
+        __syncthreads();
+        const int buf = t & 1;
+        if (threadIdx.x < LSM_PART) {
+            Fx128 s = {0, 0};
+            for (int w = 0; w < LSM_WARPS; w++) fx_add(s, s_w[w][threadIdx.x]);
+            A.part[((size_t)buf * G + blockIdx.x) * LSM_PART + threadIdx.x] = s;
+            __threadfence();
+        }
+        if (bad) atomicExch(A.status, 3);
+        ++phase;
+        __syncthreads();
+        // the last CTA to publish its sums adds them all, solves and releases the others
+        if (threadIdx.x == 0) s_last = atomicAdd(A.bar, 1u) == phase * (unsigned)G - 1;
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            if (warp < LSM_PART) {
+                const Fx128* P = A.part + (size_t)buf * G * LSM_PART + warp;
+                Fx128 s = {0, 0};
+#pragma unroll 4
+                for (int c = lane; c < G; c += 32) {
+                    const unsigned long long* e = reinterpret_cast<const unsigned long long*>(P + (size_t)c * LSM_PART);
+                    fx_add(s, (uint64_t)__ldcg(e), (uint64_t)__ldcg(e + 1));
+                }
+                warp_sum(s);
+                if (lane == 0) s_tot[warp] = s;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double b[3] = {0.0, 0.0, 0.0};
+                s_fit = s_tot[LSM_NQ].lo >= (uint64_t)A.min_itm && solve3(s_tot, b);
+                s_b[0] = b[0];
+                s_b[1] = b[1];
+                s_b[2] = b[2];
+                A.fit[t] = s_fit;
+                A.beta[3 * t] = b[0];
+                A.beta[3 * t + 1] = b[1];
+                A.beta[3 * t + 2] = b[2];
+                __threadfence();
+                st_release(A.done, phase);
+            }
+        } else if (threadIdx.x == 0) {
+            int ok = wait_for(A.done, phase, A.status);
+            if (ok) {
+                s_fit = __ldcg(A.fit + t);
+                s_b[0] = __ldcg(A.beta + 3 * t);
+                s_b[1] = __ldcg(A.beta + 3 * t + 1);
+                s_b[2] = __ldcg(A.beta + 3 * t + 2);
+            }
+            s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_last && !s_ok) return;
+        if (s_fit) {
+            const double b0 = s_b[0], b1 = s_b[1], b2 = s_b[2];
+            const double dt = A.disc[t];
+            for (int j = lane; j < nout; j += 32) {
+                const int64_t o = seg + j;
+                const double iv = A.c_iv[o];
+                if (iv >= continuation(b0, b1, b2, A.c_m[o])) {
+                    const int p = A.c_idx[o];
+                    A.cf[p] = iv;
+                    A.val[p] = __dmul_rn(iv, dt);
+                }
+            }
+        }
+    }
+
+    Fx128 v = {0, 0}, v2 = {0, 0};
+    for (int64_t p = g0; p < A.n; p += T) {
+        const double x = A.val[p];
+        fx_add_checked(v, x, bad);
+        fx_add_checked(v2, __dmul_rn(x, x), bad);
+    }
+    if (bad) atomicExch(A.status, 3);
+    Fx128* acc = A.acc + (size_t)blockIdx.x * LSM_NACC;
+    block_sum(v, s_w, 0, acc);
+    block_sum(v2, s_w, 1, acc + 1);
+    block_sum(eu, s_w, 2, acc + 2);
+}
+
+__global__ void __launch_bounds__(LSM_THREADS) lsm_apply_kernel(const LsmArgs A)
+{
+    __shared__ Fx128 s_w[LSM_WARPS][LSM_PART];
+    const int64_t T = (int64_t)gridDim.x * LSM_THREADS;
+    const int64_t g0 = (int64_t)blockIdx.x * LSM_THREADS + threadIdx.x;
+    bool bad = false;
+    Fx128 v = {0, 0}, v2 = {0, 0}, eu = {0, 0};
+    const float* last = A.S + (int64_t)(A.M - 1) * A.ld;
+    const double dT = A.disc[A.M - 1];
+    for (int64_t p = g0; p < A.n; p += T) {
+        double x = -1.0;
+        for (int t = 1; t < A.M - 1; ++t) {
+            if (!A.fit[t]) continue;
+            const float sf = A.S[(int64_t)t * A.ld + p];
+            if (!in_the_money(sf, A)) continue;
+            const double s = (double)sf;
+            const double iv = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
+            if (iv >= continuation(A.beta[3 * t], A.beta[3 * t + 1], A.beta[3 * t + 2], moneyness(s, A))) {
+                x = __dmul_rn(iv, A.disc[t]);
+                break;
+            }
+        }
+        const double e = __dmul_rn(intrinsic((double)last[p], A.strike, A.call), dT);
+        if (x < 0.0) x = e;
+        fx_add_checked(v, x, bad);
+        fx_add_checked(v2, __dmul_rn(x, x), bad);
+        fx_add_checked(eu, e, bad);
+    }
+    if (bad) atomicExch(A.status, 3);
+    Fx128* acc = A.acc + (size_t)blockIdx.x * LSM_NACC;
+    block_sum(v, s_w, 0, acc);
+    block_sum(v2, s_w, 1, acc + 1);
+    block_sum(eu, s_w, 2, acc + 2);
+}
+
+} // namespace
+
+int lsm_fit_max_grid(int sms)
+{
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lsm_fit_kernel, LSM_THREADS, 0) != cudaSuccess) return 0;
+    return per * sms;
+}
+
+cudaError_t launch_lsm_fit(const LsmArgs& A, int grid, cudaStream_t st)
+{
+    LsmArgs a = A;
+    void* args[] = {&a};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(lsm_fit_kernel), dim3(grid), dim3(LSM_THREADS),
+                                       args, 0, st);
+}
+
+cudaError_t launch_lsm_apply(const LsmArgs& A, int grid, cudaStream_t st)
+{
+    lsm_apply_kernel<<<grid, LSM_THREADS, 0, st>>>(A);
+    return cudaGetLastError();
+}

@@ -7,6 +7,7 @@
 // the reference's indicators do (monte_carlo_node.cpp:26-40).
 #include "thoth_gpu.h"
 #include "engine.cuh"
+#include "american.cuh"
 
 #include <cuda_runtime.h>
 
@@ -84,6 +85,8 @@ struct Device {
     int* cancel_dev = nullptr;
     float* paths = nullptr;          // stored paths of thoth_gpu_simulate_paths
     size_t paths_size = 0;
+    unsigned char* lsm = nullptr;    // Longstaff-Schwartz scratch
+    size_t lsm_size = 0;
 };
 Device g_dev;
 
@@ -1098,12 +1101,12 @@ int price_locked(const ThothBookDesc* book, ThothBookResult* out)
 
 // the book priced as by price_locked, with the spot of one asset stored at every
 // date of every path (date-major on the device, copied to the caller's array)
-int simulate_paths_locked(const ThothBookDesc* book, int asset, float* out, double* device_ms)
+// simulate the book and keep the spot of `asset` at every date of every path in
+// g_dev.paths, date-major ([n_steps + 1][paths])
+int simulate_device_locked(const ThothBookDesc* book, int asset, Plan& P, double* device_ms)
 {
-    if (!out) return fail(THOTH_GPU_E_INVALID, "null output");
     int rc = ensure_device();
     if (rc) return rc;
-    Plan P;
     rc = build_plan(book, P);
     if (rc) return rc;
     if (asset < 0 || asset >= P.dp.n_assets) return fail(THOTH_GPU_E_INVALID, "asset out of range");
@@ -1126,8 +1129,181 @@ int simulate_paths_locked(const ThothBookDesc* book, int asset, float* out, doub
     std::memset(&sums, 0, sizeof sums);
     rc = run_bound(P, g_dev.arena, L, grid, &sums, true);
     if (rc) return rc;
-    CUDA_TRY(cudaMemcpy(out, g_dev.paths, bytes, cudaMemcpyDeviceToHost));
     if (device_ms) *device_ms = sums.device_ms;
+    return THOTH_GPU_OK;
+}
+
+int simulate_paths_locked(const ThothBookDesc* book, int asset, float* out, double* device_ms)
+{
+    if (!out) return fail(THOTH_GPU_E_INVALID, "null output");
+    Plan P;
+    int rc = simulate_device_locked(book, asset, P, device_ms);
+    if (rc) return rc;
+    const size_t bytes = sizeof(float) * (size_t)(P.dp.n_steps + 1) * (size_t)P.paths;
+    CUDA_TRY(cudaMemcpy(out, g_dev.paths, bytes, cudaMemcpyDeviceToHost));
+    return THOTH_GPU_OK;
+}
+
+int ensure_lsm(size_t bytes)
+{
+    if (bytes <= g_dev.lsm_size) return THOTH_GPU_OK;
+    if (g_dev.lsm) cudaFree(g_dev.lsm);
+    g_dev.lsm = nullptr;
+    g_dev.lsm_size = 0;
+    CUDA_TRY(cudaMalloc(&g_dev.lsm, bytes));
+    g_dev.lsm_size = bytes;
+    return THOTH_GPU_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// float bits t such that (double) S > K <=> bits(S) >= t for a call, (double) S < K <=>
+// bits(S) <= t for a put, for every non-negative float S (their bit patterns are ordered
+// like their values): the smallest float above K, resp. the largest below it
+int32_t itm_threshold(double K, bool call)
+{
+    float f = (float)K;
+    if (call) {
+        if (!(K >= 0.0)) return 0;
+        if ((double)f <= K) f = std::nextafter(f, INFINITY);
+    } else {
+        if (!(K > 0.0)) return -1;
+        if ((double)f >= K) f = std::nextafter(f, 0.0f);
+    }
+    int32_t b;
+    std::memcpy(&b, &f, sizeof b);
+    return b;
+}
+
+// One Longstaff-Schwartz pass (american.cu) on the stored paths of io.asset: simulate the
+// book, then fit a policy and value it on the same paths, or value the given policy.
+int lsm_pass_locked(const ThothBookDesc* book, LsmPass& io)
+{
+    Plan P;
+    double sim_ms = 0;
+    int rc = simulate_device_locked(book, io.asset, P, &sim_ms);
+    if (rc) return rc;
+    const int M = io.M;
+    if (M < 2 || M > P.dp.n_steps + 1) return fail(THOTH_GPU_E_INVALID, "exercise grid outside the book's dates");
+    if (!(io.norm > 0.0) || !std::isfinite(io.norm) || !std::isfinite(io.strike))
+        return fail(THOTH_GPU_E_INVALID, "exercise fit needs a finite strike and a positive moneyness normaliser");
+    if ((int)io.df.size() != M || (int)io.disc.size() != M)
+        return fail(THOTH_GPU_E_INVALID, "discount arrays must have one entry per exercise date");
+    if (!io.fit && ((int)io.beta.size() != 3 * M || (int)io.fit_at.size() != M))
+        return fail(THOTH_GPU_E_INVALID, "frozen policy does not match the exercise grid");
+    const int64_t N = P.paths;
+    if (N >= ((int64_t)1 << 27)) return fail(THOTH_GPU_E_TOO_LARGE, "American exercise needs fewer than 2^27 paths");
+    const int64_t want = (N + LSM_THREADS - 1) / LSM_THREADS;
+    int grid;
+    if (io.fit) {
+        const int cap = lsm_fit_max_grid(g_dev.sms);
+        if (cap < 1) return fail(THOTH_GPU_E_CUDA, "no resident CTA for the exercise fit kernel");
+        grid = (int)std::min<int64_t>(want, cap);
+    } else {
+        grid = (int)std::min<int64_t>(want, (int64_t)8 * g_dev.sms);
+    }
+    grid = std::max(grid, 1);
+    // device scratch: per-path fit state, the compacted in-the-money lists, the date tables,
+    // partial sums, arrival counter, release flag and status
+    const int64_t threads = (int64_t)grid * LSM_THREADS;
+    const int64_t seg_len = 32 * ((N + threads - 1) / threads);
+    const size_t n_list = io.fit ? (size_t)(grid * (LSM_THREADS / 32)) * (size_t)seg_len : 0;
+    const size_t per_path = io.fit ? align256(sizeof(double) * (size_t)N) : 0;
+    const size_t tab = sizeof(double) * 5 * (size_t)M + sizeof(int32_t) * (size_t)M;
+    const size_t o_cf = 0, o_val = per_path;
+    const size_t o_cm = 2 * per_path, o_civ = o_cm + align256(sizeof(double) * n_list);
+    const size_t o_cidx = o_civ + align256(sizeof(double) * n_list);
+    const size_t o_tab = o_cidx + align256(sizeof(int32_t) * n_list);
+    const size_t o_part = o_tab + align256(tab);
+    const size_t o_acc = o_part + align256(sizeof(Fx128) * 2 * (size_t)grid * LSM_PART);
+    const size_t acc_bytes = sizeof(Fx128) * (size_t)grid * LSM_NACC;
+    const size_t o_ctl = o_acc + align256(acc_bytes);
+    rc = ensure_lsm(o_ctl + 256);
+    if (rc) return rc;
+    const size_t back = acc_bytes + 2 * sizeof(int) + sizeof(float) + tab;
+    rc = ensure_pinned(std::max(tab, back));
+    if (rc) return rc;
+    unsigned char* base = g_dev.lsm;
+    unsigned char* h = g_dev.pinned;
+    std::vector<int32_t> fit0(M, 0);
+    std::vector<double> beta0(3 * (size_t)M, 0.0);
+    const std::vector<double>& beta = io.fit ? beta0 : io.beta;
+    const std::vector<int32_t>& fit_at = io.fit ? fit0 : io.fit_at;
+    std::memcpy(h, io.df.data(), sizeof(double) * M);
+    std::memcpy(h + sizeof(double) * M, io.disc.data(), sizeof(double) * M);
+    std::memcpy(h + sizeof(double) * 2 * M, beta.data(), sizeof(double) * 3 * M);
+    std::memcpy(h + sizeof(double) * 5 * M, fit_at.data(), sizeof(int32_t) * M);
+    cudaStream_t st = g_dev.stream;
+    CUDA_TRY(cudaMemcpyAsync(base + o_tab, h, tab, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(base + o_ctl, 0, 3 * sizeof(int), st));
+    LsmArgs A;
+    A.S = g_dev.paths;
+    A.ld = P.paths;
+    A.n = N;
+    A.M = M;
+    A.call = io.call;
+    A.strike = io.strike;
+    A.norm = io.norm;
+    A.inv_norm = 1.0 / io.norm;
+    A.itm_bits = itm_threshold(io.strike, io.call != 0);
+    A.min_itm = io.min_itm;
+    A.df = reinterpret_cast<const double*>(base + o_tab);
+    A.disc = A.df + M;
+    A.beta = reinterpret_cast<double*>(base + o_tab) + 2 * (size_t)M;
+    A.fit = reinterpret_cast<int*>(base + o_tab + sizeof(double) * 5 * (size_t)M);
+    A.cf = reinterpret_cast<double*>(base + o_cf);
+    A.val = reinterpret_cast<double*>(base + o_val);
+    A.seg_len = seg_len;
+    A.c_m = reinterpret_cast<double*>(base + o_cm);
+    A.c_iv = reinterpret_cast<double*>(base + o_civ);
+    A.c_idx = reinterpret_cast<int32_t*>(base + o_cidx);
+    A.part = reinterpret_cast<Fx128*>(base + o_part);
+    A.acc = reinterpret_cast<Fx128*>(base + o_acc);
+    A.bar = reinterpret_cast<unsigned*>(base + o_ctl);
+    A.status = reinterpret_cast<int*>(base + o_ctl + sizeof(int));
+    A.done = reinterpret_cast<unsigned*>(base + o_ctl + 2 * sizeof(int));
+    if (!io.fit) {
+        A.cf = A.val = A.c_m = A.c_iv = nullptr;
+        A.c_idx = nullptr;
+    }
+    CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+    CUDA_TRY(io.fit ? launch_lsm_fit(A, grid, st) : launch_lsm_apply(A, grid, st));
+    CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
+    CUDA_TRY(cudaMemcpyAsync(h, base + o_acc, acc_bytes, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(h + acc_bytes, base + o_ctl, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(h + acc_bytes + 2 * sizeof(int), g_dev.paths, sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (io.fit)
+        CUDA_TRY(cudaMemcpyAsync(h + acc_bytes + 2 * sizeof(int) + sizeof(float), base + o_tab, tab,
+                                 cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+    int status;
+    std::memcpy(&status, h + acc_bytes + sizeof(int), sizeof(int));
+    if (status == 2) return fail(THOTH_GPU_E_CUDA, "exercise fit: grid barrier timed out");
+    if (status == 3) return fail(THOTH_GPU_E_INVALID, "exercise fit: a cashflow or moneyness power is out of range (>= 2^36)");
+    if (status != 0) return fail(THOTH_GPU_E_CUDA, "exercise fit: kernel status " + std::to_string(status));
+    Fx128 tot[LSM_NACC] = {};
+    const Fx128* a = reinterpret_cast<const Fx128*>(h);
+    for (int c = 0; c < grid; c++)
+        for (int k = 0; k < LSM_NACC; k++) fx_add(tot[k], a[(size_t)c * LSM_NACC + k]);
+    io.sum = fx_to_double(tot[0]);
+    io.sum2 = fx_to_double(tot[1]);
+    io.euro = fx_to_double(tot[2]);
+    float s0;
+    std::memcpy(&s0, h + acc_bytes + 2 * sizeof(int), sizeof(float));
+    io.s0 = s0;
+    if (io.fit) {
+        const unsigned char* tb = h + acc_bytes + 2 * sizeof(int) + sizeof(float);
+        io.beta.resize(3 * (size_t)M);
+        io.fit_at.resize(M);
+        std::memcpy(io.beta.data(), tb + sizeof(double) * 2 * M, sizeof(double) * 3 * M);
+        std::memcpy(io.fit_at.data(), tb + sizeof(double) * 5 * M, sizeof(int32_t) * M);
+    }
+    io.paths = N;
+    io.grid = grid;
+    io.sim_ms = sim_ms;
+    io.lsm_ms = ms;
     return THOTH_GPU_OK;
 }
 
@@ -1681,6 +1857,20 @@ struct ThothBookHandle {
     Layout layout{};
     unsigned char* dev = nullptr;
 };
+
+// the exercise pass of thoth_gpu_price_american (american_host.cu)
+int thoth_lsm_pass(const ThothBookDesc* book, LsmPass& io)
+{
+    try {
+        if (!book) return fail(THOTH_GPU_E_INVALID, "null book");
+        std::lock_guard<std::mutex> lk(g_mu);
+        return lsm_pass_locked(book, io);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
 
 // ---------------------------------------------------------------------------
 // C ABI
