@@ -228,17 +228,11 @@ def american_section(G, flush, steps):
     import numpy as np
     import torch
     from oracle import american as am
-    from thoth_gb300 import abi
-
-    def put_book(paths, days, heston=True):
-        b = abi.Book(days=np.asarray(days), paths=paths)
-        a = b.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.03) if heston else b.add_gbm(100.0, 0.30, 0.08)
-        b.add_vanilla(a, 100.0, len(days) - 1, abi.PUT, zero_rate=0.03 if heston else 0.08)
-        return b
+    from thoth_gb300 import abi, workloads as W
 
     out = {}
-    cases = (("heston_daily_2^20", put_book(1 << 20, range(0, 366))),
-             ("gbm_30day_300000", put_book(300000, list(range(0, 361, 30)) + [365], heston=False)))
+    cases = (("heston_daily_2^20", W.american_put(1 << 20)),
+             ("gbm_30day_300000", W.american_put(300000, heston=False)))
     for name, book in cases:
         G.price_american(book, 0)
         ex, dev, wall = [], [], []
@@ -267,7 +261,7 @@ def american_section(G, flush, steps):
     out["heston_daily_2^20"]["greeks_wall_ms"] = 1e3 * (time.perf_counter() - t0)
     out["heston_daily_2^20"]["greeks_device_ms"] = g["device_ms"]
     # CPU: the oracle (numpy, exact sums, one core) on the first 2^15 stored paths
-    sample = put_book(1 << 15, range(0, 366))
+    sample = W.american_put(1 << 15)
     S, _ = G.simulate_paths(sample, 0)
     t0 = time.perf_counter()
     o = am.fit(S, sample.t, np.full(sample.n_dates, 0.03), 100.0, False, 100.0)

@@ -91,6 +91,11 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
     return v;
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void st_release(unsigned* p, unsigned v)
 {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -115,13 +120,12 @@ __device__ bool wait_for(const unsigned* flag, unsigned want, int* status)
 // (X^T X) beta = X^T y for X = {1, m, m^2}: Cholesky A = L L^T in place of the lower
 // triangle, forward then back substitution (maths.cpp:354-381, 419-470). False when a pivot
 // is not positive (the date keeps no regression).
-__device__ bool solve3(const Fx128* tot, double* beta)
+__device__ bool solve3(const double* tot, double* beta)
 {
-    const double n = (double)tot[LSM_NQ].lo;
-    const double s1 = fx_to_double(tot[0]), s2 = fx_to_double(tot[1]);
-    const double s3 = fx_to_double(tot[2]), s4 = fx_to_double(tot[3]);
+    const double n = tot[LSM_NQ];
+    const double s1 = tot[0], s2 = tot[1], s3 = tot[2], s4 = tot[3];
     double A[3][3] = {{n, s1, s2}, {s1, s2, s3}, {s2, s3, s4}};
-    const double g[3] = {fx_to_double(tot[4]), fx_to_double(tot[5]), fx_to_double(tot[6])};
+    const double g[3] = {tot[4], tot[5], tot[6]};
     for (int i = 0; i < 3; i++) {
         for (int j = 0; j <= i; j++) {
             double sum = A[i][j];
@@ -187,9 +191,10 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmArgs A
     __shared__ int q_idx[LSM_WARPS][LSM_QCAP];
     __shared__ float q_s[LSM_WARPS][LSM_QCAP];
     __shared__ double q_y[LSM_WARPS][LSM_QCAP];
-    __shared__ Fx128 s_tot[LSM_PART];
+    __shared__ double s_tot[LSM_PART];
     __shared__ double s_b[3];
     __shared__ int s_fit, s_ok, s_last;
+    __shared__ uint64_t s_cnt;
     const int G = gridDim.x;
     const int64_t T = (int64_t)G * LSM_THREADS;
     const int64_t g0 = (int64_t)blockIdx.x * LSM_THREADS + threadIdx.x;
@@ -274,6 +279,12 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmArgs A
         __syncthreads();
         // the last CTA to publish its sums adds them all, solves and releases the others
         if (threadIdx.x == 0) s_last = atomicAdd(A.bar, 1u) == phase * (unsigned)G - 1;
+        // while the regression is solved: pull the next date's spots of this warp's paths
+        // into L2 (lane k takes the warp's k-th, (k+32)-th, ... line of 32 paths)
+        if (t > 1) {
+            const float* next = A.S + (int64_t)(t - 1) * A.ld;
+            for (int64_t pp = gw * 32 + (int64_t)lane * T; pp < A.n; pp += 32 * T) prefetch_l2(next + pp);
+        }
         __syncthreads();
         if (s_last) {
             __threadfence();
@@ -286,12 +297,14 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmArgs A
                     fx_add(s, (uint64_t)__ldcg(e), (uint64_t)__ldcg(e + 1));
                 }
                 warp_sum(s);
-                if (lane == 0) s_tot[warp] = s;
+                // each warp rounds its own sum to double (the count is exact below 2^53)
+                if (lane == 0) s_tot[warp] = warp == LSM_NQ ? (double)s.lo : fx_to_double(s);
+                if (warp == LSM_NQ && lane == 0) s_cnt = s.lo;
             }
             __syncthreads();
             if (threadIdx.x == 0) {
                 double b[3] = {0.0, 0.0, 0.0};
-                s_fit = s_tot[LSM_NQ].lo >= (uint64_t)A.min_itm && solve3(s_tot, b);
+                s_fit = s_cnt >= (uint64_t)A.min_itm && solve3(s_tot, b);
                 s_b[0] = b[0];
                 s_b[1] = b[1];
                 s_b[2] = b[2];

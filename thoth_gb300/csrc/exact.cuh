@@ -101,10 +101,21 @@ FX_HD double fx_u64_to_double(uint64_t v)
 #endif
 }
 
+// d 2^k for d = 0 or d >= 1, -64 <= k <= 0: exact (the result is a normal double)
+FX_HD double fx_scale(double d, int k)
+{
+#ifdef __CUDA_ARCH__
+    const long long b = __double_as_longlong(d);
+    return b == 0 ? 0.0 : __longlong_as_double(b + ((long long)k << 52));
+#else
+    return std::ldexp(d, k);
+#endif
+}
+
 // the nearest double to the fixed-point value (hi * 2^64 + lo) * 2^-64
 FX_HD double fx_to_double(const Fx128& a)
 {
-    if (a.hi == 0) return std::ldexp(fx_u64_to_double(a.lo), -64);
+    if (a.hi == 0) return fx_scale(fx_u64_to_double(a.lo), -64);
     // keep the top 64 significant bits and fold the rest into a sticky bit, which sits
     // 11 bits below the double's rounding position: rounding the 64 bits then rounds the
     // 128-bit value correctly, ties included
@@ -118,5 +129,5 @@ FX_HD double fx_to_double(const Fx128& a)
         rest = a.lo & ((1ull << s) - 1);
     }
     top |= rest ? 1u : 0u;
-    return std::ldexp(fx_u64_to_double(top), s - 64);
+    return fx_scale(fx_u64_to_double(top), s - 64);
 }

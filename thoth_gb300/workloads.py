@@ -7,6 +7,8 @@ with the shapes, sizes and parameter ranges of the workloads it is measured on:
   heston_grid         Heston vanilla grid, 9 strikes x 7 maturities x call/put
   lsv_book            5 LSV names, 20 down-and-out calls, 10 variance swaps, 20 baskets
   ragged_books        256 books of uneven path and step counts (GBM / Heston / LSV mix)
+  american_put        1 asset American put, Heston daily exercise or the reference tests'
+                      GBM case (30-day exercise grid)
 """
 import math
 
@@ -131,6 +133,22 @@ def lsv_book(paths=1 << 20, seed=20260101, horizon_days=365, n_lev_strikes=50, n
         w = 100.0 * w / w.sum() / S0[comps]          # rebased-100 index weights
         m = mats[j % 3]
         b.add_basket(comps, w, rng.uniform(90, 110), m, CALL, zero_rate=rates[0], fx=1.0)
+    return b
+
+
+def american_put(paths=1 << 20, heston=True, days=None):
+    """American put K=100 on one asset S0=100: Heston (the grid's parameters, r=3%) with a
+    year of daily exercise dates, or GBM vol 30% r=8% on the reference tests' grid (one
+    year, 30-day steps: pricer/tests/test_american.cpp). Product 0 is the put."""
+    if days is None:
+        days = range(0, 366) if heston else list(range(0, 361, 30)) + [365]
+    b = Book(days=np.asarray(days), paths=paths)
+    if heston:
+        h = HESTON
+        a = b.add_heston(100.0, h["v0"], h["kappa"], h["theta"], h["xi"], h["rho"], 0.03)
+    else:
+        a = b.add_gbm(100.0, 0.30, 0.08)
+    b.add_vanilla(a, 100.0, len(b.t) - 1, PUT, zero_rate=0.03 if heston else 0.08)
     return b
 
 
