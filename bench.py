@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-lsv", action="store_true", help="skip the multi-asset LSV book section")
     ap.add_argument("--no-paths", action="store_true", help="skip the stored-paths (HBM) section")
     ap.add_argument("--no-american", action="store_true", help="skip the American (Longstaff-Schwartz) section")
+    ap.add_argument("--no-calibration", action="store_true", help="skip the LSV leverage calibration section")
     return ap.parse_args()
 
 
@@ -276,6 +277,41 @@ def american_section(G, flush, steps):
     return out
 
 
+def calibration_section(G):
+    """LSV leverage calibration by the reference's particle method for one name: 365 daily
+    layers of 201 points, 16 384 particles (the reference's count) and 2^18; the oracle (C
+    restatement of the reference's loop, one host core) on the 16 384-particle case."""
+    import numpy as np
+    import oracle
+    from thoth_gb300 import workloads as W
+    out = {}
+    L = None
+    for P in (16384, 1 << 18):
+        c = W.lsv_calibration(horizon_days=365, particles=P)
+        G.calibrate_leverage(c)
+        dev, wall = [], []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            lev, ms = G.calibrate_leverage(c)
+            wall.append(time.perf_counter() - t0)
+            dev.append(ms)
+        if P == 16384:
+            L = lev
+        d = float(np.median(dev))
+        out["particles_%d" % P] = {"device_ms": d, "e2e_ms": 1e3 * float(np.median(wall)),
+                                   "particle_steps_per_sec": P * 365 / (d * 1e-3), "layers": 366, "points": 201}
+    c = W.lsv_calibration(horizon_days=365)
+    t0 = time.perf_counter()
+    ref = oracle.calibrate_leverage(c)
+    cpu = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": 16384 * 365 / cpu, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+                           "sample": "oracle.calibrate_leverage: 16384 particles x 365 daily layers (%.3f s)" % cpu}
+    out["max_rel_diff_vs_oracle"] = float(np.max(np.abs(L / ref - 1.0)))
+    out["note"] = ("one cooperative launch, two exact publish-and-release rounds a date (extremes and sum of v, "
+                   "then the bins); FP64-latency bound; the Rng stream is the reference's, jumped per particle")
+    return out
+
+
 def ragged_batch_section(G, steps):
     """256 ragged books (path counts log-uniform in [2^14, 2^22], 12..730 daily steps,
     40% GBM / 40% Heston / 20% LSV) priced as one CUDA graph: untuned, after the
@@ -409,6 +445,8 @@ def run_gpu(args):
             line["stored_paths"] = paths_section(G, flush)
         if not args.no_american:
             line["american_lsm"] = american_section(G, flush, args.steps)
+        if not args.no_calibration:
+            line["lsv_calibration"] = calibration_section(G)
         if not args.no_batch:
             line["ragged_batch"] = ragged_batch_section(G, args.steps)
         if not args.no_surrogate:

@@ -320,6 +320,52 @@ typedef struct ThothAmerican {
 int thoth_gpu_price_american(const ThothBookDesc* book, ThothAmerican* am);
 const char* thoth_gpu_american_last_error(void);
 
+/* ---- LSV leverage calibration (binned particle method) ----------------------
+ * Replaces Single::CalibrateLeverage (pricer/src/marketdata/single.cpp:390-473):
+ * a Heston ensemble is diffused forward over the dates with the leverage being
+ * built; before the step into date k, layer k is set from the Dupire condition
+ *   L(x_i, t_k) = clamp(sigma_loc(x_i, t_k) / sqrt(max(E[v | ln S = x_i], min_cv)),
+ *                       lev_min, lev_max)
+ * with E[v | ln S] the binned conditional mean of the current ensemble
+ * (equal-width log-spot bins between the ensemble's extremes, thin bins filled
+ * from the nearest populated one, linear between bin centres; the ensemble mean
+ * while all particles share one spot). The step is the reference's QE variance
+ * step and leveraged log-spot step, layer k read at the previous spot. Gaussians
+ * are the reference's Rng stream (xoshiro256++ seeded by splitmix64, inverse
+ * normal), two per particle and date in particle order, so the layers follow the
+ * reference's ensemble.
+ * The caller supplies each layer's grid and the target local vol on it (the
+ * reference sizes the grid from the ATM implied vol, single.cpp:432-443, and reads
+ * sigma_loc from its implied surface): the output is the leverage surface of an
+ * LSV ThothAsset (lev_ln_step = ln_step, lev_offset = offset, lev_values). */
+typedef struct ThothLeverageCalib {
+    int32_t n_dates;          /* in: layers, one per date; date 0 is today             */
+    int32_t points;           /* in: grid points per layer (the reference: 201)        */
+    const int32_t* days;      /* in: [n_dates] calendar days from today, days[0] = 0   */
+    const double* carry;      /* in: [n_dates] net carry r - q - repo to each date     */
+    double spot;              /* in: diffusion spot at today                           */
+    double v0, kappa, theta, xi, rho; /* in: the Heston base                           */
+    const double* ln_step;    /* in: [n_dates] layer grid spacing in log-spot          */
+    const int64_t* offset;    /* in: [n_dates] grid point i sits at (offset + i) ln_step */
+    const double* local_vol;  /* in: [n_dates][points] target local vol at the points */
+    int32_t particles;        /* in: ensemble size; <= 0: 16384                         */
+    int32_t bins;             /* in: conditional-mean bins; <= 0: 30                    */
+    int32_t min_bin_count;    /* in: a thinner bin takes its neighbour's mean; <= 0: 20 */
+    int32_t _pad;
+    uint64_t seed;            /* in: Rng seed (the reference's is 20260708)             */
+    double min_cond_variance; /* in: <= 0: 1e-6                                         */
+    double lev_min, lev_max;  /* in: clamp; <= 0: 0.05 and 10                          */
+    double* leverage;         /* out: [n_dates][points] layers                         */
+    double device_ms;         /* out                                                    */
+} ThothLeverageCalib;
+
+int thoth_gpu_calibrate_leverage(ThothLeverageCalib* c);
+
+/* the reference Rng's state after n draws from the state s (xoshiro256++ is
+ * linear over GF(2): a jump is a polynomial in the transition, x^n modulo its
+ * characteristic polynomial); host computation, no device needed */
+int thoth_gpu_xoshiro_jump(const uint64_t s[4], uint64_t n, uint64_t out[4]);
+
 /* Price n_books independent books (ragged path and step counts) in one CUDA
  * graph launch: all plans in one upload, each book's persistent kernel and
  * reduction on one of several streams (largest first), all sums back in one

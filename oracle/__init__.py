@@ -60,6 +60,9 @@ def port():
             getattr(lib, f).argtypes = [C.c_double] * 10 + [C.c_int]
             getattr(lib, f).restype = C.c_double
         lib.oracle_heston_prices.argtypes = [C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
+        lib.oracle_calibrate_leverage.argtypes = [C.POINTER(abi.ThothLeverageCalib)]
+        lib.oracle_xoshiro_draws.argtypes = [C.c_uint64, C.c_uint64, C.c_int64, C.POINTER(C.c_uint64),
+                                             C.POINTER(C.c_uint64)]
         rc = lib.oracle_load_direction_numbers(str(JK_TABLE).encode())
         if rc != 0:
             raise RuntimeError("cannot load %s (%d)" % (JK_TABLE, rc))
@@ -81,6 +84,8 @@ def ref():
                                               C.c_uint64, C.POINTER(C.c_double)]
         lib.ref_price_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBookResult),
                                        C.POINTER(C.c_double), C.c_int64]
+        lib.ref_rng_draws.argtypes = [C.c_uint64, C.c_uint64, C.c_int64, C.POINTER(C.c_uint64),
+                                      C.POINTER(C.c_double)]
         lib.ref_least_squares.argtypes = [C.POINTER(C.c_double), C.c_int64, C.c_int, C.POINTER(C.c_double),
                                           C.POINTER(C.c_double)]
         lib.ref_lsm.argtypes = [C.POINTER(C.c_float), C.c_int64, C.c_int, C.POINTER(C.c_double),
@@ -139,6 +144,33 @@ def price_book(book, which="port", threads=1, n_per_path=0):
         raise RuntimeError("%s price_book failed: %d" % (which, rc))
     return dict(book_premium=r.book_premium, book_trust=r.book_trust, premium=arrs["premium"].copy(),
                 trust=arrs["trust"].copy(), per_path=per[:n_per_path].copy() if n_per_path else None)
+
+
+def calibrate_leverage(calib):
+    """Single::CalibrateLeverage restated (thoth_oracle.c) on abi.LeverageCalibration inputs:
+    the layers [n_dates][points]."""
+    d = calib.desc()
+    out = np.zeros_like(calib.local_vol)
+    d.leverage = _d(out)
+    if port().oracle_calibrate_leverage(C.byref(d)) != 0:
+        raise RuntimeError("oracle calibration failed")
+    return out
+
+
+def xoshiro_draws(seed, skip, n):
+    """(n raw draws of the reference Rng after `skip`, the state after them)."""
+    out = np.zeros(max(n, 1), dtype=np.uint64)
+    st = (C.c_uint64 * 4)()
+    port().oracle_xoshiro_draws(seed, skip, n, out.ctypes.data_as(C.POINTER(C.c_uint64)), st)
+    return out[:n], [int(x) for x in st]
+
+
+def ref_rng_draws(seed, skip, n):
+    """The reference Rng: (n raw 64-bit draws, n Gaussians) after skipping `skip` draws."""
+    raw = np.zeros(n, dtype=np.uint64)
+    g = np.zeros(n)
+    ref().ref_rng_draws(seed, skip, n, raw.ctypes.data_as(C.POINTER(C.c_uint64)), _d(g))
+    return raw, g
 
 
 def ref_least_squares(X, y):

@@ -584,4 +584,22 @@ int ref_lsm( const float* S, int64_t n, int M, const double* tau, const double* 
     return 0;
 }
 
+//! raw draws and Gaussians of the reference's own Rng (helpers/rng.hpp): n draws after
+//! skipping `skip`, as Gaussian() would consume them
+int ref_rng_draws( uint64_t seed, uint64_t skip, int64_t n, uint64_t* raw, double* gauss )
+{
+    Rng a( seed ), b( seed );
+    for ( uint64_t i = 0; i < skip; i++ )
+    {
+        a();
+        b();
+    }
+    for ( int64_t i = 0; i < n; i++ )
+    {
+        raw[i] = a();
+        gauss[i] = b.Gaussian();
+    }
+    return 0;
+}
+
 } // extern "C"

@@ -872,3 +872,192 @@ int oracle_heston_prices(int64_t n, const double* args, double* out, int threads
     for (int k = 0; k < threads; k++) pthread_join(th[k], NULL);
     return 0;
 }
+
+
+/* ------------------------------------------------------------------------
+ * LSV leverage calibration: Single::CalibrateLeverage and its helpers
+ * (marketdata/single.cpp:240-473) in the same operation order.
+ * ---------------------------------------------------------------------- */
+int oracle_xoshiro_draws(uint64_t seed, uint64_t skip, int64_t n, uint64_t* out, uint64_t state_out[4])
+{
+    Xoshiro r;
+    xo_seed(&r, seed);
+    for (uint64_t i = 0; i < skip; i++) xo_next(&r);
+    for (int64_t i = 0; i < n; i++) out[i] = xo_next(&r);
+    if (state_out) memcpy(state_out, r.s, sizeof r.s);
+    return 0;
+}
+
+typedef struct {
+    double x0, dx, fallback;
+    int n;
+    double* mean;
+} CondVar;
+
+/* binned E[v | ln S] (single.cpp:256-316): equal-width bins between the extremes,
+ * thin bins from the nearest populated neighbour (left first), the ensemble mean
+ * while the extremes coincide */
+static void condvar_build(CondVar* cv, const double* ln, const double* var, int P, int bins, int min_count,
+                          double* sum, int* count)
+{
+    double fb = 0;
+    for (int p = 0; p < P; p++) fb += var[p];
+    fb /= (double)P;
+    cv->fallback = fb;
+    cv->n = 0;
+    double mn = ln[0], mx = ln[0];
+    for (int p = 1; p < P; p++) {
+        if (ln[p] < mn) mn = ln[p];
+        if (ln[p] > mx) mx = ln[p];
+    }
+    if (mx - mn < 1e-10) return;
+    const double width = (mx - mn) / bins;
+    for (int b = 0; b < bins; b++) {
+        sum[b] = 0.0;
+        count[b] = 0;
+    }
+    for (int p = 0; p < P; p++) {
+        int b = (int)((ln[p] - mn) / width);
+        b = b < 0 ? 0 : (b > bins - 1 ? bins - 1 : b);
+        sum[b] += var[p];
+        count[b]++;
+    }
+    for (int b = 0; b < bins; b++) cv->mean[b] = fb;
+    for (int b = 0; b < bins; b++)
+        if (count[b] >= min_count) cv->mean[b] = sum[b] / count[b];
+    for (int b = 0; b < bins; b++) {
+        if (count[b] >= min_count) continue;
+        for (int d = 1; d < bins; d++) {
+            if (b - d >= 0 && count[b - d] >= min_count) {
+                cv->mean[b] = sum[b - d] / count[b - d];
+                break;
+            }
+            if (b + d < bins && count[b + d] >= min_count) {
+                cv->mean[b] = sum[b + d] / count[b + d];
+                break;
+            }
+        }
+    }
+    cv->x0 = mn + 0.5 * width;
+    cv->dx = width;
+    cv->n = bins;
+}
+
+static double condvar_at(const CondVar* cv, double X)
+{
+    if (cv->n == 0) return cv->fallback;
+    const double f = (X - cv->x0) / cv->dx;
+    const double last = (double)(cv->n - 1);
+    if (f <= 0) return cv->mean[0];
+    if (f >= last) return cv->mean[cv->n - 1];
+    const size_t i = (size_t)f;
+    const double w = f - (double)i;
+    return (1.0 - w) * cv->mean[i] + w * cv->mean[i + 1];
+}
+
+/* one Andersen QE variance step (single.cpp:344-368) */
+static double calib_qe(double V, double Dt, double Z, double kappa, double theta, double xi)
+{
+    const double e = exp(-kappa * Dt);
+    const double m = theta + (V - theta) * e;
+    const double s2 = V * xi * xi * e / kappa * (1 - e) + theta * xi * xi / (2 * kappa) * (1 - e) * (1 - e);
+    const double psi = (m > 0) ? s2 / (m * m) : 0;
+    if (psi <= 1.5) {
+        const double c = 2.0 / psi;
+        const double b2 = c - 1.0 + sqrt(c) * sqrt(c - 1.0);
+        const double a = m / (1.0 + b2);
+        const double bz = sqrt(b2) + Z;
+        return a * bz * bz;
+    }
+    const double p = (psi - 1.0) / (psi + 1.0);
+    const double beta = (1.0 - p) / m;
+    const double u = 0.5 * erfc(-Z / sqrt(2.0));
+    return (u <= p) ? 0.0 : log((1.0 - p) / (1.0 - u)) / beta;
+}
+
+/* one leveraged Andersen log-spot step (single.cpp:370-388) */
+static double calib_spot(double Vp, double Vc, double Dt, double Carry, double L, double Z, double kappa,
+                         double theta, double xi, double rho)
+{
+    if (xi > 1e-12) {
+        const double g = 0.5;
+        const double k0 = -L * rho * kappa * theta / xi * Dt;
+        const double a = g * Dt * (L * kappa * rho / xi - 0.5 * L * L);
+        const double k1 = a - L * rho / xi;
+        const double k2 = a + L * rho / xi;
+        const double k3 = g * Dt * (1.0 - rho * rho) * L * L;
+        double var = k3 * (Vp + Vc);
+        if (var < 0) var = 0;
+        return Carry + k0 + k1 * Vp + k2 * Vc + sqrt(var) * Z;
+    }
+    return Carry - 0.5 * L * L * Vp * Dt + L * sqrt(Vp * Dt) * Z;
+}
+
+/* LeverageSurface::LayerAt (leverage_surface.cpp:19-40) */
+static double layer_at(const double* lev, int points, double ln_step, int64_t offset, double S)
+{
+    const double f = log(S) / ln_step - (double)offset;
+    const int last = points - 1;
+    if (!(f > 0.0)) return lev[0];
+    if (f >= (double)last) return lev[last];
+    const size_t i = (size_t)f;
+    const double w = f - (double)i;
+    return (1.0 - w) * lev[i] + w * lev[i + 1];
+}
+
+int oracle_calibrate_leverage(ThothLeverageCalib* c)
+{
+    const int P = c->particles > 0 ? c->particles : 16384;
+    const int bins = c->bins > 0 ? c->bins : 30;
+    const int min_count = c->min_bin_count > 0 ? c->min_bin_count : 20;
+    const double min_cv = c->min_cond_variance > 0 ? c->min_cond_variance : 1e-6;
+    const double lmin = c->lev_min > 0 ? c->lev_min : 0.05, lmax = c->lev_max > 0 ? c->lev_max : 10.0;
+    const int n = c->n_dates, pts = c->points;
+    if (n < 1 || pts < 2 || !c->days || !c->carry || !c->ln_step || !c->offset || !c->local_vol || !c->leverage)
+        return -1;
+    double* spot = malloc(sizeof(double) * P);
+    double* var = malloc(sizeof(double) * P);
+    double* ln = malloc(sizeof(double) * P);
+    double* mean = malloc(sizeof(double) * bins);
+    double* sum = malloc(sizeof(double) * bins);
+    int* count = malloc(sizeof(int) * bins);
+    Xoshiro rng;
+    xo_seed(&rng, c->seed);
+    for (int p = 0; p < P; p++) {
+        spot[p] = c->spot;
+        var[p] = c->v0;
+        ln[p] = log(c->spot);
+    }
+    CondVar cv = {0, 1, 0, 0, mean};
+    for (int k = 0; k < n; k++) {
+        condvar_build(&cv, ln, var, P, bins, min_count, sum, count);
+        double* layer = c->leverage + (size_t)k * pts;
+        for (int i = 0; i < pts; i++) {
+            const double x = (double)(c->offset[k] + i) * c->ln_step[k];
+            const double sig = c->local_vol[(size_t)k * pts + i];
+            double ev = condvar_at(&cv, x);
+            if (ev < min_cv) ev = min_cv;
+            double L = sig / sqrt(ev);
+            layer[i] = L < lmin ? lmin : (L > lmax ? lmax : L);
+        }
+        if (k == 0) continue;
+        const double dt = (double)(c->days[k] - c->days[k - 1]) / 365.0;
+        const double carry = c->carry[k] * ((double)c->days[k] / 365.0) - c->carry[k - 1] * ((double)c->days[k - 1] / 365.0);
+        for (int p = 0; p < P; p++) {
+            const double lp = layer_at(layer, pts, c->ln_step[k], c->offset[k], spot[p]);
+            const double vp = var[p];
+            const double vc = calib_qe(vp, dt, xo_gaussian(&rng), c->kappa, c->theta, c->xi);
+            const double step = calib_spot(vp, vc, dt, carry, lp, xo_gaussian(&rng), c->kappa, c->theta, c->xi, c->rho);
+            var[p] = vc;
+            spot[p] *= exp(step);
+            ln[p] += step;
+        }
+    }
+    free(spot);
+    free(var);
+    free(ln);
+    free(mean);
+    free(sum);
+    free(count);
+    return 0;
+}

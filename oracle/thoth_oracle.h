@@ -63,6 +63,13 @@ double oracle_heston_price_p12(double spot, double strike, double t, double r, d
 /* batch of Heston calls, args[i] = (S, K, T, r, q, v0, kappa, theta, xi, rho), on `threads` threads */
 int oracle_heston_prices(int64_t n, const double* args, double* out, int threads);
 
+/* LSV leverage calibration, Single::CalibrateLeverage (single.cpp:390-473) restated:
+ * fills c->leverage; defaults as thoth_gpu_calibrate_leverage */
+int oracle_calibrate_leverage(ThothLeverageCalib* c);
+
+/* the reference Rng's raw 64-bit draws: n draws from seed after skipping `skip` */
+int oracle_xoshiro_draws(uint64_t seed, uint64_t skip, int64_t n, uint64_t* out, uint64_t state_out[4]);
+
 #ifdef __cplusplus
 }
 #endif

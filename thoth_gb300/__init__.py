@@ -54,6 +54,8 @@ def lib():
         L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
         L.thoth_gpu_bump_greeks.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBumpGreeks)]
         L.thoth_gpu_bump_greeks_last_error.restype = C.c_char_p
+        L.thoth_gpu_calibrate_leverage.argtypes = [C.POINTER(abi.ThothLeverageCalib)]
+        L.thoth_gpu_xoshiro_jump.argtypes = [C.POINTER(C.c_uint64), C.c_uint64, C.POINTER(C.c_uint64)]
         L.thoth_gpu_price_american.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothAmerican)]
         L.thoth_gpu_american_last_error.restype = C.c_char_p
         L.thoth_gpu_simulate_paths.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(C.c_float),
@@ -138,6 +140,22 @@ def bump_greeks(book, flags=abi.BUMP_ALL):
     out["device_ms"] = g.device_ms
     out["note"] = lib().thoth_gpu_bump_greeks_last_error().decode()
     return out
+
+
+def calibrate_leverage(calib):
+    """LSV leverage calibration (abi.LeverageCalibration) on the device: returns the layers
+    [n_dates][points] (the lev_values of an LSV asset on the same grids) and device ms."""
+    d = calib.desc()
+    _check(lib().thoth_gpu_calibrate_leverage(C.byref(d)))
+    return calib.leverage.copy(), d.device_ms
+
+
+def xoshiro_jump(state, n):
+    """The reference Rng's state after n draws from `state` (4 x uint64), by jump-ahead."""
+    s = (C.c_uint64 * 4)(*[int(x) for x in state])
+    out = (C.c_uint64 * 4)()
+    _check(lib().thoth_gpu_xoshiro_jump(s, int(n), out))
+    return [int(x) for x in out]
 
 
 def price_american(book, product, flags=0, min_itm=0, zero_rates=None):

@@ -137,6 +137,59 @@ class ThothAmerican(C.Structure):
                                           "device_ms", "exercise_ms")]
 
 
+class ThothLeverageCalib(C.Structure):
+    _fields_ = [("n_dates", C.c_int32), ("points", C.c_int32), ("days", C.POINTER(C.c_int32)),
+                ("carry", C.POINTER(C.c_double)), ("spot", C.c_double), ("v0", C.c_double), ("kappa", C.c_double),
+                ("theta", C.c_double), ("xi", C.c_double), ("rho", C.c_double),
+                ("ln_step", C.POINTER(C.c_double)), ("offset", C.POINTER(C.c_int64)),
+                ("local_vol", C.POINTER(C.c_double)), ("particles", C.c_int32), ("bins", C.c_int32),
+                ("min_bin_count", C.c_int32), ("_pad", C.c_int32), ("seed", C.c_uint64),
+                ("min_cond_variance", C.c_double), ("lev_min", C.c_double), ("lev_max", C.c_double),
+                ("leverage", C.POINTER(C.c_double)), ("device_ms", C.c_double)]
+
+
+LSV_CALIB_SEED = 20260708  # the reference's fixed calibration seed (single.cpp:246)
+
+
+class LeverageCalibration:
+    """Inputs of one leverage calibration (numpy buffers kept alive) and its C view.
+
+    days: calendar days from today (days[0] = 0); carry: net carry r - q - repo to each
+    date; ln_step / offset / local_vol: each layer's log-spot grid and the target local
+    vol at its points ([n_dates][points])."""
+
+    def __init__(self, days, carry, spot, heston, ln_step, offset, local_vol, particles=0, bins=0,
+                 min_bin_count=0, seed=LSV_CALIB_SEED):
+        self.days = np.ascontiguousarray(days, dtype=np.int32)
+        n = len(self.days)
+        self.carry = np.ascontiguousarray(np.broadcast_to(carry, (n,)), dtype=np.float64)
+        self.ln_step = np.ascontiguousarray(ln_step, dtype=np.float64)
+        self.offset = np.ascontiguousarray(offset, dtype=np.int64)
+        self.local_vol = np.ascontiguousarray(local_vol, dtype=np.float64)
+        assert self.local_vol.ndim == 2 and self.local_vol.shape[0] == n
+        self.spot = float(spot)
+        self.heston = dict(heston)
+        self.particles, self.bins, self.min_bin_count, self.seed = particles, bins, min_bin_count, seed
+        self.leverage = np.zeros_like(self.local_vol)
+
+    def desc(self):
+        d = ThothLeverageCalib()
+        d.n_dates = len(self.days)
+        d.points = self.local_vol.shape[1]
+        d.days = _ptr(self.days, C.c_int32)
+        d.carry = _ptr(self.carry, C.c_double)
+        d.spot = self.spot
+        for k in ("v0", "kappa", "theta", "xi", "rho"):
+            setattr(d, k, float(self.heston[k]))
+        d.ln_step = _ptr(self.ln_step, C.c_double)
+        d.offset = _ptr(self.offset, C.c_int64)
+        d.local_vol = _ptr(self.local_vol, C.c_double)
+        d.particles, d.bins, d.min_bin_count = int(self.particles), int(self.bins), int(self.min_bin_count)
+        d.seed = int(self.seed)
+        d.leverage = _ptr(self.leverage, C.c_double)
+        return d
+
+
 def _ptr(arr, ctype):
     return arr.ctypes.data_as(C.POINTER(ctype))
 

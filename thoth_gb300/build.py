@@ -19,7 +19,7 @@ CSRC = HERE / "csrc"
 LIB = BUILD / "libthoth_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["kernels.cu", "thoth_gpu.cu", "surrogate.cu", "surrogate_host.cu", "greeks.cu", "american.cu",
-           "american_host.cu"]
+           "american_host.cu", "calib.cu"]
 # the path kernels flush FP32 denormals: no value on the path is subnormal, and
 # without it every MUFU approximation (rcp, rsqrt, lg2, ex2) carries a
 # denormal fix-up sequence (11 % of the Heston step's time)
@@ -27,7 +27,9 @@ FLAGS = {"kernels.cu": ["-ftz=true"],
          # the exercise tables and the regression solve are compared bit for bit with the
          # oracle: no contraction of a * b + c into a fused multiply-add on the host
          "american_host.cu": ["-Xcompiler", "-ffp-contract=off"],
-         "thoth_gpu.cu": ["-Xcompiler", "-ffp-contract=off"]}
+         "thoth_gpu.cu": ["-Xcompiler", "-ffp-contract=off"],
+         # the calibration ensemble rounds every expression as the reference does
+         "calib.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc():

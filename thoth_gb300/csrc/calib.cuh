@@ -1,0 +1,49 @@
+// calib.cuh — LSV leverage calibration (calib.cu): kernel arguments, launcher, and the
+// host-side jump-ahead of the reference Rng (xoshiro256++), shared with thoth_gpu.cu.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "exact.cuh"
+
+constexpr int CALIB_THREADS = 128;
+constexpr int CALIB_MAX_BINS = 128;
+constexpr int CALIB_JUMP_BITS = 40; // x^(2^i) mod chi for i < 40: particle offsets below 2^40
+
+struct CalibArgs {
+    int P, n, points, bins, min_count;
+    double s0, ln_s0, v0, kappa, theta, xi, rho, min_cv, lmin, lmax;
+    const double* dt;        // [n] year fraction of the step into date k (dt[0] unused)
+    const double* carry;     // [n] cumulative carry of date k minus date k-1
+    const double* qe_e;      // [n] exp(-kappa dt[k]), rounded on the host like the reference
+    const double* ln_step;   // [n]
+    const int64_t* offset;   // [n]
+    const double* local_vol; // [n][points]
+    double* lev;             // [n][points] out
+    double *spot, *var, *lns; // [P] the ensemble
+    uint64_t* rng;           // [4][P] each particle's Rng state
+    const uint64_t* jpow;    // [CALIB_JUMP_BITS][4] x^(2^i) mod chi
+    const uint64_t* jdate;   // [4] x^(2P - 2) mod chi: from a particle's draws of one date to the next
+    uint64_t seed_state[4];  // the Rng state after seeding
+    // per-date totals the CTAs add into with integer atomics (order-independent, exact):
+    long long *kmin, *kmax;  // [n] order-preserving integer keys of the extremes of ln S
+                             // (initialised to 0x7f.. / 0x80.. bytes: neutral for min / max)
+    Fx128* vsum;             // [n] sum of v (zero at launch)
+    unsigned* bcnt;          // [n][bins] particles per bin (zero at launch)
+    Fx128* bsum;             // [n][bins] sum of v per bin (zero at launch)
+    double* bc;              // [4] published: min ln S, bin width, ensemble mean of v, degenerate
+    unsigned *bar, *done;    // arrivals and releases, all rounds (zero at launch)
+    int* status;             // 0 ok, 2 a wait timed out, 3 a sum out of range
+};
+
+int calib_max_grid(int sms, size_t smem);
+cudaError_t launch_calib(const CalibArgs& A, int grid, size_t smem, cudaStream_t st);
+
+// host: the reference Rng's transition, seeding, and jump polynomials
+void xo_seed_state(uint64_t seed, uint64_t s[4]);
+void xo_advance(uint64_t s[4]); // one transition of the state (no output)
+// x^d mod chi, with chi the transition's characteristic polynomial (found once by
+// Berlekamp-Massey); false if chi could not be found (never for xoshiro256)
+bool xo_jump_poly(uint64_t d, uint64_t out[4]);
+void xo_apply_jump(const uint64_t poly[4], uint64_t s[4]);

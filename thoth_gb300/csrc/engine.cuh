@@ -306,8 +306,9 @@ __device__ __forceinline__ float qe_step(float v, float z, float e, float th1e, 
     const float m = fmaf(v, e, th1e);
     const float s2 = fmaf(v, A, B);
     const float m2 = m * m;
-    // quadratic branch
-    const float c = __fdividef(2.0f * m2, s2);
+    // quadratic branch; c is capped at 1e18 (psi >= 2e-18, where the step's random part is
+    // below single precision) so that c (c - 1) stays finite for a vanishing vol of vol
+    const float c = fminf(__fdividef(2.0f * m2, s2), 1e18f);
     const float b2 = c - 1.0f + fast_sqrt(fmaxf(c * (c - 1.0f), 0.0f));
     const float a = __fdividef(m, 1.0f + b2);
     const float bz = fast_sqrt(fmaxf(b2, 0.0f)) + z;

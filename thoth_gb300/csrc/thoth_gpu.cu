@@ -8,6 +8,7 @@
 #include "thoth_gpu.h"
 #include "engine.cuh"
 #include "american.cuh"
+#include "calib.cuh"
 
 #include <cuda_runtime.h>
 
@@ -87,6 +88,8 @@ struct Device {
     size_t paths_size = 0;
     unsigned char* lsm = nullptr;    // Longstaff-Schwartz scratch
     size_t lsm_size = 0;
+    unsigned char* calib = nullptr;  // leverage calibration scratch
+    size_t calib_size = 0;
 };
 Device g_dev;
 
@@ -1858,6 +1861,145 @@ struct ThothBookHandle {
     unsigned char* dev = nullptr;
 };
 
+// LSV leverage calibration (calib.cu): validate, derive the per-date step tables on the
+// host (the reference's ACT/365 fractions and exp(-kappa dt) rounded by the host libm),
+// upload, one cooperative launch, layers back
+int calibrate_locked(ThothLeverageCalib* c)
+{
+    if (!c) return fail(THOTH_GPU_E_INVALID, "null argument");
+    const int n = c->n_dates, pts = c->points;
+    const int P = c->particles > 0 ? c->particles : 16384;
+    const int bins = c->bins > 0 ? c->bins : 30;
+    const int min_count = c->min_bin_count > 0 ? c->min_bin_count : 20;
+    if (n < 1 || pts < 2 || !c->days || !c->carry || !c->ln_step || !c->offset || !c->local_vol || !c->leverage)
+        return fail(THOTH_GPU_E_INVALID, "calibration needs dates, carries, layer grids, local vols and an output");
+    if (c->days[0] != 0) return fail(THOTH_GPU_E_INVALID, "days[0] must be 0 (today)");
+    for (int k = 1; k < n; k++)
+        if (c->days[k] <= c->days[k - 1]) return fail(THOTH_GPU_E_INVALID, "days must increase");
+    if (bins > CALIB_MAX_BINS) return fail(THOTH_GPU_E_INVALID, "at most 128 bins");
+    if (P > (1 << 30)) return fail(THOTH_GPU_E_TOO_LARGE, "at most 2^30 particles");
+    if (!(c->spot > 0) || !(c->v0 >= 0) || !(c->kappa > 0) || !(c->xi >= 0) || !(c->theta >= 0) ||
+        !(c->rho >= -1 && c->rho <= 1))
+        return fail(THOTH_GPU_E_INVALID, "bad Heston base or spot");
+    for (int k = 0; k < n; k++)
+        if (!(c->ln_step[k] > 0)) return fail(THOTH_GPU_E_INVALID, "layer grid spacing must be positive");
+    int rc = ensure_device();
+    if (rc) return rc;
+    std::vector<double> dt(n, 0.0), carry(n, 0.0), qe(n, 1.0);
+    for (int k = 1; k < n; k++) {
+        dt[k] = (double)(c->days[k] - c->days[k - 1]) / 365.0;
+        carry[k] = c->carry[k] * ((double)c->days[k] / 365.0) - c->carry[k - 1] * ((double)c->days[k - 1] / 365.0);
+        qe[k] = std::exp(-c->kappa * dt[k]);
+    }
+    uint64_t jpow[CALIB_JUMP_BITS][4], jdate[4];
+    for (int i = 0; i < CALIB_JUMP_BITS; i++)
+        if (!xo_jump_poly(1ull << i, jpow[i])) return fail(THOTH_GPU_E_INVALID, "Rng jump polynomial unavailable");
+    if (!xo_jump_poly(2ull * (uint64_t)P - 2, jdate)) return fail(THOTH_GPU_E_INVALID, "Rng jump polynomial unavailable");
+    const size_t smem = sizeof(double) * (size_t)pts;
+    const int cap = calib_max_grid(g_dev.sms, smem);
+    if (cap < 1) return fail(THOTH_GPU_E_TOO_LARGE, "layer too large for shared memory");
+    const int grid = std::max(1, std::min(cap, (P + CALIB_THREADS - 1) / CALIB_THREADS));
+    // device layout: inputs | layers | ensemble | generators | partial sums | control
+    const size_t nd = (size_t)n, np = (size_t)P, npt = (size_t)pts;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = align256(o + bytes);
+        return at;
+    };
+    const size_t o_dt = take(8 * nd), o_carry = take(8 * nd), o_qe = take(8 * nd), o_ls = take(8 * nd);
+    const size_t o_off = take(8 * nd), o_lv = take(8 * nd * npt), o_jp = take(8 * 4 * CALIB_JUMP_BITS),
+                 o_jd = take(8 * 4);
+    const size_t up_bytes = o; // everything above is uploaded in one copy
+    const size_t o_lev = take(8 * nd * npt), o_spot = take(8 * np), o_var = take(8 * np), o_lns = take(8 * np);
+    const size_t o_rng = take(8 * 4 * np), o_bc = take(8 * 4);
+    // per-date totals: zeroed (sums, counts, control) or set to the neutral keys (extremes)
+    const size_t o_kmin = take(8 * nd), o_kmax = take(8 * nd);
+    const size_t o_zero = o, o_vsum = take(sizeof(Fx128) * nd), o_bcnt = take(4 * nd * (size_t)bins);
+    const size_t o_bsum = take(sizeof(Fx128) * nd * (size_t)bins), o_ctl = take(16);
+    if (o > g_dev.calib_size) {
+        if (g_dev.calib) cudaFree(g_dev.calib);
+        g_dev.calib = nullptr;
+        g_dev.calib_size = 0;
+        CUDA_TRY(cudaMalloc(&g_dev.calib, o));
+        g_dev.calib_size = o;
+    }
+    rc = ensure_pinned(std::max(up_bytes, 8 * nd * npt + 16));
+    if (rc) return rc;
+    unsigned char* h = g_dev.pinned;
+    std::memset(h, 0, up_bytes);
+    std::memcpy(h + o_dt, dt.data(), 8 * nd);
+    std::memcpy(h + o_carry, carry.data(), 8 * nd);
+    std::memcpy(h + o_qe, qe.data(), 8 * nd);
+    std::memcpy(h + o_ls, c->ln_step, 8 * nd);
+    std::memcpy(h + o_off, c->offset, 8 * nd);
+    std::memcpy(h + o_lv, c->local_vol, 8 * nd * npt);
+    std::memcpy(h + o_jp, jpow, sizeof jpow);
+    std::memcpy(h + o_jd, jdate, sizeof jdate);
+    unsigned char* base = g_dev.calib;
+    cudaStream_t st = g_dev.stream;
+    CUDA_TRY(cudaMemcpyAsync(base, h, up_bytes, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(base + o_kmin, 0x7f, 8 * nd, st));
+    CUDA_TRY(cudaMemsetAsync(base + o_kmax, 0x80, 8 * nd, st));
+    CUDA_TRY(cudaMemsetAsync(base + o_zero, 0, o - o_zero, st));
+    CalibArgs A;
+    A.P = P;
+    A.n = n;
+    A.points = pts;
+    A.bins = bins;
+    A.min_count = min_count;
+    A.s0 = c->spot;
+    A.ln_s0 = std::log(c->spot);
+    A.v0 = c->v0;
+    A.kappa = c->kappa;
+    A.theta = c->theta;
+    A.xi = c->xi;
+    A.rho = c->rho;
+    A.min_cv = c->min_cond_variance > 0 ? c->min_cond_variance : 1e-6;
+    A.lmin = c->lev_min > 0 ? c->lev_min : 0.05;
+    A.lmax = c->lev_max > 0 ? c->lev_max : 10.0;
+    A.dt = reinterpret_cast<const double*>(base + o_dt);
+    A.carry = reinterpret_cast<const double*>(base + o_carry);
+    A.qe_e = reinterpret_cast<const double*>(base + o_qe);
+    A.ln_step = reinterpret_cast<const double*>(base + o_ls);
+    A.offset = reinterpret_cast<const int64_t*>(base + o_off);
+    A.local_vol = reinterpret_cast<const double*>(base + o_lv);
+    A.lev = reinterpret_cast<double*>(base + o_lev);
+    A.spot = reinterpret_cast<double*>(base + o_spot);
+    A.var = reinterpret_cast<double*>(base + o_var);
+    A.lns = reinterpret_cast<double*>(base + o_lns);
+    A.rng = reinterpret_cast<uint64_t*>(base + o_rng);
+    A.jpow = reinterpret_cast<const uint64_t*>(base + o_jp);
+    A.jdate = reinterpret_cast<const uint64_t*>(base + o_jd);
+    xo_seed_state(c->seed, A.seed_state);
+    A.kmin = reinterpret_cast<long long*>(base + o_kmin);
+    A.kmax = reinterpret_cast<long long*>(base + o_kmax);
+    A.vsum = reinterpret_cast<Fx128*>(base + o_vsum);
+    A.bcnt = reinterpret_cast<unsigned*>(base + o_bcnt);
+    A.bsum = reinterpret_cast<Fx128*>(base + o_bsum);
+    A.bc = reinterpret_cast<double*>(base + o_bc);
+    A.bar = reinterpret_cast<unsigned*>(base + o_ctl);
+    A.done = reinterpret_cast<unsigned*>(base + o_ctl + 4);
+    A.status = reinterpret_cast<int*>(base + o_ctl + 8);
+    A.min_count = min_count;
+    CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+    CUDA_TRY(launch_calib(A, grid, smem, st));
+    CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
+    CUDA_TRY(cudaMemcpyAsync(h, base + o_lev, 8 * nd * npt, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(h + 8 * nd * npt, base + o_ctl + 8, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    int status;
+    std::memcpy(&status, h + 8 * nd * npt, sizeof(int));
+    if (status == 2) return fail(THOTH_GPU_E_CUDA, "calibration: a wait timed out");
+    if (status == 3) return fail(THOTH_GPU_E_INVALID, "calibration: a variance is out of range (>= 2^36 or negative)");
+    if (status != 0) return fail(THOTH_GPU_E_CUDA, "calibration: kernel status " + std::to_string(status));
+    std::memcpy(c->leverage, h, 8 * nd * npt);
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+    c->device_ms = ms;
+    return THOTH_GPU_OK;
+}
+
 // the exercise pass of thoth_gpu_price_american (american_host.cu)
 int thoth_lsm_pass(const ThothBookDesc* book, LsmPass& io)
 {
@@ -2348,6 +2490,32 @@ int thoth_gpu_simulate_paths(const ThothBookDesc* book, int32_t asset, float* sp
         return simulate_paths_locked(book, asset, spots, device_ms);
     } catch (const std::bad_alloc&) {
         return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_calibrate_leverage(ThothLeverageCalib* c)
+{
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        return calibrate_locked(c);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_xoshiro_jump(const uint64_t s[4], uint64_t n, uint64_t out[4])
+{
+    try {
+        if (!s || !out) return fail(THOTH_GPU_E_INVALID, "null argument");
+        uint64_t poly[4], t[4] = {s[0], s[1], s[2], s[3]};
+        if (!xo_jump_poly(n, poly)) return fail(THOTH_GPU_E_INVALID, "jump too long (at most 2^64 - 1 draws)");
+        xo_apply_jump(poly, t);
+        for (int i = 0; i < 4; i++) out[i] = t[i];
+        return THOTH_GPU_OK;
     } catch (const std::exception& e) {
         return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
     }

@@ -7,6 +7,8 @@ with the shapes, sizes and parameter ranges of the workloads it is measured on:
   heston_grid         Heston vanilla grid, 9 strikes x 7 maturities x call/put
   lsv_book            5 LSV names, 20 down-and-out calls, 10 variance swaps, 20 baskets
   ragged_books        256 books of uneven path and step counts (GBM / Heston / LSV mix)
+  lsv_calibration     leverage calibration inputs: daily dates, layer grids sized as the
+                      reference sizes them, a skewed target local-vol surface
   american_put        1 asset American put, Heston daily exercise or the reference tests'
                       GBM case (30-day exercise grid)
 """
@@ -134,6 +136,46 @@ def lsv_book(paths=1 << 20, seed=20260101, horizon_days=365, n_lev_strikes=50, n
         m = mats[j % 3]
         b.add_basket(comps, w, rng.uniform(90, 110), m, CALL, zero_rate=rates[0], fx=1.0)
     return b
+
+
+LSV_GRID_POINTS = 201          # single.cpp:179
+LSV_GRID_SIGMA_FACTOR = 8.0    # single.cpp:177
+
+
+def layer_grids(days, spot, atm_vol):
+    """Each date's leverage grid as Single::CalibrateLeverage sizes it (single.cpp:428-443):
+    +-8 ATM standard deviations around ln S0 in 201 points (today uses T = 1 day)."""
+    ln_step, offset = [], []
+    for d in days:
+        T = d / 365.0
+        if T <= 0:
+            T = 1.0 / 365.0
+        hw = LSV_GRID_SIGMA_FACTOR * atm_vol * math.sqrt(T)
+        st = 2.0 * hw / (LSV_GRID_POINTS - 1)
+        if st <= 0:
+            st = 1e-4
+        ln_step.append(st)
+        offset.append(int(math.floor((math.log(spot) - hw) / st)))
+    return np.asarray(ln_step), np.asarray(offset, dtype=np.int64)
+
+
+def skew_local_vol(S, t, atm=0.22, skew=-0.35, term=0.15):
+    """A smooth skewed local-vol surface: atm (S/100)^skew, rising slowly with t, floored."""
+    return np.maximum(atm * (np.asarray(S) / 100.0) ** skew * (1.0 + term * np.sqrt(t)), 0.05)
+
+
+def lsv_calibration(horizon_days=365, spot=100.0, particles=0, local_vol=skew_local_vol, carry=0.02,
+                    heston=None, seed=None):
+    """Leverage calibration inputs for one LSV name: daily dates to the horizon, the
+    reference's layer grids, and the target local vol on them."""
+    from .abi import LeverageCalibration, LSV_CALIB_SEED
+    days = np.arange(0, horizon_days + 1)
+    h = heston or dict(v0=0.0324, kappa=2.0, theta=0.0676, xi=0.5, rho=-0.6)
+    ln_step, offset = layer_grids(days, spot, 0.22)
+    x = (offset[:, None] + np.arange(LSV_GRID_POINTS)[None, :]) * ln_step[:, None]
+    sig = local_vol(np.exp(x), (days / 365.0)[:, None])
+    return LeverageCalibration(days, carry, spot, h, ln_step, offset, sig, particles=particles,
+                               seed=LSV_CALIB_SEED if seed is None else seed)
 
 
 def american_put(paths=1 << 20, heston=True, days=None):
