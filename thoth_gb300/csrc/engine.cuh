@@ -253,6 +253,50 @@ __device__ __forceinline__ void quantile_n(const uint32_t (&x)[N], float (&z)[N]
     for (int i = 0; i < N; ++i) z[i] *= s[i];
 }
 
+// ---- two lanes in one instruction (sm_100 and later) --------------------------------
+// A thread's two paths run the same arithmetic, so the FP32 fused multiply-adds, multiplies
+// and adds of the per-path polynomials are issued as packed pairs. Each lane rounds exactly as
+// the scalar fmaf / multiply / add, so the results are bit-identical to the scalar forms.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ float2 quantile_central2(float2 lg)
+{
+    const float2 v = __ffma2_rn(lg, f2s(-0.6931471805599453f), f2s(-3.125f));
+    float2 p = f2s(-7.202387403e-09f);
+    p = __ffma2_rn(p, v, f2s(-1.226470401e-08f));
+    p = __ffma2_rn(p, v, f2s(6.170809376e-07f));
+    p = __ffma2_rn(p, v, f2s(-2.155695626e-06f));
+    p = __ffma2_rn(p, v, f2s(-1.975007828e-05f));
+    p = __ffma2_rn(p, v, f2s(2.648245696e-04f));
+    p = __ffma2_rn(p, v, f2s(-1.047204452e-03f));
+    p = __ffma2_rn(p, v, f2s(-8.533770903e-03f));
+    p = __ffma2_rn(p, v, f2s(3.396347351e-01f));
+    p = __ffma2_rn(p, v, f2s(2.338620874e+00f));
+    return p;
+}
+
+// quantile_n for a thread's two paths: quantile_prep and the central polynomial paired
+template <>
+__device__ __forceinline__ void quantile_n<2>(const uint32_t (&x)[2], float (&z)[2])
+{
+    const uint32_t q0 = min(x[0], 0u - x[0]), q1 = min(x[1], 0u - x[1]);
+    const float2 sv = __fmul2_rn(f2(__int2float_rn((int)(x[0] ^ 0x80000000u)), __int2float_rn((int)(x[1] ^ 0x80000000u))),
+                                 f2s(4.656612873077393e-10f));
+    const float2 qf = f2(__uint2float_rn(q0), __uint2float_rn(q1));
+    const float2 one_m_q = __ffma2_rn(qf, f2s(-2.3283064365386963e-10f), f2s(1.0f));
+    const float2 arg = __fmul2_rn(__fmul2_rn(qf, f2s(9.313225746154785e-10f)), one_m_q);
+    const float lg0 = fminf(__log2f(arg.x), 0.0f), lg1 = fminf(__log2f(arg.y), 0.0f);
+    float2 zz = quantile_central2(f2(lg0, lg1));
+    if (!(lg0 > QUANTILE_TAIL_LG) || !(lg1 > QUANTILE_TAIL_LG)) {
+        if (!(lg0 > QUANTILE_TAIL_LG)) zz.x = quantile_tail(lg0);
+        if (!(lg1 > QUANTILE_TAIL_LG)) zz.y = quantile_tail(lg1);
+    }
+    zz = __fmul2_rn(zz, sv);
+    z[0] = zz.x;
+    z[1] = zz.y;
+}
+
 // counter-based uint32 for dimensions beyond the Sobol budget and use_sobol = 0
 // (splitmix64 finaliser of a Weyl combination of seed, point index and dimension)
 __device__ __forceinline__ uint32_t hash_u32(uint64_t seed, uint64_t n, uint32_t dim)
@@ -319,6 +363,57 @@ __device__ __forceinline__ float qe_step(float v, float z, float e, float th1e, 
     const float uc = phi_neg(z);
     const float ve = (uc >= one_m_p) ? 0.0f : __fdividef(num, 2.0f * m) * __logf(__fdividef(one_m_p, uc));
     return (s2 <= 1.5f * m2) ? vq : ve;
+}
+
+// phi_neg for a thread's two paths
+__device__ __forceinline__ float2 phi_neg2(float2 z)
+{
+    const float2 y = __fmul2_rn(z, f2s(0.7071067811865476f));
+    const float2 a = f2(fabsf(y.x), fabsf(y.y));
+    const float2 d = __ffma2_rn(f2s(0.5f), a, f2s(1.0f));
+    const float2 t = f2(__fdividef(1.0f, d.x), __fdividef(1.0f, d.y));
+    float2 p = f2s(0.17087277f);
+    p = __ffma2_rn(p, t, f2s(-0.82215223f));
+    p = __ffma2_rn(p, t, f2s(1.48851587f));
+    p = __ffma2_rn(p, t, f2s(-1.13520398f));
+    p = __ffma2_rn(p, t, f2s(0.27886807f));
+    p = __ffma2_rn(p, t, f2s(-0.18628806f));
+    p = __ffma2_rn(p, t, f2s(0.09678418f));
+    p = __ffma2_rn(p, t, f2s(0.37409196f));
+    p = __ffma2_rn(p, t, f2s(1.00002368f));
+    p = __ffma2_rn(p, t, f2s(-1.26551223f));
+    const float2 g = __ffma2_rn(f2(-a.x, -a.y), a, p);
+    const float2 e = __fmul2_rn(t, f2(__expf(g.x), __expf(g.y)));
+    return __fmul2_rn(f2s(0.5f), f2(y.x >= 0.f ? e.x : 2.0f - e.x, y.y >= 0.f ? e.y : 2.0f - e.y));
+}
+
+// qe_step for a thread's two paths (same expressions, paired)
+__device__ __forceinline__ float2 qe_step2(float2 v, float2 z, float e, float th1e, float A, float B)
+{
+    const float2 m = __ffma2_rn(v, f2s(e), f2s(th1e));
+    const float2 s2 = __ffma2_rn(v, f2s(A), f2s(B));
+    const float2 m2 = __fmul2_rn(m, m);
+    const float2 tm2 = __fmul2_rn(f2s(2.0f), m2);
+    const float2 c = f2(fminf(__fdividef(tm2.x, s2.x), 1e18f), fminf(__fdividef(tm2.y, s2.y), 1e18f));
+    const float2 cm1 = __fadd2_rn(c, f2s(-1.0f));
+    const float2 cc = __fmul2_rn(c, cm1);
+    // fast_sqrt(x) + y as the scalar form contracts it: x rsqrt(x) + y in one rounding
+    const float2 ccp = f2(fmaxf(cc.x, 0.0f), fmaxf(cc.y, 0.0f));
+    const float2 b2 = __ffma2_rn(ccp, f2(rsqrtf(fmaxf(ccp.x, 1e-30f)), rsqrtf(fmaxf(ccp.y, 1e-30f))), cm1);
+    const float2 d = __fadd2_rn(f2s(1.0f), b2);
+    const float2 a = f2(__fdividef(m.x, d.x), __fdividef(m.y, d.y));
+    const float2 b2p = f2(fmaxf(b2.x, 0.0f), fmaxf(b2.y, 0.0f));
+    const float2 bz = __ffma2_rn(b2p, f2(rsqrtf(fmaxf(b2p.x, 1e-30f)), rsqrtf(fmaxf(b2p.y, 1e-30f))), z);
+    const float2 vq = __fmul2_rn(__fmul2_rn(a, bz), bz);
+    const float2 num = __fadd2_rn(s2, m2);
+    const float2 one_m_p = f2(__fdividef(tm2.x, num.x), __fdividef(tm2.y, num.y));
+    const float2 uc = phi_neg2(z);
+    const float2 tm = __fmul2_rn(f2s(2.0f), m);
+    const float2 r = __fmul2_rn(f2(__fdividef(num.x, tm.x), __fdividef(num.y, tm.y)),
+                                f2(__logf(__fdividef(one_m_p.x, uc.x)), __logf(__fdividef(one_m_p.y, uc.y))));
+    const float2 ve = f2(uc.x >= one_m_p.x ? 0.0f : r.x, uc.y >= one_m_p.y ? 0.0f : r.y);
+    const float2 lim = __fmul2_rn(f2s(1.5f), m2);
+    return f2(s2.x <= lim.x ? vq.x : ve.x, s2.y <= lim.y ? vq.y : ve.y);
 }
 
 } // namespace thoth

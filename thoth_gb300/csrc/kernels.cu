@@ -154,6 +154,14 @@ __device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, con
     quantile_n<PP>(x, z);
 }
 
+// lw W_prev + (rw W_top + sd z) for a thread's two paths, paired (same roundings as the
+// scalar fmaf form)
+__device__ __forceinline__ float2 bridge_comb2(float lw, float rw, float sd, float wp0, float wp1, float tp0, float tp1,
+                                               float z0, float z1)
+{
+    return __ffma2_rn(f2s(lw), f2(wp0, wp1), __ffma2_rn(f2s(rw), f2(tp0, tp1), __fmul2_rn(f2s(sd), f2(z0, z1))));
+}
+
 // ---------------------------------------------------------------------------
 // One time step of the bridge for every active factor slot of the thread's PP
 // paths: fills nz[][] with the normalised increments
@@ -207,8 +215,16 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
                 const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
                 float z[PP];
                 gauss(P, L, n, rec.dim + fid, z);
+                if constexpr (PP == 2) {
+                    const float2 w = bridge_comb2(rec.lw, rec.rw, rec.sd, Wprev[0][f], Wprev[PP - 1][f], top[0][f],
+                                                  top[PP - 1][f], z[0], z[PP - 1]);
+                    Wi[0][f] = w.x;
+                    Wi[PP - 1][f] = w.y;
+                } else {
 #pragma unroll
-                for (int p = 0; p < PP; ++p) Wi[p][f] = fmaf(rec.lw, Wprev[p][f], fmaf(rec.rw, top[p][f], rec.sd * z[p]));
+                    for (int p = 0; p < PP; ++p)
+                        Wi[p][f] = fmaf(rec.lw, Wprev[p][f], fmaf(rec.rw, top[p][f], rec.sd * z[p]));
+                }
             }
         }
     } else {
@@ -233,9 +249,19 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
                     const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
                     float z[PP];
                     gauss(P, L, n, dim + fid, z);
+                    float Wns[PP];
+                    if constexpr (PP == 2) {
+                        const float2 w = bridge_comb2(lw, rw, sd, Wprev[0][f], Wprev[PP - 1][f], top[0][f],
+                                                      top[PP - 1][f], z[0], z[PP - 1]);
+                        Wns[0] = w.x;
+                        Wns[PP - 1] = w.y;
+                    } else {
+#pragma unroll
+                        for (int p = 0; p < PP; ++p) Wns[p] = fmaf(lw, Wprev[p][f], fmaf(rw, top[p][f], sd * z[p]));
+                    }
 #pragma unroll
                     for (int p = 0; p < PP; ++p) {
-                        const float Wn = fmaf(lw, Wprev[p][f], fmaf(rw, top[p][f], sd * z[p]));
+                        const float Wn = Wns[p];
                         if (push) {
                             S.stk[base + ci * T + p * TH] = top[p][f];
                             top[p][f] = Wn;
@@ -248,13 +274,25 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
             if (push) ++sp;
         }
     }
-#pragma unroll
-    for (int p = 0; p < PP; ++p)
+    if constexpr (PP == 2) {
 #pragma unroll
         for (int f = 0; f < FS; ++f) {
-            nz[p][f] = (Wi[p][f] - Wprev[p][f]) * rec.isd;
-            Wprev[p][f] = Wi[p][f];
+            const float2 d = __fmul2_rn(__fadd2_rn(f2(Wi[0][f], Wi[PP - 1][f]), f2(-Wprev[0][f], -Wprev[PP - 1][f])),
+                                        f2s(rec.isd));
+            nz[0][f] = d.x;
+            nz[PP - 1][f] = d.y;
+            Wprev[0][f] = Wi[0][f];
+            Wprev[PP - 1][f] = Wi[PP - 1][f];
         }
+    } else {
+#pragma unroll
+        for (int p = 0; p < PP; ++p)
+#pragma unroll
+            for (int f = 0; f < FS; ++f) {
+                nz[p][f] = (Wi[p][f] - Wprev[p][f]) * rec.isd;
+                Wprev[p][f] = Wi[p][f];
+            }
+    }
 }
 
 // leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47). The layer of
@@ -538,10 +576,38 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                         c2 = __ldg(cs + 2);
                     }
                     const int model = (MODEL == M_MIXED || SEQ) ? P.model[aid] : MODEL;
+                    // two paths a thread: the variance step and the log-spot sum paired
+                    float vcs[PP], stp[PP];
+                    if (PP == 2 && model != M_GBM) {
+                        const float2 r = qe_step2(f2(v[0][a], v[PP - 1][a]), f2(nz[0][NA + a], nz[PP - 1][NA + a]), c0.x,
+                                                  c0.y, c0.z, c0.w);
+                        vcs[0] = r.x;
+                        vcs[PP - 1] = r.y;
+                    }
+                    // Heston kernels, two paths a thread: the log-spot step paired as well
+                    constexpr bool PAIR_SPOT = PP == 2 && MODEL == M_HESTON;
+                    if constexpr (PAIR_SPOT) {
+                        if (!P.degenerate[aid]) {
+                            const float2 vp2 = f2(v[0][a], v[PP - 1][a]), vc2 = f2(vcs[0], vcs[PP - 1]);
+                            const float2 s2 = __fadd2_rn(vp2, vc2);
+                            const float2 F = __ffma2_rn(f2s(c2.y), __fadd2_rn(vc2, f2(-vp2.x, -vp2.y)),
+                                                        __ffma2_rn(f2s(c1.z), s2, f2s(c1.y)));
+                            const float2 q = __fmul2_rn(f2s(c2.x), s2);
+                            const float2 qr = __fmul2_rn(q, f2(rsqrtf(fmaxf(q.x, 1e-30f)), rsqrtf(fmaxf(q.y, 1e-30f))));
+                            const float2 B = __ffma2_rn(qr, f2(nz[0][a], nz[PP - 1][a]), F);
+                            const float2 st = __ffma2_rn(f2s(-c1.w), s2, __fadd2_rn(f2s(c1.x), B));
+                            stp[0] = st.x;
+                            stp[PP - 1] = st.y;
+                            v[0][a] = vc2.x;
+                            v[PP - 1][a] = vc2.y;
+                        }
+                    }
 #pragma unroll
                     for (int p = 0; p < PP; ++p) {
                         float step;
-                        if (model == M_GBM) {
+                        if (PAIR_SPOT && !P.degenerate[aid]) {
+                            step = stp[p];
+                        } else if (model == M_GBM) {
                             float e = nz[p][a];
                             if (MODEL == M_MIXED && P.corr) {
                                 e = 0.f;
@@ -553,7 +619,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                             Wb[p][a] = fmaf(c0.z, e, Wb[p][a]);
                         } else {
                             const float vp = v[p][a];
-                            const float vc = qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
+                            const float vc = PP == 2 ? vcs[p] : qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
                             float Lv = 1.f, dL = 0.f;
                             if (model == M_LSV) leverage(P, aid, i, x[p][a], Lv, dL);
                             const float s = vp + vc;
@@ -573,11 +639,30 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                             }
                             v[p][a] = vc;
                         }
-                        // Kahan-compensated log-spot
-                        const float yy = step - comp[p][a];
-                        const float tt = x[p][a] + yy;
-                        comp[p][a] = (tt - x[p][a]) - yy;
-                        x[p][a] = tt;
+                        stp[p] = step;
+                    }
+                    // Kahan-compensated log-spot
+                    if (PP == 2) {
+                        const float2 yy = __fadd2_rn(f2(stp[0], stp[PP - 1]), f2(-comp[0][a], -comp[PP - 1][a]));
+                        const float2 xx = f2(x[0][a], x[PP - 1][a]);
+                        const float2 tt = __fadd2_rn(xx, yy);
+                        const float2 cp = __fadd2_rn(__fadd2_rn(tt, f2(-xx.x, -xx.y)), f2(-yy.x, -yy.y));
+                        comp[0][a] = cp.x;
+                        comp[PP - 1][a] = cp.y;
+                        x[0][a] = tt.x;
+                        x[PP - 1][a] = tt.y;
+                    } else {
+#pragma unroll
+                        for (int p = 0; p < PP; ++p) {
+                            const float yy = stp[p] - comp[p][a];
+                            const float tt = x[p][a] + yy;
+                            comp[p][a] = (tt - x[p][a]) - yy;
+                            x[p][a] = tt;
+                        }
+                    }
+#pragma unroll
+                    for (int p = 0; p < PP; ++p) {
+                        const float step = stp[p];
                         if (cur.ev) apply_events(i, aid, t + p * TH, x[p][a], step, Wb[p][a], y[p][a]);
                         // stored paths: date-major, consecutive paths on consecutive threads
                         if (P.path_out && aid == P.path_asset && valid[p])
