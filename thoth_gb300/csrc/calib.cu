@@ -81,6 +81,31 @@ __host__ __device__ void xo_jump(const uint64_t* poly, uint64_t* s)
     s[3] = r3;
 }
 
+// the fixed date-to-date jump by its nibble table in shared memory: the XOR of the table
+// rows the state's 64 nibbles select (the matrix-vector product over GF(2))
+__device__ __forceinline__ void xo_jump_tab(const uint64_t* tab, uint64_t* s)
+{
+    uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+#pragma unroll
+    for (int w = 0; w < 4; w++) {
+        uint64_t x = s[w];
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const ulonglong2* t = reinterpret_cast<const ulonglong2*>(tab + ((w * 16 + k) * 16 + (int)(x & 15u)) * 4);
+            const ulonglong2 a = t[0], b = t[1];
+            r0 ^= a.x;
+            r1 ^= a.y;
+            r2 ^= b.x;
+            r3 ^= b.y;
+            x >>= 4;
+        }
+    }
+    s[0] = r0;
+    s[1] = r1;
+    s[2] = r2;
+    s[3] = r3;
+}
+
 // Acklam's inverse normal as the reference evaluates it (NormalCdfInv)
 __device__ double normal_cdf_inv(double P)
 {
@@ -276,7 +301,9 @@ __device__ void build_layer(const CalibArgs& A, int k, bool flat, double fallbac
 
 __global__ void __launch_bounds__(CALIB_THREADS) lsv_calib_kernel(const CalibArgs A)
 {
-    extern __shared__ double s_layer[]; // [points]
+    extern __shared__ __align__(16) unsigned char s_dyn[]; // the jump table, then the layer [points]
+    uint64_t* s_jtab = reinterpret_cast<uint64_t*>(s_dyn);
+    double* s_layer = reinterpret_cast<double*>(s_dyn + sizeof(uint64_t) * CALIB_JTAB_WORDS);
     __shared__ double s_min[CALIB_WARPS], s_max[CALIB_WARPS];
     __shared__ Fx128 s_sum[CALIB_WARPS];
     __shared__ unsigned s_cnt[CALIB_MAX_BINS];
@@ -291,6 +318,8 @@ __global__ void __launch_bounds__(CALIB_THREADS) lsv_calib_kernel(const CalibArg
     const int P = A.P, bins = A.bins;
     bool bad = false;
 
+    for (int i = threadIdx.x; i < (int)CALIB_JTAB_WORDS; i += CALIB_THREADS) s_jtab[i] = A.jtab[i];
+    __syncthreads();
     // the ensemble at today; particle p's generator at draw 2p of the stream
     for (int p = gt; p < P; p += T) {
         A.spot[p] = A.s0;
@@ -463,7 +492,7 @@ __global__ void __launch_bounds__(CALIB_THREADS) lsv_calib_kernel(const CalibArg
             A.var[p] = vc;
             A.spot[p] *= exp(step);
             A.lns[p] += step;
-            xo_jump(A.jdate, s);
+            xo_jump_tab(s_jtab, s);
             for (int w = 0; w < 4; w++) A.rng[(size_t)w * P + p] = s[w];
         }
         __syncthreads();
@@ -583,6 +612,26 @@ bool xo_jump_poly(uint64_t d, uint64_t out[4])
 }
 
 void xo_apply_jump(const uint64_t poly[4], uint64_t s[4]) { xo_jump(poly, s); }
+
+void xo_jump_table(const uint64_t poly[4], uint64_t* tab)
+{
+    // column i of the jump matrix: the jump of the state with only bit i set
+    std::vector<uint64_t> col(256 * 4);
+    for (int i = 0; i < 256; i++) {
+        uint64_t e[4] = {0, 0, 0, 0};
+        e[i >> 6] = 1ull << (i & 63);
+        xo_jump(poly, e);
+        for (int w = 0; w < 4; w++) col[i * 4 + w] = e[w];
+    }
+    for (int n = 0; n < 64; n++)
+        for (int v = 0; v < 16; v++) {
+            uint64_t r[4] = {0, 0, 0, 0};
+            for (int b = 0; b < 4; b++)
+                if ((v >> b) & 1)
+                    for (int w = 0; w < 4; w++) r[w] ^= col[(4 * n + b) * 4 + w];
+            for (int w = 0; w < 4; w++) tab[(n * 16 + v) * 4 + w] = r[w];
+        }
+}
 
 int calib_max_grid(int sms, size_t smem)
 {

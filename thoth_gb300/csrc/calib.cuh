@@ -24,7 +24,10 @@ struct CalibArgs {
     double *spot, *var, *lns; // [P] the ensemble
     uint64_t* rng;           // [4][P] each particle's Rng state
     const uint64_t* jpow;    // [CALIB_JUMP_BITS][4] x^(2^i) mod chi
-    const uint64_t* jdate;   // [4] x^(2P - 2) mod chi: from a particle's draws of one date to the next
+    // the jump from a particle's draws of one date to the next (2P - 2 draws) as a nibble
+    // table of its GF(2) matrix: jtab[(n 16 + v) 4 + w] = word w of the jump of the state
+    // whose nibble n is v and other bits 0 (64 nibbles x 16 values x 32 bytes, 32 KB)
+    const uint64_t* jtab;
     uint64_t seed_state[4];  // the Rng state after seeding
     // per-date totals the CTAs add into with integer atomics (order-independent, exact):
     long long *kmin, *kmax;  // [n] order-preserving integer keys of the extremes of ln S
@@ -37,6 +40,8 @@ struct CalibArgs {
     int* status;             // 0 ok, 2 a wait timed out, 3 a sum out of range
 };
 
+constexpr size_t CALIB_JTAB_WORDS = 64 * 16 * 4;
+
 int calib_max_grid(int sms, size_t smem);
 cudaError_t launch_calib(const CalibArgs& A, int grid, size_t smem, cudaStream_t st);
 
@@ -47,3 +52,5 @@ void xo_advance(uint64_t s[4]); // one transition of the state (no output)
 // Berlekamp-Massey); false if chi could not be found (never for xoshiro256)
 bool xo_jump_poly(uint64_t d, uint64_t out[4]);
 void xo_apply_jump(const uint64_t poly[4], uint64_t s[4]);
+// the nibble table of the jump poly (CALIB_JTAB_WORDS words, layout of CalibArgs::jtab)
+void xo_jump_table(const uint64_t poly[4], uint64_t* tab);

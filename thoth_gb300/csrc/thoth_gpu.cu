@@ -1895,7 +1895,9 @@ int calibrate_locked(ThothLeverageCalib* c)
     for (int i = 0; i < CALIB_JUMP_BITS; i++)
         if (!xo_jump_poly(1ull << i, jpow[i])) return fail(THOTH_GPU_E_INVALID, "Rng jump polynomial unavailable");
     if (!xo_jump_poly(2ull * (uint64_t)P - 2, jdate)) return fail(THOTH_GPU_E_INVALID, "Rng jump polynomial unavailable");
-    const size_t smem = sizeof(double) * (size_t)pts;
+    std::vector<uint64_t> jtab(CALIB_JTAB_WORDS);
+    xo_jump_table(jdate, jtab.data());
+    const size_t smem = sizeof(uint64_t) * CALIB_JTAB_WORDS + sizeof(double) * (size_t)pts;
     const int cap = calib_max_grid(g_dev.sms, smem);
     if (cap < 1) return fail(THOTH_GPU_E_TOO_LARGE, "layer too large for shared memory");
     const int grid = std::max(1, std::min(cap, (P + CALIB_THREADS - 1) / CALIB_THREADS));
@@ -1909,7 +1911,7 @@ int calibrate_locked(ThothLeverageCalib* c)
     };
     const size_t o_dt = take(8 * nd), o_carry = take(8 * nd), o_qe = take(8 * nd), o_ls = take(8 * nd);
     const size_t o_off = take(8 * nd), o_lv = take(8 * nd * npt), o_jp = take(8 * 4 * CALIB_JUMP_BITS),
-                 o_jd = take(8 * 4);
+                 o_jt = take(8 * CALIB_JTAB_WORDS);
     const size_t up_bytes = o; // everything above is uploaded in one copy
     const size_t o_lev = take(8 * nd * npt), o_spot = take(8 * np), o_var = take(8 * np), o_lns = take(8 * np);
     const size_t o_rng = take(8 * 4 * np), o_bc = take(8 * 4);
@@ -1935,7 +1937,7 @@ int calibrate_locked(ThothLeverageCalib* c)
     std::memcpy(h + o_off, c->offset, 8 * nd);
     std::memcpy(h + o_lv, c->local_vol, 8 * nd * npt);
     std::memcpy(h + o_jp, jpow, sizeof jpow);
-    std::memcpy(h + o_jd, jdate, sizeof jdate);
+    std::memcpy(h + o_jt, jtab.data(), 8 * CALIB_JTAB_WORDS);
     unsigned char* base = g_dev.calib;
     cudaStream_t st = g_dev.stream;
     CUDA_TRY(cudaMemcpyAsync(base, h, up_bytes, cudaMemcpyHostToDevice, st));
@@ -1970,7 +1972,7 @@ int calibrate_locked(ThothLeverageCalib* c)
     A.lns = reinterpret_cast<double*>(base + o_lns);
     A.rng = reinterpret_cast<uint64_t*>(base + o_rng);
     A.jpow = reinterpret_cast<const uint64_t*>(base + o_jp);
-    A.jdate = reinterpret_cast<const uint64_t*>(base + o_jd);
+    A.jtab = reinterpret_cast<const uint64_t*>(base + o_jt);
     xo_seed_state(c->seed, A.seed_state);
     A.kmin = reinterpret_cast<long long*>(base + o_kmin);
     A.kmax = reinterpret_cast<long long*>(base + o_kmax);
