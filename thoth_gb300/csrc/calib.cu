@@ -106,7 +106,10 @@ __device__ __forceinline__ void xo_jump_tab(const uint64_t* tab, uint64_t* s)
     s[3] = r3;
 }
 
-// Acklam's inverse normal as the reference evaluates it (NormalCdfInv)
+// Acklam's inverse normal as the reference evaluates it (NormalCdfInv). Both the tail and
+// the central rational are evaluated and one is selected: the selected value is the same
+// expression the reference evaluates, and without branches the compiler can interleave the
+// particle's independent FP64 chains (two Gaussians, the layer lookup).
 __device__ double normal_cdf_inv(double P)
 {
     const double a0 = -3.969683028665376e+01, a1 = 2.209460984245205e+02, a2 = -2.759285104469687e+02,
@@ -118,20 +121,18 @@ __device__ double normal_cdf_inv(double P)
     const double d0 = 7.784695709041462e-03, d1 = 3.224671290700398e-01, d2 = 2.445134137142996e+00,
                  d3 = 3.754408661907416e+00;
     const double p_low = 0.02425, p_high = 1.0 - p_low;
-    if (P < p_low) {
-        const double q = sqrt(-2.0 * log(P));
-        return (((((c0 * q + c1) * q + c2) * q + c3) * q + c4) * q + c5) /
-               ((((d0 * q + d1) * q + d2) * q + d3) * q + 1.0);
-    }
-    if (P <= p_high) {
-        const double q = P - 0.5;
-        const double r = q * q;
-        return (((((a0 * r + a1) * r + a2) * r + a3) * r + a4) * r + a5) * q /
-               (((((b0 * r + b1) * r + b2) * r + b3) * r + b4) * r + 1.0);
-    }
-    const double q = sqrt(-2.0 * log(1.0 - P));
-    return -(((((c0 * q + c1) * q + c2) * q + c3) * q + c4) * q + c5) /
-           ((((d0 * q + d1) * q + d2) * q + d3) * q + 1.0);
+    const bool lower = P < p_low, upper = !(P <= p_high);
+    // tail: q = sqrt(-2 ln P) below, sqrt(-2 ln(1 - P)) above (1 - P is exact where it is used)
+    const double qt = sqrt(-2.0 * log(lower ? P : 1.0 - P));
+    const double tn = ((((c0 * qt + c1) * qt + c2) * qt + c3) * qt + c4) * qt + c5;
+    const double td = (((d0 * qt + d1) * qt + d2) * qt + d3) * qt + 1.0;
+    const double q = P - 0.5;
+    const double r = q * q;
+    const double cn = (((((a0 * r + a1) * r + a2) * r + a3) * r + a4) * r + a5) * q;
+    const double cd = ((((b0 * r + b1) * r + b2) * r + b3) * r + b4) * r + 1.0;
+    const double num = lower ? tn : (upper ? -tn : cn);
+    const double den = (lower || upper) ? td : cd;
+    return num / den;
 }
 
 // Rng::Gaussian: a 53-bit uniform in (0, 1) through the inverse normal
@@ -177,16 +178,18 @@ __device__ double spot_step(double Vp, double Vc, double Dt, double Carry, doubl
     return Carry - 0.5 * L * L * Vp * Dt + L * sqrt(Vp * Dt) * Z;
 }
 
-// LeverageSurface::LayerAt (leverage_surface.cpp:19-40) on a layer in shared memory
+// LeverageSurface::LayerAt (leverage_surface.cpp:19-40) on a layer in shared memory: the
+// clamps select instead of branching (the interpolation index is clamped to the layer, and
+// its value is only selected where the reference interpolates)
 __device__ __forceinline__ double layer_at(const double* lev, int points, double ln_step, int64_t offset, double S)
 {
     const double f = log(S) / ln_step - (double)offset;
     const int last = points - 1;
-    if (!(f > 0.0)) return lev[0];
-    if (f >= (double)last) return lev[last];
-    const int i = (int)f;
+    const bool inside = f > 0.0 && f < (double)last;
+    const int i = inside ? (int)f : 0;
     const double w = f - (double)i;
-    return (1.0 - w) * lev[i] + w * lev[i + 1];
+    const double mid = (1.0 - w) * lev[i] + w * lev[i + 1];
+    return !(f > 0.0) ? lev[0] : (f >= (double)last ? lev[last] : mid);
 }
 
 __device__ __forceinline__ void warp_sum(Fx128& a)
@@ -485,10 +488,14 @@ __global__ void __launch_bounds__(CALIB_THREADS) lsv_calib_kernel(const CalibArg
         for (int p = gt; p < P; p += T) {
             uint64_t s[4];
             for (int w = 0; w < 4; w++) s[w] = A.rng[(size_t)w * P + p];
+            // both Gaussians in draw order (the variance's first) and the layer lookup before
+            // the branched QE step: three independent chains in one block
+            const double z1 = gaussian(s);
+            const double z2 = gaussian(s);
             const double lp = layer_at(s_layer, A.points, ls, off, A.spot[p]);
             const double vp = A.var[p];
-            const double vc = qe_step(vp, gaussian(s), e, A);
-            const double step = spot_step(vp, vc, dt, carry, lp, gaussian(s), A);
+            const double vc = qe_step(vp, z1, e, A);
+            const double step = spot_step(vp, vc, dt, carry, lp, z2, A);
             A.var[p] = vc;
             A.spot[p] *= exp(step);
             A.lns[p] += step;
