@@ -254,6 +254,25 @@ def american_section(G, flush, steps):
                      "simulate_and_fit_device_ms": float(np.median(dev)),
                      "e2e_ms": e2e_ms, "e2e_path_dates_per_sec": units / (e2e_ms * 1e-3),
                      "fit_read_gbs": 4.0 * units / (fit_ms * 1e-3) / 1e9}
+    # a grid of 27 American puts on one Heston name (9 strikes x 3 maturities, daily exercise):
+    # one batched fit, one regression round a date for all of them, against one call each
+    grid = abi.Book(days=np.arange(0, 366), paths=1 << 18)
+    hh = grid.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.03)
+    for K in range(80, 121, 5):
+        for mty in (91, 182, 365):
+            grid.add_vanilla(hh, float(K), mty, abi.PUT, zero_rate=0.03)
+    idx = list(range(len(grid.products)))
+    G.price_american_book(grid, idx)
+    t0 = time.perf_counter()
+    rg = G.price_american_book(grid, idx)
+    t_book = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for i in idx:
+        G.price_american(grid, i)
+    t_one = time.perf_counter() - t0
+    out["heston_grid_27_puts_2^18"] = {"contracts": len(idx), "book_call_ms": 1e3 * t_book,
+                                        "book_call_device_ms": rg[0]["device_ms"],
+                                        "one_call_each_ms": 1e3 * t_one, "speedup": t_one / t_book}
     book = cases[0][1]
     t0 = time.perf_counter()
     g = G.price_american(book, 0, flags=abi.BUMP_DELTA | abi.BUMP_GAMMA | abi.BUMP_VEGA | abi.BUMP_RHO |

@@ -314,10 +314,18 @@ typedef struct ThothAmerican {
     double european;          /* out: discounted maturity payoff on the same paths   */
     double delta, gamma, vega, rho, theta; /* out: NaN where not requested          */
     double device_ms;         /* out: every simulation and exercise kernel           */
-    double exercise_ms;       /* out: the base fit kernel alone                      */
+    double exercise_ms;       /* out: the base fit kernel(s) of the call alone        */
 } ThothAmerican;
 
 int thoth_gpu_price_american(const ThothBookDesc* book, ThothAmerican* am);
+/* Every American contract of a book in one call, as PriceAmerican prices all of a book's
+ * American contracts: am[0..n) as above, one per contract. Each scenario (the base, each
+ * asset's spot bumps, the vol, rate and roll scenarios) is simulated once per asset that
+ * carries contracts, and all of that asset's contracts are fitted or valued on the same
+ * stored paths; the fits of an asset's contracts share one launch, one regression round
+ * per date for all of them (the normal equations batched). device_ms and exercise_ms of
+ * every entry are the whole call's. */
+int thoth_gpu_price_american_book(const ThothBookDesc* book, ThothAmerican* am, int32_t n);
 const char* thoth_gpu_american_last_error(void);
 
 /* ---- LSV leverage calibration (binned particle method) ----------------------

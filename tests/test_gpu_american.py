@@ -214,3 +214,24 @@ def test_errors_and_maturity_today(gpu):
     t0.products[0]["maturity"] = 0
     r = gpu.price_american(t0, 0)
     assert r["premium"] == 0.0 and r["fitted_dates"] == 0
+
+
+def test_book_call_equals_contract_by_contract(gpu):
+    """thoth_gpu_price_american_book: one simulation per asset and scenario, the same
+    numbers as pricing each contract alone."""
+    b = abi.Book(days=np.asarray(DAYS), paths=20000)
+    g = b.add_gbm(100.0, 0.30, 0.05)
+    h = b.add_heston(50.0, 0.05, 1.5, 0.05, 0.5, -0.6, 0.03)
+    b.add_vanilla(g, 100.0, 13, abi.PUT, zero_rate=0.05)
+    b.add_vanilla(g, 90.0, 6, abi.PUT, zero_rate=0.05)
+    b.add_variance(g, 13, strike_variance=0.09, notional=1.0, zero_rate=0.05)   # not American: skipped
+    b.add_vanilla(h, 55.0, 13, abi.PUT, zero_rate=0.03)
+    b.add_vanilla(h, 45.0, 9, abi.CALL, zero_rate=0.03)
+    am = [0, 1, 3, 4]
+    flags = abi.BUMP_DELTA | abi.BUMP_GAMMA | abi.BUMP_VEGA | abi.BUMP_RHO | abi.BUMP_THETA
+    together = gpu.price_american_book(b, am, flags=flags)
+    for r, p in zip(together, am):
+        alone = gpu.price_american(b, p, flags=flags)
+        for k in ("premium", "trust", "european", "delta", "gamma", "vega", "rho", "theta", "fitted_dates"):
+            assert r[k] == alone[k], (p, k, r[k], alone[k])
+        np.testing.assert_array_equal(r["beta"], alone["beta"])

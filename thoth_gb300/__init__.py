@@ -57,6 +57,8 @@ def lib():
         L.thoth_gpu_calibrate_leverage.argtypes = [C.POINTER(abi.ThothLeverageCalib)]
         L.thoth_gpu_xoshiro_jump.argtypes = [C.POINTER(C.c_uint64), C.c_uint64, C.POINTER(C.c_uint64)]
         L.thoth_gpu_price_american.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothAmerican)]
+        L.thoth_gpu_price_american_book.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothAmerican),
+                                                    C.c_int32]
         L.thoth_gpu_american_last_error.restype = C.c_char_p
         L.thoth_gpu_simulate_paths.argtypes = [C.POINTER(abi.ThothBookDesc), C.c_int32, C.POINTER(C.c_float),
                                                C.POINTER(C.c_double)]
@@ -163,26 +165,44 @@ def price_american(book, product, flags=0, min_itm=0, zero_rates=None):
     stored paths, with frozen-policy Greeks (flags: abi.BUMP_DELTA | ... | BUMP_THETA).
     Returns premium, trust, european, the Greeks (NaN where not requested), beta
     [n_dates, 3] (NaN where a date has no regression), fitted_dates and the device times."""
+    return price_american_book(book, [product], flags, min_itm, zero_rates)[0]
+
+
+def price_american_book(book, products, flags=0, min_itm=0, zero_rates=None):
+    """Every listed American vanilla of the book in one call (one simulation per asset and
+    scenario): a list of dicts as price_american returns. zero_rates: one array for every
+    contract, or a list with one per contract (None: the product's zero_rate)."""
     d = book.desc()
-    a = abi.ThothAmerican()
-    a.product = int(product)
-    a.flags = int(flags)
-    a.min_itm = int(min_itm)
-    z = None
-    if zero_rates is not None:
-        z = np.ascontiguousarray(zero_rates, dtype=np.float64)
-        if z.shape != (book.n_dates,):
-            raise ValueError("zero_rates needs one rate per date")
-        a.zero_rates = z.ctypes.data_as(C.POINTER(C.c_double))
-    beta = np.full((book.n_dates, 3), np.nan)
-    a.beta = beta.ctypes.data_as(C.POINTER(C.c_double))
-    rc = lib().thoth_gpu_price_american(C.byref(d), C.byref(a))
+    n = len(products)
+    arr = (abi.ThothAmerican * max(n, 1))()
+    keep = []
+    for i, pr in enumerate(products):
+        a = arr[i]
+        a.product = int(pr)
+        a.flags = int(flags)
+        a.min_itm = int(min_itm)
+        zr = zero_rates[i] if isinstance(zero_rates, (list, tuple)) else zero_rates
+        if zr is not None:
+            z = np.ascontiguousarray(zr, dtype=np.float64)
+            if z.shape != (book.n_dates,):
+                raise ValueError("zero_rates needs one rate per date")
+            a.zero_rates = z.ctypes.data_as(C.POINTER(C.c_double))
+            keep.append(z)
+        beta = np.full((book.n_dates, 3), np.nan)
+        a.beta = beta.ctypes.data_as(C.POINTER(C.c_double))
+        keep.append(beta)
+    rc = lib().thoth_gpu_price_american_book(C.byref(d), arr, n)
     if rc != abi.THOTH_GPU_OK:
         raise ThothGpuError(rc, lib().thoth_gpu_american_last_error().decode())
-    out = {k: getattr(a, k) for k in ("premium", "trust", "european", "delta", "gamma", "vega", "rho", "theta",
-                                      "device_ms", "exercise_ms", "fitted_dates")}
-    out["beta"] = beta
-    out["note"] = lib().thoth_gpu_american_last_error().decode()
+    note = lib().thoth_gpu_american_last_error().decode()
+    out = []
+    for i in range(n):
+        a = arr[i]
+        r = {k: getattr(a, k) for k in ("premium", "trust", "european", "delta", "gamma", "vega", "rho", "theta",
+                                         "device_ms", "exercise_ms", "fitted_dates")}
+        r["beta"] = np.ctypeslib.as_array(a.beta, shape=(book.n_dates, 3)).copy()
+        r["note"] = note
+        out.append(r)
     return out
 
 

@@ -2,16 +2,18 @@
 // algorithm of pricer_mcl_american.cpp:263-447 (FitAmericanPolicy / ApplyAmericanPolicy)
 // with the normal-equation solve of helpers/maths.cpp:354-381 and 419-470.
 //
-// Fit: one cooperative, persistent launch walks the exercise dates backwards. At each date
-// every CTA discounts its paths' cashflows, sums the regression moments of its in-the-money
-// paths and publishes them; the last CTA to publish adds all the CTAs' sums, solves the 3x3
-// system and releases the others with a flag, and every CTA rolls its paths' cashflows back
-// through the exercise decision. The dates are sequential, so one launch with one
-// publish-and-release per date replaces one launch per date. The exercise decisions of the
-// backward pass are the frozen policy's decisions on the same paths (the same test at the
-// same dates), so the earliest exercise the pass records per path is the value the
-// reference's apply step finds: the base premium comes out of the fit without a second
-// walk over the paths.
+// Fit: one cooperative, persistent launch fits every contract of an asset on the same stored
+// paths, walking the exercise dates backwards. At each date, for each contract whose grid
+// reaches the date, every CTA discounts its paths' cashflows, queues the in-the-money paths so
+// that full warps do the FP64 work, and adds the regression moments into the contract's
+// per-date totals (exact 128-bit integer atomics). The last CTA to publish solves every
+// contract's 3x3 system, one thread each, and releases the others with a flag; every CTA then
+// rolls its paths' cashflows back through each contract's exercise decision. The dates are
+// sequential and the contracts share them, so one launch with one publish-and-release per
+// date replaces a launch per contract and date. The exercise decisions of the backward pass
+// are the frozen policy's decisions on the same paths (the same test at the same dates), so
+// the earliest exercise the pass records per path is the value the reference's apply step
+// finds: the premium comes out of the fit without a second walk over the paths.
 //
 // Apply: the frozen policy on another path set (the bumped scenarios of the Greeks), one
 // forward walk per path that stops at the first exercise.
@@ -41,7 +43,8 @@ __device__ __forceinline__ double intrinsic(double s, double k, int call)
 
 // intrinsic(S) > 0, decided on the single-precision bits of S (integer compare; the
 // threshold is exact, see itm_bits)
-__device__ __forceinline__ bool in_the_money(float s, const LsmArgs& A)
+template <class K>
+__device__ __forceinline__ bool in_the_money(float s, const K& A)
 {
     const int b = __float_as_int(s);
     return A.call ? b >= A.itm_bits : b <= A.itm_bits;
@@ -53,7 +56,8 @@ __device__ __forceinline__ bool in_the_money(float s, const LsmArgs& A)
 // q1 + r y rounded once is the correctly rounded quotient (P. Markstein, IBM J. Res. Dev.
 // 34(1), 1990: y within half an ulp of 1 / norm, q1 within one ulp of S / norm).
 // Five FP64 operations in place of a full division.
-__device__ __forceinline__ double moneyness(double s, const LsmArgs& A)
+template <class K>
+__device__ __forceinline__ double moneyness(double s, const K& A)
 {
     const double y = A.inv_norm, b = A.norm;
     const double q0 = __dmul_rn(s, y);
@@ -152,16 +156,39 @@ __device__ bool solve3(const double* tot, double* beta)
     return true;
 }
 
-// one in-the-money path of the current date: its regression terms into the lane's sums,
-// its moneyness and intrinsic value into the warp's compacted list at entry o
-__device__ __forceinline__ void itm_item(int p, float sf, double y, const LsmArgs& A, Fx128* q, int64_t o, bool& bad)
+// An exact 128-bit sum split into three limbs of 42, 42 and 44 bits, each added into its own
+// 64-bit word by a reduction that returns nothing (no round trip for a carry). The limbs of a
+// per-CTA sum are below 2^44, so fewer than 2^20 CTAs cannot overflow a word; the solving CTA
+// reassembles the exact value.
+constexpr uint64_t LIMB42 = (1ull << 42) - 1;
+
+__device__ __forceinline__ void fx_red3(unsigned long long* dst, const Fx128& a)
+{
+    atomicAdd(dst, (unsigned long long)(a.lo & LIMB42));
+    atomicAdd(dst + 1, (unsigned long long)((a.lo >> 42) | ((a.hi & ((1ull << 20) - 1)) << 22)));
+    atomicAdd(dst + 2, (unsigned long long)(a.hi >> 20));
+}
+
+__device__ __forceinline__ Fx128 fx_from3(const unsigned long long* src)
+{
+    const uint64_t l0 = __ldcg(src), l1 = __ldcg(src + 1), l2 = __ldcg(src + 2);
+    Fx128 r = {l0, 0};
+    fx_add(r, l1 << 42, l1 >> 22);
+    fx_add(r, 0, l2 << 20);
+    return r;
+}
+
+// one in-the-money path of contract K at the current date: its regression terms into the
+// lane's sums, its moneyness and intrinsic value into the warp's compacted list at entry o
+__device__ __forceinline__ void itm_item(int p, float sf, double y, const LsmContract& K, Fx128* q, int64_t o,
+                                         bool& bad)
 {
     const double s = (double)sf;
-    const double iv = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
-    const double m = moneyness(s, A), m2 = __dmul_rn(m, m);
-    A.c_idx[o] = p;
-    A.c_m[o] = m;
-    A.c_iv[o] = iv;
+    const double iv = K.call ? __dsub_rn(s, K.strike) : __dsub_rn(K.strike, s);
+    const double m = moneyness(s, K), m2 = __dmul_rn(m, m);
+    K.c_idx[o] = p;
+    K.c_m[o] = m;
+    K.c_iv[o] = iv;
     fx_add_checked(q[0], m, bad);
     fx_add_checked(q[1], m2, bad);
     fx_add_checked(q[2], __dmul_rn(m2, m), bad);
@@ -183,19 +210,23 @@ __device__ void block_sum(Fx128 a, Fx128 (*s_w)[LSM_PART], int slot, Fx128* out)
         for (int w = 0; w < LSM_WARPS; w++) fx_add(s, s_w[w][slot]);
         *out = s;
     }
+    __syncthreads();
 }
 
-__global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmArgs A)
+__global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmFitArgs A)
 {
     __shared__ Fx128 s_w[LSM_WARPS][LSM_PART];
     __shared__ int q_idx[LSM_WARPS][LSM_QCAP];
     __shared__ float q_s[LSM_WARPS][LSM_QCAP];
     __shared__ double q_y[LSM_WARPS][LSM_QCAP];
-    __shared__ double s_tot[LSM_PART];
-    __shared__ double s_b[3];
-    __shared__ int s_fit, s_ok, s_last;
-    __shared__ uint64_t s_cnt;
+    __shared__ LsmContract s_ct[LSM_MAX_CONTRACTS];
+    __shared__ int s_nout[LSM_WARPS][LSM_MAX_CONTRACTS];
+    __shared__ double s_b[LSM_MAX_CONTRACTS][3];
+    __shared__ double s_tot[LSM_MAX_CONTRACTS][LSM_PART];
+    __shared__ int s_fit[LSM_MAX_CONTRACTS];
+    __shared__ int s_ok, s_last;
     const int G = gridDim.x;
+    const int C = A.C;
     const int64_t T = (int64_t)G * LSM_THREADS;
     const int64_t g0 = (int64_t)blockIdx.x * LSM_THREADS + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -203,83 +234,90 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmArgs A
     const int64_t seg = gw * A.seg_len;
     const unsigned below = (1u << lane) - 1u;
     bool bad = false;
+    for (int c = threadIdx.x; c < C; c += LSM_THREADS) s_ct[c] = A.ct[c];
+    __syncthreads();
 
-    // maturity: the cashflow is the payoff, and the value if never exercised earlier
-    Fx128 eu = {0, 0};
-    {
-        const float* row = A.S + (int64_t)(A.M - 1) * A.ld;
-        const double dT = A.disc[A.M - 1];
+    // maturity: each contract's cashflow is its payoff, and its value if never exercised earlier
+    for (int c = 0; c < C; ++c) {
+        const LsmContract K = s_ct[c];
+        Fx128 eu = {0, 0};
+        const float* row = A.S + (int64_t)(K.M - 1) * A.ld;
+        const double dT = K.disc[K.M - 1];
         for (int64_t p = g0; p < A.n; p += T) {
-            const double iv = intrinsic((double)row[p], A.strike, A.call);
+            const double iv = intrinsic((double)row[p], K.strike, K.call);
             const double v = __dmul_rn(iv, dT);
-            A.cf[p] = iv;
-            A.val[p] = v;
+            K.cf[p] = iv;
+            K.val[p] = v;
             fx_add_checked(eu, v, bad);
         }
+        block_sum(eu, s_w, 2, K.acc + (size_t)blockIdx.x * LSM_NACC + 2);
     }
 
     unsigned phase = 0; // dates done
-    for (int t = A.M - 2; t >= 1; --t) {
-        const double d = A.df[t];
+    for (int t = A.Tmax - 2; t >= 1; --t) {
         const float* row = A.S + (int64_t)t * A.ld;
-        Fx128 q[LSM_NQ];
+        // every contract whose exercise grid reaches date t: discount, queue, sum, publish
+        for (int c = 0; c < C; ++c) {
+            const LsmContract K = s_ct[c];
+            if (t > K.M - 2) continue;
+            const double d = K.df[t];
+            Fx128 q[LSM_NQ];
 #pragma unroll
-        for (int i = 0; i < LSM_NQ; i++) q[i] = Fx128{0, 0};
-        // every path: discount the cashflow; the in-the-money ones queue until a full warp
-        // of them does the FP64 work (the warp's count qn and list length nout are uniform)
-        int qn = 0, nout = 0;
-        for (int64_t base = gw * 32; base < A.n; base += T) {
-            const int64_t p = base + lane;
-            bool itm = false;
-            float sf = 0.0f;
-            double y = 0.0;
-            if (p < A.n) {
-                y = __dmul_rn(A.cf[p], d);
-                A.cf[p] = y;
-                sf = row[p];
-                itm = in_the_money(sf, A);
-            }
-            const unsigned mk = __ballot_sync(0xffffffffu, itm);
-            if (itm) {
-                const int k = qn + __popc(mk & below);
-                q_idx[warp][k] = (int)p;
-                q_s[warp][k] = sf;
-                q_y[warp][k] = y;
-            }
-            qn += __popc(mk);
-            __syncwarp();
-            if (qn >= 32) {
-                qn -= 32;
-                const int k = qn + lane;
-                itm_item(q_idx[warp][k], q_s[warp][k], q_y[warp][k], A, q, seg + nout + lane, bad);
-                nout += 32;
+            for (int i = 0; i < LSM_NQ; i++) q[i] = Fx128{0, 0};
+            // in-the-money paths queue until a full warp of them does the FP64 work (the
+            // warp's count qn and list length nout are uniform)
+            int qn = 0, nout = 0;
+            for (int64_t base = gw * 32; base < A.n; base += T) {
+                const int64_t p = base + lane;
+                bool itm = false;
+                float sf = 0.0f;
+                double y = 0.0;
+                if (p < A.n) {
+                    y = __dmul_rn(K.cf[p], d);
+                    K.cf[p] = y;
+                    sf = row[p];
+                    itm = in_the_money(sf, K);
+                }
+                const unsigned mk = __ballot_sync(0xffffffffu, itm);
+                if (itm) {
+                    const int k = qn + __popc(mk & below);
+                    q_idx[warp][k] = (int)p;
+                    q_s[warp][k] = sf;
+                    q_y[warp][k] = y;
+                }
+                qn += __popc(mk);
                 __syncwarp();
+                if (qn >= 32) {
+                    qn -= 32;
+                    const int k = qn + lane;
+                    itm_item(q_idx[warp][k], q_s[warp][k], q_y[warp][k], K, q, seg + nout + lane, bad);
+                    nout += 32;
+                    __syncwarp();
+                }
             }
-        }
-        if (lane < qn) itm_item(q_idx[warp][lane], q_s[warp][lane], q_y[warp][lane], A, q, seg + nout + lane, bad);
-        nout += qn;
-        const unsigned cnt = (unsigned)nout;
+            if (lane < qn) itm_item(q_idx[warp][lane], q_s[warp][lane], q_y[warp][lane], K, q, seg + nout + lane, bad);
+            nout += qn;
 #pragma unroll
-        for (int i = 0; i < LSM_NQ; i++) warp_sum(q[i]);
-        if (lane == 0) {
+            for (int i = 0; i < LSM_NQ; i++) warp_sum(q[i]);
+            if (lane == 0) {
 #pragma unroll
-            for (int i = 0; i < LSM_NQ; i++) s_w[warp][i] = q[i];
-            s_w[warp][LSM_NQ] = Fx128{cnt, 0};
-        }
-        __syncthreads();
-        const int buf = t & 1;
-        if (threadIdx.x < LSM_PART) {
-            Fx128 s = {0, 0};
-            for (int w = 0; w < LSM_WARPS; w++) fx_add(s, s_w[w][threadIdx.x]);
-            A.part[((size_t)buf * G + blockIdx.x) * LSM_PART + threadIdx.x] = s;
-            __threadfence();
+                for (int i = 0; i < LSM_NQ; i++) s_w[warp][i] = q[i];
+                s_w[warp][LSM_NQ] = Fx128{(uint64_t)nout, 0};
+                s_nout[warp][c] = nout;
+            }
+            __syncthreads();
+            if (threadIdx.x < LSM_PART) {
+                Fx128 sm = {0, 0};
+                for (int w = 0; w < LSM_WARPS; w++) fx_add(sm, s_w[w][threadIdx.x]);
+                fx_red3(K.tot + ((size_t)t * LSM_PART + threadIdx.x) * 3, sm);
+                __threadfence();
+            }
+            __syncthreads();
         }
         if (bad) atomicExch(A.status, 3);
         ++phase;
-        __syncthreads();
-        // the last CTA to publish its sums adds them all, solves and releases the others
         if (threadIdx.x == 0) s_last = atomicAdd(A.bar, 1u) == phase * (unsigned)G - 1;
-        // while the regression is solved: pull the next date's spots of this warp's paths
+        // while the regressions are solved: pull the next date's spots of this warp's paths
         // into L2 (lane k takes the warp's k-th, (k+32)-th, ... line of 32 paths)
         if (t > 1) {
             const float* next = A.S + (int64_t)(t - 1) * A.ld;
@@ -287,72 +325,80 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmArgs A
         }
         __syncthreads();
         if (s_last) {
+            // the last CTA to publish rounds every active contract's sums (one thread a sum)
+            // and solves every contract's system (one thread a contract)
             __threadfence();
-            if (warp < LSM_PART) {
-                const Fx128* P = A.part + (size_t)buf * G * LSM_PART + warp;
-                Fx128 s = {0, 0};
-#pragma unroll 4
-                for (int c = lane; c < G; c += 32) {
-                    const unsigned long long* e = reinterpret_cast<const unsigned long long*>(P + (size_t)c * LSM_PART);
-                    fx_add(s, (uint64_t)__ldcg(e), (uint64_t)__ldcg(e + 1));
-                }
-                warp_sum(s);
-                // each warp rounds its own sum to double (the count is exact below 2^53)
-                if (lane == 0) s_tot[warp] = warp == LSM_NQ ? (double)s.lo : fx_to_double(s);
-                if (warp == LSM_NQ && lane == 0) s_cnt = s.lo;
+            for (int x = threadIdx.x; x < C * LSM_PART; x += LSM_THREADS) {
+                const int c = x / LSM_PART, i = x - c * LSM_PART;
+                if (t > s_ct[c].M - 2) continue;
+                const Fx128 v = fx_from3(s_ct[c].tot + ((size_t)t * LSM_PART + i) * 3);
+                s_tot[c][i] = i == LSM_NQ ? (double)v.lo : fx_to_double(v);
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
+            for (int c = threadIdx.x; c < C; c += LSM_THREADS) {
+                const LsmContract K = s_ct[c];
+                if (t > K.M - 2) continue;
                 double b[3] = {0.0, 0.0, 0.0};
-                s_fit = s_cnt >= (uint64_t)A.min_itm && solve3(s_tot, b);
-                s_b[0] = b[0];
-                s_b[1] = b[1];
-                s_b[2] = b[2];
-                A.fit[t] = s_fit;
-                A.beta[3 * t] = b[0];
-                A.beta[3 * t + 1] = b[1];
-                A.beta[3 * t + 2] = b[2];
+                const int f = s_tot[c][LSM_NQ] >= (double)K.min_itm && solve3(s_tot[c], b);
+                K.fit[t] = f;
+                K.beta[3 * t] = b[0];
+                K.beta[3 * t + 1] = b[1];
+                K.beta[3 * t + 2] = b[2];
+                s_fit[c] = f;
+                s_b[c][0] = b[0];
+                s_b[c][1] = b[1];
+                s_b[c][2] = b[2];
                 __threadfence();
-                st_release(A.done, phase);
             }
-        } else if (threadIdx.x == 0) {
-            int ok = wait_for(A.done, phase, A.status);
-            if (ok) {
-                s_fit = __ldcg(A.fit + t);
-                s_b[0] = __ldcg(A.beta + 3 * t);
-                s_b[1] = __ldcg(A.beta + 3 * t + 1);
-                s_b[2] = __ldcg(A.beta + 3 * t + 2);
+            __syncthreads();
+            if (threadIdx.x == 0) st_release(A.done, phase);
+        } else {
+            if (threadIdx.x == 0) s_ok = wait_for(A.done, phase, A.status);
+            __syncthreads();
+            if (!s_ok) return;
+            for (int c = threadIdx.x; c < C; c += LSM_THREADS) {
+                const LsmContract K = s_ct[c];
+                if (t > K.M - 2) continue;
+                s_fit[c] = __ldcg(K.fit + t);
+                s_b[c][0] = __ldcg(K.beta + 3 * t);
+                s_b[c][1] = __ldcg(K.beta + 3 * t + 1);
+                s_b[c][2] = __ldcg(K.beta + 3 * t + 2);
             }
-            s_ok = ok;
         }
         __syncthreads();
-        if (!s_last && !s_ok) return;
-        if (s_fit) {
-            const double b0 = s_b[0], b1 = s_b[1], b2 = s_b[2];
-            const double dt = A.disc[t];
+        // every active contract's exercise decision on its list
+        for (int c = 0; c < C; ++c) {
+            const LsmContract K = s_ct[c];
+            if (t > K.M - 2 || !s_fit[c]) continue;
+            const double b0 = s_b[c][0], b1 = s_b[c][1], b2 = s_b[c][2];
+            const double dt = K.disc[t];
+            const int nout = s_nout[warp][c];
             for (int j = lane; j < nout; j += 32) {
                 const int64_t o = seg + j;
-                const double iv = A.c_iv[o];
-                if (iv >= continuation(b0, b1, b2, A.c_m[o])) {
-                    const int p = A.c_idx[o];
-                    A.cf[p] = iv;
-                    A.val[p] = __dmul_rn(iv, dt);
+                const double iv = K.c_iv[o];
+                if (iv >= continuation(b0, b1, b2, K.c_m[o])) {
+                    const int p = K.c_idx[o];
+                    K.cf[p] = iv;
+                    K.val[p] = __dmul_rn(iv, dt);
                 }
             }
         }
+        __syncthreads();
     }
 
-    Fx128 v = {0, 0}, v2 = {0, 0};
-    for (int64_t p = g0; p < A.n; p += T) {
-        const double x = A.val[p];
-        fx_add_checked(v, x, bad);
-        fx_add_checked(v2, __dmul_rn(x, x), bad);
+    for (int c = 0; c < C; ++c) {
+        const LsmContract K = s_ct[c];
+        Fx128 v = {0, 0}, v2 = {0, 0};
+        for (int64_t p = g0; p < A.n; p += T) {
+            const double x = K.val[p];
+            fx_add_checked(v, x, bad);
+            fx_add_checked(v2, __dmul_rn(x, x), bad);
+        }
+        Fx128* acc = K.acc + (size_t)blockIdx.x * LSM_NACC;
+        block_sum(v, s_w, 0, acc);
+        block_sum(v2, s_w, 1, acc + 1);
     }
     if (bad) atomicExch(A.status, 3);
-    Fx128* acc = A.acc + (size_t)blockIdx.x * LSM_NACC;
-    block_sum(v, s_w, 0, acc);
-    block_sum(v2, s_w, 1, acc + 1);
-    block_sum(eu, s_w, 2, acc + 2);
 }
 
 __global__ void __launch_bounds__(LSM_THREADS) lsm_apply_kernel(const LsmArgs A)
@@ -399,9 +445,9 @@ int lsm_fit_max_grid(int sms)
     return per * sms;
 }
 
-cudaError_t launch_lsm_fit(const LsmArgs& A, int grid, cudaStream_t st)
+cudaError_t launch_lsm_fit(const LsmFitArgs& A, int grid, cudaStream_t st)
 {
-    LsmArgs a = A;
+    LsmFitArgs a = A;
     void* args[] = {&a};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(lsm_fit_kernel), dim3(grid), dim3(LSM_THREADS),
                                        args, 0, st);

@@ -18,6 +18,7 @@ constexpr int LSM_PART = LSM_NQ + 1;
 // per-CTA result sums: discounted exercise values, their squares, discounted maturity payoffs
 constexpr int LSM_NACC = 3;
 
+// The frozen-policy apply of one contract (lsm_apply_kernel).
 struct LsmArgs {
     const float* S;       // [n_dates][ld] spot of every date and path, date-major
     int64_t ld;           // row stride of S (the book's path count)
@@ -34,29 +35,48 @@ struct LsmArgs {
     const double* disc;   // [M] disc[t]: discount from date t to today
     double* beta;         // [3M] b0, b1, b2 of each date (written by the fit, read by the apply)
     int* fit;             // [M] 1 where date t has a regression
-    double* cf;           // [n] fit scratch: each path's cashflow, valued at the current date
-    double* val;          // [n] fit scratch: each path's exercise value discounted to today
-    // fit scratch, the in-the-money paths of the current date compacted per warp: warp w
-    // owns entries [w seg_len, (w + 1) seg_len), seg_len = 32 ceil(n / threads)
-    int64_t seg_len;
-    int32_t* c_idx;       // path index
-    double* c_m;          // moneyness
-    double* c_iv;         // intrinsic value
-    Fx128* part;          // [2][grid][LSM_PART] per-CTA regression sums, double-buffered by date
     Fx128* acc;           // [grid][LSM_NACC] per-CTA result sums
-    unsigned* bar;        // arrivals of the CTAs' sums, all dates (zero at launch)
-    unsigned* done;       // dates whose regression is published (zero at launch)
-    int* status;          // 0 ok; 2 a wait timed out; 3 an addend out of range
+    int* status;          // 0 ok; 3 an addend out of range
+};
+
+// One contract of a batched fit: its exercise grid, payoff, discount tables, outputs and
+// scratch on the device.
+constexpr int LSM_MAX_CONTRACTS = 64;
+struct LsmContract {
+    int M, call, min_itm, itm_bits; // as in LsmArgs
+    double strike, norm, inv_norm;
+    const double* df;               // [M]
+    const double* disc;             // [M]
+    double* beta;                   // [3M] out
+    int* fit;                       // [M] out (zero at launch)
+    double *cf, *val;               // [n] scratch
+    int32_t* c_idx;                 // [n_list] compacted in-the-money lists, per warp
+    double *c_m, *c_iv;             // [n_list]
+    unsigned long long* tot;        // [M][LSM_PART][3] per-date regression sums as 42/42/44-bit
+                                    // limbs (zero at launch)
+    Fx128* acc;                     // [grid][LSM_NACC] per-CTA result sums
+};
+
+// The batched fit: every contract fitted on the same stored paths in one launch, each date
+// one publish-and-release for all of them.
+struct LsmFitArgs {
+    const float* S;
+    int64_t ld, n;
+    int C;                          // contracts, <= LSM_MAX_CONTRACTS
+    int Tmax;                       // the largest M
+    const LsmContract* ct;          // [C]
+    int64_t seg_len;                // list entries of one warp, 32 ceil(n / threads)
+    unsigned *bar, *done;           // arrivals and releases, all dates (zero at launch)
+    int* status;                    // 0 ok; 2 a wait timed out; 3 an addend out of range
 };
 
 // the fit kernel is a cooperative launch: every CTA must be resident at once
 int lsm_fit_max_grid(int sms);
-cudaError_t launch_lsm_fit(const LsmArgs& A, int grid, cudaStream_t st);
+cudaError_t launch_lsm_fit(const LsmFitArgs& A, int grid, cudaStream_t st);
 cudaError_t launch_lsm_apply(const LsmArgs& A, int grid, cudaStream_t st);
 
-// One pass over the stored paths of one asset of a book (thoth_gpu.cu): the book is
-// simulated, then a policy is fitted and valued on the same paths (fit), or the given
-// frozen policy is valued (apply).
+// One pass over the stored paths of one asset of a book (thoth_gpu.cu): a policy fitted and
+// valued on the paths (fit), or the given frozen policy valued (apply).
 struct LsmPass {
     int asset = 0;                // in: the asset whose paths are stored
     int M = 0;                    // in: exercise dates 0 .. M-1
@@ -72,8 +92,12 @@ struct LsmPass {
     double s0 = 0;                // out: stored spot of path 0 at date 0
     int64_t paths = 0;            // out
     int grid = 0;                 // out: CTAs of the pass's kernel
-    double sim_ms = 0, lsm_ms = 0; // out: device time of the simulation and of the exercise kernel
+    // out: device time of the simulation and of the exercise kernel; passes that share a
+    // simulation or a batched fit launch carry its time on the first of them only
+    double sim_ms = 0, lsm_ms = 0;
 };
 
-// under the engine's lock; errors as the C ABI's, message in thoth_gpu_last_error()
-int thoth_lsm_pass(const ThothBookDesc* book, LsmPass& io);
+// Simulate the book once with the paths of `asset` stored, then run the n passes on them
+// (each pass's asset must be `asset`); under the engine's lock; errors as the C ABI's,
+// message in thoth_gpu_last_error(). sim_ms is charged to the first pass.
+int thoth_lsm_passes(const ThothBookDesc* book, int asset, LsmPass* io, int n);

@@ -1180,12 +1180,8 @@ int32_t itm_threshold(double K, bool call)
 
 // One Longstaff-Schwartz pass (american.cu) on the stored paths of io.asset: simulate the
 // book, then fit a policy and value it on the same paths, or value the given policy.
-int lsm_pass_locked(const ThothBookDesc* book, LsmPass& io)
+int lsm_check(const Plan& P, const LsmPass& io)
 {
-    Plan P;
-    double sim_ms = 0;
-    int rc = simulate_device_locked(book, io.asset, P, &sim_ms);
-    if (rc) return rc;
     const int M = io.M;
     if (M < 2 || M > P.dp.n_steps + 1) return fail(THOTH_GPU_E_INVALID, "exercise grid outside the book's dates");
     if (!(io.norm > 0.0) || !std::isfinite(io.norm) || !std::isfinite(io.strike))
@@ -1194,51 +1190,68 @@ int lsm_pass_locked(const ThothBookDesc* book, LsmPass& io)
         return fail(THOTH_GPU_E_INVALID, "discount arrays must have one entry per exercise date");
     if (!io.fit && ((int)io.beta.size() != 3 * M || (int)io.fit_at.size() != M))
         return fail(THOTH_GPU_E_INVALID, "frozen policy does not match the exercise grid");
-    const int64_t N = P.paths;
-    if (N >= ((int64_t)1 << 27)) return fail(THOTH_GPU_E_TOO_LARGE, "American exercise needs fewer than 2^27 paths");
-    const int64_t want = (N + LSM_THREADS - 1) / LSM_THREADS;
-    int grid;
+    if (P.paths >= ((int64_t)1 << 27)) return fail(THOTH_GPU_E_TOO_LARGE, "American exercise needs fewer than 2^27 paths");
+    return THOTH_GPU_OK;
+}
+
+int lsm_status(int status)
+{
+    if (status == 2) return fail(THOTH_GPU_E_CUDA, "exercise fit: a wait timed out");
+    if (status == 3) return fail(THOTH_GPU_E_INVALID, "exercise fit: a cashflow or moneyness power is out of range (>= 2^36)");
+    if (status != 0) return fail(THOTH_GPU_E_CUDA, "exercise fit: kernel status " + std::to_string(status));
+    return THOTH_GPU_OK;
+}
+
+// the table block of one contract: df [M], disc [M], beta [3M], fit [M] (int)
+size_t lsm_tab_bytes(int M) { return sizeof(double) * 5 * (size_t)M + sizeof(int32_t) * (size_t)M; }
+
+void lsm_fill_tab(unsigned char* h, const LsmPass& io)
+{
+    const int M = io.M;
+    std::memcpy(h, io.df.data(), sizeof(double) * M);
+    std::memcpy(h + sizeof(double) * M, io.disc.data(), sizeof(double) * M);
     if (io.fit) {
-        const int cap = lsm_fit_max_grid(g_dev.sms);
-        if (cap < 1) return fail(THOTH_GPU_E_CUDA, "no resident CTA for the exercise fit kernel");
-        grid = (int)std::min<int64_t>(want, cap);
+        std::memset(h + sizeof(double) * 2 * M, 0, sizeof(double) * 3 * M + sizeof(int32_t) * M);
     } else {
-        grid = (int)std::min<int64_t>(want, (int64_t)8 * g_dev.sms);
+        std::memcpy(h + sizeof(double) * 2 * M, io.beta.data(), sizeof(double) * 3 * M);
+        std::memcpy(h + sizeof(double) * 5 * M, io.fit_at.data(), sizeof(int32_t) * M);
     }
-    grid = std::max(grid, 1);
-    // device scratch: per-path fit state, the compacted in-the-money lists, the date tables,
-    // partial sums, arrival counter, release flag and status
-    const int64_t threads = (int64_t)grid * LSM_THREADS;
-    const int64_t seg_len = 32 * ((N + threads - 1) / threads);
-    const size_t n_list = io.fit ? (size_t)(grid * (LSM_THREADS / 32)) * (size_t)seg_len : 0;
-    const size_t per_path = io.fit ? align256(sizeof(double) * (size_t)N) : 0;
-    const size_t tab = sizeof(double) * 5 * (size_t)M + sizeof(int32_t) * (size_t)M;
-    const size_t o_cf = 0, o_val = per_path;
-    const size_t o_cm = 2 * per_path, o_civ = o_cm + align256(sizeof(double) * n_list);
-    const size_t o_cidx = o_civ + align256(sizeof(double) * n_list);
-    const size_t o_tab = o_cidx + align256(sizeof(int32_t) * n_list);
-    const size_t o_part = o_tab + align256(tab);
-    const size_t o_acc = o_part + align256(sizeof(Fx128) * 2 * (size_t)grid * LSM_PART);
+}
+
+// the exact result sums of `grid` CTA rows
+void lsm_results(const Fx128* a, int grid, LsmPass& io)
+{
+    Fx128 tot[LSM_NACC] = {};
+    for (int c = 0; c < grid; c++)
+        for (int k = 0; k < LSM_NACC; k++) fx_add(tot[k], a[(size_t)c * LSM_NACC + k]);
+    io.sum = fx_to_double(tot[0]);
+    io.sum2 = fx_to_double(tot[1]);
+    io.euro = fx_to_double(tot[2]);
+}
+
+// value a frozen policy on the stored paths (lsm_apply_kernel)
+int lsm_apply_locked(const Plan& P, double sim_ms, LsmPass& io)
+{
+    int rc = lsm_check(P, io);
+    if (rc) return rc;
+    const int M = io.M;
+    const int64_t N = P.paths;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((N + LSM_THREADS - 1) / LSM_THREADS,
+                                                                 (int64_t)8 * g_dev.sms));
+    const size_t tab = lsm_tab_bytes(M);
+    const size_t o_tab = 0, o_acc = align256(tab);
     const size_t acc_bytes = sizeof(Fx128) * (size_t)grid * LSM_NACC;
     const size_t o_ctl = o_acc + align256(acc_bytes);
     rc = ensure_lsm(o_ctl + 256);
     if (rc) return rc;
-    const size_t back = acc_bytes + 2 * sizeof(int) + sizeof(float) + tab;
-    rc = ensure_pinned(std::max(tab, back));
+    rc = ensure_pinned(std::max(tab, acc_bytes + 2 * sizeof(int) + sizeof(float)));
     if (rc) return rc;
     unsigned char* base = g_dev.lsm;
     unsigned char* h = g_dev.pinned;
-    std::vector<int32_t> fit0(M, 0);
-    std::vector<double> beta0(3 * (size_t)M, 0.0);
-    const std::vector<double>& beta = io.fit ? beta0 : io.beta;
-    const std::vector<int32_t>& fit_at = io.fit ? fit0 : io.fit_at;
-    std::memcpy(h, io.df.data(), sizeof(double) * M);
-    std::memcpy(h + sizeof(double) * M, io.disc.data(), sizeof(double) * M);
-    std::memcpy(h + sizeof(double) * 2 * M, beta.data(), sizeof(double) * 3 * M);
-    std::memcpy(h + sizeof(double) * 5 * M, fit_at.data(), sizeof(int32_t) * M);
+    lsm_fill_tab(h, io);
     cudaStream_t st = g_dev.stream;
     CUDA_TRY(cudaMemcpyAsync(base + o_tab, h, tab, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(base + o_ctl, 0, 3 * sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(base + o_ctl, 0, sizeof(int), st));
     LsmArgs A;
     A.S = g_dev.paths;
     A.ld = P.paths;
@@ -1254,59 +1267,194 @@ int lsm_pass_locked(const ThothBookDesc* book, LsmPass& io)
     A.disc = A.df + M;
     A.beta = reinterpret_cast<double*>(base + o_tab) + 2 * (size_t)M;
     A.fit = reinterpret_cast<int*>(base + o_tab + sizeof(double) * 5 * (size_t)M);
-    A.cf = reinterpret_cast<double*>(base + o_cf);
-    A.val = reinterpret_cast<double*>(base + o_val);
-    A.seg_len = seg_len;
-    A.c_m = reinterpret_cast<double*>(base + o_cm);
-    A.c_iv = reinterpret_cast<double*>(base + o_civ);
-    A.c_idx = reinterpret_cast<int32_t*>(base + o_cidx);
-    A.part = reinterpret_cast<Fx128*>(base + o_part);
     A.acc = reinterpret_cast<Fx128*>(base + o_acc);
-    A.bar = reinterpret_cast<unsigned*>(base + o_ctl);
-    A.status = reinterpret_cast<int*>(base + o_ctl + sizeof(int));
-    A.done = reinterpret_cast<unsigned*>(base + o_ctl + 2 * sizeof(int));
-    if (!io.fit) {
-        A.cf = A.val = A.c_m = A.c_iv = nullptr;
-        A.c_idx = nullptr;
-    }
+    A.status = reinterpret_cast<int*>(base + o_ctl);
     CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
-    CUDA_TRY(io.fit ? launch_lsm_fit(A, grid, st) : launch_lsm_apply(A, grid, st));
+    CUDA_TRY(launch_lsm_apply(A, grid, st));
     CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
     CUDA_TRY(cudaMemcpyAsync(h, base + o_acc, acc_bytes, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(h + acc_bytes, base + o_ctl, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(h + acc_bytes, base + o_ctl, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(h + acc_bytes + 2 * sizeof(int), g_dev.paths, sizeof(float), cudaMemcpyDeviceToHost, st));
-    if (io.fit)
-        CUDA_TRY(cudaMemcpyAsync(h + acc_bytes + 2 * sizeof(int) + sizeof(float), base + o_tab, tab,
-                                 cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     float ms = 0;
     CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
     int status;
-    std::memcpy(&status, h + acc_bytes + sizeof(int), sizeof(int));
-    if (status == 2) return fail(THOTH_GPU_E_CUDA, "exercise fit: grid barrier timed out");
-    if (status == 3) return fail(THOTH_GPU_E_INVALID, "exercise fit: a cashflow or moneyness power is out of range (>= 2^36)");
-    if (status != 0) return fail(THOTH_GPU_E_CUDA, "exercise fit: kernel status " + std::to_string(status));
-    Fx128 tot[LSM_NACC] = {};
-    const Fx128* a = reinterpret_cast<const Fx128*>(h);
-    for (int c = 0; c < grid; c++)
-        for (int k = 0; k < LSM_NACC; k++) fx_add(tot[k], a[(size_t)c * LSM_NACC + k]);
-    io.sum = fx_to_double(tot[0]);
-    io.sum2 = fx_to_double(tot[1]);
-    io.euro = fx_to_double(tot[2]);
+    std::memcpy(&status, h + acc_bytes, sizeof(int));
+    if ((rc = lsm_status(status))) return rc;
+    lsm_results(reinterpret_cast<const Fx128*>(h), grid, io);
     float s0;
     std::memcpy(&s0, h + acc_bytes + 2 * sizeof(int), sizeof(float));
     io.s0 = s0;
-    if (io.fit) {
-        const unsigned char* tb = h + acc_bytes + 2 * sizeof(int) + sizeof(float);
-        io.beta.resize(3 * (size_t)M);
-        io.fit_at.resize(M);
-        std::memcpy(io.beta.data(), tb + sizeof(double) * 2 * M, sizeof(double) * 3 * M);
-        std::memcpy(io.fit_at.data(), tb + sizeof(double) * 5 * M, sizeof(int32_t) * M);
-    }
     io.paths = N;
     io.grid = grid;
     io.sim_ms = sim_ms;
     io.lsm_ms = ms;
+    return THOTH_GPU_OK;
+}
+
+// fit up to LSM_MAX_CONTRACTS policies on the stored paths in one launch (lsm_fit_kernel);
+// each pass gets its sums and policy, and the launch's device time
+int lsm_fit_batch_locked(const Plan& P, double sim_ms, LsmPass* const* io, int C)
+{
+    int rc = THOTH_GPU_OK;
+    if (C < 1 || C > LSM_MAX_CONTRACTS) return fail(THOTH_GPU_E_INVALID, "bad batch of exercise fits");
+    int Tmax = 0;
+    for (int k = 0; k < C; k++) {
+        if ((rc = lsm_check(P, *io[k]))) return rc;
+        Tmax = std::max(Tmax, io[k]->M);
+    }
+    const int64_t N = P.paths;
+    const int cap = lsm_fit_max_grid(g_dev.sms);
+    if (cap < 1) return fail(THOTH_GPU_E_CUDA, "no resident CTA for the exercise fit kernel");
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((N + LSM_THREADS - 1) / LSM_THREADS, cap));
+    const int64_t threads = (int64_t)grid * LSM_THREADS;
+    const int64_t seg_len = 32 * ((N + threads - 1) / threads);
+    const size_t n_list = (size_t)(grid * (LSM_THREADS / 32)) * (size_t)seg_len;
+    const size_t acc_bytes = sizeof(Fx128) * (size_t)grid * LSM_NACC;
+    // layout: [contracts][tables of every contract] (uploaded) | per contract: cf, val, lists,
+    // totals, result rows | control
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = align256(o + bytes);
+        return at;
+    };
+    const size_t o_ct = take(sizeof(LsmContract) * C);
+    std::vector<size_t> o_tab(C);
+    for (int k = 0; k < C; k++) o_tab[k] = take(lsm_tab_bytes(io[k]->M));
+    const size_t up_bytes = o;
+    const size_t o_zero = o;
+    std::vector<size_t> o_tot(C);
+    for (int k = 0; k < C; k++) o_tot[k] = take(sizeof(unsigned long long) * 3 * (size_t)io[k]->M * LSM_PART);
+    const size_t o_ctl = take(16);
+    const size_t zero_bytes = o - o_zero;
+    std::vector<size_t> o_cf(C), o_val(C), o_cm(C), o_civ(C), o_cidx(C), o_acc(C);
+    for (int k = 0; k < C; k++) {
+        o_cf[k] = take(sizeof(double) * (size_t)N);
+        o_val[k] = take(sizeof(double) * (size_t)N);
+        o_cm[k] = take(sizeof(double) * n_list);
+        o_civ[k] = take(sizeof(double) * n_list);
+        o_cidx[k] = take(sizeof(int32_t) * n_list);
+        o_acc[k] = take(acc_bytes);
+    }
+    rc = ensure_lsm(o);
+    if (rc) return rc;
+    size_t back = sizeof(int) + sizeof(float);
+    for (int k = 0; k < C; k++) back += acc_bytes + lsm_tab_bytes(io[k]->M);
+    rc = ensure_pinned(std::max(up_bytes, back));
+    if (rc) return rc;
+    unsigned char* base = g_dev.lsm;
+    unsigned char* h = g_dev.pinned;
+    LsmContract* ct = reinterpret_cast<LsmContract*>(h + o_ct);
+    for (int k = 0; k < C; k++) {
+        const LsmPass& q = *io[k];
+        const int M = q.M;
+        lsm_fill_tab(h + o_tab[k], q);
+        LsmContract& K = ct[k];
+        K.M = M;
+        K.call = q.call;
+        K.min_itm = q.min_itm;
+        K.itm_bits = itm_threshold(q.strike, q.call != 0);
+        K.strike = q.strike;
+        K.norm = q.norm;
+        K.inv_norm = 1.0 / q.norm;
+        K.df = reinterpret_cast<const double*>(base + o_tab[k]);
+        K.disc = K.df + M;
+        K.beta = reinterpret_cast<double*>(base + o_tab[k]) + 2 * (size_t)M;
+        K.fit = reinterpret_cast<int*>(base + o_tab[k] + sizeof(double) * 5 * (size_t)M);
+        K.cf = reinterpret_cast<double*>(base + o_cf[k]);
+        K.val = reinterpret_cast<double*>(base + o_val[k]);
+        K.c_idx = reinterpret_cast<int32_t*>(base + o_cidx[k]);
+        K.c_m = reinterpret_cast<double*>(base + o_cm[k]);
+        K.c_iv = reinterpret_cast<double*>(base + o_civ[k]);
+        K.tot = reinterpret_cast<unsigned long long*>(base + o_tot[k]);
+        K.acc = reinterpret_cast<Fx128*>(base + o_acc[k]);
+    }
+    cudaStream_t st = g_dev.stream;
+    CUDA_TRY(cudaMemcpyAsync(base, h, up_bytes, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(base + o_zero, 0, zero_bytes, st));
+    LsmFitArgs A;
+    A.S = g_dev.paths;
+    A.ld = P.paths;
+    A.n = N;
+    A.C = C;
+    A.Tmax = Tmax;
+    A.ct = reinterpret_cast<const LsmContract*>(base + o_ct);
+    A.seg_len = seg_len;
+    A.bar = reinterpret_cast<unsigned*>(base + o_ctl);
+    A.done = reinterpret_cast<unsigned*>(base + o_ctl + 4);
+    A.status = reinterpret_cast<int*>(base + o_ctl + 8);
+    CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
+    CUDA_TRY(launch_lsm_fit(A, grid, st));
+    CUDA_TRY(cudaEventRecord(g_dev.ev1, st));
+    size_t hb = 0;
+    CUDA_TRY(cudaMemcpyAsync(h + hb, base + o_ctl + 8, sizeof(int), cudaMemcpyDeviceToHost, st));
+    hb += sizeof(int);
+    CUDA_TRY(cudaMemcpyAsync(h + hb, g_dev.paths, sizeof(float), cudaMemcpyDeviceToHost, st));
+    hb += sizeof(float);
+    std::vector<size_t> h_acc(C), h_tab(C);
+    for (int k = 0; k < C; k++) {
+        h_acc[k] = hb;
+        CUDA_TRY(cudaMemcpyAsync(h + hb, base + o_acc[k], acc_bytes, cudaMemcpyDeviceToHost, st));
+        hb += acc_bytes;
+        h_tab[k] = hb;
+        CUDA_TRY(cudaMemcpyAsync(h + hb, base + o_tab[k], lsm_tab_bytes(io[k]->M), cudaMemcpyDeviceToHost, st));
+        hb += lsm_tab_bytes(io[k]->M);
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+    int status;
+    std::memcpy(&status, h, sizeof(int));
+    if ((rc = lsm_status(status))) return rc;
+    float s0;
+    std::memcpy(&s0, h + sizeof(int), sizeof(float));
+    for (int k = 0; k < C; k++) {
+        LsmPass& q = *io[k];
+        const int M = q.M;
+        // unaligned pinned offsets: copy the sums out before reading them
+        std::vector<Fx128> acc((size_t)grid * LSM_NACC);
+        std::memcpy(acc.data(), h + h_acc[k], acc_bytes);
+        lsm_results(acc.data(), grid, q);
+        q.beta.resize(3 * (size_t)M);
+        q.fit_at.resize(M);
+        std::memcpy(q.beta.data(), h + h_tab[k] + sizeof(double) * 2 * M, sizeof(double) * 3 * M);
+        std::memcpy(q.fit_at.data(), h + h_tab[k] + sizeof(double) * 5 * M, sizeof(int32_t) * M);
+        q.s0 = s0;
+        q.paths = N;
+        q.grid = grid;
+        q.sim_ms = k == 0 ? sim_ms : 0.0;
+        q.lsm_ms = k == 0 ? ms : 0.0; // one launch for the batch: its time on the first pass
+    }
+    return THOTH_GPU_OK;
+}
+
+// simulate the book once with the paths of `asset` stored, then run every pass on them
+int lsm_passes_locked(const ThothBookDesc* book, int asset, LsmPass* io, int n)
+{
+    Plan P;
+    double sim_ms = 0;
+    int rc = simulate_device_locked(book, asset, P, &sim_ms);
+    if (rc) return rc;
+    // the fits in batches of LSM_MAX_CONTRACTS launches, the frozen-policy applies one by one
+    std::vector<LsmPass*> fits;
+    for (int k = 0; k < n; k++) {
+        if (io[k].asset != asset) return fail(THOTH_GPU_E_INVALID, "exercise pass on another asset's paths");
+        if (io[k].fit) fits.push_back(&io[k]);
+    }
+    bool first = true;
+    for (size_t b = 0; b < fits.size(); b += LSM_MAX_CONTRACTS) {
+        const int C = (int)std::min<size_t>(LSM_MAX_CONTRACTS, fits.size() - b);
+        rc = lsm_fit_batch_locked(P, first ? sim_ms : 0.0, fits.data() + b, C);
+        if (rc) return rc;
+        first = false;
+    }
+    for (int k = 0; k < n; k++) {
+        if (io[k].fit) continue;
+        rc = lsm_apply_locked(P, first ? sim_ms : 0.0, io[k]);
+        if (rc) return rc;
+        first = false;
+    }
     return THOTH_GPU_OK;
 }
 
@@ -2002,13 +2150,13 @@ int calibrate_locked(ThothLeverageCalib* c)
     return THOTH_GPU_OK;
 }
 
-// the exercise pass of thoth_gpu_price_american (american_host.cu)
-int thoth_lsm_pass(const ThothBookDesc* book, LsmPass& io)
+// the exercise passes of thoth_gpu_price_american (american_host.cu)
+int thoth_lsm_passes(const ThothBookDesc* book, int asset, LsmPass* io, int n)
 {
     try {
-        if (!book) return fail(THOTH_GPU_E_INVALID, "null book");
+        if (!book || (!io && n > 0) || n < 0) return fail(THOTH_GPU_E_INVALID, "null book or passes");
         std::lock_guard<std::mutex> lk(g_mu);
-        return lsm_pass_locked(book, io);
+        return lsm_passes_locked(book, asset, io, n);
     } catch (const std::bad_alloc&) {
         return fail(THOTH_GPU_E_NOMEM, "out of host memory");
     } catch (const std::exception& e) {
