@@ -34,6 +34,8 @@ def test_abi_layout_matches_header():
 int main(void){
  printf("%zu %zu %zu %zu %zu\n", sizeof(ThothAsset), sizeof(ThothProduct), sizeof(ThothBookDesc), sizeof(ThothBookResult), sizeof(ThothGbmResult));
  printf("%zu %zu %zu %zu\n", offsetof(ThothAsset, lev_values), offsetof(ThothProduct, weights), offsetof(ThothBookDesc, seed), offsetof(ThothBookResult, device_ms));
+ printf("%zu %zu %zu %zu\n", sizeof(ThothAmerican), offsetof(ThothAmerican, beta), offsetof(ThothAmerican, theta), offsetof(ThothAmerican, exercise_ms));
+ printf("%zu %zu %zu %zu\n", sizeof(ThothLeverageCalib), offsetof(ThothLeverageCalib, local_vol), offsetof(ThothLeverageCalib, seed), offsetof(ThothLeverageCalib, leverage));
  return 0;}
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -46,7 +48,11 @@ int main(void){
     want = [C.sizeof(abi.ThothAsset), C.sizeof(abi.ThothProduct), C.sizeof(abi.ThothBookDesc),
             C.sizeof(abi.ThothBookResult), C.sizeof(abi.ThothGbmResult),
             abi.ThothAsset.lev_values.offset, abi.ThothProduct.weights.offset, abi.ThothBookDesc.seed.offset,
-            abi.ThothBookResult.device_ms.offset]
+            abi.ThothBookResult.device_ms.offset,
+            C.sizeof(abi.ThothAmerican), abi.ThothAmerican.beta.offset, abi.ThothAmerican.theta.offset,
+            abi.ThothAmerican.exercise_ms.offset,
+            C.sizeof(abi.ThothLeverageCalib), abi.ThothLeverageCalib.local_vol.offset, abi.ThothLeverageCalib.seed.offset,
+            abi.ThothLeverageCalib.leverage.offset]
     assert got == want
 
 
@@ -211,3 +217,33 @@ def test_running_groups_share_nested_prefixes():
     assert G.plan_summary(b)["groups"] == 5                     # another quanto shift
     b.add_variance(h, 60, strike_variance=0.04, obs=np.arange(5, 61, 5))
     assert G.plan_summary(b)["groups"] == 6                     # discrete observations: own group
+
+
+def test_american_and_calibration_inputs_are_checked_on_the_host():
+    """Rejected before any device work, so these run without a GPU."""
+    b = abi.Book(days=[0, 30, 60], paths=1000)
+    a = b.add_gbm(100.0, 0.3, 0.05)
+    b.add_vanilla(a, 100.0, 2, abi.PUT, zero_rate=0.05)
+    b.add_barrier(a, 100.0, 2, 80.0, up=False, knock_in=False, monitor=[1, 2])
+    b.add_vanilla(a, 100.0, 2, abi.CALL, zero_rate=0.05, quanto=0.01)
+    for products, code in (([], abi.THOTH_GPU_E_INVALID), ([5], abi.THOTH_GPU_E_INVALID),
+                           ([1], abi.THOTH_GPU_E_UNSUPPORTED), ([0, 2], abi.THOTH_GPU_E_UNSUPPORTED)):
+        with pytest.raises(G.ThothGpuError) as e:
+            G.price_american_book(b, products)
+        assert e.value.code == code, products
+    c = W.lsv_calibration(horizon_days=5, particles=256)
+    c.bins = 500
+    with pytest.raises(G.ThothGpuError) as e:
+        G.calibrate_leverage(c)
+    assert e.value.code == abi.THOTH_GPU_E_INVALID
+    for change in ("days", "spot", "ln_step"):
+        c = W.lsv_calibration(horizon_days=5, particles=256)
+        if change == "days":
+            c.days = np.ascontiguousarray([0, 1, 1, 3, 4, 5], dtype=np.int32)
+        elif change == "spot":
+            c.spot = -1.0
+        else:
+            c.ln_step = np.ascontiguousarray(np.zeros_like(c.ln_step))
+        with pytest.raises(G.ThothGpuError) as e:
+            G.calibrate_leverage(c)
+        assert e.value.code == abi.THOTH_GPU_E_INVALID, change
