@@ -235,3 +235,32 @@ def test_book_call_equals_contract_by_contract(gpu):
         for k in ("premium", "trust", "european", "delta", "gamma", "vega", "rho", "theta", "fitted_dates"):
             assert r[k] == alone[k], (p, k, r[k], alone[k])
         np.testing.assert_array_equal(r["beta"], alone["beta"])
+
+
+def test_american_on_a_calibrated_lsv_name(gpu):
+    """Leverage calibrated on the device, LSV paths stored, the exercise fit on them: the fit
+    equals the oracle's on the same stored paths."""
+    from thoth_gb300 import workloads as W
+    c = W.lsv_calibration(horizon_days=182, particles=8192)
+    lev, _ = gpu.calibrate_leverage(c)
+    h = c.heston
+    b = abi.Book(days=c.days, paths=30000)
+    a = b.add_heston(100.0, h["v0"], h["kappa"], h["theta"], h["xi"], h["rho"], 0.02,
+                     leverage=(c.ln_step, c.offset, lev))
+    b.add_vanilla(a, 100.0, 182, abi.PUT, zero_rate=0.03)
+    r = gpu.price_american(b, 0)
+    o = oracle_pass(gpu, b)
+    assert_same_fit(r, o, b.n_dates)
+
+
+def test_book_call_past_one_fit_launch(gpu):
+    """70 contracts on one name: two fit launches (64 + 6), each contract as if alone."""
+    b = abi.Book(days=np.asarray(DAYS), paths=4096)
+    a = b.add_gbm(100.0, 0.30, 0.06)
+    for k in range(70):
+        b.add_vanilla(a, 70.0 + k, 13 if k % 3 else 7, abi.PUT if k % 2 else abi.CALL, zero_rate=0.06)
+    together = gpu.price_american_book(b, list(range(70)))
+    for p in (0, 1, 63, 64, 69):
+        alone = gpu.price_american(b, p)
+        assert together[p]["premium"] == alone["premium"], p
+        np.testing.assert_array_equal(together[p]["beta"], alone["beta"])
