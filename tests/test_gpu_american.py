@@ -264,3 +264,14 @@ def test_book_call_past_one_fit_launch(gpu):
         alone = gpu.price_american(b, p)
         assert together[p]["premium"] == alone["premium"], p
         np.testing.assert_array_equal(together[p]["beta"], alone["beta"])
+
+
+def test_zero_strike_normalises_by_the_initial_spot(gpu):
+    """Vanilla::LsmBasisNorm (vanilla.hpp:38-41): a non-positive strike regresses on S / S0,
+    S0 the paths' spot at date 0 (stored in single precision)."""
+    b = vanilla_book(typ=abi.CALL, K=0.0, paths=20000, r=0.02)
+    b.assets[0]["carry"] = b.assets[0]["carry"] - 0.05
+    r = gpu.price_american(b, 0)
+    S, _ = gpu.simulate_paths(b, 0)
+    o = am.fit(S, b.t, rates_of(b), 0.0, True, float(np.float32(100.0)))
+    assert r["premium"] == o["premium"] and r["fitted_dates"] == int(o["has_fit"].sum())

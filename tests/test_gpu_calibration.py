@@ -102,3 +102,13 @@ def test_invalid_inputs(gpu):
     c.days = np.ascontiguousarray(c.days[::-1])
     with pytest.raises(gpu.ThothGpuError):
         gpu.calibrate_leverage(c)
+
+
+@pytest.mark.parametrize("particles,bins,min_count", [(1000, 30, 20), (700, 12, 100), (4099, 1, 1)])
+def test_uneven_ensembles_and_thin_bins_match_the_oracle(gpu, particles, bins, min_count):
+    """Particle counts off the warp size, every bin thin (the ensemble mean everywhere), and
+    one bin: the device follows the oracle."""
+    c = W.lsv_calibration(horizon_days=30, particles=particles)
+    c.bins, c.min_bin_count = bins, min_count
+    L, _ = gpu.calibrate_leverage(c)
+    np.testing.assert_allclose(L, oracle.calibrate_leverage(c), rtol=1e-9, atol=0)
