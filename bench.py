@@ -138,6 +138,12 @@ def cpu_baseline(sample_paths, threads):
                       % (sample_paths, n_steps, threads, dt)}
 
 
+def one_core_baseline(sample_paths=1 << 13):
+    """The same oracle on one thread: the single-core figure beside the all-core one."""
+    c = cpu_baseline(sample_paths, 1)
+    return {"value": c["value"], "unit": c["unit"], "cores": 1, "sample": c["sample"]}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -152,7 +158,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * PATHS * n_steps / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(1),
-            "cpu_baseline": dict(vals[-1], value=v),
+            "cpu_baseline": dict(vals[-1], value=v, one_core=one_core_baseline()),
             "e2e": {"value": v, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference's CPU Monte-Carlo restated bit-exactly in oracle/thoth_oracle.c, all host "
                     "threads, each step a bounded sample of the workload; ms_per_step scaled to 2^20 paths"}
@@ -458,6 +464,7 @@ def run_gpu(args):
             "wall_s_timed_region": wall,
         }
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample_paths, os.cpu_count() or 1)
+        line["cpu_baseline"]["one_core"] = one_core_baseline()
         if not args.no_lsv:
             line["lsv_book"] = lsv_book_section(G, flush, args.steps)
         if not args.no_paths:
