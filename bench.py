@@ -29,6 +29,7 @@ sys.path.insert(0, ROOT)
 PATHS = 1 << 20
 STEPS_PER_YEAR = 252
 FLOPS_PER_PATH_STEP = 96  # algorithmic FP32 flops of a Heston-QE + Andersen path-step (FMA = 2)
+MUFU_PER_PATH_STEP = 8  # algorithmic special-function ops of the same path-step (rcp, sqrt, ...)
 # DRAM bytes per launch of the book kernel from the ncu capture summarised in
 # profiles/book_kernel_heston_grid.md (a 2^18-path capture; the traffic is the
 # plan, the Sobol tables and the per-CTA sums, which do not grow with paths)
@@ -395,6 +396,7 @@ def run_gpu(args):
     book = workload(rank)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     peak_fp32 = G.measure_fp32_peak()
+    peak_mufu = G.measure_mufu_peak()
 
     def barrier():
         torch.cuda.synchronize()
@@ -447,6 +449,7 @@ def run_gpu(args):
 
     if rank == 0:
         achieved = FLOPS_PER_PATH_STEP * PATHS * n_steps / (ms * 1e-3) / 1e12
+        mufu = MUFU_PER_PATH_STEP * PATHS * n_steps / (ms * 1e-3) / 1e9
         line = {
             "metric": "path-steps/sec", "value": value, "unit": "path-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -459,7 +462,11 @@ def run_gpu(args):
                          "frac": achieved / peak_fp32, "traffic": NCU_DRAM_BYTES_PER_LAUNCH,
                          "peak_source": "FMA microbenchmark in this run (thoth_gpu_measure_fp32_peak); "
                                         "MEASURED_PEAKS.json records no FP32 figure",
-                         "flops_per_unit": FLOPS_PER_PATH_STEP, "unit_of_work": "path-step"},
+                         "flops_per_unit": FLOPS_PER_PATH_STEP, "unit_of_work": "path-step",
+                         "mufu": {"achieved": mufu, "peak": peak_mufu, "unit": "Gop/s", "frac": mufu / peak_mufu,
+                                  "ops_per_unit": MUFU_PER_PATH_STEP,
+                                  "peak_source": "reciprocal-square-root microbenchmark in this run "
+                                                 "(thoth_gpu_measure_mufu_peak)"}},
             "clocks": clk.summary(),
             "wall_s_timed_region": wall,
         }

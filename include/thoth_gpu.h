@@ -206,8 +206,13 @@ int thoth_gpu_book_destroy(ThothBookHandle* handle);
 
 /* Measurement hook, no reference counterpart: FP32 FMA throughput of the
  * device from a kernel of independent FMA chains; *tflops = 2 flops per FMA
- * over the kernel's CUDA-event time; *sm_mhz = the implied SM clock. */
+ * over the kernel's CUDA-event time; *ms = that time. */
 int thoth_gpu_measure_fp32_peak(double* tflops, double* ms);
+
+/* Measurement hook, no reference counterpart: special-function-unit (MUFU)
+ * throughput from a kernel of independent reciprocal-square-root chains;
+ * *gops = 10^9 operations a second over the kernel's CUDA-event time; *ms = that time. */
+int thoth_gpu_measure_mufu_peak(double* gops, double* ms);
 
 /* Capacity of the device array behind thoth_gpu_price_book_noalloc. */
 #define THOTH_NOALLOC_SCRATCH_BYTES (2u << 20)

@@ -23,3 +23,12 @@ def test_cpp_dropin(gpu):
     parity = math.exp(-0.03) * (100 * math.exp(0.02) - 100)                      # df (F - K)
     assert abs((call - put) - parity) < 3 * book_trust + 1e-3
     assert "error" in lines and "paths must be > 1" in out.stdout
+
+
+def test_peak_microbenchmarks_are_plausible(gpu):
+    """The roofline denominators the benchmark measures in its own run: FP32 FMA and
+    special-function throughput of one GB300 (152 SMs, at most 2.07 GHz)."""
+    tf = gpu.measure_fp32_peak()
+    assert 20.0 < tf < 90.0           # 152 x 128 lanes x 2 flops x clock
+    gops = gpu.measure_mufu_peak()
+    assert 500.0 < gops < 25000.0     # 152 SMs x (16 .. 64) ops a clock x clock

@@ -51,6 +51,7 @@ def lib():
         L.thoth_gpu_book_run.argtypes = [C.c_void_p, C.POINTER(abi.ThothBookResult)]
         L.thoth_gpu_book_destroy.argtypes = [C.c_void_p]
         L.thoth_gpu_measure_fp32_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.thoth_gpu_measure_mufu_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
         L.thoth_gpu_bump_greeks.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBumpGreeks)]
         L.thoth_gpu_bump_greeks_last_error.restype = C.c_char_p
@@ -311,6 +312,13 @@ def measure_fp32_peak():
     tf, ms = C.c_double(), C.c_double()
     _check(lib().thoth_gpu_measure_fp32_peak(C.byref(tf), C.byref(ms)))
     return tf.value
+
+
+def measure_mufu_peak():
+    """Special-function-unit throughput of the device (reciprocal square roots), Gop/s."""
+    g, ms = C.c_double(), C.c_double()
+    _check(lib().thoth_gpu_measure_mufu_peak(C.byref(g), C.byref(ms)))
+    return g.value
 
 
 def to_bf16_bits(x):

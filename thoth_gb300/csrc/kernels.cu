@@ -867,6 +867,32 @@ cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// ---- MUFU peak microbenchmark: 8 independent reciprocal-square-root chains per thread ----
+// x -> 1 / sqrt(x) keeps every chain positive and finite (it converges to 1); with -ftz each
+// rsqrtf is one special-function-unit instruction.
+__global__ void __launch_bounds__(256) mufu_peak_kernel(float* out, int iters)
+{
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = 1.0f + (float)(threadIdx.x + k) * 1e-3f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) x[k] = rsqrtf(x[k]);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == 1.2345f) out[blockIdx.x] = s; // keeps the chains alive
+}
+
+cudaError_t launch_mufu_peak(float* out, int blocks, int iters, cudaStream_t st)
+{
+    mufu_peak_kernel<<<blocks, 256, 0, st>>>(out, iters);
+    return cudaGetLastError();
+}
+
 // ---- launch wrappers --------------------------------------------------------
 // Launch shapes. Single-asset variants come in four: (log2 paths per tile,
 // paths per thread) = (8, 2), (8, 1), (7, 1), (7, 2), i.e. 128, 256, 128 and 64

@@ -38,6 +38,7 @@ cudaError_t launch_quantile(const uint32_t* x, int64_t n, float* out, cudaStream
 cudaError_t launch_bridge(const DevPlan& P, int grid, size_t smem, float* out, cudaStream_t st);
 cudaError_t launch_gather_low(const uint32_t* lo_all, const int* order, int n, int T, uint32_t* out, cudaStream_t st);
 cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st);
+cudaError_t launch_mufu_peak(float* out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_tc_gemm_test(const void* A, const void* B, int N, int K, float* D, int* status, cudaStream_t st);
 } // namespace thoth
 
@@ -2388,6 +2389,35 @@ int thoth_gpu_measure_fp32_peak(double* tflops, double* ms_out)
         CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
         const double fmas = (double)blocks * 256 * iters * 16 * 8;
         *tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
+        if (ms_out) *ms_out = ms;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_measure_mufu_peak(double* gops, double* ms_out)
+{
+    try {
+        if (!gops) return fail(THOTH_GPU_E_INVALID, "null output");
+        std::lock_guard<std::mutex> lk(g_mu);
+        int rc = ensure_device();
+        if (rc) return rc;
+        rc = ensure_arena(1 << 20);
+        if (rc) return rc;
+        const int blocks = g_dev.sms * 8, iters = 1024;
+        float* d = reinterpret_cast<float*>(g_dev.arena);
+        CUDA_TRY(launch_mufu_peak(d, blocks, 16, g_dev.stream)); // warm-up
+        CUDA_TRY(cudaEventRecord(g_dev.ev0, g_dev.stream));
+        CUDA_TRY(launch_mufu_peak(d, blocks, iters, g_dev.stream));
+        CUDA_TRY(cudaEventRecord(g_dev.ev1, g_dev.stream));
+        CUDA_TRY(cudaEventSynchronize(g_dev.ev1));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, g_dev.ev0, g_dev.ev1));
+        const double ops = (double)blocks * 256 * iters * 16 * 8;
+        *gops = ops / (ms * 1e-3) / 1e9;
         if (ms_out) *ms_out = ms;
         return THOTH_GPU_OK;
     } catch (const std::bad_alloc&) {
