@@ -124,3 +124,56 @@ def test_reference_properties_on_exact_gbm_paths():
     # the tree itself: European limit and early-exercise premium
     assert am.binomial(100.0, 100.0, 1.0, 0.08, 0.0, 0.30, call=False, american=False) == pytest.approx(euro, abs=1e-2)
     assert am.binomial(60.0, 100.0, 1.0, 0.08, 0.0, 0.30, call=False) == pytest.approx(40.0, abs=1e-9)
+
+
+def _fma32(a, b, c):
+    """Single-precision fused multiply-add: the product of two floats is exact in double,
+    one rounding to double of the sum, then to float (within the screen's bound either way)."""
+    return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
+
+
+def _screen32(s, K, norm, b, call):
+    """The apply kernel's single-precision screen of the exercise test (american.cu,
+    exercise_screened), restated in numpy float32: +1 exercise, -1 hold, 0 left to double."""
+    f = np.float32
+    sf = s.astype(f)
+    Kf = f(K)
+    inv = f(1.0 / norm)
+    m = sf * inv
+    iv = (sf - Kf) if call else (Kf - sf)
+    b0, b1, b2 = (x.astype(f) for x in b)
+    c = _fma32(_fma32(b2, m, b1), m, b0)
+    d = iv - c
+    am_ = np.abs(m)
+    mag = _fma32(np.abs(b2) * am_, am_, _fma32(np.abs(b1), am_, np.abs(b0))) + (abs(Kf) + np.abs(sf))
+    e = _fma32(mag, np.full_like(mag, f(2.0 ** -19)), np.full_like(mag, f(1e-30)))
+    return np.where(d > e, 1, np.where(d < -e, -1, 0))
+
+
+@pytest.mark.parametrize("call", [False, True])
+def test_single_precision_screen_never_contradicts_the_double_test(call):
+    """Wherever the screen decides, it decides as the reference's double-precision test
+    iv >= (b0 + b1 m) + (b2 m) m does; it leaves only a thin band around the boundary."""
+    rng = np.random.default_rng(7 + call)
+    n = 400000
+    K = 100.0
+    s = (K * np.exp(0.25 * rng.standard_normal(n))).astype(np.float32)
+    sd = s.astype(np.float64)
+    iv = (sd - K) if call else (K - sd)
+    m = sd / K
+    b1 = 60.0 * rng.standard_normal(n)
+    b2 = 30.0 * rng.standard_normal(n)
+    # b0 puts the continuation a signed distance from the intrinsic value, from 1e-14 to 10
+    gap = np.sign(rng.standard_normal(n)) * 10.0 ** rng.uniform(-14, 1, n)
+    b0 = iv - (b1 * m + (b2 * m) * m) - gap
+    cont = (b0 + b1 * m) + (b2 * m) * m
+    exact = np.where(iv >= cont, 1, -1)
+    sc = _screen32(s, K, K, (b0, b1, b2), call)
+    decided = sc != 0
+    assert np.array_equal(sc[decided], exact[decided])
+    # gaps above the bound are decided: the band is at most 2^-19 mag wide
+    mag = np.abs(K) + np.abs(sd) + np.abs(b0) + np.abs(b1 * m) + np.abs(b2) * m * m
+    assert decided[np.abs(gap) > 2.0 ** -18 * mag].all()
+    # on generic policies the band is rare
+    sg = _screen32(s, K, K, (iv - 5.0 * rng.standard_normal(n), b1 * 0.0, b2 * 0.0), call)
+    assert np.mean(sg == 0) < 1e-3

@@ -145,6 +145,31 @@ def test_frozen_policy_greeks_equal_the_oracle(gpu):
         assert g[k] == pytest.approx(w, rel=1e-12, abs=1e-13), (k, g[k], w)
 
 
+def test_frozen_policy_on_daily_dates_equals_the_oracle(gpu):
+    """The apply walk on many dates and paths: single-precision screening of each exercise
+    test, double precision near the boundary; the bumped premiums equal the oracle's."""
+    days = np.arange(0, 151)
+    b = vanilla_book(paths=(1 << 16) + 3, days=days, K=104.0, model="heston")
+    S0 = b.assets[0]["spot"]
+    g = gpu.price_american(b, 0, flags=abi.BUMP_DELTA | abi.BUMP_GAMMA)
+    base = oracle_pass(gpu, b)
+    A0 = base["premium"]
+    assert g["premium"] == A0
+
+    def frozen(book):
+        return oracle_pass(gpu, book, policy=base)["premium"]
+
+    def spot(h):
+        c = b.copy()
+        c.assets[0]["spot"] *= 1 + h
+        return frozen(c)
+
+    want = {"delta": (spot(0.01) - A0) / (0.01 * S0),
+            "gamma": (spot(0.1) - 2.0 * A0 + spot(-0.1)) / ((0.1 * S0) * (0.1 * S0))}
+    for k, w in want.items():
+        assert g[k] == pytest.approx(w, rel=1e-12, abs=1e-13), (k, g[k], w)
+
+
 def test_reference_american_call_equals_the_european_call(gpu):
     """test_american.cpp:8-20: no dividend, so never exercised early (200 000 paths)."""
     b = vanilla_book(typ=abi.CALL, paths=200000)

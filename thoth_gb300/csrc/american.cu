@@ -401,6 +401,35 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmFitArg
     if (bad) atomicExch(A.status, 3);
 }
 
+// The frozen policy's exercise test at date t for an in-the-money spot sf: the reference's
+// double-precision test iv >= b0 + b1 m + b2 m^2 (iv = phi (S - K), m = S / norm), decided in
+// single precision wherever that cannot differ from it.
+// With u = 2^-24 and mag = |K| + |S| + |b0| + |b1 m| + |b2| m^2, the single-precision
+// difference d = iv - c (the inputs rounded to float, then five rounded operations) is within
+// 8 u mag of the real iv - c, and the double-precision operands are within 6 * 2^-53 mag of it.
+// So |d| > 2^-19 mag (four times that bound, computed from the rounded inputs) fixes the sign of
+// the double-precision difference and hence the test; an absolute floor keeps underflow out of
+// the bound. Inputs too large for single precision give an infinite or NaN d or bound and take
+// the double-precision test, as does the thin band around the exercise boundary.
+template <class K>
+__device__ __forceinline__ bool exercise_screened(float sf, float4 b, int t, const K& A)
+{
+    const float m = sf * A.inv_norm_f;
+    const float iv = A.call ? sf - A.strike_f : A.strike_f - sf;
+    const float c = fmaf(fmaf(b.z, m, b.y), m, b.x);
+    const float d = iv - c;
+    const float am = fabsf(m);
+    const float mag = fmaf(fabsf(b.z) * am, am, fmaf(fabsf(b.y), am, fabsf(b.x))) + (fabsf(A.strike_f) + fabsf(sf));
+    const float e = fmaf(mag, 0x1p-19f, 1e-30f);
+    if (d > e) return true;
+    if (d < -e) return false;
+    const double s = (double)sf;
+    const double ivd = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
+    return ivd >= continuation(A.beta[3 * t], A.beta[3 * t + 1], A.beta[3 * t + 2], moneyness(s, A));
+}
+
+constexpr int APPLY_UNROLL = 8; // dates whose spots one thread loads together
+
 __global__ void __launch_bounds__(LSM_THREADS) lsm_apply_kernel(const LsmArgs A)
 {
     __shared__ Fx128 s_w[LSM_WARPS][LSM_PART];
@@ -410,17 +439,28 @@ __global__ void __launch_bounds__(LSM_THREADS) lsm_apply_kernel(const LsmArgs A)
     Fx128 v = {0, 0}, v2 = {0, 0}, eu = {0, 0};
     const float* last = A.S + (int64_t)(A.M - 1) * A.ld;
     const double dT = A.disc[A.M - 1];
+    const int tend = A.M - 1; // exercise dates 1 .. M-2; the maturity pays the European payoff
     for (int64_t p = g0; p < A.n; p += T) {
         double x = -1.0;
-        for (int t = 1; t < A.M - 1; ++t) {
-            if (!A.fit[t]) continue;
-            const float sf = A.S[(int64_t)t * A.ld + p];
-            if (!in_the_money(sf, A)) continue;
-            const double s = (double)sf;
-            const double iv = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
-            if (iv >= continuation(A.beta[3 * t], A.beta[3 * t + 1], A.beta[3 * t + 2], moneyness(s, A))) {
-                x = __dmul_rn(iv, A.disc[t]);
-                break;
+        // forward walk to the first exercise, APPLY_UNROLL dates at a time so that their
+        // loads are in flight together (row t + u of the date-major paths: coalesced in p)
+        for (int t = 1; t < tend && x < 0.0; t += APPLY_UNROLL) {
+            float sv[APPLY_UNROLL];
+#pragma unroll
+            for (int u = 0; u < APPLY_UNROLL; ++u)
+                sv[u] = t + u < tend ? __ldg(A.S + (int64_t)(t + u) * A.ld + p) : 0.f;
+#pragma unroll
+            for (int u = 0; u < APPLY_UNROLL; ++u) {
+                const int tu = t + u;
+                if (tu >= tend) break;
+                const float4 b = __ldg(A.screen + tu);
+                if (b.w == 0.f || !in_the_money(sv[u], A)) continue;
+                if (exercise_screened(sv[u], b, tu, A)) {
+                    const double s = (double)sv[u];
+                    const double iv = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
+                    x = __dmul_rn(iv, A.disc[tu]);
+                    break;
+                }
             }
         }
         const double e = __dmul_rn(intrinsic((double)last[p], A.strike, A.call), dT);

@@ -37,6 +37,10 @@ struct LsmArgs {
     int* fit;             // [M] 1 where date t has a regression
     Fx128* acc;           // [grid][LSM_NACC] per-CTA result sums
     int* status;          // 0 ok; 3 an addend out of range
+    // apply only: the exercise test in single precision first (exercise_screened)
+    const float4* screen; // [M] b0, b1, b2 rounded to float; w = 1 where date t has a regression
+    float strike_f;       // strike rounded to float
+    float inv_norm_f;     // 1 / norm rounded to float
 };
 
 // One contract of a batched fit: its exercise grid, payoff, discount tables, outputs and

@@ -1240,18 +1240,26 @@ int lsm_apply_locked(const Plan& P, double sim_ms, LsmPass& io)
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((N + LSM_THREADS - 1) / LSM_THREADS,
                                                                  (int64_t)8 * g_dev.sms));
     const size_t tab = lsm_tab_bytes(M);
-    const size_t o_tab = 0, o_acc = align256(tab);
+    const size_t o_tab = 0, o_scr = align256(tab), scr_bytes = sizeof(float4) * (size_t)M;
+    const size_t o_acc = o_scr + align256(scr_bytes);
     const size_t acc_bytes = sizeof(Fx128) * (size_t)grid * LSM_NACC;
     const size_t o_ctl = o_acc + align256(acc_bytes);
     rc = ensure_lsm(o_ctl + 256);
     if (rc) return rc;
-    rc = ensure_pinned(std::max(tab, acc_bytes + 2 * sizeof(int) + sizeof(float)));
+    rc = ensure_pinned(std::max(o_scr + scr_bytes, acc_bytes + 2 * sizeof(int) + sizeof(float)));
     if (rc) return rc;
     unsigned char* base = g_dev.lsm;
     unsigned char* h = g_dev.pinned;
     lsm_fill_tab(h, io);
+    // the single-precision screen of each date: b0, b1, b2 rounded to float, and 1 where the
+    // date has a regression (lsm_apply_kernel)
+    float4* scr = reinterpret_cast<float4*>(h + o_scr);
+    for (int t = 0; t < M; t++)
+        scr[t] = io.fit_at[t] ? make_float4((float)io.beta[3 * (size_t)t], (float)io.beta[3 * (size_t)t + 1],
+                                            (float)io.beta[3 * (size_t)t + 2], 1.0f)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
     cudaStream_t st = g_dev.stream;
-    CUDA_TRY(cudaMemcpyAsync(base + o_tab, h, tab, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(base + o_tab, h, o_scr + scr_bytes, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(base + o_ctl, 0, sizeof(int), st));
     LsmArgs A;
     A.S = g_dev.paths;
@@ -1268,6 +1276,9 @@ int lsm_apply_locked(const Plan& P, double sim_ms, LsmPass& io)
     A.disc = A.df + M;
     A.beta = reinterpret_cast<double*>(base + o_tab) + 2 * (size_t)M;
     A.fit = reinterpret_cast<int*>(base + o_tab + sizeof(double) * 5 * (size_t)M);
+    A.screen = reinterpret_cast<const float4*>(base + o_scr);
+    A.strike_f = (float)io.strike;
+    A.inv_norm_f = (float)A.inv_norm;
     A.acc = reinterpret_cast<Fx128*>(base + o_acc);
     A.status = reinterpret_cast<int*>(base + o_ctl);
     CUDA_TRY(cudaEventRecord(g_dev.ev0, st));
