@@ -24,7 +24,10 @@
 // multiply-adds (those inside the moneyness quotient give its correctly rounded value).
 // GB300 runs FP64 at a small fraction of its FP32 rate, so the per-path work keeps FP64
 // to what the result depends on: the in-the-money test is an integer compare on the
-// spot's bits, and the quotient S / norm is one multiply and four fused multiply-adds.
+// spot's bits, and the quotient S / norm is one multiply and four fused multiply-adds. In
+// the apply the exercise test runs in FP32 wherever a proven margin shows that it decides as
+// the FP64 test (screen_exercise), which then runs only in a thin band around the boundary.
+// (The fit's test, on its compacted lists of full warps, measured faster in FP64.)
 #include "american.cuh"
 
 namespace {
@@ -176,6 +179,37 @@ __device__ __forceinline__ Fx128 fx_from3(const unsigned long long* src)
     fx_add(r, l1 << 42, l1 >> 22);
     fx_add(r, 0, l2 << 20);
     return r;
+}
+
+// The exercise test iv >= b0 + b1 m + b2 m^2 (iv = phi (S - K), m = S / norm) of an
+// in-the-money spot sf, in single precision: 1 exercise, 0 hold, -1 too close to call.
+// With u = 2^-24 and mag = |K| + |S| + |b0| + |b1 m| + |b2| m^2, the single-precision
+// difference d = iv - c (the inputs rounded to float, then five rounded operations) is within
+// 8 u mag of the real iv - c, and the reference's double-precision operands are within
+// 6 * 2^-53 mag of it. So |d| > 2^-19 mag (four times that bound, computed from the rounded
+// inputs) fixes the sign of the double-precision difference and hence the reference's test;
+// an absolute floor keeps underflow out of the bound. Inputs too large for single precision
+// give an infinite or NaN d or bound and come back undecided, as does the thin band around
+// the exercise boundary: the caller then runs the double-precision test.
+template <class K>
+__device__ __forceinline__ int screen_exercise(float sf, float b0, float b1, float b2, const K& A)
+{
+    const float m = sf * A.inv_norm_f;
+    const float iv = A.call ? sf - A.strike_f : A.strike_f - sf;
+    const float c = fmaf(fmaf(b2, m, b1), m, b0);
+    const float d = iv - c;
+    const float am = fabsf(m);
+    const float mag = fmaf(fabsf(b2) * am, am, fmaf(fabsf(b1), am, fabsf(b0))) + (fabsf(A.strike_f) + fabsf(sf));
+    const float e = fmaf(mag, 0x1p-19f, 1e-30f);
+    return d > e ? 1 : (d < -e ? 0 : -1);
+}
+
+// phi (S - K) in double precision, the reference's intrinsic value of an in-the-money spot
+template <class K>
+__device__ __forceinline__ double itm_value(float sf, const K& A)
+{
+    const double s = (double)sf;
+    return A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
 }
 
 // one in-the-money path of contract K at the current date: its regression terms into the
@@ -401,33 +435,6 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmFitArg
     if (bad) atomicExch(A.status, 3);
 }
 
-// The frozen policy's exercise test at date t for an in-the-money spot sf: the reference's
-// double-precision test iv >= b0 + b1 m + b2 m^2 (iv = phi (S - K), m = S / norm), decided in
-// single precision wherever that cannot differ from it.
-// With u = 2^-24 and mag = |K| + |S| + |b0| + |b1 m| + |b2| m^2, the single-precision
-// difference d = iv - c (the inputs rounded to float, then five rounded operations) is within
-// 8 u mag of the real iv - c, and the double-precision operands are within 6 * 2^-53 mag of it.
-// So |d| > 2^-19 mag (four times that bound, computed from the rounded inputs) fixes the sign of
-// the double-precision difference and hence the test; an absolute floor keeps underflow out of
-// the bound. Inputs too large for single precision give an infinite or NaN d or bound and take
-// the double-precision test, as does the thin band around the exercise boundary.
-template <class K>
-__device__ __forceinline__ bool exercise_screened(float sf, float4 b, int t, const K& A)
-{
-    const float m = sf * A.inv_norm_f;
-    const float iv = A.call ? sf - A.strike_f : A.strike_f - sf;
-    const float c = fmaf(fmaf(b.z, m, b.y), m, b.x);
-    const float d = iv - c;
-    const float am = fabsf(m);
-    const float mag = fmaf(fabsf(b.z) * am, am, fmaf(fabsf(b.y), am, fabsf(b.x))) + (fabsf(A.strike_f) + fabsf(sf));
-    const float e = fmaf(mag, 0x1p-19f, 1e-30f);
-    if (d > e) return true;
-    if (d < -e) return false;
-    const double s = (double)sf;
-    const double ivd = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
-    return ivd >= continuation(A.beta[3 * t], A.beta[3 * t + 1], A.beta[3 * t + 2], moneyness(s, A));
-}
-
 constexpr int APPLY_UNROLL = 8; // dates whose spots one thread loads together
 
 __global__ void __launch_bounds__(LSM_THREADS) lsm_apply_kernel(const LsmArgs A)
@@ -455,10 +462,12 @@ __global__ void __launch_bounds__(LSM_THREADS) lsm_apply_kernel(const LsmArgs A)
                 if (tu >= tend) break;
                 const float4 b = __ldg(A.screen + tu);
                 if (b.w == 0.f || !in_the_money(sv[u], A)) continue;
-                if (exercise_screened(sv[u], b, tu, A)) {
-                    const double s = (double)sv[u];
-                    const double iv = A.call ? __dsub_rn(s, A.strike) : __dsub_rn(A.strike, s);
-                    x = __dmul_rn(iv, A.disc[tu]);
+                int ex = screen_exercise(sv[u], b.x, b.y, b.z, A);
+                if (ex < 0)
+                    ex = itm_value(sv[u], A) >= continuation(A.beta[3 * tu], A.beta[3 * tu + 1], A.beta[3 * tu + 2],
+                                                             moneyness((double)sv[u], A));
+                if (ex) {
+                    x = __dmul_rn(itm_value(sv[u], A), A.disc[tu]);
                     break;
                 }
             }
