@@ -301,15 +301,24 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmFitArg
             // in-the-money paths queue until a full warp of them does the FP64 work (the
             // warp's count qn and list length nout are uniform)
             int qn = 0, nout = 0;
+            // each lane's next cashflow and spot are loaded one iteration ahead
+            double cf_next = gw * 32 + lane < A.n ? K.cf[gw * 32 + lane] : 0.0;
+            float s_next = gw * 32 + lane < A.n ? row[gw * 32 + lane] : 0.0f;
             for (int64_t base = gw * 32; base < A.n; base += T) {
                 const int64_t p = base + lane;
+                const double cf_p = cf_next;
+                const float s_p = s_next;
+                if (p + T < A.n) {
+                    cf_next = K.cf[p + T];
+                    s_next = row[p + T];
+                }
                 bool itm = false;
                 float sf = 0.0f;
                 double y = 0.0;
                 if (p < A.n) {
-                    y = __dmul_rn(K.cf[p], d);
+                    y = __dmul_rn(cf_p, d);
                     K.cf[p] = y;
-                    sf = row[p];
+                    sf = s_p;
                     itm = in_the_money(sf, K);
                 }
                 const unsigned mk = __ballot_sync(0xffffffffu, itm);
@@ -407,13 +416,21 @@ __global__ void __launch_bounds__(LSM_THREADS, 1) lsm_fit_kernel(const LsmFitArg
             const double b0 = s_b[c][0], b1 = s_b[c][1], b2 = s_b[c][2];
             const double dt = K.disc[t];
             const int nout = s_nout[warp][c];
-            for (int j = lane; j < nout; j += 32) {
-                const int64_t o = seg + j;
-                const double iv = K.c_iv[o];
-                if (iv >= continuation(b0, b1, b2, K.c_m[o])) {
-                    const int p = K.c_idx[o];
-                    K.cf[p] = iv;
-                    K.val[p] = __dmul_rn(iv, dt);
+            // two entries a lane per pass, their loads issued together
+            for (int j = lane; j < nout; j += 64) {
+                const int64_t o0 = seg + j, o1 = o0 + 32;
+                const bool h1 = j + 32 < nout;
+                const double iv0 = K.c_iv[o0], m0 = K.c_m[o0];
+                const double iv1 = h1 ? K.c_iv[o1] : 0.0, m1 = h1 ? K.c_m[o1] : 0.0;
+                if (iv0 >= continuation(b0, b1, b2, m0)) {
+                    const int p = K.c_idx[o0];
+                    K.cf[p] = iv0;
+                    K.val[p] = __dmul_rn(iv0, dt);
+                }
+                if (h1 && iv1 >= continuation(b0, b1, b2, m1)) {
+                    const int p = K.c_idx[o1];
+                    K.cf[p] = iv1;
+                    K.val[p] = __dmul_rn(iv1, dt);
                 }
             }
         }
