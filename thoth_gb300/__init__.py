@@ -6,6 +6,7 @@ point, all calling the C ABI of ``libthoth_gpu.so`` (include/thoth_gpu.h).
 There is no CPU fallback: without the built library every call raises.
 """
 import ctypes as C
+import os
 import pathlib
 
 import numpy as np
@@ -14,7 +15,8 @@ from . import abi
 from .abi import Book  # noqa: F401
 
 HERE = pathlib.Path(__file__).resolve().parent
-LIB_PATH = HERE / "_build" / "libthoth_gpu.so"
+# THOTH_GPU_LIB selects another build of the same library (the sanitized host build)
+LIB_PATH = pathlib.Path(os.environ.get("THOTH_GPU_LIB") or HERE / "_build" / "libthoth_gpu.so")
 
 _lib = None
 

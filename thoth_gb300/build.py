@@ -1,6 +1,8 @@
 """Build the engine's shared library for sm_103a, in-tree.
 
-    python -m thoth_gb300.build        # -> thoth_gb300/_build/libthoth_gpu.so
+    python -m thoth_gb300.build             # -> thoth_gb300/_build/libthoth_gpu.so
+    python -m thoth_gb300.build --sanitize  # -> thoth_gb300/_build_san/libthoth_gpu.so, host
+                                            #    code under AddressSanitizer and UBSan
 
 nvcc cross-compiles without a GPU. The Joe-Kuo table is embedded into the
 library from thoth_gb300/data/joe_kuo_6_21201.bin through a generated C file.
@@ -15,8 +17,11 @@ import sys
 HERE = pathlib.Path(__file__).resolve().parent
 ROOT = HERE.parent
 BUILD = HERE / "_build"
+BUILD_SAN = HERE / "_build_san"
 CSRC = HERE / "csrc"
 LIB = BUILD / "libthoth_gpu.so"
+# host code of the sanitized build (nvcc splits -Xcompiler values at commas: one flag each)
+SAN_HOST = ["-fsanitize=address", "-fsanitize=undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["kernels.cu", "thoth_gpu.cu", "surrogate.cu", "surrogate_host.cu", "greeks.cu", "american.cu",
            "american_host.cu", "calib.cu"]
@@ -53,16 +58,41 @@ def _gen_blob():
     return out
 
 
-def _compile(src, verbose):
-    obj = BUILD / (pathlib.Path(src).stem + ".o")
-    cmd = [nvcc(), "-c", str(CSRC / src), "-o", str(obj), "-O3", "-lineinfo", "-std=c++17",
+def _xc(flags):
+    return [x for f in flags for x in ("-Xcompiler", f)]
+
+
+def _compile(src, verbose, out=BUILD, sanitize=False):
+    obj = out / (pathlib.Path(src).stem + ".o")
+    cmd = [nvcc(), "-c", str(CSRC / src), "-o", str(obj), "-O1" if sanitize else "-O3", "-lineinfo", "-std=c++17",
            "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"), "-I", str(CSRC)] + ARCH + FLAGS.get(src, [])
+    if sanitize:
+        cmd += ["-g"] + _xc(SAN_HOST)
     if verbose:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s" % (src, r.stderr))
     return obj, r.stderr
+
+
+def build_sanitized():
+    """The library with its host code under AddressSanitizer and UBSan, in _build_san (the
+    device code is the same). A process loads it with THOTH_GPU_LIB pointing at it and the
+    sanitizer runtimes preloaded (LD_PRELOAD)."""
+    BUILD_SAN.mkdir(exist_ok=True)
+    BUILD.mkdir(exist_ok=True)
+    blob = _gen_blob()
+    blob_o = BUILD_SAN / "jk_blob.o"
+    subprocess.run(["gcc", "-c", "-fPIC", "-O1", str(blob), "-o", str(blob_o)], check=True)
+    with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
+        objs = [r[0] for r in ex.map(lambda s: _compile(s, False, BUILD_SAN, True), SOURCES)]
+    lib = BUILD_SAN / LIB.name
+    tmp = BUILD_SAN / (LIB.name + ".tmp")
+    cmd = [nvcc(), "-shared", "-o", str(tmp)] + [str(o) for o in objs] + [str(blob_o)] + ARCH + ["-lcudart"]
+    subprocess.run(cmd + _xc(SAN_HOST[:2]), check=True)
+    os.replace(tmp, lib)
+    return lib
 
 
 def build(verbose=False):
@@ -92,4 +122,4 @@ def build(verbose=False):
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build_sanitized() if "--sanitize" in sys.argv else build(verbose="-v" in sys.argv))
