@@ -48,3 +48,17 @@ def test_books(book):
     assert np.array_equal(r1["per_path"], r2["per_path"])
     assert np.array_equal(r1["premium"], r2["premium"])
     assert r1["book_premium"] == r2["book_premium"]
+
+
+def test_pseudo_random_single_factor_book():
+    """use_sobol: false on a one-factor book: one noise node, so the reference's schedule
+    draws its dates in order and the oracle's stream is the reference's, path for path.
+    (With several noise nodes the reference draws in its topological schedule's order,
+    which the oracle does not restate.)"""
+    b = W.gbm_call(paths=3000, greeks=False)
+    b.use_sobol = False
+    b.seed = 11
+    r1 = oracle.price_book(b, n_per_path=32)
+    r2 = oracle.price_book(b, "ref", n_per_path=32)
+    assert np.array_equal(r1["per_path"], r2["per_path"])
+    assert np.array_equal(r1["premium"], r2["premium"])
