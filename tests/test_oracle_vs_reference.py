@@ -50,11 +50,11 @@ def test_books(book):
     assert r1["book_premium"] == r2["book_premium"]
 
 
-def test_pseudo_random_single_factor_book():
-    """use_sobol: false on a one-factor book: one noise node, so the reference's schedule
-    draws its dates in order and the oracle's stream is the reference's, path for path.
-    (With several noise nodes the reference draws in its topological schedule's order,
-    which the oracle does not restate.)"""
+def test_pseudo_random_one_draw_per_path():
+    """use_sobol: false on a one-step, one-factor book: one draw per path, so the oracle's
+    stream is the reference's, path for path. (Otherwise the reference draws in the order of
+    its topological schedule, e.g. a 30-date GBM book's dates last to first, which the
+    oracle does not restate.)"""
     b = W.gbm_call(paths=3000, greeks=False)
     b.use_sobol = False
     b.seed = 11
