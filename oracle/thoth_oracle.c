@@ -451,7 +451,10 @@ static void* run_job(void* arg)
             W[a * nd] = 0.0;
         }
         for (int i = 1; i <= N; i++) {
-            /* noise nodes (noise_node.cpp:20-25) */
+            /* noise nodes (noise_node.cpp:20-25). use_sobol = 0: drawn date by date in factor
+             * order; the reference draws in the order of its topological schedule
+             * (core/node_collector.cpp:225-340), the same stream only where a path takes one
+             * draw, so that mode is compared statistically */
             for (int f = 0; f < F; f++) noise[f] = d->use_sobol ? B.noise[(size_t)f * (N + 1) + i] : xo_gaussian(&rng);
             for (int a = 0; a < na; a++) {
                 const ThothAsset* A = &d->assets[a];
