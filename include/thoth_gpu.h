@@ -21,6 +21,12 @@
  * reference server prices on a per-request std::thread, run_server.cpp:110-116).
  * Calls are serialised by an internal mutex; the device arena and stream are
  * created lazily on the first call and reused.
+ *
+ * Device: the engine binds to the calling thread's current CUDA device at its
+ * first call and sets that device on every later call, from any thread. A
+ * process drives one GPU: with one process per GPU, each selects its device
+ * (cudaSetDevice) before its first call. A surrogate handle binds to the device
+ * current when it is created.
  */
 #ifndef THOTH_GPU_H
 #define THOTH_GPU_H

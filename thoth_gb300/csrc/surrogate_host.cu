@@ -79,6 +79,7 @@ struct ThothSurrogate {
     __nv_bfloat16* wbf = nullptr;
     int* status = nullptr;
     cudaStream_t st = nullptr;
+    int dev = 0; // the device current when the handle was created; every call sets it
     int sms = 0;
     int64_t step = 0;
     // training buffers (grown on demand)
@@ -214,10 +215,13 @@ int thoth_gpu_surrogate_create(ThothSurrogate** out, uint64_t seed)
         std::lock_guard<std::mutex> lk(s_mu);
         int n = 0;
         if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return sfail(THOTH_GPU_E_NODEVICE, "no CUDA device");
+        int dev = 0;
+        STRY(cudaGetDevice(&dev));
         cudaDeviceProp p;
-        STRY(cudaGetDeviceProperties(&p, 0));
+        STRY(cudaGetDeviceProperties(&p, dev));
         if (!(p.major == 10 && p.minor == 3)) return sfail(THOTH_GPU_E_NODEVICE, "not an sm_103 device");
         ThothSurrogate* s = new ThothSurrogate();
+        s->dev = dev;
         s->np = mlp_n_params();
         s->nbf = mlp_n_bf();
         s->sms = p.multiProcessorCount;
@@ -270,6 +274,7 @@ int thoth_gpu_surrogate_destroy(ThothSurrogate* s)
     try {
         if (!s) return THOTH_GPU_OK;
         std::lock_guard<std::mutex> lk(s_mu);
+        cudaSetDevice(s->dev); // frees below whatever this returns
         cudaFree(s->params);
         cudaFree(s->wbf);
         cudaFree(s->status);
@@ -295,6 +300,7 @@ int thoth_gpu_surrogate_get_params(ThothSurrogate* s, float* params)
     try {
         if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
         std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaSetDevice(s->dev));
         STRY(cudaMemcpyAsync(params, s->params, sizeof(float) * s->np, cudaMemcpyDeviceToHost, s->st));
         STRY(cudaStreamSynchronize(s->st));
         return THOTH_GPU_OK;
@@ -310,6 +316,7 @@ int thoth_gpu_surrogate_set_params(ThothSurrogate* s, const float* params)
     try {
         if (!s || !params) return sfail(THOTH_GPU_E_INVALID, "null argument");
         std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaSetDevice(s->dev));
         std::vector<float> h(params, params + s->np);
         return upload_params(s, h);
     } catch (const std::bad_alloc&) {
@@ -325,6 +332,7 @@ int thoth_gpu_surrogate_gradient(ThothSurrogate* s, const float* x, const float*
     try {
         if (!s || !x || !y || !grad || rows < 128 || rows % 128) return sfail(THOTH_GPU_E_INVALID, "rows must be a multiple of 128");
         std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaSetDevice(s->dev));
         int rc = ensure_train(s, rows);
         if (rc) return rc;
         std::vector<__nv_bfloat16> hx;
@@ -368,6 +376,7 @@ int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y,
         if (!s || !x || !y || n < 128 || epochs < 1 || batch < 128 || batch % 128 || !(lr > 0))
             return sfail(THOTH_GPU_E_INVALID, "bad training arguments (batch must be a multiple of 128)");
         std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaSetDevice(s->dev));
         const int B = (int)std::min<int64_t>(batch, n / 128 * 128);
         int rc = ensure_train(s, B);
         if (rc) return rc;
@@ -451,6 +460,7 @@ int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, fl
     try {
         if (!s || !x || !y || n < 1 || n > ((int64_t)1 << 30)) return sfail(THOTH_GPU_E_INVALID, "bad predict arguments");
         std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaSetDevice(s->dev));
         if (n > s->cap_inf) {
             if (s->ib) cudaFree(s->ib);
             s->ib = nullptr;

@@ -151,12 +151,16 @@ int ensure_device()
     }
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(THOTH_GPU_E_NODEVICE, "no CUDA device");
+    // the engine binds to the calling thread's current device at its first call (one process
+    // per GPU: each rank selects its device before it calls in), and every later call sets it
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
     cudaDeviceProp p;
-    CUDA_TRY(cudaGetDeviceProperties(&p, 0));
+    CUDA_TRY(cudaGetDeviceProperties(&p, dev));
     if (!(p.major == 10 && p.minor == 3))
         return fail(THOTH_GPU_E_NODEVICE, std::string("device ") + p.name + " is not sm_103 (built for sm_103a only)");
-    g_dev.id = 0;
-    CUDA_TRY(cudaSetDevice(0));
+    g_dev.id = dev;
+    CUDA_TRY(cudaSetDevice(dev));
     g_dev.sms = p.multiProcessorCount;
     g_dev.name = p.name;
     CUDA_TRY(cudaStreamCreateWithFlags(&g_dev.stream, cudaStreamNonBlocking));
@@ -2460,7 +2464,8 @@ int thoth_gpu_device_info(char* buf, size_t n)
             s = "no CUDA device found";
         } else {
             cudaDeviceProp p;
-            if (cudaGetDeviceProperties(&p, 0) != cudaSuccess) {
+            int dev = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess) {
                 s = "CUDA device query failed";
             } else {
                 s = std::string(p.name) + " (sm_" + std::to_string(p.major) + std::to_string(p.minor) + ", " +
