@@ -470,19 +470,25 @@ def run_gpu(args):
             "clocks": clk.summary(),
             "wall_s_timed_region": wall,
         }
-        line["cpu_baseline"] = cpu_baseline(args.cpu_sample_paths, os.cpu_count() or 1)
-        line["cpu_baseline"]["one_core"] = one_core_baseline()
-        if not args.no_lsv:
+        # the CPU baseline and the other workloads run at N = 1 only: at N > 1 the line
+        # carries the headline, so that the other ranks' GPUs are not held while rank 0 runs them
+        solo = world == 1
+        if solo:
+            line["cpu_baseline"] = cpu_baseline(args.cpu_sample_paths, os.cpu_count() or 1)
+            line["cpu_baseline"]["one_core"] = one_core_baseline()
+        else:
+            line["sections"] = "CPU baseline and single-GPU sections reported at N = 1"
+        if solo and not args.no_lsv:
             line["lsv_book"] = lsv_book_section(G, flush, args.steps)
-        if not args.no_paths:
+        if solo and not args.no_paths:
             line["stored_paths"] = paths_section(G, flush)
-        if not args.no_american:
+        if solo and not args.no_american:
             line["american_lsm"] = american_section(G, flush, args.steps)
-        if not args.no_calibration:
+        if solo and not args.no_calibration:
             line["lsv_calibration"] = calibration_section(G)
-        if not args.no_batch:
+        if solo and not args.no_batch:
             line["ragged_batch"] = ragged_batch_section(G, args.steps)
-        if not args.no_surrogate:
+        if solo and not args.no_surrogate:
             from thoth_gb300 import surrogate as S
             info = S.benchmark()
             line["grid_cells_per_sec"] = {
