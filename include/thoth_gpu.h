@@ -215,6 +215,14 @@ int thoth_gpu_book_destroy(ThothBookHandle* handle);
  * over the kernel's CUDA-event time; *ms = that time. */
 int thoth_gpu_measure_fp32_peak(double* tflops, double* ms);
 
+/* Test hook, no reference counterpart (host-side fault injection): drops the
+ * engine's working buffers (arena, staging, stored paths, exercise and
+ * calibration scratch, batch buffers), so that the next calls allocate them
+ * afresh, and makes the next n of those allocations fail as on a full device:
+ * the calls return THOTH_GPU_E_NOMEM and later calls succeed. n = 0 clears it.
+ * Handles (resident books, surrogates) keep their memory. */
+int thoth_gpu_debug_fail_allocations(int32_t n);
+
 /* Measurement hook, no reference counterpart: special-function-unit (MUFU)
  * throughput from a kernel of independent reciprocal-square-root chains;
  * *gops = 10^9 operations a second over the kernel's CUDA-event time; *ms = that time. */

@@ -54,6 +54,7 @@ def lib():
         L.thoth_gpu_book_destroy.argtypes = [C.c_void_p]
         L.thoth_gpu_measure_fp32_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.thoth_gpu_measure_mufu_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.thoth_gpu_debug_fail_allocations.argtypes = [C.c_int32]
         L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
         L.thoth_gpu_bump_greeks.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBumpGreeks)]
         L.thoth_gpu_bump_greeks_last_error.restype = C.c_char_p
@@ -314,6 +315,12 @@ def measure_fp32_peak():
     tf, ms = C.c_double(), C.c_double()
     _check(lib().thoth_gpu_measure_fp32_peak(C.byref(tf), C.byref(ms)))
     return tf.value
+
+
+def debug_fail_allocations(n):
+    """Test hook: drop the engine's working buffers and make the next n allocations of
+    them fail as on a full device (THOTH_GPU_E_NOMEM); n = 0 clears it."""
+    _check(lib().thoth_gpu_debug_fail_allocations(int(n)))
 
 
 def measure_mufu_peak():

@@ -180,6 +180,33 @@ int ensure_device()
     return THOTH_GPU_OK;
 }
 
+// Allocation fault injection (a test hook, thoth_gpu_debug_fail_allocations): the next
+// g_fail_allocs allocations of the engine's working buffers fail as on a full device.
+// Guarded by g_mu like every other engine state.
+int g_fail_allocs = 0;
+
+template <class T>
+cudaError_t dev_alloc(T** p, size_t bytes)
+{
+    if (g_fail_allocs > 0) {
+        --g_fail_allocs;
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+template <class T>
+cudaError_t host_alloc(T** p, size_t bytes)
+{
+    if (g_fail_allocs > 0) {
+        --g_fail_allocs;
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
 int ensure_arena(size_t bytes)
 {
     if (bytes <= g_dev.arena_size) return THOTH_GPU_OK;
@@ -187,7 +214,7 @@ int ensure_arena(size_t bytes)
     g_dev.arena = nullptr;
     g_dev.arena_size = 0;
     const size_t sz = std::max(bytes, (size_t)1 << 22) * 5 / 4;
-    CUDA_TRY(cudaMalloc(&g_dev.arena, sz));
+    CUDA_TRY(dev_alloc(&g_dev.arena, sz));
     g_dev.arena_size = sz;
     return THOTH_GPU_OK;
 }
@@ -198,7 +225,7 @@ int ensure_paths(size_t bytes)
     if (g_dev.paths) cudaFree(g_dev.paths);
     g_dev.paths = nullptr;
     g_dev.paths_size = 0;
-    CUDA_TRY(cudaMalloc(&g_dev.paths, bytes));
+    CUDA_TRY(dev_alloc(&g_dev.paths, bytes));
     g_dev.paths_size = bytes;
     return THOTH_GPU_OK;
 }
@@ -210,7 +237,7 @@ int ensure_pinned(size_t bytes)
     g_dev.pinned = nullptr;
     g_dev.pinned_size = 0;
     const size_t sz = std::max(bytes, (size_t)1 << 20) * 5 / 4;
-    CUDA_TRY(cudaHostAlloc(&g_dev.pinned, sz, cudaHostAllocDefault));
+    CUDA_TRY(host_alloc(&g_dev.pinned, sz));
     g_dev.pinned_size = sz;
     return THOTH_GPU_OK;
 }
@@ -1158,7 +1185,7 @@ int ensure_lsm(size_t bytes)
     if (g_dev.lsm) cudaFree(g_dev.lsm);
     g_dev.lsm = nullptr;
     g_dev.lsm_size = 0;
-    CUDA_TRY(cudaMalloc(&g_dev.lsm, bytes));
+    CUDA_TRY(dev_alloc(&g_dev.lsm, bytes));
     g_dev.lsm_size = bytes;
     return THOTH_GPU_OK;
 }
@@ -1704,14 +1731,14 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
         if (g_batch.dev) cudaFree(g_batch.dev);
         g_batch.dev = nullptr;
         g_batch.dev_size = 0; // stays empty if the allocation fails
-        CUDA_TRY(cudaMalloc(&g_batch.dev, total));
+        CUDA_TRY(dev_alloc(&g_batch.dev, total));
         g_batch.dev_size = total;
     }
     if (std::max(o_outs, back) > g_batch.host_size) {
         if (g_batch.host) cudaFreeHost(g_batch.host);
         g_batch.host = nullptr;
         g_batch.host_size = 0;
-        CUDA_TRY(cudaHostAlloc(&g_batch.host, std::max(o_outs, back), cudaHostAllocDefault));
+        CUDA_TRY(host_alloc(&g_batch.host, std::max(o_outs, back)));
         g_batch.host_size = std::max(o_outs, back);
     }
     for (int b = 0; b < n; b++)
@@ -2087,7 +2114,7 @@ int calibrate_locked(ThothLeverageCalib* c)
         if (g_dev.calib) cudaFree(g_dev.calib);
         g_dev.calib = nullptr;
         g_dev.calib_size = 0;
-        CUDA_TRY(cudaMalloc(&g_dev.calib, o));
+        CUDA_TRY(dev_alloc(&g_dev.calib, o));
         g_dev.calib_size = o;
     }
     rc = ensure_pinned(std::max(up_bytes, 8 * nd * npt + 16));
@@ -2293,7 +2320,7 @@ int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out)
         }
         h->grid = grid_for(h->plan);
         h->layout = layout_of(h->plan, h->grid);
-        cudaError_t e = cudaMalloc(&h->dev, h->layout.total);
+        cudaError_t e = dev_alloc(&h->dev, h->layout.total);
         if (e != cudaSuccess) {
             delete h;
             return fail(THOTH_GPU_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
@@ -2434,6 +2461,41 @@ int thoth_gpu_measure_mufu_peak(double* gops, double* ms_out)
         const double ops = (double)blocks * 256 * iters * 16 * 8;
         *gops = ops / (ms * 1e-3) / 1e9;
         if (ms_out) *ms_out = ms;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_debug_fail_allocations(int32_t n)
+{
+    try {
+        if (n < 0) return fail(THOTH_GPU_E_INVALID, "n must be >= 0");
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (g_dev.ready) {
+            // every call has finished its device work before it returned; drop the working
+            // buffers so that the next calls allocate them afresh
+            CUDA_TRY(cudaSetDevice(g_dev.id));
+            CUDA_TRY(cudaDeviceSynchronize());
+            if (g_batch.exec) cudaGraphExecDestroy(g_batch.exec);
+            g_batch.exec = nullptr;
+            g_batch.signature.clear();
+            cudaFree(g_batch.dev);
+            cudaFreeHost(g_batch.host);
+            g_batch.dev = g_batch.host = nullptr;
+            g_batch.dev_size = g_batch.host_size = 0;
+            cudaFree(g_dev.arena);
+            cudaFree(g_dev.paths);
+            cudaFree(g_dev.lsm);
+            cudaFree(g_dev.calib);
+            cudaFreeHost(g_dev.pinned);
+            g_dev.arena = g_dev.lsm = g_dev.calib = g_dev.pinned = nullptr;
+            g_dev.paths = nullptr;
+            g_dev.arena_size = g_dev.paths_size = g_dev.lsm_size = g_dev.calib_size = g_dev.pinned_size = 0;
+        }
+        g_fail_allocs = n;
         return THOTH_GPU_OK;
     } catch (const std::bad_alloc&) {
         return fail(THOTH_GPU_E_NOMEM, "out of host memory");
