@@ -3,7 +3,7 @@
 The reference runs its test binary in an ASan + UBSan build. Here the same library is built
 with its host code sanitized (thoth_gb300.build.build_sanitized) and loaded in a child
 process with the sanitizer runtimes preloaded. The child runs the host-logic tests and
-prices nothing: it validates and plans thousands of mutated book descriptors (indices,
+prices nothing: it validates and plans 900 mutated book descriptors (indices,
 dates, counts, model parameters and leverage grids out of range or not finite). Every
 descriptor must come back planned or rejected with an error code, and the sanitizers must
 report nothing.
@@ -23,13 +23,13 @@ def _runtime(name):
 
 
 @pytest.fixture(scope="module")
-def sanitized_env():
+def sanitized_env(tmp_path_factory):
     asan, ubsan = _runtime("libasan.so"), _runtime("libubsan.so")
     if not asan or not ubsan:
         pytest.skip("no AddressSanitizer / UBSan runtime for this compiler")
     sys.path.insert(0, ROOT)
     from thoth_gb300 import build as B
-    lib = B.build_sanitized()
+    lib = B.build_sanitized(tmp_path_factory.mktemp("build_san"))
     env = dict(os.environ)
     env.update(THOTH_GPU_LIB=str(lib), LD_PRELOAD=asan + " " + ubsan,
                ASAN_OPTIONS="detect_leaks=0:protect_shadow_gap=0:halt_on_error=1",

@@ -76,19 +76,20 @@ def _compile(src, verbose, out=BUILD, sanitize=False):
     return obj, r.stderr
 
 
-def build_sanitized():
-    """The library with its host code under AddressSanitizer and UBSan, in _build_san (the
+def build_sanitized(out=BUILD_SAN):
+    """The library with its host code under AddressSanitizer and UBSan, in `out` (the
     device code is the same). A process loads it with THOTH_GPU_LIB pointing at it and the
     sanitizer runtimes preloaded (LD_PRELOAD)."""
-    BUILD_SAN.mkdir(exist_ok=True)
+    out = pathlib.Path(out)
+    out.mkdir(parents=True, exist_ok=True)
     BUILD.mkdir(exist_ok=True)
     blob = _gen_blob()
-    blob_o = BUILD_SAN / "jk_blob.o"
+    blob_o = out / "jk_blob.o"
     subprocess.run(["gcc", "-c", "-fPIC", "-O1", str(blob), "-o", str(blob_o)], check=True)
     with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
-        objs = [r[0] for r in ex.map(lambda s: _compile(s, False, BUILD_SAN, True), SOURCES)]
-    lib = BUILD_SAN / LIB.name
-    tmp = BUILD_SAN / (LIB.name + ".tmp")
+        objs = [r[0] for r in ex.map(lambda s: _compile(s, False, out, True), SOURCES)]
+    lib = out / LIB.name
+    tmp = out / (LIB.name + ".tmp")
     cmd = [nvcc(), "-shared", "-o", str(tmp)] + [str(o) for o in objs] + [str(blob_o)] + ARCH + ["-lcudart"]
     subprocess.run(cmd + _xc(SAN_HOST[:2]), check=True)
     os.replace(tmp, lib)
