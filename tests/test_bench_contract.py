@@ -43,3 +43,22 @@ def test_reference_arm_runs_on_rank_zero_only():
                   env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert p.returncode == 0, p.stderr
     assert p.stdout.strip() == ""
+
+
+def test_clock_summary_counts_samples_from_the_mark_and_reports_throttling():
+    """The bench's clocks record: nvidia-smi CSV samples from the start of the timed region,
+    median SM clock, and every throttle reason seen active."""
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.Clocks(0)
+    c.lines = ["0, 1200, 2070, 300.0, 0x0, Not Active, Not Active, Not Active, Not Active",  # before the region
+               "0, 2070, 2070, 900.5, 0x0, Not Active, Not Active, Not Active, Not Active",
+               "0, 2055, 2070, 1100.2, 0x4, Not Active, Not Active, Not Active, Active",
+               "not a sample"]
+    s = c.summary(since=1)
+    assert s["samples"] == 2 and s["sm_mhz"] == 2062.5 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    assert c.summary()["sm_mhz"] == 2055.0                      # the idle sample counts without a mark
+    c.lines.append("0, 1900, 2070, 1300.0, 0x40, Not Active, Active, Not Active, Not Active")
+    assert c.summary(since=1)["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+    assert bench.Clocks(0).summary()["reasons"] == ["unsampled"]
