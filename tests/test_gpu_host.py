@@ -23,6 +23,10 @@ def test_cpp_dropin(gpu):
     parity = math.exp(-0.03) * (100 * math.exp(0.02) - 100)                      # df (F - K)
     assert abs((call - put) - parity) < 3 * book_trust + 1e-3
     assert "error" in lines and "paths must be > 1" in out.stdout
+    am, euro, delta = (float(v) for v in lines["american"])
+    assert am > euro > 0 and -1.0 < delta < 0.0                            # early exercise pays for a put
+    lo, hi = (float(v) for v in lines["calib"])
+    assert 0.5 < lo <= hi < 3.0                                            # about 0.25 / 0.20
 
 
 def test_peak_microbenchmarks_are_plausible(gpu):

@@ -1,6 +1,7 @@
 // C++ host side of the GPU boundary over the C ABI (see mcl_gpu.hpp).
 #include "mcl_gpu.hpp"
 
+#include <algorithm>
 #include <stdexcept>
 
 namespace gpu
@@ -68,6 +69,33 @@ BookResult PriceBook( const ThothBookDesc& Book )
     out.trust = r.book_trust;
     out.device_ms = r.device_ms;
     return out;
+}
+
+void PriceAmericanBook( const ThothBookDesc& Book, std::vector<ThothAmerican>& Contracts )
+{
+    if ( Contracts.empty() )
+    {
+        return;
+    }
+    const int rc = thoth_gpu_price_american_book( &Book, Contracts.data(), (int32_t)Contracts.size() );
+    if ( rc != THOTH_GPU_OK )
+    {
+        throw std::runtime_error( "ERR> gpu PriceAmericanBook failed (" + std::to_string( rc ) +
+                                  "): " + thoth_gpu_american_last_error() );
+    }
+}
+
+std::vector<double> CalibrateLeverage( const ThothLeverageCalib& Calib )
+{
+    ThothLeverageCalib c = Calib;
+    std::vector<double> lev( (size_t)std::max( c.n_dates, 0 ) * (size_t)std::max( c.points, 0 ) );
+    c.leverage = lev.data();
+    const int rc = thoth_gpu_calibrate_leverage( &c );
+    if ( rc != THOTH_GPU_OK )
+    {
+        Err( "CalibrateLeverage", rc );
+    }
+    return lev;
 }
 
 } // namespace gpu

@@ -42,4 +42,13 @@ struct BookResult
 //! price every product of a flat book descriptor in one GPU sweep
 BookResult PriceBook( const ThothBookDesc& Book );
 
+//! the American vanillas of a book by Longstaff-Schwartz (reference: PricerMCL::PriceAmerican,
+//! pricer_mcl_american.cpp:137-261): each entry's product and flags (and optionally min_itm,
+//! zero_rates, beta) in, its premium, trust and Greeks out
+void PriceAmericanBook( const ThothBookDesc& Book, std::vector<ThothAmerican>& Contracts );
+
+//! leverage layers [n_dates][points] by the reference's particle method
+//! (Single::CalibrateLeverage, single.cpp:390-473); Calib.leverage is not used
+std::vector<double> CalibrateLeverage( const ThothLeverageCalib& Calib );
+
 } // namespace gpu
