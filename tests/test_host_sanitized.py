@@ -4,9 +4,9 @@ The reference runs its test binary in an ASan + UBSan build. Here the same libra
 with its host code sanitized (thoth_gb300.build.build_sanitized) and loaded in a child
 process with the sanitizer runtimes preloaded. The child runs the host-logic tests and
 prices nothing: it validates and plans 900 mutated book descriptors (indices,
-dates, counts, model parameters and leverage grids out of range or not finite). Every
-descriptor must come back planned or rejected with an error code, and the sanitizers must
-report nothing.
+dates, counts, model parameters and leverage grids out of range or not finite), and checks
+300 mutated calibration inputs and 200 American requests. Every descriptor must come back
+planned or rejected with an error code, and the sanitizers must report nothing.
 """
 import os
 import subprocess
@@ -136,3 +136,65 @@ def test_mutated_descriptors_are_planned_or_rejected_under_sanitizers(sanitized_
     assert "ERROR: AddressSanitizer" not in p.stderr and "runtime error" not in p.stderr
     planned, rejected = (int(x) for x in p.stdout.split()[1::2])
     assert planned + rejected == 900 and rejected > 600
+
+
+FUZZ_INPUTS = r'''
+import copy, math, random
+import numpy as np
+import thoth_gb300 as G
+from thoth_gb300 import abi, workloads as W
+
+rng = random.Random(9)
+ok_codes = (abi.THOTH_GPU_E_INVALID, abi.THOTH_GPU_E_UNSUPPORTED, abi.THOTH_GPU_E_TOO_LARGE,
+            abi.THOTH_GPU_E_NODEVICE)
+seen = 0
+base = W.lsv_calibration(horizon_days=20, particles=1024)
+for _ in range(300):
+    c = copy.deepcopy(base)
+    what = rng.randrange(8)
+    if what == 0:
+        c.days = c.days.copy(); c.days[rng.randrange(1, len(c.days))] = rng.choice([-1, 0, 10 ** 9])
+    elif what == 1:
+        c.ln_step = c.ln_step * rng.choice([0.0, -1.0, math.nan, 1e300])
+    elif what == 2:
+        c.offset = c.offset + rng.choice([-(1 << 62), 1 << 62, -10 ** 15])
+    elif what == 3:
+        c.local_vol = c.local_vol.copy(); c.local_vol.flat[rng.randrange(c.local_vol.size)] = rng.choice([math.nan, -0.1, 0.0, math.inf])
+    elif what == 4:
+        c.particles, c.bins, c.min_bin_count = rng.choice([(-5, 0, 0), (1, 0, 0), (1 << 30, 0, 0), (0, 1 << 20, 0), (0, -3, 7), (0, 0, 1 << 30)])
+    elif what == 5:
+        c.heston[rng.choice(["v0", "kappa", "theta", "xi", "rho"])] = rng.choice([math.nan, -1.0, 5.0, 0.0])
+    elif what == 6:
+        c.spot = rng.choice([0.0, -1.0, math.nan, math.inf])
+    else:
+        c.carry = c.carry * rng.choice([math.nan, 1e300])
+    try:
+        G.calibrate_leverage(c)
+        raise SystemExit("calibration ran without a device")
+    except G.ThothGpuError as e:
+        assert e.code in ok_codes, e
+        seen += 1
+b = W.american_put(4096)
+for _ in range(200):
+    p = rng.choice([-1, 0, 1, 5, 1 << 20])
+    kw = dict(flags=rng.choice([0, 31, 1 << 20]), min_itm=rng.choice([0, -5, 10 ** 9]))
+    if rng.random() < 0.3:
+        kw["zero_rates"] = np.full(b.n_dates, rng.choice([0.01, math.nan]))
+    try:
+        G.price_american(b, p, **kw)
+        raise SystemExit("American pricing ran without a device")
+    except G.ThothGpuError as e:
+        assert e.code in ok_codes, e
+        seen += 1
+    except ValueError:
+        seen += 1
+print("checked", seen)
+'''
+
+
+def test_calibration_and_american_inputs_are_checked_under_sanitizers(sanitized_env):
+    p = subprocess.run([sys.executable, "-c", FUZZ_INPUTS], cwd=ROOT, env=sanitized_env, capture_output=True,
+                       text=True, timeout=900)
+    assert p.returncode == 0, p.stdout[-3000:] + p.stderr[-3000:]
+    assert "ERROR: AddressSanitizer" not in p.stderr and "runtime error" not in p.stderr
+    assert p.stdout.split() == ["checked", "500"]
