@@ -7,7 +7,9 @@
  * Every function states the reference lines whose arithmetic it restates, in
  * the same operation order so that a single-threaded run reproduces the
  * reference node graph bit for bit (pinned by tests/test_oracle_vs_reference.py
- * against the reference compiled into oracle/_ref/, and by tests/golden/).
+ * against the reference compiled into oracle/_ref/, and by tests/golden/): with
+ * Sobol points, and with use_sobol = 0 only where a path takes one draw (the
+ * reference otherwise draws in its topological schedule's order).
  * Compile with -ffp-contract=off: fused multiply-adds would change the bits.
  */
 #include "thoth_oracle.h"
