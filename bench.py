@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="thoth", choices=["thoth", "reference"])
     ap.add_argument("--cpu-sample-paths", type=int, default=1 << 18)
+    ap.add_argument("--paths", type=int, default=PATHS, help="paths of the headline workload (default 2^20)")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain-MC grid section")
     ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch (256 books) section")
     ap.add_argument("--no-lsv", action="store_true", help="skip the multi-asset LSV book section")
@@ -56,15 +57,15 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def workload(rank=0):
+def workload(rank=0, paths=PATHS):
     from thoth_gb300 import workloads as W
-    b = W.heston_grid(paths=PATHS, steps_per_year=STEPS_PER_YEAR)
-    b.sobol_skip = rank * PATHS  # disjoint Sobol block per rank
+    b = W.heston_grid(paths=paths, steps_per_year=STEPS_PER_YEAR)
+    b.sobol_skip = rank * paths  # disjoint Sobol block per rank
     return b
 
 
-def config(world):
-    return {"workload": "heston_vanilla_grid", "paths": PATHS, "steps": 2 * STEPS_PER_YEAR,
+def config(world, paths=PATHS):
+    return {"workload": "heston_vanilla_grid", "paths": paths, "steps": 2 * STEPS_PER_YEAR,
             "steps_per_year": STEPS_PER_YEAR, "cells": 126, "strikes": "80..120 step 5",
             "maturities_months": [1, 2, 3, 4, 5, 12, 24], "sobol_dims": 1008, "brownian_bridge": True,
             "parallelism": "dp%d" % world if world > 1 else "single",
@@ -154,23 +155,44 @@ def one_core_baseline(sample_paths=1 << 13):
 
 
 def run_reference(args):
+    """The reference's CPU Monte-Carlo (its node-graph arithmetic, restated bit for bit in
+    oracle/thoth_oracle.c) on all host cores. Every step, warm-up included, prices the whole
+    workload of this arm's config: the 126-cell Heston grid on 2^20 paths x 504 steps (--paths),
+    about 2 s on 16 Arm cores. ms_per_step is the mean wall time of the timed steps."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    import oracle
     threads = os.cpu_count() or 1
     n_steps = 2 * STEPS_PER_YEAR
+    book = workload(0, args.paths)
     for _ in range(args.warmup):
-        cpu_baseline(1 << 12, threads)
-    vals = [cpu_baseline(args.cpu_sample_paths, threads) for _ in range(args.steps)]
-    v = statistics.median(x["value"] for x in vals)
+        oracle.price_book(book, "port", threads=threads)
+    secs = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.price_book(book, "port", threads=threads)
+        secs.append(time.perf_counter() - t0)
+    wall = time.perf_counter() - t_all
+    ms = 1e3 * sum(secs) / len(secs)
+    v = args.paths * n_steps / (ms * 1e-3)
     line = {"metric": "path-steps/sec", "value": v, "unit": "path-steps/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * PATHS * n_steps / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(1),
-            "cpu_baseline": dict(vals[-1], value=v, one_core=one_core_baseline()),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(world, args.paths),
+            "cpu_baseline": {"value": v, "unit": "path-steps/s", "cores": threads, "kind": "port",
+                             "sample": "the whole workload every step: %d paths x %d steps, 126 cells, %d threads"
+                                       % (args.paths, n_steps, threads),
+                             "one_core": one_core_baseline()},
             "e2e": {"value": v, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference's CPU Monte-Carlo restated bit-exactly in oracle/thoth_oracle.c, all host "
-                    "threads, each step a bounded sample of the workload; ms_per_step scaled to 2^20 paths"}
+            "wall_s_timed_region": wall,
+            "note": "the reference's CPU Monte-Carlo restated bit for bit in oracle/thoth_oracle.c (kind port: "
+                    "the build of the reference's own sources needs its checkout, which the GPU host does not "
+                    "have), all host threads, "
+                    "each step the full workload of config"}
+    if world > 1:
+        line["note"] += "; at N > 1 rank 0 prices one rank's path block (the host's cores do not grow with N)"
     print(json.dumps(line), flush=True)
 
 
@@ -346,6 +368,47 @@ def calibration_section(G):
     return out
 
 
+def _first_paths(book, n):
+    """A copy of `book` priced on its first n Sobol points (the same indices as the book's)."""
+    import copy
+    b = copy.copy(book)
+    b.paths = int(n)
+    return b
+
+
+def batch_parity(G, books, check_paths=1 << 16):
+    """Every book of a batch against the oracle: each book is re-priced on its first
+    min(paths, check_paths) Sobol points, in one batch call together with the full books,
+    and those premiums are compared with the oracle's on the same points (all host cores).
+    A book fails where any product (or the book value) is further from the oracle than
+    0.5 standard errors or 1e-4 relative + 1e-5, the bar of the GPU parity tests."""
+    import numpy as np
+    import oracle
+    trunc = [_first_paths(b, min(b.paths, check_paths)) for b in books]
+    t0 = time.perf_counter()
+    res = G.price_batch(list(books) + trunc)[len(books):]
+    gpu_s = time.perf_counter() - t0
+    threads = os.cpu_count() or 1
+    failing, worst_se, worst_rel, t0 = [], 0.0, 0.0, time.perf_counter()
+    for i, (b, r) in enumerate(zip(trunc, res)):
+        ref = oracle.price_book(b, "port", threads=threads)
+        g = np.append(r["premium"], r["book_premium"])
+        o = np.append(ref["premium"], ref["book_premium"])
+        se = np.append(ref["trust"], ref["book_trust"])
+        err = np.abs(g - o)
+        bad = (err > 0.5 * se + 1e-12) | (err > 1e-4 * np.abs(o) + 1e-5)
+        if bad.any():
+            failing.append(i)
+        worst_se = max(worst_se, float(np.max(err / np.maximum(se, 1e-300))))
+        worst_rel = max(worst_rel, float(np.max(err / (np.abs(o) + 1e-300))))
+    return {"books_checked": len(books), "books_failing_parity": len(failing), "failing_books": failing[:16],
+            "worst_error_in_se": worst_se, "worst_rel_error": worst_rel,
+            "paths_per_book": "min(paths, %d): the book's first Sobol points" % check_paths,
+            "bar": "every product and the book value within 0.5 SE and 1e-4 relative + 1e-5 of the oracle",
+            "path_steps_checked": float(sum(b.paths * (len(b.days) - 1) for b in trunc)),
+            "batch_call_s": gpu_s, "oracle_s": time.perf_counter() - t0, "oracle_threads": threads}
+
+
 def ragged_batch_section(G, steps):
     """256 ragged books (path counts log-uniform in [2^14, 2^22], 12..730 daily steps,
     40% GBM / 40% Heston / 20% LSV) priced as one CUDA graph: untuned, after the
@@ -389,6 +452,7 @@ def ragged_batch_section(G, steps):
                               "(-1: each book's default) and grid policy, timed on the batch graph"),
         "gpu_launches_per_batch": 3 * len(books),  # gather, book kernel, reduction per book
         "books_nonfinite": int(sum(not np.all(np.isfinite(r["premium"])) for r in res)),
+        "parity": batch_parity(G, books),
     }
 
 
@@ -401,7 +465,7 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     n_steps = 2 * STEPS_PER_YEAR
-    book = workload(rank)
+    book = workload(rank, args.paths)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     peak_fp32 = G.measure_fp32_peak()
     peak_mufu = G.measure_mufu_peak()
@@ -441,7 +505,7 @@ def run_gpu(args):
         t = torch.tensor([ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * PATHS * n_steps / (ms * 1e-3)
+    value = world * args.paths * n_steps / (ms * 1e-3)
 
     # ---- end to end through the C ABI from host descriptors ---------------
     for _ in range(2):
@@ -461,16 +525,16 @@ def run_gpu(args):
         t = torch.tensor([e_ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e_ms = float(t.item())
-    e2e = world * PATHS * n_steps / (e_ms * 1e-3)
+    e2e = world * args.paths * n_steps / (e_ms * 1e-3)
 
     if rank == 0:
-        achieved = FLOPS_PER_PATH_STEP * PATHS * n_steps / (ms * 1e-3) / 1e12
-        mufu = MUFU_PER_PATH_STEP * PATHS * n_steps / (ms * 1e-3) / 1e9
+        achieved = FLOPS_PER_PATH_STEP * args.paths * n_steps / (ms * 1e-3) / 1e12
+        mufu = MUFU_PER_PATH_STEP * args.paths * n_steps / (ms * 1e-3) / 1e9
         line = {
             "metric": "path-steps/sec", "value": value, "unit": "path-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(world),
+            "config": config(world, args.paths),
             "e2e": {"value": e2e, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms},
             "gpu_launches": 2 * args.steps,

@@ -242,11 +242,15 @@ int thoth_gpu_measure_mufu_peak(double* gops, double* ms);
  * (2 MiB), which every GPU that loads the library holds until the process
  * exits. Books that do not fit return THOTH_GPU_E_TOO_LARGE (large books use
  * fewer CTAs before that). The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture. The
- * call is synchronous on the legacy default stream. Every call reuses the same
- * array and leaves its contents behind; the library serialises its own calls,
- * and work that overlaps one of these calls on the same GPU and touches the
- * array races with it. Same inputs, outputs and results as
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; make that first call
+ * before any stream capture, and do not reset the device's context (cudaDeviceReset)
+ * between calls. The call prices on the device the engine is bound to once any other
+ * entry point has run (as they do), else on the calling thread's current device. It
+ * honours thoth_gpu_request_cancel once the engine is set up, through the engine's
+ * existing mapped cancel word. The call is synchronous on the legacy default stream.
+ * Every call reuses the same array and leaves its contents behind; the library
+ * serialises its own calls, and work that overlaps one of these calls on the same GPU
+ * and touches the array races with it. Same inputs, outputs and results as
  * thoth_gpu_price_book, except device_ms, which is not measured here (NaN). */
 int thoth_gpu_price_book_noalloc(const ThothBookDesc* book, ThothBookResult* out);
 

@@ -25,13 +25,24 @@ _port = None
 _ref = None
 
 
+def reference_root(ref=None):
+    """The reference checkout (GValas/Thoth): `ref`, else $THOTH_REFERENCE, else a
+    directory named `reference` beside this repository. None where none of them holds
+    the pricer's sources."""
+    for cand in (ref, os.environ.get("THOTH_REFERENCE"), ROOT.parent / "reference"):
+        if cand and (pathlib.Path(cand) / "pricer" / "src").is_dir():
+            return pathlib.Path(cand)
+    return None
+
+
 def build(ref=None):
     """Compile the port (and the reference build when its sources exist)."""
     targets = ["port"]
-    refroot = pathlib.Path(ref or os.environ.get("THOTH_REFERENCE", "/root/reference"))
-    if (refroot / "pricer" / "src").is_dir():
+    refroot = reference_root(ref)
+    if refroot is not None:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "REF=%s" % refroot] + targets, check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE)] + (["REF=%s" % refroot] if refroot else []) + targets,
+                   check=True)
 
 
 def port():

@@ -20,7 +20,7 @@ def run_bench(*args, env=None):
 
 
 def test_reference_arm_prints_one_line_with_the_contract_keys():
-    p = run_bench("--impl", "reference", "--steps", "2", "--warmup", "1", "--cpu-sample-paths", "1024")
+    p = run_bench("--impl", "reference", "--steps", "2", "--warmup", "1", "--paths", "1024")
     assert p.returncode == 0, p.stderr
     lines = [ln for ln in p.stdout.splitlines() if ln.strip()]
     assert len(lines) == 1
@@ -28,8 +28,11 @@ def test_reference_arm_prints_one_line_with_the_contract_keys():
     assert line["impl"] == "reference"
     assert line["metric"] == "path-steps/sec" and line["unit"] == "path-steps/s"
     assert line["higher_is_better"] is True and line["steps"] == 2 and line["warmup"] == 1
-    assert line["config"]["workload"] == "heston_vanilla_grid" and line["config"]["paths"] == 1 << 20
+    assert line["config"]["workload"] == "heston_vanilla_grid" and line["config"]["paths"] == 1024
     assert line["value"] > 0 and line["ms_per_step"] > 0
+    # the timed steps are the whole workload: ms_per_step is what the timed region took per step
+    assert line["steps"] * line["ms_per_step"] <= 1e3 * line["wall_s_timed_region"] * 1.001
+    assert abs(line["value"] - 1024 * 504 / (line["ms_per_step"] * 1e-3)) <= 1e-6 * line["value"]
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] == (os.cpu_count() or 1) and cb["value"] == line["value"]
     assert "1024 paths" in cb["sample"]
@@ -39,7 +42,7 @@ def test_reference_arm_prints_one_line_with_the_contract_keys():
 
 
 def test_reference_arm_runs_on_rank_zero_only():
-    p = run_bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample-paths", "1024",
+    p = run_bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--paths", "1024",
                   env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert p.returncode == 0, p.stderr
     assert p.stdout.strip() == ""

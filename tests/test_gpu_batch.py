@@ -41,6 +41,23 @@ def test_every_book_of_a_ragged_batch_vs_oracle(gpu):
         assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"] + 1e-4 * abs(ref["book_premium"])
 
 
+def test_long_books_with_lsv_barriers_vs_oracle(gpu):
+    """Step counts up to the workload's 730 daily steps, every model, and LSV books with
+    daily-monitored barriers (down-and-out call, up-and-in put) among them: every book of
+    the batch against the oracle on the same Sobol paths."""
+    books = W.ragged_books(n_books=12, seed=29, min_paths=1 << 10, max_paths=1 << 12, min_steps=600,
+                           max_steps=730)
+    books += W.ragged_books(n_books=6, seed=31, min_paths=1 << 10, max_paths=1 << 12, min_steps=700,
+                            max_steps=730, model_mix=(0.0, 0.0, 1.0), payoffs=(1,))
+    assert max(len(b.days) - 1 for b in books) >= 725
+    assert sum(b.assets[0]["model"] == abi.MODEL_LSV and b.products[0]["kind"] == abi.BARRIER for b in books) >= 6
+    res = gpu.price_batch(books)
+    for i, (b, r) in enumerate(zip(books, res)):
+        ref = oracle.price_book(b, threads=THREADS)
+        assert_shared_path_parity(r, ref["premium"], ref["trust"], "book %d (%d steps)" % (i, len(b.days) - 1))
+        assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"] + 1e-4 * abs(ref["book_premium"])
+
+
 def test_batch_equals_one_at_a_time(gpu):
     books = small_batch(n=20, seed=3)
     res = gpu.price_batch(books)

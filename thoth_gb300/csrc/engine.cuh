@@ -101,6 +101,15 @@ struct DevProduct {
     int g_snap;         // 1: slot_g is a snapshot slot of a running group, 0: the group itself
 };
 
+// a vanilla product in the lean form used when every product of a book is a vanilla and no
+// pathwise Greek is asked: discounted flow f = max(a S + b, 0) with a = phi qfac df and
+// b = -phi K df (phi = +1 call, -1 put; df > 0), its weight in the book value w = fx, and
+// the observation slot of S at maturity
+struct alignas(16) VanTerm {
+    float a, b, w;
+    int slot;
+};
+
 struct Comp {
     int slot;
     float w;   // weight * quanto factor
@@ -152,6 +161,8 @@ struct DevPlan {
     int lev_row_stride;          // floats per leverage layer (max points over the assets)
     const float* grp_init;       // [n_groups] +inf (min), -inf (max), 0 (sums)
     const DevProduct* products;
+    const VanTerm* vterms;       // [n_products] lean vanilla terms (vanilla_only)
+    int vanilla_only;            // 1: every product a vanilla and no pathwise Greek
     const Comp* comps;
     const uint32_t* sobol_v;     // [4097][32] direction numbers
     const int* sobol_order;      // [n_sobol] Sobol dimensions in the order the step loop consumes them

@@ -9,13 +9,13 @@ namespace thoth {
 // shared-memory carve-up (host and device compute the same sizes)
 // ---------------------------------------------------------------------------
 struct Smem {
-    uint32_t* hs;   // [min(sobol_dims, HS_CHUNK)] tile parts of the current chunk of Sobol entries
-    float* stk;     // [stack_depth][stack_factors][T]
+    uint2* hs;      // [min(sobol_dims, HS_CHUNK)] tile parts of the current chunk of Sobol entries,
+                    // for tile columns t and t + T/2 (see tile_high_bits)
+    float* stk;     // [stack_depth][stack_factors][T]; after the time loop, the product partials
     float* slots;   // [n_slots][T + 1]
     float* grp;     // [n_groups][T + 1]
     float* last;    // [n_last][T + 1] previous observation of each discretely observed variance group
-    int* valid;     // [T]
-    float* part;    // [T * 6]
+    float* part;    // [T * 6] product partials: the bridge stack's space, free once the paths are built
     double* red;    // [2 * warps]
 };
 
@@ -27,17 +27,22 @@ __host__ __device__ constexpr int log2i(int x) { return x <= 1 ? 0 : 1 + log2i(x
 constexpr int HS_CHUNK = 512;
 __host__ __device__ inline int hs_words(int sobol_dims) { return sobol_dims < HS_CHUNK ? sobol_dims : HS_CHUNK; }
 
+// the bridge stack, or the product partials that reuse its space after the time loop
+__host__ __device__ inline size_t stack_part_bytes(int T, int stack_depth, int nfa)
+{
+    const size_t stk = sizeof(float) * (size_t)stack_depth * nfa * T, part = sizeof(float) * (size_t)T * 6;
+    return align16(stk > part ? stk : part);
+}
+
 __host__ __device__ inline size_t smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots,
                                              int n_groups, int n_last)
 {
     size_t b = 0;
-    b += align16(sizeof(uint32_t) * (size_t)hs_words(sobol_dims));
-    b += align16(sizeof(float) * (size_t)stack_depth * nfa * T);
+    b += align16(sizeof(uint2) * (size_t)hs_words(sobol_dims));
+    b += stack_part_bytes(T, stack_depth, nfa);
     b += align16(sizeof(float) * (size_t)n_slots * (T + 1));
     b += align16(sizeof(float) * (size_t)n_groups * (T + 1));
     b += align16(sizeof(float) * (size_t)n_last * (T + 1));
-    b += align16(sizeof(int) * (size_t)T);
-    b += align16(sizeof(float) * (size_t)T * 6);
     b += align16(sizeof(double) * 2 * (T / 32));
     return b;
 }
@@ -46,20 +51,17 @@ __device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
 {
     Smem s;
     size_t o = 0;
-    s.hs = reinterpret_cast<uint32_t*>(base + o);
-    o += align16(sizeof(uint32_t) * (size_t)hs_words(P.sobol_dims));
+    s.hs = reinterpret_cast<uint2*>(base + o);
+    o += align16(sizeof(uint2) * (size_t)hs_words(P.sobol_dims));
     s.stk = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * (size_t)P.stack_depth * P.stack_factors * T);
+    s.part = s.stk;
+    o += stack_part_bytes(T, P.stack_depth, P.stack_factors);
     s.slots = reinterpret_cast<float*>(base + o);
     o += align16(sizeof(float) * (size_t)P.n_slots_used * (T + 1));
     s.grp = reinterpret_cast<float*>(base + o);
     o += align16(sizeof(float) * (size_t)P.n_groups * (T + 1));
     s.last = reinterpret_cast<float*>(base + o);
     o += align16(sizeof(float) * (size_t)P.n_last * (T + 1));
-    s.valid = reinterpret_cast<int*>(base + o);
-    o += align16(sizeof(int) * (size_t)T);
-    s.part = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * (size_t)T * 6);
     s.red = reinterpret_cast<double*>(base + o);
     return s;
 }
@@ -77,9 +79,15 @@ __device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
 // entry j is used. Every thread of the CTA consumes the same entries in the
 // same order, so all of them reach a chunk boundary at the same call, where
 // the next chunk is computed between two barriers.
+//
+// Columns t and t + T/2 (t < T/2) differ in their low bits by gray(T/2) =
+// 3 << (TB - 2), so lo[d][t + T/2] = lo[d][t] ^ V[d][TB-1] ^ V[d][TB-2], a word
+// shared by the tile. The tile part is therefore kept as a pair, hs[j] and
+// hs[j] ^ V[d][TB-1] ^ V[d][TB-2]: a thread with two paths (columns t and
+// t + T/2) reads one low word per entry, and one 8-byte broadcast of the pair.
 // ---------------------------------------------------------------------------
 template <int TB>
-__device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m, int j0)
+__device__ inline void tile_high_bits(const DevPlan& P, uint2* hs, int64_t m, int j0)
 {
     const uint64_t g = (uint64_t)m ^ ((uint64_t)m >> 1);
     const int j1 = min(j0 + HS_CHUNK, P.n_sobol);
@@ -89,25 +97,33 @@ __device__ inline void tile_high_bits(const DevPlan& P, uint32_t* hs, int64_t m,
         uint64_t gg = g;
         for (int k = 0; gg != 0 && k < SOBOL_BITS - TB; ++k, gg >>= 1)
             if (gg & 1u) acc ^= __ldg(V + TB + k);
-        hs[j - j0] = acc;
+        hs[j - j0] = make_uint2(acc, acc ^ __ldg(V + TB - 1) ^ __ldg(V + TB - 2));
     }
 }
 
+// low words a thread loads per Sobol entry: one for its two paths (columns t and t + T/2,
+// through the tile-part pair), else one per path
+template <int PP>
+struct LoadsPerEntry {
+    static constexpr int value = PP == 2 ? 1 : PP;
+};
+
 template <int T, int PP>
 struct SobolLane {
-    uint32_t* hs;          // tile parts of entries [jend - HS_CHUNK, jend), smem
+    static constexpr int LW = LoadsPerEntry<PP>::value;
+    uint2* hs;             // tile parts of entries [jend - HS_CHUNK, jend), smem
     const uint32_t* lo;    // column threadIdx.x of the book's low words
     int64_t m;             // tile index
     int j, jend;           // next entry; end of the chunk in shared memory
-    uint32_t cur[PP], nxt[PP]; // low words of entries j and j + 1, per path of the thread
+    uint32_t cur[LW], nxt[LW]; // low words of entries j and j + 1
 };
 
 // path p of a thread is tile column threadIdx.x + p * (T / PP); the first chunk
 // of tile parts must already be in hs
 template <int TB, int PP>
-__device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, uint32_t* hs, int64_t m)
+__device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, uint2* hs, int64_t m)
 {
-    constexpr int T = 1 << TB, TH = T / PP;
+    constexpr int T = 1 << TB, TH = T / PP, LW = LoadsPerEntry<PP>::value;
     SobolLane<T, PP> L;
     L.hs = hs;
     L.lo = P.sobol_lo + threadIdx.x;
@@ -115,7 +131,7 @@ __device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, u
     L.j = 0;
     L.jend = HS_CHUNK;
 #pragma unroll
-    for (int p = 0; p < PP; ++p) {
+    for (int p = 0; p < LW; ++p) {
         L.cur[p] = P.n_sobol > 0 ? __ldg(L.lo + p * TH) : 0u;
         L.nxt[p] = P.n_sobol > 1 ? __ldg(L.lo + T + p * TH) : 0u;
     }
@@ -128,7 +144,7 @@ template <int T, int PP>
 __device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, const uint64_t (&n)[PP], int dim,
                                       float (&z)[PP])
 {
-    constexpr int TH = T / PP;
+    constexpr int TH = T / PP, LW = LoadsPerEntry<PP>::value;
     uint32_t x[PP];
     if (dim < P.sobol_dims) {
         if (L.j == L.jend) { // next chunk of tile parts (uniform across the CTA, see above)
@@ -137,12 +153,18 @@ __device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, con
             __syncthreads();
             L.jend += HS_CHUNK;
         }
-        const uint32_t h = L.hs[L.j - (L.jend - HS_CHUNK)];
+        const uint2 h = L.hs[L.j - (L.jend - HS_CHUNK)];
         const int jn = L.j + 2;
         const bool more = jn < P.n_sobol;
+        if constexpr (PP == 2) {
+            x[0] = h.x ^ L.cur[0];
+            x[1] = h.y ^ L.cur[0];
+        } else {
 #pragma unroll
-        for (int p = 0; p < PP; ++p) {
-            x[p] = h ^ L.cur[p];
+            for (int p = 0; p < PP; ++p) x[p] = h.x ^ L.cur[p];
+        }
+#pragma unroll
+        for (int p = 0; p < LW; ++p) {
             L.cur[p] = L.nxt[p];
             L.nxt[p] = more ? __ldg(L.lo + jn * T + p * TH) : 0u;
         }
@@ -671,11 +693,17 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                 }
             }
         }
-#pragma unroll
-        for (int p = 0; p < PP; ++p) S.valid[t + p * TH] = valid[p] ? 1 : 0;
-        __syncthreads();
+        __syncthreads(); // every path of the tile observed
 
         // ---- product evaluation: thread per product, FP32 tile partials ----
+        // The tile's valid paths are the contiguous columns [k0, k0 + nv). Every sum of the tile
+        // is shifted by the value at column k0 (payoff, pathwise delta, pathwise vega of the
+        // product): the FP32 partials hold f - c and (f - c)^2, and the shift is added back in
+        // FP64. So the sum of squares keeps its precision where the payoff's variance is small
+        // next to its square (deep in-the-money cells), and the trust with it.
+        const int k0 = (int)max((int64_t)0, P.skip + 1 - m * T);
+        const int kend = (int)min((int64_t)T, P.skip + P.paths - m * T + 1);
+        const int nv = kend - k0;
         const int C = P.n_products;
         for (int pc = 0; pc < C; pc += TH) {
             const int CP = min(C - pc, TH);
@@ -683,19 +711,39 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
             const int pl = t % CP, g = t / CP;
             float a6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (g < G) {
-                const DevProduct pr = P.products[pc + pl];
-                for (int k = g; k < T; k += G) {
-                    if (!S.valid[k]) continue;
-                    const float f = payoff(P, pr, S.slots, S.grp, stride, k);
-                    a6[0] += f;
-                    a6[1] = fmaf(f, f, a6[1]);
-                    if (P.greeks) {
-                        float d, gg;
-                        greeks_of(P, pr, S.slots, stride, k, d, gg);
-                        a6[2] += d;
-                        a6[3] = fmaf(d, d, a6[3]);
-                        a6[4] += gg;
-                        a6[5] = fmaf(gg, gg, a6[5]);
+                if (P.vanilla_only) {
+                    // lean vanilla loop: f = max(a S + b, 0), no dispatch
+                    const VanTerm vt = P.vterms[pc + pl];
+                    const float* col = S.slots + vt.slot * stride;
+                    const float c0 = fmaxf(fmaf(vt.a, col[k0], vt.b), 0.f);
+                    float s1 = 0.f, s2 = 0.f;
+#pragma unroll 4
+                    for (int k = k0 + g; k < kend; k += G) {
+                        const float f = fmaxf(fmaf(vt.a, col[k], vt.b), 0.f) - c0;
+                        s1 += f;
+                        s2 = fmaf(f, f, s2);
+                    }
+                    a6[0] = s1;
+                    a6[1] = s2;
+                } else {
+                    const DevProduct pr = P.products[pc + pl];
+                    const float c0 = payoff(P, pr, S.slots, S.grp, stride, k0);
+                    float cd = 0.f, cg = 0.f;
+                    if (P.greeks) greeks_of(P, pr, S.slots, stride, k0, cd, cg);
+                    for (int k = k0 + g; k < kend; k += G) {
+                        const float f = payoff(P, pr, S.slots, S.grp, stride, k) - c0;
+                        a6[0] += f;
+                        a6[1] = fmaf(f, f, a6[1]);
+                        if (P.greeks) {
+                            float d, gg;
+                            greeks_of(P, pr, S.slots, stride, k, d, gg);
+                            d -= cd;
+                            gg -= cg;
+                            a6[2] += d;
+                            a6[3] = fmaf(d, d, a6[3]);
+                            a6[4] += gg;
+                            a6[5] = fmaf(gg, gg, a6[5]);
+                        }
                     }
                 }
 #pragma unroll
@@ -703,10 +751,27 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
             }
             __syncthreads();
             if (t < CP) {
+                float cf = 0.f, cd = 0.f, cg = 0.f;
+                if (P.vanilla_only) {
+                    const VanTerm vt = P.vterms[pc + t];
+                    cf = fmaxf(fmaf(vt.a, S.slots[vt.slot * stride + k0], vt.b), 0.f);
+                } else {
+                    const DevProduct pr = P.products[pc + t];
+                    cf = payoff(P, pr, S.slots, S.grp, stride, k0);
+                    if (P.greeks) greeks_of(P, pr, S.slots, stride, k0, cd, cg);
+                }
+                const float c3[3] = {cf, cd, cg};
                 double s6[6] = {0, 0, 0, 0, 0, 0};
                 for (int g2 = 0; g2 < G; ++g2)
 #pragma unroll
                     for (int j = 0; j < 6; ++j) s6[j] += (double)S.part[(g2 * CP + t) * 6 + j];
+                // sum f = sum (f - c) + n c;  sum f^2 = sum (f - c)^2 + 2 c sum (f - c) + n c^2
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const double c = c3[q], d1 = s6[2 * q];
+                    s6[2 * q + 1] += 2.0 * c * d1 + (double)nv * c * c;
+                    s6[2 * q] = d1 + (double)nv * c;
+                }
 #pragma unroll
                 for (int j = 0; j < 6; ++j) acc[(size_t)(pc + t) * 6 + j] += s6[j];
             }
@@ -714,14 +779,28 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
         }
         // ---- book value per path (book_node.cpp:16-31) ---------------------
         double b1 = 0.0, b2 = 0.0;
+        float bv[PP];
 #pragma unroll
-        for (int p = 0; p < PP; ++p) {
-            float b = 0.f;
-            if (valid[p])
+        for (int p = 0; p < PP; ++p) bv[p] = 0.f;
+        if (P.vanilla_only) {
+            // the thread's paths share each product's terms
+            for (int q = 0; q < C; ++q) {
+                const VanTerm vt = P.vterms[q];
+                const float* col = S.slots + vt.slot * stride + t;
+#pragma unroll
+                for (int p = 0; p < PP; ++p) bv[p] = fmaf(vt.w, fmaxf(fmaf(vt.a, col[p * TH], vt.b), 0.f), bv[p]);
+            }
+        } else {
+#pragma unroll
+            for (int p = 0; p < PP; ++p)
                 for (int q = 0; q < C; ++q) {
                     const DevProduct pr = P.products[q];
-                    b = fmaf(payoff(P, pr, S.slots, S.grp, stride, t + p * TH), pr.fx, b);
+                    bv[p] = fmaf(payoff(P, pr, S.slots, S.grp, stride, t + p * TH), pr.fx, bv[p]);
                 }
+        }
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+            const float b = valid[p] ? bv[p] : 0.f;
             b1 += b;
             b2 += (double)b * b;
         }

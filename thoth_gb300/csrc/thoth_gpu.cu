@@ -438,7 +438,8 @@ struct Plan {
     DevPlan dp{};
     Blob blob;
     // offsets of the sections inside the blob
-    size_t o_steps, o_isd, o_prog, o_nodes, o_recs, o_evr, o_ev, o_lay, o_map, o_levv, o_ginit, o_prod, o_comp, o_sord;
+    size_t o_steps, o_isd, o_prog, o_nodes, o_recs, o_evr, o_ev, o_lay, o_map, o_levv, o_ginit, o_prod, o_vterm, o_comp,
+        o_sord;
     int variant = 1, base_variant = 1, shape = 0, T = 256;
     size_t smem = 0;
     int n_products = 0;
@@ -914,6 +915,15 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
         R.greek_mask = P.greek_mask[p];
     }
     if (comps.empty()) comps.push_back(Comp{0, 0.f, -1, 0.f});
+    // every product a vanilla and no pathwise Greek: the kernel's lean product loops
+    D.vanilla_only = D.greeks == 0;
+    for (int p = 0; p < d->n_products; p++) D.vanilla_only &= prods[p].kind == P_VANILLA;
+    std::vector<VanTerm> vterms(d->n_products);
+    for (int p = 0; p < d->n_products; p++) {
+        const DevProduct& R = prods[p];
+        const float phi = R.call ? 1.f : -1.f;
+        vterms[p] = VanTerm{phi * R.qfac * R.df, -phi * R.K * R.df, R.fx, R.slot_s};
+    }
     D.n_slots_used = std::max(n_slots, 1);
     D.n_groups = (int)grp_init.size();
     if (grp_init.empty()) grp_init.push_back(0.f);
@@ -958,6 +968,7 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     P.o_levv = P.blob.put(lev_values);
     P.o_ginit = P.blob.put(grp_init);
     P.o_prod = P.blob.put(prods);
+    P.o_vterm = P.blob.put(vterms);
     P.o_comp = P.blob.put(comps);
     P.o_sord = P.blob.put(order);
     // shapes 0 and 1 share the 256-path tile, so the plan above serves both
@@ -980,6 +991,7 @@ void bind(Plan& P, unsigned char* base)
     D.lev_values = reinterpret_cast<const float*>(base + P.o_levv);
     D.grp_init = reinterpret_cast<const float*>(base + P.o_ginit);
     D.products = reinterpret_cast<const DevProduct*>(base + P.o_prod);
+    D.vterms = reinterpret_cast<const VanTerm*>(base + P.o_vterm);
     D.comps = reinterpret_cast<const Comp*>(base + P.o_comp);
     D.sobol_order = reinterpret_cast<const int*>(base + P.o_sord);
     D.sobol_v = g_dev.sobol_v;
@@ -1514,7 +1526,8 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[THOTH_NOALLOC_S
 static constexpr int kMaxDevices = 64;
 static unsigned char* g_noalloc_ptr[kMaxDevices] = {};
 
-// once per device, with that device current
+// once per device, with that device current. The address is cached for the life of the
+// process: a context reset (cudaDeviceReset) between calls is not supported.
 static int noalloc_address(int dev, unsigned char** out)
 {
     if (dev < 0 || dev >= kMaxDevices) return fail(THOTH_GPU_E_NODEVICE, "device index out of range");
@@ -1533,7 +1546,12 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     if (!out) return fail(THOTH_GPU_E_INVALID, "null result");
     int dev = 0, count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return fail(THOTH_GPU_E_NODEVICE, "no CUDA device");
+    // once the engine is bound to a device (any earlier call of the other entry points), this
+    // call prices on that device as they do; before that, on the calling thread's current one
+    if (g_dev.ready) CUDA_TRY(cudaSetDevice(g_dev.id));
     CUDA_TRY(cudaGetDevice(&dev));
+    // a cancel requested before the call ends it here, as at the first tile of the other entry points
+    if (g_dev.ready && *(volatile int*)g_dev.cancel_host) return fail(THOTH_GPU_E_CANCELLED, "pricing cancelled");
     cudaDeviceProp prop;
     CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
     if (!(prop.major == 10 && prop.minor == 3))
@@ -1583,7 +1601,9 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     bind(P, base);
     P.dp.sobol_v = reinterpret_cast<const uint32_t*>(base + o_v);
     P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(base + o_lo);
-    P.dp.cancel = nullptr;
+    // the engine's host-mapped cancel word, where the engine set it up (it needs no allocation
+    // here); the kernel reads it at every tile
+    P.dp.cancel = g_dev.ready ? g_dev.cancel_dev : nullptr;
     P.dp.acc = reinterpret_cast<double*>(base + o_acc);
     P.dp.status = reinterpret_cast<int*>(base + o_st);
     CUDA_TRY(launch_book(P.dp, P.variant, P.shape, grid, P.smem, 0));

@@ -15,8 +15,10 @@ file once and writes the compact binary joe_kuo_6_21201.bin next to it:
     MOFF    uint32[dims + 1]
     M       uint32[nm]
 
-All integers little-endian. Usage: python extract_joe_kuo.py <reference root>
+All integers little-endian. Usage: python extract_joe_kuo.py [reference root]
+(default: $THOTH_REFERENCE).
 """
+import os
 import pathlib
 import re
 import struct
@@ -31,7 +33,10 @@ def parse_array(text, name):
 
 
 def main():
-    root = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("THOTH_REFERENCE")
+    if not arg:
+        raise SystemExit("usage: extract_joe_kuo.py <reference root> (or set THOTH_REFERENCE)")
+    root = pathlib.Path(arg)
     src = (root / "pricer/src/nodes/sobol_direction_numbers.cpp").read_text()
     dims = int(re.search(r"FILE_DIMS\s*=\s*(\d+)", src).group(1))
     S = parse_array(src, "S")

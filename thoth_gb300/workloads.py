@@ -195,9 +195,11 @@ def american_put(paths=1 << 20, heston=True, days=None):
 
 
 def ragged_books(n_books=256, seed=7, min_paths=1 << 14, max_paths=1 << 22, min_steps=12, max_steps=730,
-                 path_scale=1.0):
+                 path_scale=1.0, model_mix=(0.4, 0.4, 0.2), payoffs=(0, 1, 2)):
     """Batched ragged workload: path counts log-uniform in [min, max], step counts uniform,
-    model mix 40% GBM / 40% Heston / 20% LSV, payoff mix vanilla / barrier / variance."""
+    model mix 40% GBM / 40% Heston / 20% LSV, payoff mix vanilla / barrier / variance.
+    model_mix (GBM, Heston, LSV shares) and payoffs (0 vanilla, 1 barrier, 2 variance) narrow
+    the mix; at their defaults the draws are those of the ragged-book workload."""
     rng = np.random.default_rng(seed)
     books = []
     for _ in range(n_books):
@@ -208,11 +210,11 @@ def ragged_books(n_books=256, seed=7, min_paths=1 << 14, max_paths=1 << 22, min_
         b = Book(days=days, paths=paths)
         u = rng.random()
         r = 0.03
-        if u < 0.4:
+        if u < model_mix[0]:
             a = b.add_gbm(100.0, 0.25, r - 0.01)
         else:
             lev = None
-            if u >= 0.8:
+            if u >= model_mix[0] + model_mix[1]:
                 nd = steps + 1
                 ln_step = (math.log(250.0) - math.log(30.0)) / 49
                 offset = int(math.floor(math.log(30.0) / ln_step))
@@ -220,7 +222,7 @@ def ragged_books(n_books=256, seed=7, min_paths=1 << 14, max_paths=1 << 22, min_
                 lev = (np.full(nd, ln_step), np.full(nd, offset, dtype=np.int64), vals)
             a = b.add_heston(100.0, HESTON["v0"], HESTON["kappa"], HESTON["theta"], HESTON["xi"], HESTON["rho"], r,
                              leverage=lev)
-        kind = rng.integers(0, 3)
+        kind = payoffs[int(rng.integers(0, len(payoffs)))]
         mat = steps
         if kind == 0:
             for K in (90.0, 100.0, 110.0):
