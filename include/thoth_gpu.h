@@ -505,6 +505,19 @@ int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y,
 int thoth_gpu_surrogate_gradient(ThothSurrogate* s, const float* x, const float* y, const float* scale, int32_t rows,
                                  float* grad, double* loss);
 int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, float* y, double* device_ms);
+/* Prices of a lattice grid in units of spot, every step on the device: the cells are
+ * every (parameter set, maturity, log-moneyness), cell (s, j, k) at index
+ * (s * n_T + j) * n_lm + k, with raw features (lms[k], Ts[j], params[s * 5 + 0..4] =
+ * kappa, theta, xi, rho, v0). Each cell's features are clipped to the training box
+ * [box_lo, box_hi] (7 each, in that feature order) and normalised to [-1, 1], the network
+ * is evaluated, and its output is multiplied by the scale it was trained against:
+ * sqrt(bs^2 + floor^2), bs the Black-Scholes call (S = 1, r = q = 0) at the expected
+ * average Heston variance theta + (v0 - theta)(1 - e^-kT)/(kT) over [0, T]. Only the
+ * parameter sets and the lattice axes cross to the device and only the prices come back.
+ * *device_ms: the three kernels' device time. */
+int thoth_gpu_surrogate_price_lattice(ThothSurrogate* s, const double* params, int32_t n_sets, const double* lms,
+                                      int32_t n_lm, const double* Ts, int32_t n_T, const double* box_lo,
+                                      const double* box_hi, double floor, float* prices, double* device_ms);
 const char* thoth_gpu_surrogate_last_error(void);
 
 /* Cooperative cancellation (reference: helpers/cancellation.hpp:9-15): a

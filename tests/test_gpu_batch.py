@@ -13,7 +13,7 @@ import pytest
 
 import oracle
 from thoth_gb300 import abi, workloads as W
-from tests.test_gpu_parity import assert_shared_path_parity
+from tests.test_gpu_parity import assert_shared_path_parity, leg_scale
 
 pytestmark = pytest.mark.gpu
 
@@ -54,8 +54,11 @@ def test_long_books_with_lsv_barriers_vs_oracle(gpu):
     res = gpu.price_batch(books)
     for i, (b, r) in enumerate(zip(books, res)):
         ref = oracle.price_book(b, threads=THREADS)
-        assert_shared_path_parity(r, ref["premium"], ref["trust"], "book %d (%d steps)" % (i, len(b.days) - 1))
-        assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"] + 1e-4 * abs(ref["book_premium"])
+        sc = leg_scale(b)
+        assert_shared_path_parity(r, ref["premium"], ref["trust"], "book %d (%d steps)" % (i, len(b.days) - 1),
+                                  scale=sc)
+        assert abs(r["book_premium"] - ref["book_premium"]) <= (0.5 * ref["book_trust"] +
+                                                                1e-4 * max(abs(ref["book_premium"]), sc.sum()))
 
 
 def test_batch_equals_one_at_a_time(gpu):
@@ -115,7 +118,7 @@ def test_autotune_book_keeps_parity(gpu, make, tmp_path):
     t = gpu.autotune_book(b, reps=2)
     # every launch shape (paths per thread x tile size) and grid was timed; the default is among them
     assert t["candidates"] >= 8 and 1 <= t["grid"]
-    assert t["shape"] in (0, 1, 2, 3) and t["threads"] in (64, 128, 256) and t["tile_paths"] in (128, 256)
+    assert t["shape"] in (0, 1, 2, 3, 4) and t["threads"] in (64, 128, 256) and t["tile_paths"] in (128, 256)
     assert t["best_ms"] <= t["default_ms"] * (1 + 1e-9)
     plan = gpu.plan_summary(b)
     assert plan["shape"] == t["shape"] and plan["threads"] == t["threads"] and plan["tile"] == t["tile_paths"]
@@ -149,7 +152,7 @@ def test_every_launch_shape_matches_the_oracle(gpu, variant, shape_paths, tmp_pa
     base = tmp_path / "base.txt"
     gpu.autotune_save(base)                 # header lines of this device, nothing tuned
     ref = oracle.price_book(b, threads=THREADS)
-    for shape in range(4):
+    for shape in range(5):
         f = tmp_path / ("s%d.txt" % shape)
         f.write_text(base.read_text() + "%s %d 0 0\n" % (key, shape))
         gpu.autotune_clear()
@@ -162,7 +165,7 @@ def test_every_launch_shape_matches_the_oracle(gpu, variant, shape_paths, tmp_pa
 def test_autotune_batch_save_load(gpu, tmp_path):
     books = small_batch(n=16, seed=21)
     t = gpu.autotune_batch(books, reps=1)
-    assert t["streams"] in (1, 2, 4, 8, 16) and t["policy"] in (0, 1, 2) and t["shape"] in (-1, 0, 1, 2, 3)
+    assert t["streams"] in (1, 2, 4, 8, 16) and t["policy"] in (0, 1, 2) and t["shape"] in (-1, 0, 1, 2, 3, 4)
     assert t["candidates"] >= 10
     path = tmp_path / "tune.txt"
     gpu.autotune_save(path)

@@ -22,10 +22,24 @@ pytestmark = pytest.mark.gpu
 REL, ABS = 1e-4, 1e-5
 
 
-def assert_shared_path_parity(gpu_res, premium, trust, label=""):
+def leg_scale(book):
+    """Per product, the size the relative bar applies to: the premium itself, except for a
+    variance swap, whose premium is the difference of its two legs, notional * (realised
+    variance - strike variance), and can sit near zero. There the bar applies to the
+    variance leg, notional * strike variance (realised variance is summed in FP32 on the
+    device, in FP64 by the oracle)."""
+    out = np.zeros(len(book.products))
+    for k, p in enumerate(book.products):
+        if p["kind"] == abi.VARIANCE:
+            out[k] = abs(p.get("notional", 1.0) * p.get("strike_variance", 0.0))
+    return out
+
+
+def assert_shared_path_parity(gpu_res, premium, trust, label="", scale=None):
     g = np.asarray(gpu_res["premium"])
     err = np.abs(g - premium)
-    bad = (err > 0.5 * trust + 1e-12) | (err > REL * np.abs(premium) + ABS)
+    size = np.abs(premium) if scale is None else np.maximum(np.abs(premium), scale)
+    bad = (err > 0.5 * trust + 1e-12) | (err > REL * size + ABS)
     assert not bad.any(), "%s: worst product %d gpu %.8g ref %.8g se %.3g" % (
         label, int(np.argmax(err)), g[np.argmax(err)], premium[np.argmax(err)], trust[np.argmax(err)])
 

@@ -52,6 +52,26 @@ def test_inference_matches_cpu_oracle(gpu):
     m.close()
 
 
+def test_lattice_serving_matches_host_features(gpu):
+    """Features, clipping, normalisation and price scale built on the device give the prices
+    of the host path (predict_prices on the clipped lattice features), and the oracle's
+    network with the same scale; sets outside the box are clipped the same way."""
+    m = S.Surrogate(seed=6)
+    rng = np.random.default_rng(7)
+    sets = rng.uniform(S.BOX_LO[2:], S.BOX_HI[2:], size=(37, 5))
+    sets[3] = S.BOX_HI[2:] * 1.2                         # outside the box: clipped
+    lms, Ts = S.LATTICE_LM[::3], S.LATTICE_T[::2]
+    got, ms = m.price_lattice(sets, lms, Ts)
+    X = np.concatenate([S.lattice_features(p, lms, Ts) for p in sets])
+    Xc = np.clip(X, S.BOX_LO, S.BOX_HI)
+    want, _ = S.predict_prices(m, Xc)
+    assert got.shape == want.shape and ms > 0
+    assert np.abs(got - want).max() <= 1e-6 * max(1.0, np.abs(want).max())
+    yo, _, _ = MO.forward(m.params().astype(np.float64), S.normalise(Xc).astype(np.float64))
+    assert np.abs(got - yo * S.price_scale(Xc)).max() <= 1e-3 * max(1.0, np.abs(want).max())
+    m.close()
+
+
 def test_adam_step_matches_cpu(gpu):
     m = S.Surrogate(seed=5)
     p0 = m.params().astype(np.float64)
@@ -105,6 +125,10 @@ def test_price_grid_pipeline_small(gpu):
         price, info = S.price_grid(m, ev, mc_paths=1 << 14, judge_frac=0.25, judge_paths=1 << 16, policy=policy)
         assert price.shape == (8 * 252,) and np.isfinite(price).all()
         assert info["judge_sets"] == 2 and info["cells"] == 8 * 252 and info["policy"] == policy
+        # every flagged bucket of every in-box set went to MC, timed as run
+        assert info["fallback_cells"] == info["failing_buckets"] * 8 + 252 * info["out_of_box_sets"]
+        assert info["seconds"] == info["inference_s"] + info["judge_s"] + info["fallback_s"]
+        assert np.isfinite(info["estimated_p90"]) and info["judge_noise_rms"] > 0
         fails[policy] = info["failing_buckets"]
     # the grid policy never takes over more buckets than the per-bucket one
     assert fails["grid"] <= fails["bucket"]

@@ -113,10 +113,10 @@ def build(verbose=False):
     os.replace(tmp, LIB)
     # C++ host drop-in (namespace gpu over the C ABI) and its check program
     host = HERE / "host"
-    subprocess.run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-I", str(ROOT / "include"),
+    subprocess.run(["g++", "-std=c++23", "-O2", "-fPIC", "-shared", "-I", str(ROOT / "include"),
                     str(host / "mcl_gpu.cpp"), "-L", str(BUILD), "-lthoth_gpu", "-Wl,-rpath,$ORIGIN",
                     "-o", str(BUILD / "libthoth_mcl_gpu.so")], check=True)
-    subprocess.run(["g++", "-std=c++20", "-O2", "-I", str(ROOT / "include"), "-I", str(host),
+    subprocess.run(["g++", "-std=c++23", "-O2", "-I", str(ROOT / "include"), "-I", str(host),
                     str(host / "host_check.cpp"), "-L", str(BUILD), "-lthoth_mcl_gpu", "-lthoth_gpu",
                     "-Wl,-rpath,$ORIGIN", "-o", str(BUILD / "host_check")], check=True)
     return LIB

@@ -181,9 +181,10 @@ struct DevPlan {
 // Inverse normal CDF in FP32 for a uniform u = x * 2^-32, x a nonzero uint32.
 // Method: Giles (2010, "Approximating the erfinv function") change of variable
 // w = -ln(4 q (1 - q)), q = min(u, 1 - u), with polynomials in w (central) and
-// sqrt(w) (tail) whose coefficients were fitted for this project by weighted
-// least squares against 40-digit reference values; max relative error of the
-// FP32 evaluation 2.2e-7 over the full uint32 range. Both q and 2u - 1 are
+// sqrt(w) (tail) whose coefficients are fitted for this project: minimax in
+// relative error against 40-digit values, rounded to float32 with refits and a
+// one-ulp polish; thoth_gb300/csrc/fit_quantile.py prints them. The polynomials'
+// FP32 evaluation is within 1.5e-7 (central) and 1.1e-7 (tail) of the target. Both q and 2u - 1 are
 // formed from the integer (q = min(x, 2^32 - x), 2u - 1 = (x - 2^31) 2^-31),
 // so the tails keep their relative accuracy.
 // ---------------------------------------------------------------------------
@@ -204,16 +205,16 @@ constexpr float QUANTILE_TAIL_LG = -9.016844005556021f; // w = -ln2 lg = 6.25
 __device__ __forceinline__ float quantile_central(float lg)
 {
     const float v = fmaf(lg, -0.6931471805599453f, -3.125f);
-    float p = -7.202387403e-09f;
-    p = fmaf(p, v, -1.226470401e-08f);
-    p = fmaf(p, v, 6.170809376e-07f);
-    p = fmaf(p, v, -2.155695626e-06f);
-    p = fmaf(p, v, -1.975007828e-05f);
-    p = fmaf(p, v, 2.648245696e-04f);
-    p = fmaf(p, v, -1.047204452e-03f);
-    p = fmaf(p, v, -8.533770903e-03f);
-    p = fmaf(p, v, 3.396347351e-01f);
-    p = fmaf(p, v, 2.338620874e+00f);
+    float p = -7.086651266e-09f;
+    p = fmaf(p, v, -1.266508587e-08f);
+    p = fmaf(p, v, 6.137755690e-07f);
+    p = fmaf(p, v, -2.147811756e-06f);
+    p = fmaf(p, v, -1.971671372e-05f);
+    p = fmaf(p, v, 2.647771616e-04f);
+    p = fmaf(p, v, -1.047342434e-03f);
+    p = fmaf(p, v, -8.533691987e-03f);
+    p = fmaf(p, v, 3.396349251e-01f);
+    p = fmaf(p, v, 2.338620901e+00f);
     return p;
 }
 
@@ -221,16 +222,16 @@ __device__ __forceinline__ float quantile_central(float lg)
 __device__ __forceinline__ float quantile_tail(float lg)
 {
     const float v = sqrtf(lg * -0.6931471805599453f) - 3.6479158f;
-    float p = 6.598971903e-06f;
-    p = fmaf(p, v, 5.795662157e-05f);
-    p = fmaf(p, v, -2.423309240e-04f);
-    p = fmaf(p, v, 3.854843299e-04f);
-    p = fmaf(p, v, -5.190533957e-04f);
-    p = fmaf(p, v, 9.818501131e-04f);
-    p = fmaf(p, v, -2.186479756e-03f);
-    p = fmaf(p, v, 3.518813816e-03f);
-    p = fmaf(p, v, 1.425832630e+00f);
-    p = fmaf(p, v, 4.927907588e+00f);
+    float p = 3.439537977e-05f;
+    p = fmaf(p, v, 1.085241311e-04f);
+    p = fmaf(p, v, -2.765924437e-04f);
+    p = fmaf(p, v, 2.949863265e-04f);
+    p = fmaf(p, v, -5.131622893e-04f);
+    p = fmaf(p, v, 1.033666427e-03f);
+    p = fmaf(p, v, -2.182901371e-03f);
+    p = fmaf(p, v, 3.508982947e-03f);
+    p = fmaf(p, v, 1.425832033e+00f);
+    p = fmaf(p, v, 4.927907944e+00f);
     return p;
 }
 
@@ -274,25 +275,24 @@ __device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 quantile_central2(float2 lg)
 {
     const float2 v = __ffma2_rn(lg, f2s(-0.6931471805599453f), f2s(-3.125f));
-    float2 p = f2s(-7.202387403e-09f);
-    p = __ffma2_rn(p, v, f2s(-1.226470401e-08f));
-    p = __ffma2_rn(p, v, f2s(6.170809376e-07f));
-    p = __ffma2_rn(p, v, f2s(-2.155695626e-06f));
-    p = __ffma2_rn(p, v, f2s(-1.975007828e-05f));
-    p = __ffma2_rn(p, v, f2s(2.648245696e-04f));
-    p = __ffma2_rn(p, v, f2s(-1.047204452e-03f));
-    p = __ffma2_rn(p, v, f2s(-8.533770903e-03f));
-    p = __ffma2_rn(p, v, f2s(3.396347351e-01f));
-    p = __ffma2_rn(p, v, f2s(2.338620874e+00f));
+    float2 p = f2s(-7.086651266e-09f);
+    p = __ffma2_rn(p, v, f2s(-1.266508587e-08f));
+    p = __ffma2_rn(p, v, f2s(6.137755690e-07f));
+    p = __ffma2_rn(p, v, f2s(-2.147811756e-06f));
+    p = __ffma2_rn(p, v, f2s(-1.971671372e-05f));
+    p = __ffma2_rn(p, v, f2s(2.647771616e-04f));
+    p = __ffma2_rn(p, v, f2s(-1.047342434e-03f));
+    p = __ffma2_rn(p, v, f2s(-8.533691987e-03f));
+    p = __ffma2_rn(p, v, f2s(3.396349251e-01f));
+    p = __ffma2_rn(p, v, f2s(2.338620901e+00f));
     return p;
 }
 
-// quantile_n for a thread's two paths: quantile_prep and the central polynomial paired
-template <>
-__device__ __forceinline__ void quantile_n<2>(const uint32_t (&x)[2], float (&z)[2])
+// quantiles of two words, quantile_prep and the central polynomial paired
+__device__ __forceinline__ void quantile_pair(uint32_t x0, uint32_t x1, float& z0, float& z1)
 {
-    const uint32_t q0 = min(x[0], 0u - x[0]), q1 = min(x[1], 0u - x[1]);
-    const float2 sv = __fmul2_rn(f2(__int2float_rn((int)(x[0] ^ 0x80000000u)), __int2float_rn((int)(x[1] ^ 0x80000000u))),
+    const uint32_t q0 = min(x0, 0u - x0), q1 = min(x1, 0u - x1);
+    const float2 sv = __fmul2_rn(f2(__int2float_rn((int)(x0 ^ 0x80000000u)), __int2float_rn((int)(x1 ^ 0x80000000u))),
                                  f2s(4.656612873077393e-10f));
     const float2 qf = f2(__uint2float_rn(q0), __uint2float_rn(q1));
     const float2 one_m_q = __ffma2_rn(qf, f2s(-2.3283064365386963e-10f), f2s(1.0f));
@@ -304,8 +304,22 @@ __device__ __forceinline__ void quantile_n<2>(const uint32_t (&x)[2], float (&z)
         if (!(lg1 > QUANTILE_TAIL_LG)) zz.y = quantile_tail(lg1);
     }
     zz = __fmul2_rn(zz, sv);
-    z[0] = zz.x;
-    z[1] = zz.y;
+    z0 = zz.x;
+    z1 = zz.y;
+}
+
+// quantile_n for an even number of paths a thread: their quantiles in pairs
+template <>
+__device__ __forceinline__ void quantile_n<2>(const uint32_t (&x)[2], float (&z)[2])
+{
+    quantile_pair(x[0], x[1], z[0], z[1]);
+}
+
+template <>
+__device__ __forceinline__ void quantile_n<4>(const uint32_t (&x)[4], float (&z)[4])
+{
+    quantile_pair(x[0], x[1], z[0], z[1]);
+    quantile_pair(x[2], x[3], z[2], z[3]);
 }
 
 // counter-based uint32 for dimensions beyond the Sobol budget and use_sobol = 0
@@ -320,10 +334,44 @@ __device__ __forceinline__ uint32_t hash_u32(uint64_t seed, uint64_t n, uint32_t
     return r ? r : 1u;
 }
 
-// sqrt for x >= 0 on the MUFU rsqrt path (x * rsqrt(x); 0 maps to 0)
+// The special-function unit's approximate square root (one MUFU instruction, sqrt(0) = 0)
+// and reciprocal, for x >= 0 and x > 0 respectively. a * rcp_approx(b) is the same
+// computation as __fdividef(a, b) in the range used here.
 __device__ __forceinline__ float fast_sqrt(float x)
 {
-    return x * rsqrtf(fmaxf(x, 1e-30f));
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float2 sqrt2_approx(float2 x) { return make_float2(fast_sqrt(x.x), fast_sqrt(x.y)); }
+__device__ __forceinline__ float2 rcp2_approx(float2 x) { return make_float2(rcp_approx(x.x), rcp_approx(x.y)); }
+
+// a - b as one fused multiply-add (b * -1 + a: the product is exact, so this rounds as the
+// subtraction does); for pairs it avoids forming -b lane by lane
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+constexpr float LN2 = 0.6931471805599453f, LOG2E = 1.4426950408889634f;
+
+__device__ __forceinline__ float exp2f_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float log2f_approx(float x)
+{
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
 // Phi(-z) = erfc(z / sqrt 2) / 2 with the Chebyshev-fitted erfc of Press et al.
@@ -333,8 +381,9 @@ __device__ __forceinline__ float fast_sqrt(float x)
 __device__ __forceinline__ float phi_neg(float z)
 {
     const float y = z * 0.7071067811865476f;
+    const float ny = z * -0.7071067811865476f;
     const float a = fabsf(y);
-    const float t = __fdividef(1.0f, fmaf(0.5f, a, 1.0f));
+    const float t = rcp_approx(fmaf(0.5f, a, 1.0f));
     float p = 0.17087277f;
     p = fmaf(p, t, -0.82215223f);
     p = fmaf(p, t, 1.48851587f);
@@ -345,8 +394,11 @@ __device__ __forceinline__ float phi_neg(float z)
     p = fmaf(p, t, 0.37409196f);
     p = fmaf(p, t, 1.00002368f);
     p = fmaf(p, t, -1.26551223f);
-    const float e = t * __expf(fmaf(-a, a, p));
-    return 0.5f * (y >= 0.f ? e : 2.0f - e);
+    // h = erfc(|y|) / 2; Phi(-z) = h for y >= 0 (sign bit clear), 1 - h otherwise, as
+    // sg h + off with sg = +-1, off = 0 or 1 (at y = -0, h = 1/2 and both forms give 1/2)
+    const float h = 0.5f * (t * exp2f_approx(fmaf(y, ny, p) * LOG2E));
+    const float sg = copysignf(1.0f, y);
+    return fmaf(sg, h, fmaf(sg, -0.5f, 0.5f));
 }
 
 // Andersen QE variance step in FP32 (heston_variance_node.cpp:17-57).
@@ -361,28 +413,31 @@ __device__ __forceinline__ float qe_step(float v, float z, float e, float th1e, 
     const float m = fmaf(v, e, th1e);
     const float s2 = fmaf(v, A, B);
     const float m2 = m * m;
+    const float tm2 = 2.0f * m2;
     // quadratic branch; c is capped at 1e18 (psi >= 2e-18, where the step's random part is
     // below single precision) so that c (c - 1) stays finite for a vanishing vol of vol
-    const float c = fminf(__fdividef(2.0f * m2, s2), 1e18f);
-    const float b2 = c - 1.0f + fast_sqrt(fmaxf(c * (c - 1.0f), 0.0f));
-    const float a = __fdividef(m, 1.0f + b2);
+    const float c = fminf(tm2 * rcp_approx(s2), 1e18f);
+    const float cm1 = c - 1.0f;
+    const float b2 = cm1 + fast_sqrt(fmaxf(c * cm1, 0.0f));
+    const float a = m * rcp_approx(1.0f + b2);
     const float bz = fast_sqrt(fmaxf(b2, 0.0f)) + z;
-    const float vq = a * bz * bz;
+    const float vq = (a * bz) * bz;
     // exponential branch
     const float num = s2 + m2;
-    const float one_m_p = __fdividef(2.0f * m2, num);
+    const float one_m_p = tm2 * rcp_approx(num);
     const float uc = phi_neg(z);
-    const float ve = (uc >= one_m_p) ? 0.0f : __fdividef(num, 2.0f * m) * __logf(__fdividef(one_m_p, uc));
+    const float r = (num * rcp_approx(2.0f * m)) * (log2f_approx(one_m_p * rcp_approx(uc)) * LN2);
+    const float ve = (uc >= one_m_p) ? 0.0f : r;
     return (s2 <= 1.5f * m2) ? vq : ve;
 }
 
-// phi_neg for a thread's two paths
+// phi_neg for a thread's two paths (same expressions, paired)
 __device__ __forceinline__ float2 phi_neg2(float2 z)
 {
     const float2 y = __fmul2_rn(z, f2s(0.7071067811865476f));
+    const float2 ny = __fmul2_rn(z, f2s(-0.7071067811865476f));
     const float2 a = f2(fabsf(y.x), fabsf(y.y));
-    const float2 d = __ffma2_rn(f2s(0.5f), a, f2s(1.0f));
-    const float2 t = f2(__fdividef(1.0f, d.x), __fdividef(1.0f, d.y));
+    const float2 t = rcp2_approx(__ffma2_rn(f2s(0.5f), a, f2s(1.0f)));
     float2 p = f2s(0.17087277f);
     p = __ffma2_rn(p, t, f2s(-0.82215223f));
     p = __ffma2_rn(p, t, f2s(1.48851587f));
@@ -393,9 +448,10 @@ __device__ __forceinline__ float2 phi_neg2(float2 z)
     p = __ffma2_rn(p, t, f2s(0.37409196f));
     p = __ffma2_rn(p, t, f2s(1.00002368f));
     p = __ffma2_rn(p, t, f2s(-1.26551223f));
-    const float2 g = __ffma2_rn(f2(-a.x, -a.y), a, p);
-    const float2 e = __fmul2_rn(t, f2(__expf(g.x), __expf(g.y)));
-    return __fmul2_rn(f2s(0.5f), f2(y.x >= 0.f ? e.x : 2.0f - e.x, y.y >= 0.f ? e.y : 2.0f - e.y));
+    const float2 g = __fmul2_rn(__ffma2_rn(y, ny, p), f2s(LOG2E));
+    const float2 h = __fmul2_rn(f2s(0.5f), __fmul2_rn(t, f2(exp2f_approx(g.x), exp2f_approx(g.y))));
+    const float2 sg = f2(copysignf(1.0f, y.x), copysignf(1.0f, y.y));
+    return __ffma2_rn(sg, h, __ffma2_rn(sg, f2s(-0.5f), f2s(0.5f)));
 }
 
 // qe_step for a thread's two paths (same expressions, paired)
@@ -405,23 +461,20 @@ __device__ __forceinline__ float2 qe_step2(float2 v, float2 z, float e, float th
     const float2 s2 = __ffma2_rn(v, f2s(A), f2s(B));
     const float2 m2 = __fmul2_rn(m, m);
     const float2 tm2 = __fmul2_rn(f2s(2.0f), m2);
-    const float2 c = f2(fminf(__fdividef(tm2.x, s2.x), 1e18f), fminf(__fdividef(tm2.y, s2.y), 1e18f));
+    const float2 cr = __fmul2_rn(tm2, rcp2_approx(s2));
+    const float2 c = f2(fminf(cr.x, 1e18f), fminf(cr.y, 1e18f));
     const float2 cm1 = __fadd2_rn(c, f2s(-1.0f));
     const float2 cc = __fmul2_rn(c, cm1);
-    // fast_sqrt(x) + y as the scalar form contracts it: x rsqrt(x) + y in one rounding
-    const float2 ccp = f2(fmaxf(cc.x, 0.0f), fmaxf(cc.y, 0.0f));
-    const float2 b2 = __ffma2_rn(ccp, f2(rsqrtf(fmaxf(ccp.x, 1e-30f)), rsqrtf(fmaxf(ccp.y, 1e-30f))), cm1);
-    const float2 d = __fadd2_rn(f2s(1.0f), b2);
-    const float2 a = f2(__fdividef(m.x, d.x), __fdividef(m.y, d.y));
-    const float2 b2p = f2(fmaxf(b2.x, 0.0f), fmaxf(b2.y, 0.0f));
-    const float2 bz = __ffma2_rn(b2p, f2(rsqrtf(fmaxf(b2p.x, 1e-30f)), rsqrtf(fmaxf(b2p.y, 1e-30f))), z);
+    const float2 b2 = __fadd2_rn(cm1, sqrt2_approx(f2(fmaxf(cc.x, 0.0f), fmaxf(cc.y, 0.0f))));
+    const float2 a = __fmul2_rn(m, rcp2_approx(__fadd2_rn(f2s(1.0f), b2)));
+    const float2 bz = __fadd2_rn(sqrt2_approx(f2(fmaxf(b2.x, 0.0f), fmaxf(b2.y, 0.0f))), z);
     const float2 vq = __fmul2_rn(__fmul2_rn(a, bz), bz);
     const float2 num = __fadd2_rn(s2, m2);
-    const float2 one_m_p = f2(__fdividef(tm2.x, num.x), __fdividef(tm2.y, num.y));
+    const float2 one_m_p = __fmul2_rn(tm2, rcp2_approx(num));
     const float2 uc = phi_neg2(z);
-    const float2 tm = __fmul2_rn(f2s(2.0f), m);
-    const float2 r = __fmul2_rn(f2(__fdividef(num.x, tm.x), __fdividef(num.y, tm.y)),
-                                f2(__logf(__fdividef(one_m_p.x, uc.x)), __logf(__fdividef(one_m_p.y, uc.y))));
+    const float2 q = __fmul2_rn(one_m_p, rcp2_approx(uc));
+    const float2 r = __fmul2_rn(__fmul2_rn(num, rcp2_approx(__fmul2_rn(f2s(2.0f), m))),
+                                __fmul2_rn(f2(log2f_approx(q.x), log2f_approx(q.y)), f2s(LN2)));
     const float2 ve = f2(uc.x >= one_m_p.x ? 0.0f : r.x, uc.y >= one_m_p.y ? 0.0f : r.y);
     const float2 lim = __fmul2_rn(f2s(1.5f), m2);
     return f2(s2.x <= lim.x ? vq.x : ve.x, s2.y <= lim.y ? vq.y : ve.y);

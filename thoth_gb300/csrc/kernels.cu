@@ -101,11 +101,12 @@ __device__ inline void tile_high_bits(const DevPlan& P, uint2* hs, int64_t m, in
     }
 }
 
-// low words a thread loads per Sobol entry: one for its two paths (columns t and t + T/2,
-// through the tile-part pair), else one per path
+// low words a thread loads per Sobol entry: with an even number of paths, one for each pair
+// of columns t + k T/PP and t + k T/PP + T/2 (k < PP/2), through the tile-part pair; else
+// one per path
 template <int PP>
 struct LoadsPerEntry {
-    static constexpr int value = PP == 2 ? 1 : PP;
+    static constexpr int value = PP % 2 == 0 ? PP / 2 : PP;
 };
 
 template <int T, int PP>
@@ -156,9 +157,13 @@ __device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, con
         const uint2 h = L.hs[L.j - (L.jend - HS_CHUNK)];
         const int jn = L.j + 2;
         const bool more = jn < P.n_sobol;
-        if constexpr (PP == 2) {
-            x[0] = h.x ^ L.cur[0];
-            x[1] = h.y ^ L.cur[0];
+        if constexpr (PP % 2 == 0) {
+            // path k is column t + k TH; path k + PP/2 is column t + k TH + T/2
+#pragma unroll
+            for (int k = 0; k < PP / 2; ++k) {
+                x[k] = h.x ^ L.cur[k];
+                x[k + PP / 2] = h.y ^ L.cur[k];
+            }
         } else {
 #pragma unroll
             for (int p = 0; p < PP; ++p) x[p] = h.x ^ L.cur[p];
@@ -237,11 +242,14 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
                 const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
                 float z[PP];
                 gauss(P, L, n, rec.dim + fid, z);
-                if constexpr (PP == 2) {
-                    const float2 w = bridge_comb2(rec.lw, rec.rw, rec.sd, Wprev[0][f], Wprev[PP - 1][f], top[0][f],
-                                                  top[PP - 1][f], z[0], z[PP - 1]);
-                    Wi[0][f] = w.x;
-                    Wi[PP - 1][f] = w.y;
+                if constexpr (PP % 2 == 0) {
+#pragma unroll
+                    for (int h = 0; h < PP; h += 2) {
+                        const float2 w = bridge_comb2(rec.lw, rec.rw, rec.sd, Wprev[h][f], Wprev[h + 1][f], top[h][f],
+                                                      top[h + 1][f], z[h], z[h + 1]);
+                        Wi[h][f] = w.x;
+                        Wi[h + 1][f] = w.y;
+                    }
                 } else {
 #pragma unroll
                     for (int p = 0; p < PP; ++p)
@@ -272,11 +280,14 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
                     float z[PP];
                     gauss(P, L, n, dim + fid, z);
                     float Wns[PP];
-                    if constexpr (PP == 2) {
-                        const float2 w = bridge_comb2(lw, rw, sd, Wprev[0][f], Wprev[PP - 1][f], top[0][f],
-                                                      top[PP - 1][f], z[0], z[PP - 1]);
-                        Wns[0] = w.x;
-                        Wns[PP - 1] = w.y;
+                    if constexpr (PP % 2 == 0) {
+#pragma unroll
+                        for (int h = 0; h < PP; h += 2) {
+                            const float2 w = bridge_comb2(lw, rw, sd, Wprev[h][f], Wprev[h + 1][f], top[h][f],
+                                                          top[h + 1][f], z[h], z[h + 1]);
+                            Wns[h] = w.x;
+                            Wns[h + 1] = w.y;
+                        }
                     } else {
 #pragma unroll
                         for (int p = 0; p < PP; ++p) Wns[p] = fmaf(lw, Wprev[p][f], fmaf(rw, top[p][f], sd * z[p]));
@@ -296,16 +307,18 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
             if (push) ++sp;
         }
     }
-    if constexpr (PP == 2) {
+    if constexpr (PP % 2 == 0) {
 #pragma unroll
-        for (int f = 0; f < FS; ++f) {
-            const float2 d = __fmul2_rn(__fadd2_rn(f2(Wi[0][f], Wi[PP - 1][f]), f2(-Wprev[0][f], -Wprev[PP - 1][f])),
-                                        f2s(rec.isd));
-            nz[0][f] = d.x;
-            nz[PP - 1][f] = d.y;
-            Wprev[0][f] = Wi[0][f];
-            Wprev[PP - 1][f] = Wi[PP - 1][f];
-        }
+        for (int h = 0; h < PP; h += 2)
+#pragma unroll
+            for (int f = 0; f < FS; ++f) {
+                const float2 d =
+                    __fmul2_rn(sub2(f2(Wi[h][f], Wi[h + 1][f]), f2(Wprev[h][f], Wprev[h + 1][f])), f2s(rec.isd));
+                nz[h][f] = d.x;
+                nz[h + 1][f] = d.y;
+                Wprev[h][f] = Wi[h][f];
+                Wprev[h + 1][f] = Wi[h + 1][f];
+            }
     } else {
 #pragma unroll
         for (int p = 0; p < PP; ++p)
@@ -433,8 +446,15 @@ __device__ __forceinline__ StepRec load_rec(const DevPlan& P, int i)
 //           with correlated GBM names, M_SEQ for other multi-asset books
 //   UNIFORM every step has the same per-asset constants (kept in registers)
 // ---------------------------------------------------------------------------
+// resident CTAs per SM the registers are bounded for: 768 threads per SM worth for one or two
+// paths a thread, 7 CTAs of 64 threads (146 registers each) for four, 3 for the mixed kernel
+template <int TB, int NA, int PP>
+struct MinBlocks {
+    static constexpr int value = NA != 1 ? 3 : (PP == 4 ? 7 : 768 / ((1 << TB) / PP));
+};
+
 template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-__global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / PP) : 3) book_kernel(const DevPlan P)
+__global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) book_kernel(const DevPlan P)
 {
     constexpr int T = 1 << TB;  // paths per tile
     constexpr int TH = T / PP;  // threads per CTA; path p of thread t is tile column t + p * TH
@@ -598,30 +618,36 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                         c2 = __ldg(cs + 2);
                     }
                     const int model = (MODEL == M_MIXED || SEQ) ? P.model[aid] : MODEL;
-                    // two paths a thread: the variance step and the log-spot sum paired
+                    // an even number of paths a thread: the variance step and the log-spot sum paired
+                    constexpr bool PAIRED = PP % 2 == 0;
                     float vcs[PP], stp[PP];
-                    if (PP == 2 && model != M_GBM) {
-                        const float2 r = qe_step2(f2(v[0][a], v[PP - 1][a]), f2(nz[0][NA + a], nz[PP - 1][NA + a]), c0.x,
-                                                  c0.y, c0.z, c0.w);
-                        vcs[0] = r.x;
-                        vcs[PP - 1] = r.y;
+                    if (PAIRED && model != M_GBM) {
+#pragma unroll
+                        for (int h = 0; h < PP; h += 2) {
+                            const float2 r = qe_step2(f2(v[h][a], v[h + 1][a]), f2(nz[h][NA + a], nz[h + 1][NA + a]),
+                                                      c0.x, c0.y, c0.z, c0.w);
+                            vcs[h] = r.x;
+                            vcs[h + 1] = r.y;
+                        }
                     }
-                    // Heston kernels, two paths a thread: the log-spot step paired as well
-                    constexpr bool PAIR_SPOT = PP == 2 && MODEL == M_HESTON;
+                    // Heston kernels, paired paths: the log-spot step paired as well
+                    constexpr bool PAIR_SPOT = PAIRED && MODEL == M_HESTON;
                     if constexpr (PAIR_SPOT) {
                         if (!P.degenerate[aid]) {
-                            const float2 vp2 = f2(v[0][a], v[PP - 1][a]), vc2 = f2(vcs[0], vcs[PP - 1]);
-                            const float2 s2 = __fadd2_rn(vp2, vc2);
-                            const float2 F = __ffma2_rn(f2s(c2.y), __fadd2_rn(vc2, f2(-vp2.x, -vp2.y)),
-                                                        __ffma2_rn(f2s(c1.z), s2, f2s(c1.y)));
-                            const float2 q = __fmul2_rn(f2s(c2.x), s2);
-                            const float2 qr = __fmul2_rn(q, f2(rsqrtf(fmaxf(q.x, 1e-30f)), rsqrtf(fmaxf(q.y, 1e-30f))));
-                            const float2 B = __ffma2_rn(qr, f2(nz[0][a], nz[PP - 1][a]), F);
-                            const float2 st = __ffma2_rn(f2s(-c1.w), s2, __fadd2_rn(f2s(c1.x), B));
-                            stp[0] = st.x;
-                            stp[PP - 1] = st.y;
-                            v[0][a] = vc2.x;
-                            v[PP - 1][a] = vc2.y;
+#pragma unroll
+                            for (int h = 0; h < PP; h += 2) {
+                                const float2 vp2 = f2(v[h][a], v[h + 1][a]), vc2 = f2(vcs[h], vcs[h + 1]);
+                                const float2 s2 = __fadd2_rn(vp2, vc2);
+                                const float2 F =
+                                    __ffma2_rn(f2s(c2.y), sub2(vc2, vp2), __ffma2_rn(f2s(c1.z), s2, f2s(c1.y)));
+                                const float2 qr = sqrt2_approx(__fmul2_rn(f2s(c2.x), s2));
+                                const float2 B = __ffma2_rn(qr, f2(nz[h][a], nz[h + 1][a]), F);
+                                const float2 st = __ffma2_rn(f2s(-c1.w), s2, __fadd2_rn(f2s(c1.x), B));
+                                stp[h] = st.x;
+                                stp[h + 1] = st.y;
+                                v[h][a] = vc2.x;
+                                v[h + 1][a] = vc2.y;
+                            }
                         }
                     }
 #pragma unroll
@@ -641,7 +667,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                             Wb[p][a] = fmaf(c0.z, e, Wb[p][a]);
                         } else {
                             const float vp = v[p][a];
-                            const float vc = PP == 2 ? vcs[p] : qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
+                            const float vc = PAIRED ? vcs[p] : qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
                             float Lv = 1.f, dL = 0.f;
                             if (model == M_LSV) leverage(P, aid, i, x[p][a], Lv, dL);
                             const float s = vp + vc;
@@ -664,15 +690,18 @@ __global__ void __launch_bounds__((1 << TB) / PP, NA == 1 ? 768 / ((1 << TB) / P
                         stp[p] = step;
                     }
                     // Kahan-compensated log-spot
-                    if (PP == 2) {
-                        const float2 yy = __fadd2_rn(f2(stp[0], stp[PP - 1]), f2(-comp[0][a], -comp[PP - 1][a]));
-                        const float2 xx = f2(x[0][a], x[PP - 1][a]);
-                        const float2 tt = __fadd2_rn(xx, yy);
-                        const float2 cp = __fadd2_rn(__fadd2_rn(tt, f2(-xx.x, -xx.y)), f2(-yy.x, -yy.y));
-                        comp[0][a] = cp.x;
-                        comp[PP - 1][a] = cp.y;
-                        x[0][a] = tt.x;
-                        x[PP - 1][a] = tt.y;
+                    if constexpr (PAIRED) {
+#pragma unroll
+                        for (int h = 0; h < PP; h += 2) {
+                            const float2 yy = sub2(f2(stp[h], stp[h + 1]), f2(comp[h][a], comp[h + 1][a]));
+                            const float2 xx = f2(x[h][a], x[h + 1][a]);
+                            const float2 tt = __fadd2_rn(xx, yy);
+                            const float2 cp = sub2(sub2(tt, xx), yy);
+                            comp[h][a] = cp.x;
+                            comp[h + 1][a] = cp.y;
+                            x[h][a] = tt.x;
+                            x[h + 1][a] = tt.y;
+                        }
                     } else {
 #pragma unroll
                         for (int p = 0; p < PP; ++p) {
@@ -973,14 +1002,14 @@ cudaError_t launch_mufu_peak(float* out, int blocks, int iters, cudaStream_t st)
 }
 
 // ---- launch wrappers --------------------------------------------------------
-// Launch shapes. Single-asset variants come in four: (log2 paths per tile,
-// paths per thread) = (8, 2), (8, 1), (7, 1), (7, 2), i.e. 128, 256, 128 and 64
-// threads per CTA, each bounded to 768 resident threads per SM worth of
-// registers; the autotuner picks one per book size. The mixed variant has one:
-// (7, 1).
-constexpr int N_SHAPES = 4;
-constexpr int SHAPE_TB[N_SHAPES] = {8, 8, 7, 7};
-constexpr int SHAPE_PP[N_SHAPES] = {2, 1, 1, 2};
+// Launch shapes. Single-asset variants come in five: (log2 paths per tile,
+// paths per thread) = (8, 2), (8, 1), (7, 1), (7, 2), (8, 4), i.e. 128, 256, 128, 64
+// and 64 threads per CTA, the first four bounded to 768 resident threads per SM
+// worth of registers, the last to 7 CTAs of 64 threads; the autotuner picks one per
+// book size. The mixed variant has one: (7, 1).
+constexpr int N_SHAPES = 5;
+constexpr int SHAPE_TB[N_SHAPES] = {8, 8, 7, 7, 8};
+constexpr int SHAPE_PP[N_SHAPES] = {2, 1, 1, 2, 4};
 
 int book_shape_count(int variant) { return variant == 3 ? 1 : N_SHAPES; }
 int book_shape_tile_bits(int variant, int shape) { return variant == 3 ? 7 : SHAPE_TB[shape]; }
@@ -1038,9 +1067,12 @@ static int single_t(const DevPlan* P, int shape, int grid, size_t smem, cudaStre
     case 2:
         if (grid) *err = launch_book_t<7, 1, MODEL, UNIFORM, 1>(*P, grid, smem, st);
         return grid ? 0 : occ_t<7, 1, MODEL, UNIFORM, 1>(smem);
-    default:
+    case 3:
         if (grid) *err = launch_book_t<7, 1, MODEL, UNIFORM, 2>(*P, grid, smem, st);
         return grid ? 0 : occ_t<7, 1, MODEL, UNIFORM, 2>(smem);
+    default:
+        if (grid) *err = launch_book_t<8, 1, MODEL, UNIFORM, 4>(*P, grid, smem, st);
+        return grid ? 0 : occ_t<8, 1, MODEL, UNIFORM, 4>(smem);
     }
 }
 

@@ -593,4 +593,80 @@ cudaError_t mlp_gather_batch(const __nv_bfloat16* X, const float* Y, const float
 int mlp_n_params() { return mlp::N_PARAMS; }
 int mlp_n_bf() { return mlp::N_BF; }
 
+// ---------------------------------------------------------------------------
+// Lattice serving: the cells of n_sets parameter sets x n_T maturities x n_lm
+// log-moneyness, cell c = (set * n_T + j) * n_lm + k with raw features
+// (lm[k], T[j], kappa, theta, xi, rho, v0 of the set), built, clipped to the
+// training box and normalised on the device (the network's hi/lo bf16 input
+// split), and the network's output scaled back to a price in units of spot.
+// ---------------------------------------------------------------------------
+struct LatticeArgs {
+    const double* params; // [n_sets][5] kappa, theta, xi, rho, v0
+    const double* lms;    // [n_lm]
+    const double* Ts;     // [n_T]
+    double lo[7], hi[7];  // training box
+    double floor;         // scale floor (units of spot)
+    int64_t n;            // cells
+    int n_lm, n_T;
+};
+
+__device__ __forceinline__ void lattice_cell(const LatticeArgs& A, int64_t c, double (&f)[7])
+{
+    const int64_t per = (int64_t)A.n_lm * A.n_T;
+    const int64_t set = c / per;
+    const int r = (int)(c % per);
+    f[0] = A.lms[r % A.n_lm];
+    f[1] = A.Ts[r / A.n_lm];
+    for (int q = 0; q < 5; ++q) f[2 + q] = A.params[set * 5 + q];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) f[q] = fmin(fmax(f[q], A.lo[q]), A.hi[q]);
+}
+
+__global__ void lattice_features_kernel(const LatticeArgs A, __nv_bfloat16* __restrict__ x)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.n) return;
+    double f[7];
+    lattice_cell(A, c, f);
+    __nv_bfloat16* row = x + c * mlp::KIN;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        // 2 (f - lo) / (hi - lo) - 1 in FP64, then to FP32, as the host normalisation
+        const float v = (float)(2.0 * (f[q] - A.lo[q]) / (A.hi[q] - A.lo[q]) - 1.0);
+        const __nv_bfloat16 h = __float2bfloat16(v);
+        row[q] = h;
+        row[7 + q] = __float2bfloat16(v - __bfloat162float(h));
+    }
+    row[14] = row[15] = __float2bfloat16(0.f);
+}
+
+// y (the network's normalised price) times sqrt(bs^2 + floor^2), bs the Black-Scholes call
+// (S = 1, r = q = 0) at the expected average Heston variance over [0, T]
+__global__ void lattice_scale_kernel(const LatticeArgs A, const float* __restrict__ y, float* __restrict__ price)
+{
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.n) return;
+    double f[7];
+    lattice_cell(A, c, f);
+    const double lm = f[0], T = f[1], kappa = f[2], theta = f[3], v0 = f[6];
+    const double kt = kappa * T;
+    const double var = theta + (v0 - theta) * (1.0 - exp(-kt)) / kt;
+    const double sd = sqrt(fmax(var, 1e-8) * T);
+    const double d1 = -lm / sd + 0.5 * sd;
+    const double bs = normcdf(d1) - exp(lm) * normcdf(d1 - sd);
+    price[c] = (float)((double)y[c] * sqrt(bs * bs + A.floor * A.floor));
+}
+
+cudaError_t lattice_features(const LatticeArgs& A, __nv_bfloat16* x, cudaStream_t st)
+{
+    lattice_features_kernel<<<(unsigned)((A.n + 255) / 256), 256, 0, st>>>(A, x);
+    return cudaGetLastError();
+}
+
+cudaError_t lattice_scale(const LatticeArgs& A, const float* y, float* price, cudaStream_t st)
+{
+    lattice_scale_kernel<<<(unsigned)((A.n + 255) / 256), 256, 0, st>>>(A, y, price);
+    return cudaGetLastError();
+}
+
 } // namespace thoth

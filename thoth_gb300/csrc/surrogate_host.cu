@@ -41,6 +41,17 @@ cudaError_t mlp_gather_batch(const __nv_bfloat16* X, const float* Y, const float
                              int rows, __nv_bfloat16* xb, float* yb, float* wb, cudaStream_t st);
 int mlp_n_params();
 int mlp_n_bf();
+struct LatticeArgs {
+    const double* params;
+    const double* lms;
+    const double* Ts;
+    double lo[7], hi[7];
+    double floor;
+    int64_t n;
+    int n_lm, n_T;
+};
+cudaError_t lattice_features(const LatticeArgs& A, __nv_bfloat16* x, cudaStream_t st);
+cudaError_t lattice_scale(const LatticeArgs& A, const float* y, float* price, cudaStream_t st);
 } // namespace thoth
 
 using namespace thoth;
@@ -90,6 +101,9 @@ struct ThothSurrogate {
     // inference buffers
     int64_t cap_inf = 0;
     unsigned char* ib = nullptr;
+    // lattice serving: parameter sets and lattice axes, scaled prices
+    int64_t cap_lat = 0;
+    unsigned char* lb = nullptr;
     // device copy of a training set and its per-epoch permutation (grown on demand)
     int64_t cap_ds = 0;
     unsigned char* ds = nullptr;
@@ -280,6 +294,7 @@ int thoth_gpu_surrogate_destroy(ThothSurrogate* s)
         cudaFree(s->status);
         if (s->tb) cudaFree(s->tb);
         if (s->ib) cudaFree(s->ib);
+        if (s->lb) cudaFree(s->lb);
         if (s->ds) cudaFree(s->ds);
         if (s->perm_host) cudaFreeHost(s->perm_host);
         if (s->perm_copied) cudaEventDestroy(s->perm_copied);
@@ -490,6 +505,85 @@ int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, fl
         STRY(mlp_infer(dx, (int)n, s->params, s->wbf, dy, s->status, grid, s->st));
         STRY(cudaEventRecord(e1, s->st));
         STRY(cudaMemcpyAsync(y, dy, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
+        STRY(cudaStreamSynchronize(s->st));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (device_ms) *device_ms = ms;
+        return check_status(s);
+    } catch (const std::bad_alloc&) {
+        return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return sfail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_surrogate_price_lattice(ThothSurrogate* s, const double* params, int32_t n_sets, const double* lms,
+                                      int32_t n_lm, const double* Ts, int32_t n_T, const double* box_lo,
+                                      const double* box_hi, double floor, float* prices, double* device_ms)
+{
+    try {
+        if (!s || !params || !lms || !Ts || !box_lo || !box_hi || !prices || n_sets < 1 || n_lm < 1 || n_T < 1 ||
+            !(floor > 0))
+            return sfail(THOTH_GPU_E_INVALID, "bad lattice arguments");
+        const int64_t n = (int64_t)n_sets * n_lm * n_T;
+        if (n > ((int64_t)1 << 30)) return sfail(THOTH_GPU_E_TOO_LARGE, "more than 2^30 lattice cells");
+        for (int q = 0; q < 7; q++)
+            if (!(box_hi[q] > box_lo[q])) return sfail(THOTH_GPU_E_INVALID, "empty training box");
+        std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaSetDevice(s->dev));
+        auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+        if (n > s->cap_inf) {
+            if (s->ib) cudaFree(s->ib);
+            s->ib = nullptr;
+            s->cap_inf = 0;
+            const int64_t cap = (n + 127) / 128 * 128;
+            STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 4) + 256));
+            s->cap_inf = cap;
+        }
+        const size_t in_bytes = up(sizeof(double) * ((size_t)n_sets * 5 + n_lm + n_T));
+        const int64_t need = (int64_t)(in_bytes + up(sizeof(float) * (size_t)n));
+        if (need > s->cap_lat) {
+            if (s->lb) cudaFree(s->lb);
+            s->lb = nullptr;
+            s->cap_lat = 0;
+            STRY(cudaMalloc(&s->lb, (size_t)need));
+            s->cap_lat = need;
+        }
+        double* dp = reinterpret_cast<double*>(s->lb);
+        double* dlm = dp + (size_t)n_sets * 5;
+        double* dT = dlm + n_lm;
+        float* dprice = reinterpret_cast<float*>(s->lb + in_bytes);
+        STRY(cudaMemcpyAsync(dp, params, sizeof(double) * (size_t)n_sets * 5, cudaMemcpyHostToDevice, s->st));
+        STRY(cudaMemcpyAsync(dlm, lms, sizeof(double) * n_lm, cudaMemcpyHostToDevice, s->st));
+        STRY(cudaMemcpyAsync(dT, Ts, sizeof(double) * n_T, cudaMemcpyHostToDevice, s->st));
+        LatticeArgs A{};
+        A.params = dp;
+        A.lms = dlm;
+        A.Ts = dT;
+        for (int q = 0; q < 7; q++) {
+            A.lo[q] = box_lo[q];
+            A.hi[q] = box_hi[q];
+        }
+        A.floor = floor;
+        A.n = n;
+        A.n_lm = n_lm;
+        A.n_T = n_T;
+        __nv_bfloat16* dx = reinterpret_cast<__nv_bfloat16*>(s->ib);
+        float* dy = reinterpret_cast<float*>(s->ib + (size_t)s->cap_inf * KIN * 2);
+        STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+        cudaEvent_t e0, e1;
+        STRY(cudaEventCreate(&e0));
+        STRY(cudaEventCreate(&e1));
+        const int tiles = (int)((n + 127) / 128);
+        const int grid = std::min(tiles, s->sms);
+        STRY(cudaEventRecord(e0, s->st));
+        STRY(lattice_features(A, dx, s->st));
+        STRY(mlp_infer(dx, (int)n, s->params, s->wbf, dy, s->status, grid, s->st));
+        STRY(lattice_scale(A, dy, dprice, s->st));
+        STRY(cudaEventRecord(e1, s->st));
+        STRY(cudaMemcpyAsync(prices, dprice, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
         STRY(cudaStreamSynchronize(s->st));
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);

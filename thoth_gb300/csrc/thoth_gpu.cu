@@ -2054,7 +2054,8 @@ static int autotune_load_locked(const char* path)
         } else if (line[0] != '\n') bad = true;
     }
     std::fclose(f);
-    if (version != 1 || bad || streams < 1 || streams > 64 || policy < 0 || policy > 2 || bshape < -1 || bshape > 3)
+    if (version != 1 || bad || streams < 1 || streams > 64 || policy < 0 || policy > 2 || bshape < -1 ||
+        bshape >= book_shape_count(0))
         return fail(THOTH_GPU_E_INVALID, std::string("malformed autotune file ") + path);
     if (sms != g_dev.sms || name != g_dev.name)
         return fail(THOTH_GPU_E_UNSUPPORTED, "autotune file was measured on another device (" + name + ")");

@@ -88,29 +88,43 @@ def lattice_book(params, paths, lms=LATTICE_LM, Ts=LATTICE_T, skip=0):
 
 
 def lattice_features(params, lms=LATTICE_LM, Ts=LATTICE_T):
-    rows = []
-    for T in Ts:
-        for lm in lms:
-            rows.append([lm, T] + list(params))
-    return np.array(rows)
+    """Feature rows of one set's lattice, maturity-major: [len(Ts) * len(lms)][7]."""
+    return grid_features(np.asarray(params, dtype=np.float64)[None, :], lms, Ts)
 
 
-def mc_labels(param_sets, paths, lms=LATTICE_LM, Ts=LATTICE_T, distinct=False):
+def grid_features(param_sets, lms=LATTICE_LM, Ts=LATTICE_T):
+    """Feature rows of every set's lattice, set-major then maturity-major:
+    [n_sets * len(Ts) * len(lms)][7] (log-moneyness, T, kappa, theta, xi, rho, v0)."""
+    P = np.asarray(param_sets, dtype=np.float64).reshape(-1, 5)
+    lms, Ts = np.asarray(lms, dtype=np.float64), np.asarray(Ts, dtype=np.float64)
+    n, nT, nl = len(P), len(Ts), len(lms)
+    X = np.empty((n, nT, nl, 7))
+    X[..., 0] = lms[None, None, :]
+    X[..., 1] = Ts[None, :, None]
+    X[..., 2:] = P[:, None, None, :]
+    return X.reshape(n * nT * nl, 7)
+
+
+def mc_labels(param_sets, paths, lms=LATTICE_LM, Ts=LATTICE_T, distinct=False, skip=0):
     """Price each parameter set's lattice with the GPU MC engine: (features, prices, trusts, seconds).
 
     distinct=True gives set i its own block of Sobol points (skip = i * paths), so
     label errors are independent across sets and the fit averages them out;
     with shared points they are a smooth function of the parameters, which the
-    network would learn as if it were the price."""
-    from . import price_book
-    X, Y, S = [], [], []
+    network would learn as if it were the price. skip offsets every set's points."""
+    from . import price_batch
+    Y, S = [], []
     t0 = time.perf_counter()
-    for i, p in enumerate(param_sets):
-        r = price_book(lattice_book(p, paths, lms, Ts, skip=i * paths if distinct else 0))
-        X.append(lattice_features(p, lms, Ts))
-        Y.append(r["premium"])
-        S.append(r["trust"])
-    return np.concatenate(X), np.concatenate(Y), np.concatenate(S), time.perf_counter() - t0
+    chunk = 256  # books per batch call (one CUDA graph each)
+    for c0 in range(0, len(param_sets), chunk):
+        sets = param_sets[c0:c0 + chunk]
+        books = [lattice_book(p, paths, lms, Ts, skip=skip + ((c0 + i) * paths if distinct else 0))
+                 for i, p in enumerate(sets)]
+        for r in price_batch(books):
+            Y.append(r["premium"])
+            S.append(r["trust"])
+    secs = time.perf_counter() - t0
+    return grid_features(param_sets, lms, Ts), np.concatenate(Y), np.concatenate(S), secs
 
 
 def train_targets(X, Y):
@@ -145,6 +159,10 @@ class Surrogate:
                                                    C.POINTER(C.c_double)]
         L.thoth_gpu_surrogate_predict.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float),
                                                   C.POINTER(C.c_double)]
+        L.thoth_gpu_surrogate_price_lattice.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int32,
+                                                        C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_double),
+                                                        C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                                        C.c_double, C.POINTER(C.c_float), C.POINTER(C.c_double)]
         L.thoth_gpu_surrogate_last_error.restype = C.c_char_p
         self.n_params = L.thoth_gpu_surrogate_n_params()
         self.h = C.c_void_p()
@@ -196,6 +214,22 @@ class Surrogate:
                                                        C.byref(ms)))
         return y, ms.value
 
+    def price_lattice(self, param_sets, lms=LATTICE_LM, Ts=LATTICE_T):
+        """Prices (units of spot) of every (set, maturity, log-moneyness) cell, features,
+        clipping, normalisation and price scale on the device: the same cells and order as
+        lattice_features and the same prices as predict_prices of the clipped features."""
+        d = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        P, lm, T, lo, hi = d(param_sets), d(lms), d(Ts), d(BOX_LO), d(BOX_HI)
+        if P.ndim != 2 or P.shape[1] != 5:
+            raise ValueError("param_sets must be [n][5] (kappa, theta, xi, rho, v0)")
+        out = np.zeros(len(P) * len(lm) * len(T), dtype=np.float32)
+        ms = C.c_double()
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._check(self.L.thoth_gpu_surrogate_price_lattice(self.h, ptr(P), len(P), ptr(lm), len(lm), ptr(T), len(T),
+                                                             ptr(lo), ptr(hi), FLOOR,
+                                                             out.ctypes.data_as(C.POINTER(C.c_float)), C.byref(ms)))
+        return out, ms.value
+
     def close(self):
         if self.h:
             self.L.thoth_gpu_surrogate_destroy(self.h)
@@ -217,123 +251,149 @@ def _mc_subset(param_sets, paths, lms, Ts):
 
 
 POLICIES = ("bucket", "grid")
+Z90 = 1.6448536269514722  # the 90th percentile of |Z|, Z ~ N(0, 1)
+JUDGE_SECOND_BLOCK = 1 << 31  # Sobol skip of the judge's second, independent block
 
 
-def choose_fallback(jerr, tol=TOL, policy="bucket", margin=1.0, n_T=None):
-    """Buckets (columns of jerr [judged sets][buckets], the surrogate's judged cell
-    errors, maturity-major with n_T maturities) that MC takes over; see judge().
-    The grid policy is cost-aware: an MC fallback book runs to its longest
-    maturity, so it looks for the shortest maturity horizon within which taking
-    over the worst buckets (worst first) brings the grid to the target."""
-    jerr = np.asarray(jerr, dtype=np.float64)
-    bucket = np.quantile(jerr, 0.9, axis=0)
+def grid_p90(sigma):
+    """90th percentile of |e| over a grid whose cells in bucket b have errors N(0, sigma_b^2):
+    the x at which the mean over buckets of P(|e| > x) = 2 Phi(-x / sigma_b) is 0.1."""
+    from scipy.special import ndtr
+    s = np.asarray(sigma, dtype=np.float64).ravel()
+    if not np.any(s > 0):
+        return 0.0
+    frac = lambda x: float(np.mean(np.where(s > 0, 2.0 * ndtr(-x / np.maximum(s, 1e-300)), 0.0)))
+    lo, hi = 0.0, 10.0 * float(s.max())
+    for _ in range(80):
+        mid = 0.5 * (lo + hi)
+        lo, hi = (mid, hi) if frac(mid) > 0.1 else (lo, mid)
+    return hi
+
+
+def choose_fallback(sigma, tol=TOL, policy="grid", margin=1.0, n_T=None):
+    """Buckets (lattice cells, maturity-major with n_T maturities) that MC takes over, from
+    each bucket's surrogate error scale sigma_b (see judge()).
+    policy "bucket": every bucket whose own 90th-percentile error, Z90 sigma_b, exceeds tol.
+    policy "grid": the grid as a whole meets the target: buckets are taken over worst first,
+    within the shortest maturity horizon that suffices (an MC fallback book runs to its
+    longest maturity), until grid_p90 is at most margin * tol, a taken-over bucket counting
+    at the plain-MC accuracy (90th percentile tol: sigma = tol / Z90)."""
+    sigma = np.asarray(sigma, dtype=np.float64).ravel()
     if policy == "bucket":
-        return bucket > tol
+        return Z90 * sigma > tol
     if policy != "grid":
         raise ValueError("policy must be one of %s" % (POLICIES,))
-    nb = bucket.size
+    nb = sigma.size
     n_T = n_T or nb
     mat = np.arange(nb) // (nb // n_T)        # maturity index of each bucket
-    if np.quantile(jerr, 0.9) <= margin * tol:
+    if grid_p90(sigma) <= margin * tol:
         return np.zeros(nb, dtype=bool)
+    fb_sigma = tol / Z90
     best = None
     for h in range(n_T):                       # horizon: maturities 0 .. h may fall back
         bad = np.zeros(nb, dtype=bool)
-        e = jerr.copy()
-        for b in np.argsort(-bucket, kind="stable"):
-            if mat[b] > h or bucket[b] <= 0.5 * tol:
+        s = sigma.copy()
+        for b in np.argsort(-sigma, kind="stable"):
+            if mat[b] > h or sigma[b] <= fb_sigma:
                 continue
             bad[b] = True
-            e[:, b] = 0.5 * tol
-            if np.quantile(e, 0.9) <= margin * tol:
+            s[b] = fb_sigma
+            if grid_p90(s) <= margin * tol:
                 break
-        if np.quantile(e, 0.9) <= margin * tol:
+        if grid_p90(s) <= margin * tol:
             return bad
         best = bad
-    return best | (bucket > tol)               # the target is out of reach: every bucket above tol too
+    return best | (Z90 * sigma > tol)          # the target is out of reach: every bucket above tol too
 
 
-def judge(model, param_sets, judge_frac=0.01, judge_paths=1 << 20, tol=TOL, seed=0, lms=LATTICE_LM, Ts=LATTICE_T,
-          policy="bucket", margin=1.0):
-    """MC judge: re-price a random judge_frac of the sets with judge_paths (whose Sobol
-    error is below tol) and choose the lattice buckets (maturity, log-moneyness) that
-    MC takes over.
+def judge(model, param_sets, judge_frac=0.01, judge_paths=1 << 19, tol=TOL, seed=0, lms=LATTICE_LM, Ts=LATTICE_T,
+          policy="grid", margin=1.0):
+    """MC judge with its own noise removed: re-price a random judge_frac of the sets by MC
+    and estimate, per lattice bucket (maturity, log-moneyness), the surrogate's error.
 
-    policy "bucket": every bucket whose 90th-percentile surrogate error on the judged
-    sets exceeds tol (each bucket meets the target on its own).
-    policy "grid": buckets, worst first and within the shortest maturity horizon
-    that suffices, such that the judged grid's 90th-percentile error, with the
-    taken-over cells counted at tol / 2 (the MC fallback's own accuracy,
-    calibrated to stay below tol), is at most margin * tol (the grid as a whole
-    meets the target). The judge's own MC error adds to the measured one (the
-    measured error is an upper estimate), so judge_paths should be well above the
-    plain-MC count."""
+    The judged sets are priced twice, on two Sobol blocks of judge_paths / 2 points far
+    apart in the sequence (the first points, and points from 2^31 on), whose errors are
+    independent; ybar is their mean. (The two halves of one block of judge_paths points
+    would not do: their errors partly cancel in the full block, so their difference would
+    overstate the error of the mean.) With r = (s - ybar) / w the surrogate's judged cell
+    error (w the cell's error floor, max(|ybar|, 1% of spot)) and n = (y1 - y2) / (2 w), n
+    has the variance of the judge's own error in r, so per bucket
+        sigma_b^2 = mean(r^2) - mean(n^2)
+    is the surrogate's mean-square error with the judge's noise taken out. The judge can
+    then run at the plain-MC path count (1% of the sets costs about 1% of plain MC) without
+    its own error flagging healthy buckets. choose_fallback then picks the buckets MC takes
+    over, and grid_p90(sigma) is the estimated 90th-percentile error of the judged grid."""
     rng = np.random.default_rng(seed)
     n_judge = max(1, int(round(judge_frac * len(param_sets))))
     judged = np.sort(rng.choice(len(param_sets), size=n_judge, replace=False))
-    Xj = np.concatenate([lattice_features(p, lms, Ts) for p in param_sets[judged]])
+    sets = param_sets[judged]
+    half = max(1, judge_paths // 2)
     t0 = time.perf_counter()
-    _, jy, js, t_mc = mc_labels(param_sets[judged], judge_paths, lms, Ts)
-    pj, _ = predict_prices(model, Xj)
+    _, y1, _, _ = mc_labels(sets, half, lms, Ts)
+    _, y2, _, _ = mc_labels(sets, half, lms, Ts, skip=JUDGE_SECOND_BLOCK)
+    pj, _ = model.price_lattice(sets, lms, Ts)
     t_judge = time.perf_counter() - t0
-    jerr = cell_error(pj, jy).reshape(n_judge, -1)
-    bad = choose_fallback(jerr, tol, policy, margin, n_T=len(Ts))
-    return dict(judged=judged, bad=bad.reshape(len(Ts), len(lms)), judge_s=t_judge,
-                judge_mc_seconds_per_set=t_mc / n_judge, judged_p90=float(np.quantile(jerr, 0.9)))
+    ybar = 0.5 * (y1 + y2)
+    w = np.maximum(np.abs(ybar), FLOOR)
+    r = ((pj - ybar) / w).reshape(n_judge, -1)
+    noise = (0.5 * (y1 - y2) / w).reshape(n_judge, -1)
+    sigma = np.sqrt(np.maximum(np.mean(r * r, axis=0) - np.mean(noise * noise, axis=0), 0.0))
+    bad = choose_fallback(sigma, tol, policy, margin, n_T=len(Ts))
+    return dict(judged=judged, bad=bad.reshape(len(Ts), len(lms)), judge_s=t_judge, sigma=sigma,
+                judge_mc_seconds_per_set=t_judge / n_judge, judged_p90=float(np.quantile(np.abs(r), 0.9)),
+                estimated_p90=grid_p90(sigma), judge_noise_rms=float(np.sqrt(np.mean(noise * noise))))
 
 
-def price_grid(model, param_sets, mc_paths, judge_frac=0.01, judge_paths=1 << 20, fallback_sample=None, seed=0,
-               tol=TOL, lms=LATTICE_LM, Ts=LATTICE_T, policy="bucket"):
+def price_grid(model, param_sets, mc_paths, judge_frac=0.01, judge_paths=None, seed=0, tol=TOL, lms=LATTICE_LM,
+               Ts=LATTICE_T, policy="grid"):
     """Price a grid of (parameter set x lattice) cells with the surrogate, judged by MC.
 
-    1. inference for every cell (out-of-box features are clipped, then re-priced by MC);
-    2. the MC judge (see judge(), with its policy) marks the lattice buckets MC takes over;
-    3. the failing buckets of every set, and every set with out-of-box cells, are
-       re-priced by MC with mc_paths (the plain-MC path count for the same accuracy),
-       on books cut to the failing maturities and strikes. With fallback_sample = k only k sets are
-       re-priced and the fallback time is scaled to all sets (used by the benchmark).
-    Returns (prices [cells], info dict with timings and counts).
-    """
+    1. inference for every cell on the device (price_lattice: features, clipping and the
+       price scale on the GPU; sets outside the training box are re-priced by MC);
+    2. the MC judge (see judge(), at judge_paths, by default the plain-MC count mc_paths)
+       marks the lattice buckets MC takes over;
+    3. those buckets of every set are re-priced by MC with mc_paths (the plain-MC path
+       count for the same accuracy), on books cut to the failing maturities and strikes.
+    Every stage runs on every set it concerns and is timed as run.
+    Returns (prices [cells], info dict with timings and counts)."""
     n_sets = len(param_sets)
     ncell = len(lms) * len(Ts)
-    X = np.concatenate([lattice_features(p, lms, Ts) for p in param_sets])
+    judge_paths = judge_paths or mc_paths
     t0 = time.perf_counter()
-    inside = in_box(X)
-    price, dev_ms = predict_prices(model, np.clip(X, BOX_LO, BOX_HI))
+    price, dev_ms = model.price_lattice(param_sets, lms, Ts)
+    price = price.astype(np.float64)
+    inside = np.all((param_sets >= BOX_LO[2:] - 1e-12) & (param_sets <= BOX_HI[2:] + 1e-12), axis=1)
     t_inf = time.perf_counter() - t0
     J = judge(model, param_sets, judge_frac, judge_paths, tol, seed, lms, Ts, policy=policy)
     bad2 = J["bad"]
     t2 = time.perf_counter()
     fb_T = np.nonzero(bad2.any(axis=1))[0]
     fb_lm = np.nonzero(bad2.any(axis=0))[0]
-    fb_sets = np.arange(n_sets)
-    if fallback_sample is not None and fallback_sample < n_sets:
-        fb_sets = np.linspace(0, n_sets - 1, fallback_sample).astype(int)
+    in_sets = np.nonzero(inside)[0]
     n_fb = 0
-    if len(fb_T):
-        fy, _ = _mc_subset(param_sets[fb_sets], mc_paths, lms[fb_lm], Ts[fb_T])
-        fy = fy.reshape(len(fb_sets), len(fb_T), len(fb_lm))
+    if len(fb_T) and len(in_sets):
+        fy, _ = _mc_subset(param_sets[in_sets], mc_paths, lms[fb_lm], Ts[fb_T])
+        fy = fy.reshape(len(in_sets), len(fb_T), len(fb_lm))
         for a, ti in enumerate(fb_T):
             for b, li in enumerate(fb_lm):
                 if bad2[ti, li]:
-                    price[fb_sets * ncell + ti * len(lms) + li] = fy[:, a, b]
-                    n_fb += len(fb_sets)
-    out_sets = np.unique(np.nonzero(~inside)[0] // ncell)
+                    price[in_sets * ncell + ti * len(lms) + li] = fy[:, a, b]
+                    n_fb += len(in_sets)
+    out_sets = np.nonzero(~inside)[0]
     if len(out_sets):
         oy, _ = _mc_subset(param_sets[out_sets], mc_paths, lms, Ts)
         for j, k in enumerate(out_sets):
-            sel = ~inside[k * ncell:(k + 1) * ncell]
-            price[k * ncell:(k + 1) * ncell][sel] = oy[j][sel]
-            n_fb += int(sel.sum())
+            price[k * ncell:(k + 1) * ncell] = oy[j]
+            n_fb += ncell
     t_fb = time.perf_counter() - t2
-    scale_fb = n_sets / len(fb_sets) if len(fb_T) else 1.0
-    total = t_inf + J["judge_s"] + t_fb * scale_fb
-    return price, dict(cells=len(X), seconds=total, inference_s=t_inf, inference_device_ms=dev_ms,
+    total = t_inf + J["judge_s"] + t_fb
+    cells = n_sets * ncell
+    return price, dict(cells=cells, seconds=total, inference_s=t_inf, inference_device_ms=dev_ms,
                        judge_s=J["judge_s"], judge_sets=len(J["judged"]), judge_paths=judge_paths,
-                       fallback_s=t_fb * scale_fb, fallback_sets_run=int(len(fb_sets)) if len(fb_T) else 0,
-                       fallback_cells=int(bad2.sum()) * n_sets + int((~inside).sum()),
-                       failing_buckets=int(bad2.sum()), mc_paths=mc_paths, cells_per_sec=len(X) / total,
-                       policy=policy, judged_p90=J["judged_p90"])
+                       fallback_s=t_fb, fallback_cells=n_fb, failing_buckets=int(bad2.sum()),
+                       out_of_box_sets=int(len(out_sets)), mc_paths=mc_paths, cells_per_sec=cells / total,
+                       policy=policy, judged_p90=J["judged_p90"], estimated_p90=J["estimated_p90"],
+                       judge_noise_rms=J["judge_noise_rms"])
 
 
 def calibrate_plain_mc(param_sets, cf, tol=TOL, lo=10, hi=24):
@@ -347,51 +407,3 @@ def calibrate_plain_mc(param_sets, cf, tol=TOL, lo=10, hi=24):
         if np.quantile(e, 0.9) <= tol:
             return 1 << k, secs / len(param_sets), e
     return 1 << hi, secs / len(param_sets), e
-
-
-def benchmark(n_train=4096, n_eval=4096, train_paths=1 << 18, epochs=3000, lr=2e-3, batch=8192, cf_sets=16, seed=1,
-              fallback_sample=16, judge_factor=8):
-    """Train on MC labels, then price an n_eval x 252-cell grid at the same accuracy
-    target (90th-percentile cell error <= 1e-3 against the FP64 closed form):
-      plain MC   — every cell by MC at the path count calibrated on cf_sets sets;
-      surrogate  — inference + 1% MC judge (judge_factor x the plain-MC path count)
-                   + MC fallback, once per judge policy ("grid": the grid meets
-                   the target; "bucket": every bucket does).
-    The fallback runs on fallback_sample sets and is scaled to the grid. Errors are
-    measured against the closed form on cf_sets sets spread over the grid."""
-    import oracle  # the FP64 closed form, as the checker only
-    t0 = time.perf_counter()
-    X, Y, _, t_labels = mc_labels(sobol_params(n_train, 0), train_paths, distinct=True)
-    model = Surrogate(seed=seed)
-    xn, yt, st = train_targets(X, Y)
-    t1 = time.perf_counter()
-    loss = model.train(xn, yt, st, epochs=epochs, batch=batch, lr=lr)
-    t_train = time.perf_counter() - t1
-    ev = sobol_params(n_eval, n_train)
-    ncell = len(LATTICE_LM) * len(LATTICE_T)
-    pick = np.linspace(0, n_eval - 1, cf_sets).astype(int)
-    Xs = np.concatenate([lattice_features(ev[k]) for k in pick])
-    t2 = time.perf_counter()
-    cf = oracle.heston_prices(1.0, np.exp(Xs[:, 0]), Xs[:, 1], 0, 0, Xs[:, 6], Xs[:, 2], Xs[:, 3], Xs[:, 4], Xs[:, 5])
-    t_cf = time.perf_counter() - t2
-    mc_paths, mc_set_s, e_mc = calibrate_plain_mc(ev[pick], cf)
-    plain = ncell / mc_set_s
-    raw, _ = predict_prices(model, Xs)
-    q = lambda e: {"median": float(np.median(e)), "p90": float(np.quantile(e, 0.9)),
-                   "p99": float(np.quantile(e, 0.99)), "max": float(e.max()), "frac_above_tol": float(np.mean(e > TOL))}
-    policies = {}
-    for policy in POLICIES:
-        price, pinfo = price_grid(model, ev, mc_paths, judge_paths=judge_factor * mc_paths,
-                                  fallback_sample=fallback_sample, policy=policy)
-        pipe = np.concatenate([price[k * ncell:(k + 1) * ncell] for k in pick])
-        pinfo.update(error_pipeline=q(cell_error(pipe, cf)), speedup=pinfo["cells_per_sec"] / plain)
-        policies[policy] = pinfo
-    info = dict(policies["grid"])
-    info.update(train_sets=n_train, train_labels=len(Y), train_paths=train_paths, label_seconds=t_labels,
-                train_seconds=t_train, epochs=epochs, final_loss=loss, cf_cells=len(cf), cf_seconds=t_cf,
-                plain_mc_paths=mc_paths, plain_mc_seconds_per_set=mc_set_s, plain_mc_cells_per_sec=plain,
-                inference_cells_per_sec=info["cells"] / info["inference_s"],
-                error_surrogate_raw=q(cell_error(raw, cf)), error_surrogate_pipeline=info["error_pipeline"],
-                error_plain_mc=q(e_mc), policies=policies, total_seconds=time.perf_counter() - t0)
-    model.close()
-    return info
