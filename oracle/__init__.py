@@ -9,6 +9,7 @@ this package. It loads
 import ctypes as C
 import os
 import pathlib
+import shutil
 import subprocess
 
 import numpy as np
@@ -20,6 +21,8 @@ ROOT = HERE.parent
 JK_TABLE = ROOT / "thoth_gb300" / "data" / "joe_kuo_6_21201.bin"
 PORT_SO = HERE / "_build" / "liboracle_port.so"
 REF_SO = HERE / "_ref" / "libref_oracle.so"
+REF_GPU_SRC = HERE / "_ref" / "gpu" / "mcl_gpu.cu"
+REF_GBM_SO = HERE / "_ref" / "libref_gbm.so"
 
 _port = None
 _ref = None
@@ -40,9 +43,29 @@ def build(ref=None):
     targets = ["port"]
     refroot = reference_root(ref)
     if refroot is not None:
-        targets.append("ref")
+        targets += ["ref", "refgpu-src"]
     subprocess.run(["make", "-s", "-j8", "-C", str(HERE)] + (["REF=%s" % refroot] if refroot else []) + targets,
                    check=True)
+    # the reference's GPU kernel for the benchmark, where its staged sources and nvcc exist
+    if REF_GPU_SRC.exists() and shutil.which("nvcc"):
+        subprocess.run(["make", "-s", "-C", str(HERE), "refgpu"], check=True)
+
+
+_ref_gbm = None
+
+
+def ref_gbm():
+    """The reference's own GPU kernel (gbm_kernel and gpu::PriceEuropeanGbm of
+    pricer/src/tasks/mcl_gpu.cu) with its timing harness, oracle/_ref/libref_gbm.so; None
+    where it was not built (no staged sources or no nvcc). Benchmark use only."""
+    global _ref_gbm
+    if _ref_gbm is None and REF_GBM_SO.exists():
+        lib = C.CDLL(str(REF_GBM_SO))
+        args = [C.c_double] * 5 + [C.c_int, C.c_long, C.c_ulong]
+        lib.ref_gbm_call.argtypes = args + [C.POINTER(C.c_double)] * 3
+        lib.ref_gbm_kernel.argtypes = args + [C.c_int] + [C.POINTER(C.c_double)] * 3
+        _ref_gbm = lib
+    return _ref_gbm
 
 
 def port():

@@ -128,7 +128,7 @@ def test_price_grid_pipeline_small(gpu):
         # every flagged bucket of every in-box set went to MC, timed as run
         assert info["fallback_cells"] == info["failing_buckets"] * 8 + 252 * info["out_of_box_sets"]
         assert info["seconds"] == info["inference_s"] + info["judge_s"] + info["fallback_s"]
-        assert np.isfinite(info["estimated_p90"]) and info["judge_noise_rms"] > 0
+        assert 0 <= info["estimated_p90"] <= info["judged_p90"] and info["judge_noise_p90"] > 0
         fails[policy] = info["failing_buckets"]
     # the grid policy never takes over more buckets than the per-bucket one
     assert fails["grid"] <= fails["bucket"]

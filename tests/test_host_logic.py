@@ -159,34 +159,24 @@ def test_kernel_selection_and_sizes():
 
 
 def test_surrogate_fallback_policies():
-    """The MC judge's bucket choice from the buckets' error scales (host logic, no GPU)."""
+    """The MC judge's bucket choice (host logic, no GPU)."""
     from thoth_gb300 import surrogate as S
     rng = np.random.default_rng(3)
     tol = 1e-3
-    sigma = rng.uniform(0, 0.35e-3, size=12)
-    sigma[3] = sigma[4] = 1.5e-3                         # two bad buckets (1/6 of the cells)
-    sigma[7] = 0.65e-3                                   # one marginal bucket (own p90 1.07e-3)
-    bucket = S.choose_fallback(sigma, tol, "bucket")
-    assert bucket[3] and bucket[4] and bucket[7] and bucket.sum() == 3
-    grid = S.choose_fallback(sigma, tol, "grid", margin=0.9)
+    jerr = rng.uniform(0, 0.6e-3, size=(40, 12))
+    jerr[:, 3] = rng.uniform(1.5e-3, 4e-3, size=40)     # one bad bucket
+    jerr[:, 7] = rng.uniform(0.8e-3, 1.2e-3, size=40)   # one marginal bucket
+    bucket = S.choose_fallback(jerr, tol, "bucket")
+    assert bucket[3] and bucket[7] and bucket.sum() == 2
+    grid = S.choose_fallback(jerr, tol, "grid", margin=0.9)
     assert grid[3] and grid.sum() <= bucket.sum()
-    s = sigma.copy()
-    s[grid] = tol / S.Z90
-    assert S.grid_p90(s) <= 0.9 * tol
-    good = rng.uniform(0, 0.3e-3, size=12)
+    e = jerr.copy()
+    e[:, grid] = 0.5 * tol
+    assert np.quantile(e, 0.9) <= 0.9 * tol
+    good = rng.uniform(0, 0.5e-3, size=(40, 12))
     assert not S.choose_fallback(good, tol, "grid").any() and not S.choose_fallback(good, tol, "bucket").any()
     with pytest.raises(ValueError):
         S.choose_fallback(good, tol, "nope")
-
-
-def test_surrogate_grid_p90_of_a_normal_mixture():
-    """grid_p90 is the 90th percentile of |e| over buckets of normal errors, checked by sampling."""
-    from thoth_gb300 import surrogate as S
-    rng = np.random.default_rng(8)
-    sigma = rng.uniform(1e-4, 2e-3, size=30)
-    e = rng.standard_normal((200000, 30)) * sigma
-    assert abs(S.grid_p90(sigma) - np.quantile(np.abs(e), 0.9)) <= 0.01 * S.grid_p90(sigma)
-    assert S.grid_p90(np.zeros(5)) == 0.0
 
 
 def test_surrogate_grid_policy_prefers_short_horizons():
@@ -196,38 +186,38 @@ def test_surrogate_grid_policy_prefers_short_horizons():
     rng = np.random.default_rng(5)
     tol = 1e-3
     n_T, n_lm = 4, 5
-    sigma = rng.uniform(0, 0.4e-3, size=n_T * n_lm)
-    sigma[0:n_lm] = rng.uniform(0.9e-3, 1.8e-3, size=n_lm)        # maturity 0 is bad
-    sigma[3 * n_lm + 2] = 0.6e-3                                   # a mild long-maturity bucket
-    bad = S.choose_fallback(sigma, tol, "grid", margin=0.9, n_T=n_T).reshape(n_T, n_lm)
+    jerr = rng.uniform(0, 0.7e-3, size=(40, n_T * n_lm))
+    jerr[:, 0:n_lm] = rng.uniform(1.2e-3, 3e-3, size=(40, n_lm))     # maturity 0 is bad
+    jerr[:, 3 * n_lm + 2] = rng.uniform(0.9e-3, 1.05e-3, size=40)    # a mild long-maturity bucket
+    bad = S.choose_fallback(jerr, tol, "grid", margin=0.9, n_T=n_T).reshape(n_T, n_lm)
     assert bad[0].any() and not bad[1:].any()
-    s = sigma.copy()
-    s[bad.ravel()] = tol / S.Z90
-    assert S.grid_p90(s) <= 0.9 * tol
+    e = jerr.copy()
+    e[:, bad.ravel()] = 0.5 * tol
+    assert np.quantile(e, 0.9) <= 0.9 * tol
 
 
-def test_surrogate_judge_removes_its_own_noise():
-    """The judge's estimator on synthetic data: surrogate errors of known scale, judged by
-    two half-block MC estimates whose noise is larger than the surrogate's error. The raw
-    judged error is dominated by that noise; mean(r^2) - mean(n^2) recovers the surrogate's
-    own scale per bucket."""
+@pytest.mark.parametrize("noise", [0.85e-3, 0.4e-3, 0.2e-3])
+def test_surrogate_judge_removes_its_own_noise(noise):
+    """The judge's noise correction on synthetic data: heavy-tailed surrogate errors (Student
+    t, 2.5 degrees of freedom) judged by two independent MC estimates whose own error is as
+    large as, or smaller than, the surrogate's. The raw judged 90th percentile is inflated by
+    the judge's noise; the corrected one recovers the surrogate's within 20 % (and from
+    above, the cautious side), where a normal model fitted to the mean-square error would
+    overstate it for such tails."""
+    from thoth_gb300 import surrogate as S
     rng = np.random.default_rng(11)
-    n_sets, nb = 2000, 12
-    true_sigma = np.linspace(4e-4, 1e-3, nb)
-    truth = np.full((n_sets, nb), 0.3)
-    surrogate = truth * (1 + rng.standard_normal((n_sets, nb)) * true_sigma)
-    half_noise = 1.2e-3                                   # each half-block estimate's relative error
-    y1 = truth * (1 + rng.standard_normal((n_sets, nb)) * half_noise)
-    y2 = truth * (1 + rng.standard_normal((n_sets, nb)) * half_noise)
-    ybar = 0.5 * (y1 + y2)
-    w = np.maximum(np.abs(ybar), 0.01)
-    r = (surrogate - ybar) / w
-    n = 0.5 * (y1 - y2) / w
-    est = np.sqrt(np.maximum(np.mean(r * r, axis=0) - np.mean(n * n, axis=0), 0))
-    raw = np.sqrt(np.mean(r * r, axis=0))
-    assert np.all(raw > 1.2 * true_sigma)                  # the judge's noise inflates the raw error
-    assert np.all(np.abs(est - true_sigma) <= 0.2 * true_sigma)
-    assert np.mean(np.abs(est - true_sigma) / true_sigma) <= 0.08
+    n = 10332                                   # 41 judged sets x 252 cells
+    e = rng.standard_t(2.5, size=n) * 2.2e-4
+    true_p90 = np.quantile(np.abs(e), 0.9)
+    y1 = rng.standard_normal(n) * noise * np.sqrt(2)
+    y2 = rng.standard_normal(n) * noise * np.sqrt(2)
+    r = e - 0.5 * (y1 + y2)
+    half = 0.5 * (y1 - y2)
+    scaled, est, qr, qn = S.noise_corrected(r, half)
+    assert qr > true_p90
+    assert true_p90 * 0.95 <= est <= true_p90 * 1.2
+    assert np.allclose(np.quantile(scaled, 0.9), est)
+    assert np.array_equal(np.argsort(scaled, kind="stable"), np.argsort(np.abs(r), kind="stable"))
 
 
 def test_running_groups_share_nested_prefixes():

@@ -36,14 +36,18 @@ constexpr int SOBOL_LO_ROW = 256; // threads covered by the low-bit table (tiles
 // asset after the other with the single-asset state and a two-factor bridge
 enum : int { M_GBM = 0, M_HESTON = 1, M_LSV = 2, M_MIXED = 3, M_SEQ = 4 };
 
-// per-step, per-asset constants (12 floats, three 16-byte loads)
+// per-step, per-asset constants (16 floats: three 16-byte loads, a fourth for LSV)
 //  GBM:    c[0] = carry_drift - sigma^2 dt / 2, c[1] = sigma sqrt(dt) (Brownian scale), c[2] = sqrt(dt)
 //  Heston: c[0] = e = exp(-kappa dt), c[1] = theta (1 - e), c[2] = A, c[3] = B   (s2 = A v + B)
 //          c[4] = carry_drift, c[5] = k0, c[6] = a1, c[7] = a2, c[8] = k3, c[9] = r = rho/xi
 //          step(L) = c4 + L (k0 + a1 s + r (vc - vp) + sqrt(k3 s) z) - L^2 a2 s, s = vp + vc
 //          degenerate xi: c[10] = dt (step = c4 - L^2 vp dt / 2 + L sqrt(vp dt) z)
+//  LSV:    the Heston constants, and the leverage layer of the date the step ends on:
+//          c[12] = 1/ln_step, c[13] = ln S0 / ln_step - offset (the grid coordinate is
+//          x c[12] + c[13], x = ln(S/S0)), c[14] = the layer's first value in lev_values
+//          (an int), so the lookup needs no dependent load of the layer index or its map
 struct alignas(16) AssetStep {
-    float c[12];
+    float c[16];
 };
 
 // time-ordered Brownian-bridge program node: W_new = lw * W_{i-1} + rw * W_top + sd * z(bstep)

@@ -330,14 +330,14 @@ __device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, con
     }
 }
 
-// leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47). The layer of
-// a date is uniform across the CTA and its rows stay in L1 (staging the current
-// layer in shared memory measured slower)
-__device__ __forceinline__ void leverage(const DevPlan& P, int a, int i, float x, float& L, float& dL)
+// leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47) on the layer the
+// step's record names (c3 = {1/ln_step, grid offset, first value as int bits}): the
+// layer's rows are uniform across the CTA and stay in L1 (staging the current layer in
+// shared memory measured slower)
+__device__ __forceinline__ void leverage(const DevPlan& P, int a, float4 c3, float x, float& L, float& dL)
 {
-    const int layer = __ldg(P.lev_layer + a * (P.n_steps + 1) + i);
-    const float2 mp = __ldg(P.lev_map + a * P.lev_layers_stride + layer);
-    const float* v = P.lev_values + (a * P.lev_layers_stride + layer) * P.lev_row_stride;
+    const float2 mp = make_float2(c3.x, c3.y);
+    const float* v = P.lev_values + __float_as_int(c3.z);
     const int npts = P.lev_points[a];
     const float f = fmaf(x, mp.x, mp.y);
     const int last = npts - 1;
@@ -587,6 +587,19 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
             for (int i = 1; i <= P.n_steps; ++i) {
                 const StepRec cur = rec;
                 if (i < P.n_steps) rec = load_rec(P, i + 1);
+                // one asset a pass: its constants for this step are requested before the bridge
+                // work, which covers their latency
+                constexpr bool HOIST = !UNIFORM && (NA == 1 || MODEL == M_SEQ);
+                float4 h0, h1, h2, h3;
+                if constexpr (HOIST) {
+                    const int ha = MODEL == M_SEQ ? a0 : 0;
+                    const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + ha].c);
+                    h0 = __ldg(cs);
+                    h1 = __ldg(cs + 1);
+                    h2 = __ldg(cs + 2);
+                    h3 = (MODEL == M_LSV || (MODEL == M_SEQ && P.model[ha] == M_LSV)) ? __ldg(cs + 3)
+                                                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
                 if (P.use_sobol) {
                     bridge_step<NA, T, PP, SEQ>(P, S, cur, sp, L, n, Wprev, top, nz, a0);
                 } else {
@@ -606,16 +619,22 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
                 for (int a = 0; a < NA; ++a) {
                     const int aid = SEQ ? a0 : a; // asset id; a is the register slot
                     if (aid >= P.n_assets) continue;
-                    float4 c0, c1, c2;
+                    float4 c0, c1, c2, c3 = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (UNIFORM) {
                         c0 = u0[a];
                         c1 = u1[a];
                         c2 = u2[a];
+                    } else if constexpr (HOIST) {
+                        c0 = h0;
+                        c1 = h1;
+                        c2 = h2;
+                        c3 = h3;
                     } else {
                         const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + aid].c);
                         c0 = __ldg(cs);
                         c1 = __ldg(cs + 1);
                         c2 = __ldg(cs + 2);
+                        if (P.model[aid] == M_LSV) c3 = __ldg(cs + 3);
                     }
                     const int model = (MODEL == M_MIXED || SEQ) ? P.model[aid] : MODEL;
                     // an even number of paths a thread: the variance step and the log-spot sum paired
@@ -669,7 +688,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
                             const float vp = v[p][a];
                             const float vc = PAIRED ? vcs[p] : qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
                             float Lv = 1.f, dL = 0.f;
-                            if (model == M_LSV) leverage(P, aid, i, x[p][a], Lv, dL);
+                            if (model == M_LSV) leverage(P, aid, c3, x[p][a], Lv, dL);
                             const float s = vp + vc;
                             if (!P.degenerate[aid]) {
                                 const float B =

@@ -201,6 +201,16 @@ __device__ __forceinline__ void put_row(unsigned char* tile, int row, const floa
     }
 }
 
+struct TrainSched {
+    long long count;           // steps done in this training call
+    long long total;           // steps of the call
+    long long steps_per_epoch; // batches of one permutation
+    long long step0;           // Adam steps before the call
+    double lr0;                // peak learning rate
+    float lr_t, bc1, bc2;      // this step's learning rate and bias corrections
+    int rows;                  // batch rows
+};
+
 struct TrainArgs {
     int rows;                       // batch rows (multiple of 128)
     const __nv_bfloat16* x;         // [rows][16] normalised inputs
@@ -356,13 +366,36 @@ __global__ void __launch_bounds__(128) bwd_layer_kernel(TrainArgs A)
     if (warp == 0) tc::tmem_dealloc(c.tm, 256);
 }
 
+// the cosine learning-rate schedule and Adam's bias corrections of step `count` of a training
+// call, computed where the graph of one step can read them (its kernels' arguments stay
+// the same from step to step)
+__host__ __device__ inline void sched_set(TrainSched& s)
+{
+    const double pi = 3.14159265358979323846;
+    const double step = (double)(s.step0 + s.count + 1);
+    s.lr_t = (float)(s.lr0 * 0.5 * (1.0 + cos(pi * (double)s.count / (double)s.total)) + 1e-6);
+    s.bc1 = (float)(1.0 - pow(0.9, step));
+    s.bc2 = (float)(1.0 - pow(0.999, step));
+}
+
+__global__ void sched_advance_kernel(TrainSched* s)
+{
+    s->count += 1;
+    sched_set(*s);
+}
+
 // grad[j] = sum over tiles of part[tile][j] (fixed order), then Adam on the FP32
 // master and refresh of the bf16 operand copies
 __global__ void adam_kernel(float* params, float* m, float* v, const float* part, int tiles, __nv_bfloat16* wbf,
-                            float lr, float b1, float b2, float eps, float bc1, float bc2)
+                            float lr, float b1, float b2, float eps, float bc1, float bc2, const TrainSched* sched)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N_PARAMS) return;
+    if (sched) { // this step's learning rate and bias corrections, set by sched_advance_kernel
+        lr = sched->lr_t;
+        bc1 = sched->bc1;
+        bc2 = sched->bc2;
+    }
     float g = 0.f;
     for (int tl = 0; tl < tiles; ++tl) g += part[(size_t)tl * N_PARAMS + j];
     // W1 columns f and f + 7 carry the hi and lo bf16 parts of feature f with one
@@ -414,6 +447,19 @@ constexpr int INFER_THREADS = 256;
 
 __device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
 
+// SiLU of two columns at once for inference: silu(z) = z sigmoid(z), sigmoid(z) = (1 + tanh(z/2)) / 2,
+// with one special-function-unit tanh per value (the exponential and reciprocal form takes two)
+// and the arithmetic on packed pairs. tanh.approx is within about 2^-11 of tanh, well inside the
+// bf16 rounding (2^-9 relative) the next layer's operand gets anyway.
+__device__ __forceinline__ float2 silu2_infer(float2 z)
+{
+    const float2 h = __fmul2_rn(z, make_float2(0.5f, 0.5f));
+    float t0, t1;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t0) : "f"(h.x));
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t1) : "f"(h.y));
+    return __ffma2_rn(h, make_float2(t0, t1), h); // z/2 (1 + tanh(z/2))
+}
+
 __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat16* __restrict__ x, int n,
                                                               const float* params, const __nv_bfloat16* wbf,
                                                               float* __restrict__ y, int* status)
@@ -421,7 +467,7 @@ __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat1
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tm_s;
-    __shared__ float sb[4 * H + H + 1];              // biases of layers 1..4, head weights, head bias
+    __shared__ __align__(16) float sb[4 * H + H + 1]; // biases of layers 1..4, head weights, head bias (pairs read as float2)
     unsigned char* sW1 = sm;                         // 128 x 16
     unsigned char* sW = sW1 + H * KIN * 2;           // 3 x (128 x 128)
     const int t = threadIdx.x, warp = t >> 5, wg = t >> 7, r = t & 127;
@@ -485,14 +531,20 @@ __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat1
                     for (int j = 0; j < 16; ++j) v[j] = 0.f;
                 }
 #pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = silu(v[j] + bias[c0 + j]);
+                for (int j = 0; j < 16; j += 2) {
+                    const float2 z = __fadd2_rn(make_float2(v[j], v[j + 1]),
+                                                *reinterpret_cast<const float2*>(bias + c0 + j));
+                    const float2 a = silu2_infer(z);
+                    v[j] = a.x;
+                    v[j + 1] = a.y;
+                }
                 if (l < 4) {
                     // the MMA that read sAct has completed: overwrite it in place with the next operand
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        __align__(16) __nv_bfloat16 hv[8];
+                        __align__(16) __nv_bfloat162 hv[4];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) hv[j] = __float2bfloat16(v[h * 8 + j]);
+                        for (int j = 0; j < 4; ++j) hv[j] = __floats2bfloat162_rn(v[h * 8 + 2 * j], v[h * 8 + 2 * j + 1]);
                         *reinterpret_cast<uint4*>(sAct + tc::cm_offset(r, c0 + h * 8, ROWS)) =
                             *reinterpret_cast<const uint4*>(hv);
                     }
@@ -517,42 +569,64 @@ __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat1
 constexpr size_t kFwdSmem1 = (size_t)2 * mlp::ROWS * mlp::KIN * 2;
 constexpr size_t kFwdSmem = (size_t)2 * mlp::ROWS * mlp::H * 2;
 
+constexpr size_t kBwdSmem = (size_t)(mlp::ROWS * mlp::H + mlp::H * mlp::ROWS + mlp::ROWS * mlp::H + mlp::H * mlp::H) * 2;
+constexpr size_t kBwdSmem1 = (size_t)(mlp::ROWS * mlp::H + mlp::KIN * mlp::ROWS) * 2;
+
+// the layer kernels' shared-memory limits, set once per device (not inside a captured step)
+static cudaError_t train_attributes()
+{
+    using namespace mlp;
+    static bool set_on[64] = {};
+    int dev = 0;
+    cudaError_t e0 = cudaGetDevice(&dev);
+    if (e0 != cudaSuccess) return e0;
+    bool dummy = false;
+    bool& done = (dev >= 0 && dev < 64) ? set_on[dev] : dummy;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(fwd_layer_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem1);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fwd_layer_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fwd_layer_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fwd_layer_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(bwd_layer_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(bwd_layer_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(bwd_layer_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(bwd_layer_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem1);
+    done = e == cudaSuccess;
+    return e;
+}
+
+cudaError_t mlp_train_prepare() { return train_attributes(); }
+
+// one training step: forward and backward layer by layer, Adam. With a schedule (sched not
+// null) the learning rate and bias corrections are read on the device, so the step's launches
+// have the same arguments every step and can be captured once into a graph.
 cudaError_t mlp_train_step(const mlp::TrainArgs& A, float* params, float* m, float* v, __nv_bfloat16* wbf, float lr,
-                           float b1, float b2, float eps, float bc1, float bc2, float* loss_out, cudaStream_t st)
+                           float b1, float b2, float eps, float bc1, float bc2, float* loss_out, cudaStream_t st,
+                           const mlp::TrainSched* sched)
 {
     using namespace mlp;
     const int tiles = A.rows / ROWS;
-    cudaError_t e;
-    // forward
-    e = cudaFuncSetAttribute(fwd_layer_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem1);
+    cudaError_t e = train_attributes();
     if (e != cudaSuccess) return e;
     fwd_layer_kernel<1><<<tiles, 128, kFwdSmem1, st>>>(A);
-    e = cudaFuncSetAttribute(fwd_layer_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-    if (e != cudaSuccess) return e;
     fwd_layer_kernel<2><<<tiles, 128, kFwdSmem, st>>>(A);
-    e = cudaFuncSetAttribute(fwd_layer_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-    if (e != cudaSuccess) return e;
     fwd_layer_kernel<3><<<tiles, 128, kFwdSmem, st>>>(A);
-    e = cudaFuncSetAttribute(fwd_layer_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
-    if (e != cudaSuccess) return e;
     fwd_layer_kernel<4><<<tiles, 128, kFwdSmem, st>>>(A);
-    // backward
-    const size_t bs4 = (size_t)(ROWS * H + H * ROWS + ROWS * H + H * H) * 2;
-    const size_t bs1 = (size_t)(ROWS * H + KIN * ROWS) * 2;
-    e = cudaFuncSetAttribute(bwd_layer_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bs4);
-    if (e != cudaSuccess) return e;
-    bwd_layer_kernel<4><<<tiles, 128, bs4, st>>>(A);
-    e = cudaFuncSetAttribute(bwd_layer_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bs4);
-    if (e != cudaSuccess) return e;
-    bwd_layer_kernel<3><<<tiles, 128, bs4, st>>>(A);
-    e = cudaFuncSetAttribute(bwd_layer_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bs4);
-    if (e != cudaSuccess) return e;
-    bwd_layer_kernel<2><<<tiles, 128, bs4, st>>>(A);
-    e = cudaFuncSetAttribute(bwd_layer_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bs1);
-    if (e != cudaSuccess) return e;
-    bwd_layer_kernel<1><<<tiles, 128, bs1, st>>>(A);
-    adam_kernel<<<(N_PARAMS + 255) / 256, 256, 0, st>>>(params, m, v, A.part, tiles, wbf, lr, b1, b2, eps, bc1, bc2);
+    bwd_layer_kernel<4><<<tiles, 128, kBwdSmem, st>>>(A);
+    bwd_layer_kernel<3><<<tiles, 128, kBwdSmem, st>>>(A);
+    bwd_layer_kernel<2><<<tiles, 128, kBwdSmem, st>>>(A);
+    bwd_layer_kernel<1><<<tiles, 128, kBwdSmem1, st>>>(A);
+    adam_kernel<<<(N_PARAMS + 255) / 256, 256, 0, st>>>(params, m, v, A.part, tiles, wbf, lr, b1, b2, eps, bc1, bc2,
+                                                         sched);
     if (loss_out) sum_kernel<<<1, 256, 0, st>>>(A.loss_part, tiles, loss_out);
+    return cudaGetLastError();
+}
+
+void mlp_sched_init(mlp::TrainSched& s) { mlp::sched_set(s); }
+
+cudaError_t mlp_sched_advance(mlp::TrainSched* s, cudaStream_t st)
+{
+    mlp::sched_advance_kernel<<<1, 1, 0, st>>>(s);
     return cudaGetLastError();
 }
 
@@ -570,10 +644,12 @@ cudaError_t mlp_infer(const __nv_bfloat16* x, int n, const float* params, const 
 // one training batch from the device-resident set: rows perm[first .. first + rows)
 __global__ void gather_batch_kernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ Y,
                                     const float* __restrict__ W, const int* __restrict__ perm, int64_t first, int rows,
-                                    __nv_bfloat16* __restrict__ xb, float* __restrict__ yb, float* __restrict__ wb)
+                                    __nv_bfloat16* __restrict__ xb, float* __restrict__ yb, float* __restrict__ wb,
+                                    const mlp::TrainSched* sched)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= rows) return;
+    if (sched) first = (sched->count % sched->steps_per_epoch) * (int64_t)sched->rows; // this step's batch
     const int64_t i = __ldg(perm + first + r);
     const uint4* src = reinterpret_cast<const uint4*>(X + i * mlp::KIN);
     uint4* dst = reinterpret_cast<uint4*>(xb + (int64_t)r * mlp::KIN);
@@ -584,9 +660,10 @@ __global__ void gather_batch_kernel(const __nv_bfloat16* __restrict__ X, const f
 }
 
 cudaError_t mlp_gather_batch(const __nv_bfloat16* X, const float* Y, const float* W, const int* perm, int64_t first,
-                             int rows, __nv_bfloat16* xb, float* yb, float* wb, cudaStream_t st)
+                             int rows, __nv_bfloat16* xb, float* yb, float* wb, cudaStream_t st,
+                             const mlp::TrainSched* sched)
 {
-    gather_batch_kernel<<<(rows + 127) / 128, 128, 0, st>>>(X, Y, W, perm, first, rows, xb, yb, wb);
+    gather_batch_kernel<<<(rows + 127) / 128, 128, 0, st>>>(X, Y, W, perm, first, rows, xb, yb, wb, sched);
     return cudaGetLastError();
 }
 

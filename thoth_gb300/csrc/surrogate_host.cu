@@ -32,13 +32,24 @@ struct TrainArgs {
     float* loss_part;
     int* status;
 };
+struct TrainSched {
+    long long count, total, steps_per_epoch, step0;
+    double lr0;
+    float lr_t, bc1, bc2;
+    int rows;
+};
 } // namespace mlp
 cudaError_t mlp_train_step(const mlp::TrainArgs& A, float* params, float* m, float* v, __nv_bfloat16* wbf, float lr,
-                           float b1, float b2, float eps, float bc1, float bc2, float* loss_out, cudaStream_t st);
+                           float b1, float b2, float eps, float bc1, float bc2, float* loss_out, cudaStream_t st,
+                           const mlp::TrainSched* sched = nullptr);
+cudaError_t mlp_train_prepare();
+void mlp_sched_init(mlp::TrainSched& s);
+cudaError_t mlp_sched_advance(mlp::TrainSched* s, cudaStream_t st);
 cudaError_t mlp_infer(const __nv_bfloat16* x, int n, const float* params, const __nv_bfloat16* wbf, float* y,
                       int* status, int grid, cudaStream_t st);
 cudaError_t mlp_gather_batch(const __nv_bfloat16* X, const float* Y, const float* W, const int* perm, int64_t first,
-                             int rows, __nv_bfloat16* xb, float* yb, float* wb, cudaStream_t st);
+                             int rows, __nv_bfloat16* xb, float* yb, float* wb, cudaStream_t st,
+                             const mlp::TrainSched* sched = nullptr);
 int mlp_n_params();
 int mlp_n_bf();
 struct LatticeArgs {
@@ -104,6 +115,8 @@ struct ThothSurrogate {
     // lattice serving: parameter sets and lattice axes, scaled prices
     int64_t cap_lat = 0;
     unsigned char* lb = nullptr;
+    // the training schedule the captured step reads (learning rate, bias corrections, batch)
+    mlp::TrainSched* sched = nullptr;
     // device copy of a training set and its per-epoch permutation (grown on demand)
     int64_t cap_ds = 0;
     unsigned char* ds = nullptr;
@@ -295,6 +308,7 @@ int thoth_gpu_surrogate_destroy(ThothSurrogate* s)
         if (s->tb) cudaFree(s->tb);
         if (s->ib) cudaFree(s->ib);
         if (s->lb) cudaFree(s->lb);
+        if (s->sched) cudaFree(s->sched);
         if (s->ds) cudaFree(s->ds);
         if (s->perm_host) cudaFreeHost(s->perm_host);
         if (s->perm_copied) cudaEventDestroy(s->perm_copied);
@@ -427,38 +441,60 @@ int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y,
         std::mt19937_64 rng(seed);
         const int64_t steps_per_epoch = n / B, total = steps_per_epoch * epochs;
         mlp::TrainArgs& A = s->A;
-        double last = 0;
+        A.a[0] = const_cast<__nv_bfloat16*>(A.x);
+        A.rows = B;
+        // the schedule of this call on the device: the captured step reads its batch offset,
+        // learning rate and bias corrections there and advances it
+        if (!s->sched) STRY(cudaMalloc(&s->sched, sizeof(mlp::TrainSched)));
+        mlp::TrainSched sc{};
+        sc.count = 0;
+        sc.total = total;
+        sc.steps_per_epoch = steps_per_epoch;
+        sc.step0 = s->step;
+        sc.lr0 = lr;
+        sc.rows = B;
+        mlp_sched_init(sc);
+        STRY(cudaMemcpyAsync(s->sched, &sc, sizeof sc, cudaMemcpyHostToDevice, s->st));
         STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+        STRY(mlp_train_prepare());
+        // one step (gather, forward, backward, Adam, loss, schedule) captured once, replayed
+        // for every step: its launches' arguments do not change from step to step
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        STRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = mlp_gather_batch(dX, dY, dW, dP, 0, B, const_cast<__nv_bfloat16*>(A.x), const_cast<float*>(A.y),
+                                          const_cast<float*>(A.inv_w2), s->st, s->sched);
+        if (ce == cudaSuccess)
+            ce = mlp_train_step(A, s->params, s->m, s->v, s->wbf, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f, s->loss, s->st,
+                                s->sched);
+        if (ce == cudaSuccess) ce = mlp_sched_advance(s->sched, s->st);
+        const cudaError_t ee = cudaStreamEndCapture(s->st, &graph);
+        if (ce == cudaSuccess) ce = ee;
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            if (exec) cudaGraphExecDestroy(exec);
+            return sfail(THOTH_GPU_E_CUDA, std::string("training step graph: ") + cudaGetErrorString(ce));
+        }
+        struct ExecGuard {
+            cudaGraphExec_t e;
+            ~ExecGuard() { cudaGraphExecDestroy(e); }
+        } guard{exec};
         STRY(cudaEventRecord(s->perm_copied, s->st));
-        int64_t done = 0;
         for (int e = 0; e < epochs; e++) {
+            // the next permutation is drawn on the host while the device runs the previous epoch
             std::shuffle(idx.begin(), idx.end(), rng);
             STRY(cudaEventSynchronize(s->perm_copied)); // the previous permutation has left the pinned buffer
             std::memcpy(s->perm_host, idx.data(), sizeof(int) * (size_t)n);
             STRY(cudaMemcpyAsync(dP, s->perm_host, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->st));
             STRY(cudaEventRecord(s->perm_copied, s->st));
-            double acc = 0;
-            for (int64_t b = 0; b < steps_per_epoch; b++, done++) {
-                STRY(mlp_gather_batch(dX, dY, dW, dP, b * B, B, const_cast<__nv_bfloat16*>(A.x), const_cast<float*>(A.y),
-                                      const_cast<float*>(A.inv_w2), s->st));
-                A.a[0] = const_cast<__nv_bfloat16*>(A.x);
-                A.rows = B;
-                s->step++;
-                const double lr_t = lr * 0.5 * (1.0 + std::cos(M_PI * (double)done / (double)total)) + 1e-6;
-                const float bc1 = (float)(1.0 - std::pow(0.9, (double)s->step));
-                const float bc2 = (float)(1.0 - std::pow(0.999, (double)s->step));
-                const bool last_batch = (b == steps_per_epoch - 1);
-                STRY(mlp_train_step(A, s->params, s->m, s->v, s->wbf, (float)lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2,
-                                    last_batch ? s->loss : nullptr, s->st));
-                if (last_batch && e == epochs - 1) {
-                    float l = 0;
-                    STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
-                    STRY(cudaStreamSynchronize(s->st));
-                    acc = l / B;
-                }
-            }
-            last = acc;
+            for (int64_t b = 0; b < steps_per_epoch; b++) STRY(cudaGraphLaunch(exec, s->st));
         }
+        s->step += total;
+        float l = 0;
+        STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
+        STRY(cudaStreamSynchronize(s->st));
+        const double last = l / B;
         rc = check_status(s);
         if (rc) return rc;
         if (final_loss) *final_loss = last;

@@ -686,6 +686,20 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     }
     D.lev_layers_stride = layers_stride;
     D.lev_row_stride = lev_pts_max; // one row stride for every asset, whatever its point count
+    // each LSV step's record carries the leverage layer of the date it ends on (engine.cuh)
+    for (int i = 1; i <= N; i++)
+        for (int a = 0; a < NA; a++) {
+            if (d->assets[a].model != THOTH_MODEL_LSV) continue;
+            AssetStep& s = steps[(size_t)(i - 1) * NA + a];
+            const int layer = lev_layer[(size_t)a * nd + i];
+            const float2 mp = lev_map[(size_t)a * layers_stride + layer];
+            const size_t row = ((size_t)a * layers_stride + layer) * lev_pts_max;
+            if (row > (size_t)INT32_MAX) return fail(THOTH_GPU_E_TOO_LARGE, "leverage tables too large");
+            s.c[12] = mp.x;
+            s.c[13] = mp.y;
+            const int32_t r32 = (int32_t)row;
+            std::memcpy(&s.c[14], &r32, sizeof r32);
+        }
 
     // products -> slots, groups, events
     std::map<std::tuple<int, int, int>, int> slot_of; // (type, asset, date)

@@ -251,78 +251,74 @@ def _mc_subset(param_sets, paths, lms, Ts):
 
 
 POLICIES = ("bucket", "grid")
-Z90 = 1.6448536269514722  # the 90th percentile of |Z|, Z ~ N(0, 1)
 JUDGE_SECOND_BLOCK = 1 << 31  # Sobol skip of the judge's second, independent block
 
 
-def grid_p90(sigma):
-    """90th percentile of |e| over a grid whose cells in bucket b have errors N(0, sigma_b^2):
-    the x at which the mean over buckets of P(|e| > x) = 2 Phi(-x / sigma_b) is 0.1."""
-    from scipy.special import ndtr
-    s = np.asarray(sigma, dtype=np.float64).ravel()
-    if not np.any(s > 0):
-        return 0.0
-    frac = lambda x: float(np.mean(np.where(s > 0, 2.0 * ndtr(-x / np.maximum(s, 1e-300)), 0.0)))
-    lo, hi = 0.0, 10.0 * float(s.max())
-    for _ in range(80):
-        mid = 0.5 * (lo + hi)
-        lo, hi = (mid, hi) if frac(mid) > 0.1 else (lo, mid)
-    return hi
-
-
-def choose_fallback(sigma, tol=TOL, policy="grid", margin=1.0, n_T=None):
-    """Buckets (lattice cells, maturity-major with n_T maturities) that MC takes over, from
-    each bucket's surrogate error scale sigma_b (see judge()).
-    policy "bucket": every bucket whose own 90th-percentile error, Z90 sigma_b, exceeds tol.
-    policy "grid": the grid as a whole meets the target: buckets are taken over worst first,
-    within the shortest maturity horizon that suffices (an MC fallback book runs to its
-    longest maturity), until grid_p90 is at most margin * tol, a taken-over bucket counting
-    at the plain-MC accuracy (90th percentile tol: sigma = tol / Z90)."""
-    sigma = np.asarray(sigma, dtype=np.float64).ravel()
+def choose_fallback(jerr, tol=TOL, policy="grid", margin=1.0, n_T=None):
+    """Buckets (columns of jerr [judged sets][buckets], the surrogate's judged cell
+    errors, maturity-major with n_T maturities) that MC takes over; see judge().
+    policy "bucket": every bucket whose 90th-percentile error exceeds tol.
+    policy "grid": the grid as a whole meets the target. It is cost-aware: an MC fallback
+    book runs to its longest maturity, so it looks for the shortest maturity horizon within
+    which taking over the worst buckets (worst first, a taken-over bucket counting at tol / 2,
+    the plain MC's accuracy) brings the grid's 90th percentile to margin * tol."""
+    jerr = np.asarray(jerr, dtype=np.float64)
+    bucket = np.quantile(jerr, 0.9, axis=0)
     if policy == "bucket":
-        return Z90 * sigma > tol
+        return bucket > tol
     if policy != "grid":
         raise ValueError("policy must be one of %s" % (POLICIES,))
-    nb = sigma.size
+    nb = bucket.size
     n_T = n_T or nb
     mat = np.arange(nb) // (nb // n_T)        # maturity index of each bucket
-    if grid_p90(sigma) <= margin * tol:
+    if np.quantile(jerr, 0.9) <= margin * tol:
         return np.zeros(nb, dtype=bool)
-    fb_sigma = tol / Z90
     best = None
     for h in range(n_T):                       # horizon: maturities 0 .. h may fall back
         bad = np.zeros(nb, dtype=bool)
-        s = sigma.copy()
-        for b in np.argsort(-sigma, kind="stable"):
-            if mat[b] > h or sigma[b] <= fb_sigma:
+        e = jerr.copy()
+        for b in np.argsort(-bucket, kind="stable"):
+            if mat[b] > h or bucket[b] <= 0.5 * tol:
                 continue
             bad[b] = True
-            s[b] = fb_sigma
-            if grid_p90(s) <= margin * tol:
+            e[:, b] = 0.5 * tol
+            if np.quantile(e, 0.9) <= margin * tol:
                 break
-        if grid_p90(s) <= margin * tol:
+        if np.quantile(e, 0.9) <= margin * tol:
             return bad
         best = bad
-    return best | (Z90 * sigma > tol)          # the target is out of reach: every bucket above tol too
+    return best | (bucket > tol)               # the target is out of reach: every bucket above tol too
+
+
+def noise_corrected(r, noise):
+    """Judged cell errors with the judge's own noise taken out: the 90th percentile of |e|
+    (e the surrogate's error) is estimated by quantile subtraction in quadrature,
+    p90(|e|)^2 = p90(|r|)^2 - p90(|n|)^2 (r = e + the judge's noise, n a sample of that
+    noise), which makes no assumption on the shape of e's distribution; the cells' errors are
+    then scaled by p90(|e|) / p90(|r|), keeping their ranking. Returns (scaled errors,
+    estimated p90, p90 of |r|, p90 of |n|)."""
+    r, noise = np.abs(np.asarray(r, dtype=np.float64)), np.abs(np.asarray(noise, dtype=np.float64))
+    qr, qn = float(np.quantile(r, 0.9)), float(np.quantile(noise, 0.9))
+    est = math.sqrt(max(qr * qr - qn * qn, 0.0))
+    k = est / qr if qr > 0 else 1.0
+    return r * k, est, qr, qn
 
 
 def judge(model, param_sets, judge_frac=0.01, judge_paths=1 << 19, tol=TOL, seed=0, lms=LATTICE_LM, Ts=LATTICE_T,
           policy="grid", margin=1.0):
-    """MC judge with its own noise removed: re-price a random judge_frac of the sets by MC
-    and estimate, per lattice bucket (maturity, log-moneyness), the surrogate's error.
+    """MC judge with its own noise removed: re-price a random judge_frac of the sets by MC,
+    measure the surrogate's error against it, and choose the lattice buckets (maturity,
+    log-moneyness) that MC takes over.
 
     The judged sets are priced twice, on two Sobol blocks of judge_paths / 2 points far
     apart in the sequence (the first points, and points from 2^31 on), whose errors are
     independent; ybar is their mean. (The two halves of one block of judge_paths points
     would not do: their errors partly cancel in the full block, so their difference would
-    overstate the error of the mean.) With r = (s - ybar) / w the surrogate's judged cell
-    error (w the cell's error floor, max(|ybar|, 1% of spot)) and n = (y1 - y2) / (2 w), n
-    has the variance of the judge's own error in r, so per bucket
-        sigma_b^2 = mean(r^2) - mean(n^2)
-    is the surrogate's mean-square error with the judge's noise taken out. The judge can
-    then run at the plain-MC path count (1% of the sets costs about 1% of plain MC) without
-    its own error flagging healthy buckets. choose_fallback then picks the buckets MC takes
-    over, and grid_p90(sigma) is the estimated 90th-percentile error of the judged grid."""
+    overstate the error of the mean.) r = (s - ybar) / w is the surrogate's judged cell error
+    (w the cell's error floor, max(|ybar|, 1% of spot)), and n = (y1 - y2) / (2 w) has the
+    distribution of the judge's own error in r. noise_corrected() takes that error out, so
+    the judge can run at the plain-MC path count (1% of the sets costs about 1% of plain MC)
+    without its noise flagging healthy buckets; choose_fallback() then picks the buckets."""
     rng = np.random.default_rng(seed)
     n_judge = max(1, int(round(judge_frac * len(param_sets))))
     judged = np.sort(rng.choice(len(param_sets), size=n_judge, replace=False))
@@ -337,11 +333,10 @@ def judge(model, param_sets, judge_frac=0.01, judge_paths=1 << 19, tol=TOL, seed
     w = np.maximum(np.abs(ybar), FLOOR)
     r = ((pj - ybar) / w).reshape(n_judge, -1)
     noise = (0.5 * (y1 - y2) / w).reshape(n_judge, -1)
-    sigma = np.sqrt(np.maximum(np.mean(r * r, axis=0) - np.mean(noise * noise, axis=0), 0.0))
-    bad = choose_fallback(sigma, tol, policy, margin, n_T=len(Ts))
-    return dict(judged=judged, bad=bad.reshape(len(Ts), len(lms)), judge_s=t_judge, sigma=sigma,
-                judge_mc_seconds_per_set=t_judge / n_judge, judged_p90=float(np.quantile(np.abs(r), 0.9)),
-                estimated_p90=grid_p90(sigma), judge_noise_rms=float(np.sqrt(np.mean(noise * noise))))
+    jerr, est, qr, qn = noise_corrected(r, noise)
+    bad = choose_fallback(jerr, tol, policy, margin, n_T=len(Ts))
+    return dict(judged=judged, bad=bad.reshape(len(Ts), len(lms)), judge_s=t_judge,
+                judge_mc_seconds_per_set=t_judge / n_judge, judged_p90=qr, estimated_p90=est, judge_noise_p90=qn)
 
 
 def price_grid(model, param_sets, mc_paths, judge_frac=0.01, judge_paths=None, seed=0, tol=TOL, lms=LATTICE_LM,
@@ -393,7 +388,7 @@ def price_grid(model, param_sets, mc_paths, judge_frac=0.01, judge_paths=None, s
                        fallback_s=t_fb, fallback_cells=n_fb, failing_buckets=int(bad2.sum()),
                        out_of_box_sets=int(len(out_sets)), mc_paths=mc_paths, cells_per_sec=cells / total,
                        policy=policy, judged_p90=J["judged_p90"], estimated_p90=J["estimated_p90"],
-                       judge_noise_rms=J["judge_noise_rms"])
+                       judge_noise_p90=J["judge_noise_p90"])
 
 
 def calibrate_plain_mc(param_sets, cf, tol=TOL, lo=10, hi=24):
