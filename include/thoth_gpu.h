@@ -475,8 +475,10 @@ int thoth_gpu_bridge_program(const double* t, int32_t n_dates, int32_t* first_co
 /* Host-only test hook: validate a descriptor and report the launch plan.
  * out[0] kernel variant, [1] paths per tile, [2] shared-memory bytes per CTA,
  * [3] observation slots, [4] path groups, [5] bridge stack depth,
- * [6] Sobol dimensions, [7] tiles, [8] launch shape, [9] threads per CTA
- * (out holds 10 values). Returns the descriptor's status code. */
+ * [6] Sobol dimensions, [7] tiles, [8] launch shape, [9] threads per CTA,
+ * [10] moments summed per thread across tiles (books of at most four products;
+ * 0: sums reduced per tile) (out holds 11 values). Returns the descriptor's
+ * status code. */
 int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out);
 
 /* Test hook, no reference counterpart: one tcgen05 BF16 tensor-core GEMM,

@@ -112,6 +112,54 @@ def test_config1_gbm_call(gpu):
     assert abs(r["vega"][0] - oracle.bs_vega(100, 100, 1.0, 0.25, 0.03, 0.01)) < 3 * r["vega_trust"][0] + 1e-3
 
 
+def test_few_product_books_shared_paths(gpu):
+    """Books of at most four products sum their paths per thread across tiles (few-product
+    mode): a Heston book of a vanilla, a barrier, a variance swap and a one-name basket, and
+    a GBM book of two products with pathwise delta and vega, against the oracle on the same
+    paths, trust included."""
+    b = abi.Book(days=np.arange(0, 61), paths=(1 << 14) + 77)
+    h = b.add_heston(100.0, 0.04, 1.5, 0.04, 0.6, -0.7, 0.01)
+    b.add_vanilla(h, 95.0, 60, abi.PUT, zero_rate=0.02)
+    b.add_barrier(h, 100.0, 60, 85.0, up=False, knock_in=False, monitor=np.arange(1, 61), zero_rate=0.02)
+    b.add_variance(h, 45, strike_variance=0.04, notional=100.0, zero_rate=0.02)
+    b.add_basket([h], [1.0], 100.0, 30, zero_rate=0.02)
+    assert gpu.plan_summary(b)["few_moments"] == 10
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "few products", scale=leg_scale(b))
+    np.testing.assert_allclose(r["trust"], ref["trust"], rtol=1e-3, atol=1e-9)
+    assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"] + 1e-4 * abs(ref["book_premium"])
+
+    g = abi.Book(days=[0, 180, 365], paths=(1 << 15) + 3, greeks=abi.GREEK_DELTA | abi.GREEK_VEGA)
+    a = g.add_gbm(100.0, 0.25, 0.02)
+    g.add_vanilla(a, 105.0, 2, abi.CALL, zero_rate=0.03)
+    g.add_vanilla(a, 95.0, 1, abi.PUT, zero_rate=0.03)
+    assert gpu.plan_summary(g)["few_moments"] == 14
+    r = gpu.price_book(g, greeks=True)
+    ref = oracle.price_book(g)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "few products, Greeks")
+    np.testing.assert_allclose(r["trust"], ref["trust"], rtol=1e-3, atol=1e-9)
+    for k, (s, K, T, phi) in enumerate(((100.0, 105.0, 1.0, 1), (100.0, 95.0, 180 / 365.0, -1))):
+        # pathwise Greeks against the closed forms (Sobol error only)
+        d = oracle.bs_delta(s, K, T, 0.25, 0.03, 0.01) - (0 if phi > 0 else np.exp(-0.01 * T))
+        assert abs(r["delta"][k] - d) < 3 * r["delta_trust"][k] + 1e-4
+
+
+def test_few_product_book_across_folds(gpu):
+    """Config 1 at 2^22 paths (about 18 tiles per CTA): the per-thread sums are folded into
+    the per-warp totals every 16 tiles and at the end; the price, its trust and the book
+    value equal the oracle's on the same paths, and reruns are bit-identical."""
+    b = W.gbm_call(paths=1 << 22, greeks=False)
+    assert gpu.plan_summary(b)["few_moments"] == 4
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "cfg1 2^22")
+    np.testing.assert_allclose(r["trust"], ref["trust"], rtol=1e-3)
+    assert abs(r["book_premium"] - ref["book_premium"]) <= 1e-4 * abs(ref["book_premium"])
+    r2 = gpu.price_book(b)
+    assert r2["premium"][0] == r["premium"][0] and r2["book_premium"] == r["book_premium"]
+
+
 def test_drop_in_price_european_gbm(gpu):
     # gpu::PriceEuropeanGbm semantics: forward measure, df given
     F, K, T, vol, df = 100 * np.exp(0.02), 95.0, 1.0, 0.25, np.exp(-0.03)

@@ -391,7 +391,8 @@ def bridge_program(t):
 def plan_summary(book):
     """Host-only: validate a book and return its launch plan as a dict."""
     d = book.desc()
-    out = np.zeros(10, dtype=np.int64)
+    out = np.zeros(11, dtype=np.int64)
     _check(lib().thoth_gpu_plan_summary(C.byref(d), out.ctypes.data_as(C.POINTER(C.c_int64))))
-    keys = ("variant", "tile", "smem", "slots", "groups", "stack_depth", "sobol_dims", "tiles", "shape", "threads")
+    keys = ("variant", "tile", "smem", "slots", "groups", "stack_depth", "sobol_dims", "tiles", "shape", "threads",
+            "few_moments")
     return dict(zip(keys, (int(v) for v in out)))

@@ -174,6 +174,7 @@ struct DevPlan {
     int n_sobol;
     double* acc;                 // [gridDim][n_acc] per-CTA FP64 sums
     int n_acc;
+    int few_m;                   // > 0: few-product accumulation over few_m moments (see book_kernel)
     float* path_out;             // [n_steps + 1][path_ld] spot of asset path_asset at every date (null: not stored)
     int64_t path_ld;             // paths per stored date (the book's path count)
     int path_asset;

@@ -1,877 +1,11 @@
-// kernels.cu — sm_103a kernels of the Monte-Carlo engine (see engine.cuh).
-#include "engine.cuh"
+// kernels.cu — sm_103a kernels of the Monte-Carlo engine (see engine.cuh) other
+// than the book kernel itself (book.cuh): the fixed-order reduction, the Sobol
+// low-word gather, test hooks, peak microbenchmarks and the book launch dispatch.
+#include "book.cuh"
 
 #include <cuda_runtime.h>
 
 namespace thoth {
-
-// ---------------------------------------------------------------------------
-// shared-memory carve-up (host and device compute the same sizes)
-// ---------------------------------------------------------------------------
-struct Smem {
-    uint2* hs;      // [min(sobol_dims, HS_CHUNK)] tile parts of the current chunk of Sobol entries,
-                    // for tile columns t and t + T/2 (see tile_high_bits)
-    float* stk;     // [stack_depth][stack_factors][T]; after the time loop, the product partials
-    float* slots;   // [n_slots][T + 1]
-    float* grp;     // [n_groups][T + 1]
-    float* last;    // [n_last][T + 1] previous observation of each discretely observed variance group
-    float* part;    // [T * 6] product partials: the bridge stack's space, free once the paths are built
-    double* red;    // [2 * warps]
-};
-
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
-
-__host__ __device__ constexpr int log2i(int x) { return x <= 1 ? 0 : 1 + log2i(x / 2); }
-
-// Sobol entries whose tile parts are held in shared memory at a time
-constexpr int HS_CHUNK = 512;
-__host__ __device__ inline int hs_words(int sobol_dims) { return sobol_dims < HS_CHUNK ? sobol_dims : HS_CHUNK; }
-
-// the bridge stack, or the product partials that reuse its space after the time loop
-__host__ __device__ inline size_t stack_part_bytes(int T, int stack_depth, int nfa)
-{
-    const size_t stk = sizeof(float) * (size_t)stack_depth * nfa * T, part = sizeof(float) * (size_t)T * 6;
-    return align16(stk > part ? stk : part);
-}
-
-__host__ __device__ inline size_t smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots,
-                                             int n_groups, int n_last)
-{
-    size_t b = 0;
-    b += align16(sizeof(uint2) * (size_t)hs_words(sobol_dims));
-    b += stack_part_bytes(T, stack_depth, nfa);
-    b += align16(sizeof(float) * (size_t)n_slots * (T + 1));
-    b += align16(sizeof(float) * (size_t)n_groups * (T + 1));
-    b += align16(sizeof(float) * (size_t)n_last * (T + 1));
-    b += align16(sizeof(double) * 2 * (T / 32));
-    return b;
-}
-
-__device__ inline Smem carve(unsigned char* base, const DevPlan& P, int T)
-{
-    Smem s;
-    size_t o = 0;
-    s.hs = reinterpret_cast<uint2*>(base + o);
-    o += align16(sizeof(uint2) * (size_t)hs_words(P.sobol_dims));
-    s.stk = reinterpret_cast<float*>(base + o);
-    s.part = s.stk;
-    o += stack_part_bytes(T, P.stack_depth, P.stack_factors);
-    s.slots = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * (size_t)P.n_slots_used * (T + 1));
-    s.grp = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * (size_t)P.n_groups * (T + 1));
-    s.last = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * (size_t)P.n_last * (T + 1));
-    s.red = reinterpret_cast<double*>(base + o);
-    return s;
-}
-
-// ---------------------------------------------------------------------------
-// Sobol for the current tile. Path n = m * T + t (T = 2^TB). gray(n) splits
-// into bits >= TB, shared by the whole tile, and the thread's low TB bits
-// gray(t) ^ ((m & 1) << (TB - 1)). The XOR of V[d][j] over the bits of gray(t)
-// depends on the thread only: a fixed word lo[d][t]. Every Sobol dimension is
-// used once per path, in an order fixed by the bridge program, so the book's
-// low words are laid out in that order (sobol_lo[j][t], j the j-th dimension
-// consumed) and the tile part likewise (hs[j], computed per tile in chunks of
-// HS_CHUNK entries). The step loop then reads both sequentially:
-// x = hs[j] ^ lo[j][t], with the coalesced load of entry j + 2 in flight while
-// entry j is used. Every thread of the CTA consumes the same entries in the
-// same order, so all of them reach a chunk boundary at the same call, where
-// the next chunk is computed between two barriers.
-//
-// Columns t and t + T/2 (t < T/2) differ in their low bits by gray(T/2) =
-// 3 << (TB - 2), so lo[d][t + T/2] = lo[d][t] ^ V[d][TB-1] ^ V[d][TB-2], a word
-// shared by the tile. The tile part is therefore kept as a pair, hs[j] and
-// hs[j] ^ V[d][TB-1] ^ V[d][TB-2]: a thread with two paths (columns t and
-// t + T/2) reads one low word per entry, and one 8-byte broadcast of the pair.
-// ---------------------------------------------------------------------------
-template <int TB>
-__device__ inline void tile_high_bits(const DevPlan& P, uint2* hs, int64_t m, int j0)
-{
-    const uint64_t g = (uint64_t)m ^ ((uint64_t)m >> 1);
-    const int j1 = min(j0 + HS_CHUNK, P.n_sobol);
-    for (int j = j0 + (int)threadIdx.x; j < j1; j += blockDim.x) {
-        const uint32_t* V = P.sobol_v + __ldg(P.sobol_order + j) * SOBOL_BITS;
-        uint32_t acc = (m & 1) ? __ldg(V + TB - 1) : 0u;
-        uint64_t gg = g;
-        for (int k = 0; gg != 0 && k < SOBOL_BITS - TB; ++k, gg >>= 1)
-            if (gg & 1u) acc ^= __ldg(V + TB + k);
-        hs[j - j0] = make_uint2(acc, acc ^ __ldg(V + TB - 1) ^ __ldg(V + TB - 2));
-    }
-}
-
-// low words a thread loads per Sobol entry: with an even number of paths, one for each pair
-// of columns t + k T/PP and t + k T/PP + T/2 (k < PP/2), through the tile-part pair; else
-// one per path
-template <int PP>
-struct LoadsPerEntry {
-    static constexpr int value = PP % 2 == 0 ? PP / 2 : PP;
-};
-
-template <int T, int PP>
-struct SobolLane {
-    static constexpr int LW = LoadsPerEntry<PP>::value;
-    uint2* hs;             // tile parts of entries [jend - HS_CHUNK, jend), smem
-    const uint32_t* lo;    // column threadIdx.x of the book's low words
-    int64_t m;             // tile index
-    int j, jend;           // next entry; end of the chunk in shared memory
-    uint32_t cur[LW], nxt[LW]; // low words of entries j and j + 1
-};
-
-// path p of a thread is tile column threadIdx.x + p * (T / PP); the first chunk
-// of tile parts must already be in hs
-template <int TB, int PP>
-__device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, uint2* hs, int64_t m)
-{
-    constexpr int T = 1 << TB, TH = T / PP, LW = LoadsPerEntry<PP>::value;
-    SobolLane<T, PP> L;
-    L.hs = hs;
-    L.lo = P.sobol_lo + threadIdx.x;
-    L.m = m;
-    L.j = 0;
-    L.jend = HS_CHUNK;
-#pragma unroll
-    for (int p = 0; p < LW; ++p) {
-        L.cur[p] = P.n_sobol > 0 ? __ldg(L.lo + p * TH) : 0u;
-        L.nxt[p] = P.n_sobol > 1 ? __ldg(L.lo + T + p * TH) : 0u;
-    }
-    return L;
-}
-
-// Gaussians of reference dimension `dim` for the thread's PP paths (Sobol
-// indices n[p]); a Sobol dimension is the lane's next entry
-template <int T, int PP>
-__device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, const uint64_t (&n)[PP], int dim,
-                                      float (&z)[PP])
-{
-    constexpr int TH = T / PP, LW = LoadsPerEntry<PP>::value;
-    uint32_t x[PP];
-    if (dim < P.sobol_dims) {
-        if (L.j == L.jend) { // next chunk of tile parts (uniform across the CTA, see above)
-            __syncthreads();
-            tile_high_bits<log2i(T)>(P, L.hs, L.m, L.j);
-            __syncthreads();
-            L.jend += HS_CHUNK;
-        }
-        const uint2 h = L.hs[L.j - (L.jend - HS_CHUNK)];
-        const int jn = L.j + 2;
-        const bool more = jn < P.n_sobol;
-        if constexpr (PP % 2 == 0) {
-            // path k is column t + k TH; path k + PP/2 is column t + k TH + T/2
-#pragma unroll
-            for (int k = 0; k < PP / 2; ++k) {
-                x[k] = h.x ^ L.cur[k];
-                x[k + PP / 2] = h.y ^ L.cur[k];
-            }
-        } else {
-#pragma unroll
-            for (int p = 0; p < PP; ++p) x[p] = h.x ^ L.cur[p];
-        }
-#pragma unroll
-        for (int p = 0; p < LW; ++p) {
-            L.cur[p] = L.nxt[p];
-            L.nxt[p] = more ? __ldg(L.lo + jn * T + p * TH) : 0u;
-        }
-        ++L.j;
-    } else {
-#pragma unroll
-        for (int p = 0; p < PP; ++p) x[p] = hash_u32(P.seed, n[p], (uint32_t)dim);
-    }
-    quantile_n<PP>(x, z);
-}
-
-// lw W_prev + (rw W_top + sd z) for a thread's two paths, paired (same roundings as the
-// scalar fmaf form)
-__device__ __forceinline__ float2 bridge_comb2(float lw, float rw, float sd, float wp0, float wp1, float tp0, float tp1,
-                                               float z0, float z1)
-{
-    return __ffma2_rn(f2s(lw), f2(wp0, wp1), __ffma2_rn(f2s(rw), f2(tp0, tp1), __fmul2_rn(f2s(sd), f2(z0, z1))));
-}
-
-// ---------------------------------------------------------------------------
-// One time step of the bridge for every active factor slot of the thread's PP
-// paths: fills nz[][] with the normalised increments
-// n_i = (W_i - W_{i-1}) / sqrt(t_i - t_{i-1}). Stack entry of path column k:
-// stk[(level * nfa + factor) * T + k].
-// ---------------------------------------------------------------------------
-// SEQ: one asset, a0, per pass; its spot and variance factors are stack rows 0 and 1
-template <int NA, int T, int PP, bool SEQ>
-__device__ __forceinline__ void bridge_step(const DevPlan& P, const Smem& S, const StepRec& rec, int& sp,
-                                            SobolLane<T, PP>& L, const uint64_t (&n)[PP],
-                                            float (&Wprev)[PP][2 * NA], float (&top)[PP][2 * NA],
-                                            float (&nz)[PP][2 * NA], int a0)
-{
-    constexpr int FS = 2 * NA, TH = T / PP;
-    const int t = threadIdx.x;
-    const int nfa = P.stack_factors;
-    // asset and stack row of factor slot f (stack row < 0: slot inactive)
-    auto slot = [&](int f, int& a, int& ci) {
-        const int s_ = f < NA ? f : f - NA;
-        a = SEQ ? a0 : s_;
-        const int c = f < NA ? P.cidx_spot[a] : P.cidx_var[a];
-        ci = (a < P.n_assets && c >= 0) ? (SEQ ? (f < NA ? 0 : 1) : c) : -1;
-    };
-    float Wi[PP][FS];
-#pragma unroll
-    for (int p = 0; p < PP; ++p)
-#pragma unroll
-        for (int f = 0; f < FS; ++f) Wi[p][f] = 0.f;
-    if (rec.count == 0) {
-        const int base = (sp - 1) * nfa * T + t;
-#pragma unroll
-        for (int f = 0; f < FS; ++f) {
-            int a, ci;
-            slot(f, a, ci);
-            if (ci >= 0) {
-#pragma unroll
-                for (int p = 0; p < PP; ++p) {
-                    Wi[p][f] = top[p][f];
-                    top[p][f] = S.stk[base + ci * T + p * TH];
-                }
-            }
-        }
-        --sp;
-    } else if (rec.count == 1) {
-        // a single node ending at this date (about a quarter of the steps): no push
-#pragma unroll
-        for (int f = 0; f < FS; ++f) {
-            int a, ci;
-            slot(f, a, ci);
-            if (ci >= 0) {
-                const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
-                float z[PP];
-                gauss(P, L, n, rec.dim + fid, z);
-                if constexpr (PP % 2 == 0) {
-#pragma unroll
-                    for (int h = 0; h < PP; h += 2) {
-                        const float2 w = bridge_comb2(rec.lw, rec.rw, rec.sd, Wprev[h][f], Wprev[h + 1][f], top[h][f],
-                                                      top[h + 1][f], z[h], z[h + 1]);
-                        Wi[h][f] = w.x;
-                        Wi[h + 1][f] = w.y;
-                    }
-                } else {
-#pragma unroll
-                    for (int p = 0; p < PP; ++p)
-                        Wi[p][f] = fmaf(rec.lw, Wprev[p][f], fmaf(rec.rw, top[p][f], rec.sd * z[p]));
-                }
-            }
-        }
-    } else {
-        float lw = rec.lw, rw = rec.rw, sd = rec.sd;
-        int dim = rec.dim;
-        BridgeNode nd = P.nodes[rec.first]; // node 1 of the chain, loaded one node ahead
-        for (int k = 0; k < rec.count; ++k) {
-            if (k > 0) {
-                lw = nd.lw;
-                rw = nd.rw;
-                sd = nd.sd;
-                dim = nd.bstep * P.ref_factors;
-                if (k + 1 < rec.count) nd = P.nodes[rec.first + k];
-            }
-            const bool push = k + 1 < rec.count;
-            const int base = sp * nfa * T + t;
-#pragma unroll
-            for (int f = 0; f < FS; ++f) {
-                int a, ci;
-                slot(f, a, ci);
-                if (ci >= 0) {
-                    const int fid = f < NA ? P.fid_spot[a] : P.fid_var[a];
-                    float z[PP];
-                    gauss(P, L, n, dim + fid, z);
-                    float Wns[PP];
-                    if constexpr (PP % 2 == 0) {
-#pragma unroll
-                        for (int h = 0; h < PP; h += 2) {
-                            const float2 w = bridge_comb2(lw, rw, sd, Wprev[h][f], Wprev[h + 1][f], top[h][f],
-                                                          top[h + 1][f], z[h], z[h + 1]);
-                            Wns[h] = w.x;
-                            Wns[h + 1] = w.y;
-                        }
-                    } else {
-#pragma unroll
-                        for (int p = 0; p < PP; ++p) Wns[p] = fmaf(lw, Wprev[p][f], fmaf(rw, top[p][f], sd * z[p]));
-                    }
-#pragma unroll
-                    for (int p = 0; p < PP; ++p) {
-                        const float Wn = Wns[p];
-                        if (push) {
-                            S.stk[base + ci * T + p * TH] = top[p][f];
-                            top[p][f] = Wn;
-                        } else {
-                            Wi[p][f] = Wn;
-                        }
-                    }
-                }
-            }
-            if (push) ++sp;
-        }
-    }
-    if constexpr (PP % 2 == 0) {
-#pragma unroll
-        for (int h = 0; h < PP; h += 2)
-#pragma unroll
-            for (int f = 0; f < FS; ++f) {
-                const float2 d =
-                    __fmul2_rn(sub2(f2(Wi[h][f], Wi[h + 1][f]), f2(Wprev[h][f], Wprev[h + 1][f])), f2s(rec.isd));
-                nz[h][f] = d.x;
-                nz[h + 1][f] = d.y;
-                Wprev[h][f] = Wi[h][f];
-                Wprev[h + 1][f] = Wi[h + 1][f];
-            }
-    } else {
-#pragma unroll
-        for (int p = 0; p < PP; ++p)
-#pragma unroll
-            for (int f = 0; f < FS; ++f) {
-                nz[p][f] = (Wi[p][f] - Wprev[p][f]) * rec.isd;
-                Wprev[p][f] = Wi[p][f];
-            }
-    }
-}
-
-// leverage L(X_{i-1}) and dL/dX (local_volatility_node.cpp:19-47) on the layer the
-// step's record names (c3 = {1/ln_step, grid offset, first value as int bits}): the
-// layer's rows are uniform across the CTA and stay in L1 (staging the current layer in
-// shared memory measured slower)
-__device__ __forceinline__ void leverage(const DevPlan& P, int a, float4 c3, float x, float& L, float& dL)
-{
-    const float2 mp = make_float2(c3.x, c3.y);
-    const float* v = P.lev_values + __float_as_int(c3.z);
-    const int npts = P.lev_points[a];
-    const float f = fmaf(x, mp.x, mp.y);
-    const int last = npts - 1;
-    if (f <= 0.f) {
-        L = __ldg(v);
-        dL = 0.f;
-    } else if (f >= (float)last) {
-        L = __ldg(v + last);
-        dL = 0.f;
-    } else {
-        const int k = (int)f;
-        const float w = f - (float)k;
-        const float v0 = __ldg(v + k), v1 = __ldg(v + k + 1);
-        L = fmaf(w, v1 - v0, v0);
-        dL = (v1 - v0) * mp.x;
-    }
-}
-
-__device__ __forceinline__ float intrinsic(const DevProduct& pr, float s)
-{
-    const float iv = pr.call ? s - pr.K : pr.K - s;
-    return fmaxf(iv, 0.f);
-}
-
-// discounted flow of product pr on tile path k (contract_node.cpp:16-51)
-__device__ __forceinline__ float payoff(const DevPlan& P, const DevProduct& pr, const float* slots, const float* grp,
-                                       int stride, int k)
-{
-    float s;
-    switch (pr.kind) {
-    case P_VARIANCE: {
-        const float sum2 = (pr.g_snap ? slots : grp)[pr.slot_g * stride + k];
-        return pr.notional * ((pr.past + sum2) * pr.inv_T - pr.kvar) * pr.df;
-    }
-    case P_BARRIER: {
-        const float ext = (pr.g_snap ? slots : grp)[pr.slot_g * stride + k];
-        const bool hit = pr.up ? (ext >= pr.level) : (ext <= pr.level);
-        const bool alive = pr.knock_in ? hit : !hit;
-        if (!alive) return 0.f;
-        s = slots[pr.slot_s * stride + k] * pr.qfac;
-        break;
-    }
-    case P_BASKET: {
-        s = 0.f;
-        for (int c = 0; c < pr.comp_n; ++c) {
-            const Comp cp = P.comps[pr.comp_first + c];
-            s = fmaf(slots[cp.slot * stride + k], cp.w, s);
-        }
-        break;
-    }
-    default:
-        s = slots[pr.slot_s * stride + k] * pr.qfac;
-    }
-    return intrinsic(pr, s) * pr.df;
-}
-
-// pathwise delta and vega of product pr on tile path k
-__device__ __forceinline__ void greeks_of(const DevPlan& P, const DevProduct& pr, const float* slots, int stride,
-                                          int k, float& d, float& g)
-{
-    d = 0.f;
-    g = 0.f;
-    const float sgn = pr.call ? 1.f : -1.f;
-    if (pr.kind == P_VANILLA) {
-        const float sT = slots[pr.slot_s * stride + k];
-        const float s = sT * pr.qfac;
-        if (intrinsic(pr, s) > 0.f) {
-            const float y = pr.slot_y >= 0 ? slots[pr.slot_y * stride + k] : 1.f;
-            d = sgn * s * pr.inv_s0 * y * pr.df;
-            if (pr.slot_w >= 0) g = sgn * s * (slots[pr.slot_w * stride + k] - pr.vol_t) * pr.df;
-        }
-    } else if (pr.kind == P_BASKET) {
-        float s = 0.f, ds = 0.f;
-        for (int c = 0; c < pr.comp_n; ++c) {
-            const Comp cp = P.comps[pr.comp_first + c];
-            const float sc = slots[cp.slot * stride + k] * cp.w;
-            s += sc;
-            const float y = cp.slot_y >= 0 ? slots[cp.slot_y * stride + k] : 1.f;
-            ds = fmaf(sc * cp.inv_s0, y, ds);
-        }
-        if (intrinsic(pr, s) > 0.f) d = sgn * ds * pr.df;
-    }
-}
-
-__device__ __forceinline__ StepRec load_rec(const DevPlan& P, int i)
-{
-    const float4* r = reinterpret_cast<const float4*>(P.recs + (i - 1));
-    const float4 a = __ldg(r), b = __ldg(r + 1);
-    StepRec s;
-    s.lw = a.x;
-    s.rw = a.y;
-    s.sd = a.z;
-    s.dim = __float_as_int(a.w);
-    s.isd = b.x;
-    s.count = __float_as_int(b.y);
-    s.first = __float_as_int(b.z);
-    s.ev = __float_as_int(b.w);
-    return s;
-}
-
-// ---------------------------------------------------------------------------
-// The book kernel. Template parameters:
-//   TB      log2 paths per tile (= threads per CTA)
-//   NA      compile-time asset slots (1 = single-asset fast path)
-//   MODEL   M_GBM / M_HESTON / M_LSV for single-model books, M_MIXED for books
-//           with correlated GBM names, M_SEQ for other multi-asset books
-//   UNIFORM every step has the same per-asset constants (kept in registers)
-// ---------------------------------------------------------------------------
-// resident CTAs per SM the registers are bounded for: 768 threads per SM worth for one or two
-// paths a thread, 7 CTAs of 64 threads (146 registers each) for four, 3 for the mixed kernel
-template <int TB, int NA, int PP>
-struct MinBlocks {
-    static constexpr int value = NA != 1 ? 3 : (PP == 4 ? 7 : 768 / ((1 << TB) / PP));
-};
-
-template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-__global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) book_kernel(const DevPlan P)
-{
-    constexpr int T = 1 << TB;  // paths per tile
-    constexpr int TH = T / PP;  // threads per CTA; path p of thread t is tile column t + p * TH
-    constexpr int FS = 2 * NA;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const Smem S = carve(smem_raw, P, T);
-    const int t = threadIdx.x;
-    const int stride = T + 1;
-    __shared__ int s_cancel;
-
-    double* acc = P.acc + (size_t)blockIdx.x * P.n_acc;
-    for (int j = t; j < P.n_acc; j += TH) acc[j] = 0.0;
-
-    // uniform step constants (UNIFORM: step 1's for every step)
-    float4 u0[NA], u1[NA], u2[NA];
-#pragma unroll
-    for (int a = 0; a < NA; ++a) {
-        if (UNIFORM && a < P.n_assets) {
-            const float4* cs = reinterpret_cast<const float4*>(P.steps[a].c);
-            u0[a] = __ldg(cs);
-            u1[a] = __ldg(cs + 1);
-            u2[a] = __ldg(cs + 2);
-        } else {
-            u0[a] = u1[a] = u2[a] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-
-    for (int64_t tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
-        const int64_t m = P.tile_first + tile;
-        uint64_t n[PP];
-        bool valid[PP];
-#pragma unroll
-        for (int p = 0; p < PP; ++p) {
-            n[p] = (uint64_t)m * T + (uint64_t)(t + p * TH);
-            valid[p] = n[p] >= (uint64_t)P.skip + 1 && n[p] <= (uint64_t)(P.skip + P.paths);
-        }
-        __syncthreads(); // previous tile fully evaluated
-        if (t == 0) s_cancel = (P.cancel != nullptr) ? *P.cancel : 0;
-        if (P.use_sobol) tile_high_bits<TB>(P, S.hs, m, 0);
-        __syncthreads();
-        if (s_cancel) {
-            if (t == 0) atomicExch(P.status, 1);
-            return;
-        }
-        SobolLane<T, PP> L = sobol_lane<TB, PP>(P, S.hs, m);
-
-        for (int g = 0; g < P.n_groups; ++g)
-#pragma unroll
-            for (int p = 0; p < PP; ++p) S.grp[g * stride + t + p * TH] = P.grp_init[g];
-        for (int g = 0; g < P.n_last; ++g)
-#pragma unroll
-            for (int p = 0; p < PP; ++p) S.last[g * stride + t + p * TH] = 0.f;
-
-        // events on date index i for asset a of tile column k (after the state at date i is known)
-        auto apply_events = [&](int i, int a, int k, float xa, float step, float wa, float ya) {
-            const int2 r = P.ev_range[i * P.n_assets + a];
-            for (int e = r.x; e < r.x + r.y; ++e) {
-                const Event ev = P.events[e];
-                switch (ev.type) {
-                case EV_SNAP_S: S.slots[ev.a * stride + k] = P.s0[a] * expf(xa); break;
-                case EV_SNAP_W: S.slots[ev.a * stride + k] = wa; break;
-                case EV_SNAP_Y: S.slots[ev.a * stride + k] = ya; break;
-                case EV_GRP_MIN: {
-                    float* g = S.grp + ev.a * stride + k;
-                    *g = fminf(*g, xa - ev.p);
-                    break;
-                }
-                case EV_GRP_MAX: {
-                    float* g = S.grp + ev.a * stride + k;
-                    *g = fmaxf(*g, xa - ev.p);
-                    break;
-                }
-                case EV_GRP_SQ_STEP: {
-                    float* g = S.grp + ev.a * stride + k;
-                    const float d = step - ev.p;
-                    *g = fmaf(d, d, *g);
-                    break;
-                }
-                case EV_SNAP_G: S.slots[ev.a * stride + k] = S.grp[ev.pad * stride + k]; break;
-                default: { // EV_GRP_SQ_OBS
-                    float* g = S.grp + ev.a * stride + k;
-                    float* l = S.last + ev.pad * stride + k; // pad: the group's row of last
-                    const float d = xa - *l - ev.p;
-                    *g = fmaf(d, d, *g);
-                    *l = xa;
-                }
-                }
-            }
-        };
-
-        // one pass per asset for M_SEQ (asset a0), one pass for every asset otherwise
-        constexpr bool SEQ = (MODEL == M_SEQ);
-        const int n_pass = SEQ ? P.n_assets : 1;
-        for (int a0 = 0; a0 < n_pass; ++a0) {
-            // ---- path state -------------------------------------------------
-            float x[PP][NA], comp[PP][NA], v[PP][NA], Wb[PP][NA], y[PP][NA];
-            float Wprev[PP][FS], top[PP][FS], nz[PP][FS];
-#pragma unroll
-            for (int p = 0; p < PP; ++p) {
-#pragma unroll
-                for (int a = 0; a < NA; ++a) {
-                    x[p][a] = 0.f;
-                    comp[p][a] = 0.f;
-                    v[p][a] = P.v0[SEQ ? a0 : a];
-                    Wb[p][a] = 0.f;
-                    y[p][a] = 1.f;
-                }
-#pragma unroll
-                for (int f = 0; f < FS; ++f) {
-                    Wprev[p][f] = 0.f;
-                    top[p][f] = 0.f;
-                    nz[p][f] = 0.f;
-                }
-            }
-            int sp = 0;
-#pragma unroll
-            for (int a = 0; a < NA; ++a) {
-                const int aid = SEQ ? a0 : a;
-                if (aid < P.n_assets)
-#pragma unroll
-                    for (int p = 0; p < PP; ++p) apply_events(0, aid, t + p * TH, 0.f, 0.f, 0.f, 1.f);
-                if (P.path_out && aid == P.path_asset)
-#pragma unroll
-                    for (int p = 0; p < PP; ++p)
-                        if (valid[p]) P.path_out[n[p] - (uint64_t)P.skip - 1] = P.s0[aid];
-            }
-
-            // ---- time loop (step records prefetched one step ahead) ------------
-            StepRec rec = load_rec(P, 1);
-            for (int i = 1; i <= P.n_steps; ++i) {
-                const StepRec cur = rec;
-                if (i < P.n_steps) rec = load_rec(P, i + 1);
-                // one asset a pass: its constants for this step are requested before the bridge
-                // work, which covers their latency
-                constexpr bool HOIST = !UNIFORM && (NA == 1 || MODEL == M_SEQ);
-                float4 h0, h1, h2, h3;
-                if constexpr (HOIST) {
-                    const int ha = MODEL == M_SEQ ? a0 : 0;
-                    const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + ha].c);
-                    h0 = __ldg(cs);
-                    h1 = __ldg(cs + 1);
-                    h2 = __ldg(cs + 2);
-                    h3 = (MODEL == M_LSV || (MODEL == M_SEQ && P.model[ha] == M_LSV)) ? __ldg(cs + 3)
-                                                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-                if (P.use_sobol) {
-                    bridge_step<NA, T, PP, SEQ>(P, S, cur, sp, L, n, Wprev, top, nz, a0);
-                } else {
-#pragma unroll
-                    for (int f = 0; f < FS; ++f) {
-                        const int sa = f < NA ? f : f - NA;
-                        const int aid = SEQ ? a0 : sa;
-                        const int fid = f < NA ? P.fid_spot[aid] : P.fid_var[aid];
-                        if (aid < P.n_assets && fid >= 0)
-#pragma unroll
-                            for (int p = 0; p < PP; ++p)
-                                nz[p][f] = quantile_u32(
-                                    hash_u32(P.seed, n[p], (uint32_t)((i - 1) * P.ref_factors + fid)));
-                    }
-                }
-#pragma unroll
-                for (int a = 0; a < NA; ++a) {
-                    const int aid = SEQ ? a0 : a; // asset id; a is the register slot
-                    if (aid >= P.n_assets) continue;
-                    float4 c0, c1, c2, c3 = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (UNIFORM) {
-                        c0 = u0[a];
-                        c1 = u1[a];
-                        c2 = u2[a];
-                    } else if constexpr (HOIST) {
-                        c0 = h0;
-                        c1 = h1;
-                        c2 = h2;
-                        c3 = h3;
-                    } else {
-                        const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + aid].c);
-                        c0 = __ldg(cs);
-                        c1 = __ldg(cs + 1);
-                        c2 = __ldg(cs + 2);
-                        if (P.model[aid] == M_LSV) c3 = __ldg(cs + 3);
-                    }
-                    const int model = (MODEL == M_MIXED || SEQ) ? P.model[aid] : MODEL;
-                    // an even number of paths a thread: the variance step and the log-spot sum paired
-                    constexpr bool PAIRED = PP % 2 == 0;
-                    float vcs[PP], stp[PP];
-                    if (PAIRED && model != M_GBM) {
-#pragma unroll
-                        for (int h = 0; h < PP; h += 2) {
-                            const float2 r = qe_step2(f2(v[h][a], v[h + 1][a]), f2(nz[h][NA + a], nz[h + 1][NA + a]),
-                                                      c0.x, c0.y, c0.z, c0.w);
-                            vcs[h] = r.x;
-                            vcs[h + 1] = r.y;
-                        }
-                    }
-                    // Heston kernels, paired paths: the log-spot step paired as well
-                    constexpr bool PAIR_SPOT = PAIRED && MODEL == M_HESTON;
-                    if constexpr (PAIR_SPOT) {
-                        if (!P.degenerate[aid]) {
-#pragma unroll
-                            for (int h = 0; h < PP; h += 2) {
-                                const float2 vp2 = f2(v[h][a], v[h + 1][a]), vc2 = f2(vcs[h], vcs[h + 1]);
-                                const float2 s2 = __fadd2_rn(vp2, vc2);
-                                const float2 F =
-                                    __ffma2_rn(f2s(c2.y), sub2(vc2, vp2), __ffma2_rn(f2s(c1.z), s2, f2s(c1.y)));
-                                const float2 qr = sqrt2_approx(__fmul2_rn(f2s(c2.x), s2));
-                                const float2 B = __ffma2_rn(qr, f2(nz[h][a], nz[h + 1][a]), F);
-                                const float2 st = __ffma2_rn(f2s(-c1.w), s2, __fadd2_rn(f2s(c1.x), B));
-                                stp[h] = st.x;
-                                stp[h + 1] = st.y;
-                                v[h][a] = vc2.x;
-                                v[h + 1][a] = vc2.y;
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int p = 0; p < PP; ++p) {
-                        float step;
-                        if (PAIR_SPOT && !P.degenerate[aid]) {
-                            step = stp[p];
-                        } else if (model == M_GBM) {
-                            float e = nz[p][a];
-                            if (MODEL == M_MIXED && P.corr) {
-                                e = 0.f;
-#pragma unroll
-                                for (int u = 0; u < NA; ++u)
-                                    if (u < P.n_assets) e = fmaf(P.chol[a * MAX_ASSETS + u], nz[p][u], e);
-                            }
-                            step = fmaf(c0.y, e, c0.x);
-                            Wb[p][a] = fmaf(c0.z, e, Wb[p][a]);
-                        } else {
-                            const float vp = v[p][a];
-                            const float vc = PAIRED ? vcs[p] : qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
-                            float Lv = 1.f, dL = 0.f;
-                            if (model == M_LSV) leverage(P, aid, c3, x[p][a], Lv, dL);
-                            const float s = vp + vc;
-                            if (!P.degenerate[aid]) {
-                                const float B =
-                                    fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * nz[p][a];
-                                if (model == M_LSV) {
-                                    step = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
-                                    y[p][a] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
-                                } else {
-                                    step = c1.x + B - c1.w * s;
-                                }
-                            } else {
-                                const float sq = fast_sqrt(vp * c2.z) * nz[p][a];
-                                step = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
-                                if (model == M_LSV) y[p][a] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
-                            }
-                            v[p][a] = vc;
-                        }
-                        stp[p] = step;
-                    }
-                    // Kahan-compensated log-spot
-                    if constexpr (PAIRED) {
-#pragma unroll
-                        for (int h = 0; h < PP; h += 2) {
-                            const float2 yy = sub2(f2(stp[h], stp[h + 1]), f2(comp[h][a], comp[h + 1][a]));
-                            const float2 xx = f2(x[h][a], x[h + 1][a]);
-                            const float2 tt = __fadd2_rn(xx, yy);
-                            const float2 cp = sub2(sub2(tt, xx), yy);
-                            comp[h][a] = cp.x;
-                            comp[h + 1][a] = cp.y;
-                            x[h][a] = tt.x;
-                            x[h + 1][a] = tt.y;
-                        }
-                    } else {
-#pragma unroll
-                        for (int p = 0; p < PP; ++p) {
-                            const float yy = stp[p] - comp[p][a];
-                            const float tt = x[p][a] + yy;
-                            comp[p][a] = (tt - x[p][a]) - yy;
-                            x[p][a] = tt;
-                        }
-                    }
-#pragma unroll
-                    for (int p = 0; p < PP; ++p) {
-                        const float step = stp[p];
-                        if (cur.ev) apply_events(i, aid, t + p * TH, x[p][a], step, Wb[p][a], y[p][a]);
-                        // stored paths: date-major, consecutive paths on consecutive threads
-                        if (P.path_out && aid == P.path_asset && valid[p])
-                            P.path_out[(size_t)i * P.path_ld + (n[p] - (uint64_t)P.skip - 1)] = P.s0[aid] * expf(x[p][a]);
-                    }
-                }
-            }
-        }
-        __syncthreads(); // every path of the tile observed
-
-        // ---- product evaluation: thread per product, FP32 tile partials ----
-        // The tile's valid paths are the contiguous columns [k0, k0 + nv). Every sum of the tile
-        // is shifted by the value at column k0 (payoff, pathwise delta, pathwise vega of the
-        // product): the FP32 partials hold f - c and (f - c)^2, and the shift is added back in
-        // FP64. So the sum of squares keeps its precision where the payoff's variance is small
-        // next to its square (deep in-the-money cells), and the trust with it.
-        const int k0 = (int)max((int64_t)0, P.skip + 1 - m * T);
-        const int kend = (int)min((int64_t)T, P.skip + P.paths - m * T + 1);
-        const int nv = kend - k0;
-        const int C = P.n_products;
-        for (int pc = 0; pc < C; pc += TH) {
-            const int CP = min(C - pc, TH);
-            const int G = TH / CP;
-            const int pl = t % CP, g = t / CP;
-            float a6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (g < G) {
-                if (P.vanilla_only) {
-                    // lean vanilla loop: f = max(a S + b, 0), no dispatch
-                    const VanTerm vt = P.vterms[pc + pl];
-                    const float* col = S.slots + vt.slot * stride;
-                    const float c0 = fmaxf(fmaf(vt.a, col[k0], vt.b), 0.f);
-                    float s1 = 0.f, s2 = 0.f;
-#pragma unroll 4
-                    for (int k = k0 + g; k < kend; k += G) {
-                        const float f = fmaxf(fmaf(vt.a, col[k], vt.b), 0.f) - c0;
-                        s1 += f;
-                        s2 = fmaf(f, f, s2);
-                    }
-                    a6[0] = s1;
-                    a6[1] = s2;
-                } else {
-                    const DevProduct pr = P.products[pc + pl];
-                    const float c0 = payoff(P, pr, S.slots, S.grp, stride, k0);
-                    float cd = 0.f, cg = 0.f;
-                    if (P.greeks) greeks_of(P, pr, S.slots, stride, k0, cd, cg);
-                    for (int k = k0 + g; k < kend; k += G) {
-                        const float f = payoff(P, pr, S.slots, S.grp, stride, k) - c0;
-                        a6[0] += f;
-                        a6[1] = fmaf(f, f, a6[1]);
-                        if (P.greeks) {
-                            float d, gg;
-                            greeks_of(P, pr, S.slots, stride, k, d, gg);
-                            d -= cd;
-                            gg -= cg;
-                            a6[2] += d;
-                            a6[3] = fmaf(d, d, a6[3]);
-                            a6[4] += gg;
-                            a6[5] = fmaf(gg, gg, a6[5]);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < 6; ++j) S.part[(g * CP + pl) * 6 + j] = a6[j];
-            }
-            __syncthreads();
-            if (t < CP) {
-                float cf = 0.f, cd = 0.f, cg = 0.f;
-                if (P.vanilla_only) {
-                    const VanTerm vt = P.vterms[pc + t];
-                    cf = fmaxf(fmaf(vt.a, S.slots[vt.slot * stride + k0], vt.b), 0.f);
-                } else {
-                    const DevProduct pr = P.products[pc + t];
-                    cf = payoff(P, pr, S.slots, S.grp, stride, k0);
-                    if (P.greeks) greeks_of(P, pr, S.slots, stride, k0, cd, cg);
-                }
-                const float c3[3] = {cf, cd, cg};
-                double s6[6] = {0, 0, 0, 0, 0, 0};
-                for (int g2 = 0; g2 < G; ++g2)
-#pragma unroll
-                    for (int j = 0; j < 6; ++j) s6[j] += (double)S.part[(g2 * CP + t) * 6 + j];
-                // sum f = sum (f - c) + n c;  sum f^2 = sum (f - c)^2 + 2 c sum (f - c) + n c^2
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    const double c = c3[q], d1 = s6[2 * q];
-                    s6[2 * q + 1] += 2.0 * c * d1 + (double)nv * c * c;
-                    s6[2 * q] = d1 + (double)nv * c;
-                }
-#pragma unroll
-                for (int j = 0; j < 6; ++j) acc[(size_t)(pc + t) * 6 + j] += s6[j];
-            }
-            __syncthreads();
-        }
-        // ---- book value per path (book_node.cpp:16-31) ---------------------
-        double b1 = 0.0, b2 = 0.0;
-        float bv[PP];
-#pragma unroll
-        for (int p = 0; p < PP; ++p) bv[p] = 0.f;
-        if (P.vanilla_only) {
-            // the thread's paths share each product's terms
-            for (int q = 0; q < C; ++q) {
-                const VanTerm vt = P.vterms[q];
-                const float* col = S.slots + vt.slot * stride + t;
-#pragma unroll
-                for (int p = 0; p < PP; ++p) bv[p] = fmaf(vt.w, fmaxf(fmaf(vt.a, col[p * TH], vt.b), 0.f), bv[p]);
-            }
-        } else {
-#pragma unroll
-            for (int p = 0; p < PP; ++p)
-                for (int q = 0; q < C; ++q) {
-                    const DevProduct pr = P.products[q];
-                    bv[p] = fmaf(payoff(P, pr, S.slots, S.grp, stride, t + p * TH), pr.fx, bv[p]);
-                }
-        }
-#pragma unroll
-        for (int p = 0; p < PP; ++p) {
-            const float b = valid[p] ? bv[p] : 0.f;
-            b1 += b;
-            b2 += (double)b * b;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            b1 += __shfl_xor_sync(0xffffffffu, b1, o);
-            b2 += __shfl_xor_sync(0xffffffffu, b2, o);
-        }
-        if ((t & 31) == 0) {
-            S.red[2 * (t >> 5)] = b1;
-            S.red[2 * (t >> 5) + 1] = b2;
-        }
-        __syncthreads();
-        if (t == 0) {
-            double s1 = 0, s2 = 0;
-            for (int w = 0; w < TH / 32; ++w) {
-                s1 += S.red[2 * w];
-                s2 += S.red[2 * w + 1];
-            }
-            acc[(size_t)C * 6] += s1;
-            acc[(size_t)C * 6 + 1] += s2;
-        }
-    }
-}
 
 // fixed-order FP64 reduction of the per-CTA rows
 // (32 columns per CTA; row group g of REDUCE_GROUPS sums rows g, g + GROUPS, ...
@@ -1020,80 +154,9 @@ cudaError_t launch_mufu_peak(float* out, int blocks, int iters, cudaStream_t st)
     return cudaGetLastError();
 }
 
-// ---- launch wrappers --------------------------------------------------------
-// Launch shapes. Single-asset variants come in five: (log2 paths per tile,
-// paths per thread) = (8, 2), (8, 1), (7, 1), (7, 2), (8, 4), i.e. 128, 256, 128, 64
-// and 64 threads per CTA, the first four bounded to 768 resident threads per SM
-// worth of registers, the last to 7 CTAs of 64 threads; the autotuner picks one per
-// book size. The mixed variant has one: (7, 1).
-constexpr int N_SHAPES = 5;
-constexpr int SHAPE_TB[N_SHAPES] = {8, 8, 7, 7, 8};
-constexpr int SHAPE_PP[N_SHAPES] = {2, 1, 1, 2, 4};
-
 int book_shape_count(int variant) { return variant == 3 ? 1 : N_SHAPES; }
 int book_shape_tile_bits(int variant, int shape) { return variant == 3 ? 7 : SHAPE_TB[shape]; }
 int book_shape_threads(int variant, int shape) { return variant == 3 ? 128 : (1 << SHAPE_TB[shape]) / SHAPE_PP[shape]; }
-
-template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-static cudaError_t smem_attr_t()
-{
-    // once per variant: allow the device's opt-in maximum, so that launches of
-    // any size (and graph nodes captured earlier) stay valid whatever runs next
-    static bool done = false;
-    if (done) return cudaSuccess;
-    int dev = 0, mx = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncAttributes fa;
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, book_kernel<TB, NA, MODEL, UNIFORM, PP>);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(book_kernel<TB, NA, MODEL, UNIFORM, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 mx - (int)fa.sharedSizeBytes);
-    done = e == cudaSuccess;
-    return e;
-}
-
-template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-static cudaError_t launch_book_t(const DevPlan& P, int grid, size_t smem, cudaStream_t st)
-{
-    cudaError_t e = smem_attr_t<TB, NA, MODEL, UNIFORM, PP>();
-    if (e != cudaSuccess) return e;
-    book_kernel<TB, NA, MODEL, UNIFORM, PP><<<grid, (1 << TB) / PP, smem, st>>>(P);
-    return cudaGetLastError();
-}
-
-template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-static int occ_t(size_t smem)
-{
-    auto k = book_kernel<TB, NA, MODEL, UNIFORM, PP>;
-    if (smem_attr_t<TB, NA, MODEL, UNIFORM, PP>() != cudaSuccess) return 1;
-    int n = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, (1 << TB) / PP, smem) != cudaSuccess) return 1;
-    return n < 1 ? 1 : n;
-}
-
-// one single-asset model in each of the four shapes: launch (grid > 0) or occupancy (grid == 0)
-template <int MODEL, bool UNIFORM>
-static int single_t(const DevPlan* P, int shape, int grid, size_t smem, cudaStream_t st, cudaError_t* err)
-{
-    switch (shape) {
-    case 0:
-        if (grid) *err = launch_book_t<8, 1, MODEL, UNIFORM, 2>(*P, grid, smem, st);
-        return grid ? 0 : occ_t<8, 1, MODEL, UNIFORM, 2>(smem);
-    case 1:
-        if (grid) *err = launch_book_t<8, 1, MODEL, UNIFORM, 1>(*P, grid, smem, st);
-        return grid ? 0 : occ_t<8, 1, MODEL, UNIFORM, 1>(smem);
-    case 2:
-        if (grid) *err = launch_book_t<7, 1, MODEL, UNIFORM, 1>(*P, grid, smem, st);
-        return grid ? 0 : occ_t<7, 1, MODEL, UNIFORM, 1>(smem);
-    case 3:
-        if (grid) *err = launch_book_t<7, 1, MODEL, UNIFORM, 2>(*P, grid, smem, st);
-        return grid ? 0 : occ_t<7, 1, MODEL, UNIFORM, 2>(smem);
-    default:
-        if (grid) *err = launch_book_t<8, 1, MODEL, UNIFORM, 4>(*P, grid, smem, st);
-        return grid ? 0 : occ_t<8, 1, MODEL, UNIFORM, 4>(smem);
-    }
-}
 
 static int dispatch(const DevPlan* P, int variant, int shape, int grid, size_t smem, cudaStream_t st, cudaError_t* err)
 {
@@ -1103,15 +166,13 @@ static int dispatch(const DevPlan* P, int variant, int shape, int grid, size_t s
         return 1;
     }
     switch (variant) {
-    case 0: return single_t<M_GBM, false>(P, shape, grid, smem, st, err);
-    case 1: return single_t<M_HESTON, false>(P, shape, grid, smem, st, err);
-    case 2: return single_t<M_LSV, false>(P, shape, grid, smem, st, err);
-    case 3:
-        if (grid) *err = launch_book_t<7, MAX_ASSETS, M_MIXED, false, 1>(*P, grid, smem, st);
-        return grid ? 0 : occ_t<7, MAX_ASSETS, M_MIXED, false, 1>(smem);
-    case 4: return single_t<M_HESTON, true>(P, shape, grid, smem, st, err);
-    case 5: return single_t<M_GBM, true>(P, shape, grid, smem, st, err);
-    case 6: return single_t<M_SEQ, false>(P, shape, grid, smem, st, err);
+    case 0: return book_dispatch_gbm(P, false, shape, grid, smem, st, err);
+    case 1: return book_dispatch_heston(P, false, shape, grid, smem, st, err);
+    case 2: return book_dispatch_lsv(P, shape, grid, smem, st, err);
+    case 3: return book_dispatch_multi(P, 3, shape, grid, smem, st, err);
+    case 4: return book_dispatch_heston(P, true, shape, grid, smem, st, err);
+    case 5: return book_dispatch_gbm(P, true, shape, grid, smem, st, err);
+    case 6: return book_dispatch_multi(P, 6, shape, grid, smem, st, err);
     default: *err = cudaErrorInvalidValue; return 1;
     }
 }
@@ -1135,9 +196,10 @@ int book_occupancy(int variant, int shape, size_t smem)
     return e == cudaSuccess ? n : 1;
 }
 
-size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups, int n_last)
+size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups, int n_last,
+                       int few_m)
 {
-    return smem_bytes(T, sobol_dims, stack_depth, nfa, n_slots, n_groups, n_last);
+    return smem_bytes(T, sobol_dims, stack_depth, nfa, n_slots, n_groups, n_last, few_m);
 }
 
 cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st)

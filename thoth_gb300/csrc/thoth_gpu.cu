@@ -30,7 +30,8 @@ int book_shape_count(int variant);
 int book_shape_tile_bits(int variant, int shape);
 int book_shape_threads(int variant, int shape);
 int book_occupancy(int variant, int shape, size_t smem);
-size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups, int n_last);
+size_t book_smem_bytes(int T, int sobol_dims, int stack_depth, int nfa, int n_slots, int n_groups, int n_last,
+                       int few_m = 0);
 cudaError_t launch_reduce(const double* acc, int rows, int n_acc, double* out, cudaStream_t st);
 cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64_t n_points, uint32_t* out,
                                 cudaStream_t st);
@@ -962,7 +963,14 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     const int64_t lo = d->sobol_skip + 1, hi = d->sobol_skip + d->paths;
     D.tile_first = lo / T;
     D.n_tiles = hi / T - lo / T + 1;
-    P.smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, D.stack_factors, D.n_slots_used, D.n_groups, D.n_last);
+    // few-product accumulation (kernels.cu, FEW_PRODUCTS): books of at most 4 products whose
+    // per-thread moment sums fit in 16 KB of shared memory
+    {
+        const int few_m = 2 * (1 + (D.greeks ? 3 : 1) * d->n_products);
+        D.few_m = (d->n_products <= 4 && (size_t)few_m * T * sizeof(float) <= 16384) ? few_m : 0;
+    }
+    P.smem = book_smem_bytes(T, D.sobol_dims, D.stack_depth, D.stack_factors, D.n_slots_used, D.n_groups, D.n_last,
+                             D.few_m);
     if (P.smem > 227 * 1024) return fail(THOTH_GPU_E_TOO_LARGE, "book needs more shared memory than one SM has");
     D.n_acc = 6 * d->n_products + 2;
     P.n_products = d->n_products;
@@ -2919,6 +2927,7 @@ int thoth_gpu_plan_summary(const ThothBookDesc* book, int64_t* out)
         out[7] = P.dp.n_tiles;
         out[8] = P.shape;
         out[9] = book_shape_threads(P.variant, P.shape);
+        out[10] = P.dp.few_m;
         return THOTH_GPU_OK;
     } catch (const std::bad_alloc&) {
         return fail(THOTH_GPU_E_NOMEM, "out of host memory");
