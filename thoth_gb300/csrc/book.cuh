@@ -539,6 +539,189 @@ __device__ __forceinline__ StepRec load_rec(const DevPlan& P, int i)
 }
 
 // ---------------------------------------------------------------------------
+// One asset's pass over a tile for two paths a thread (tile columns t and t + T/2), held as
+// packed pairs: the paths' state is float2 throughout, the bridge stack holds one float2 per
+// thread and row (one 8-byte shared access per stack entry for both paths), and every FP32
+// operation on the paths issues as one FFMA2 / FMUL2 / FADD2. The operations and their order
+// are those of the generic loop in book_kernel, lane by lane.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 comb2(float lw, float rw, float sd, float2 wp, float2 tp, float2 z)
+{
+    return __ffma2_rn(f2s(lw), wp, __ffma2_rn(f2s(rw), tp, __fmul2_rn(f2s(sd), z)));
+}
+
+template <int T>
+__device__ __forceinline__ float2 pair_gauss(const DevPlan& P, SobolLane<T, 2>& L, const uint64_t (&n)[2], int dim)
+{
+    float z[2];
+    gauss<T, 2>(P, L, n, dim, z);
+    return f2(z[0], z[1]);
+}
+
+template <int TB, int MODEL, bool UNIFORM, class Ev>
+__device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, SobolLane<1 << TB, 2>& L,
+                                          const uint64_t (&n)[2], const bool (&valid)[2], int a0, float4 u0,
+                                          float4 u1, float4 u2, Ev& apply_events)
+{
+    constexpr int T = 1 << TB, TH = T / 2;
+    constexpr bool SEQ = MODEL == M_SEQ;
+    const int t = threadIdx.x;
+    const int aid = SEQ ? a0 : 0;
+    const int model = SEQ ? P.model[aid] : MODEL;
+    // the spot factor, and the variance factor where the model has one: compact stack row and
+    // reference factor index (the dimension of a node is its bridge step * F + that index)
+    const bool act1 = MODEL != M_GBM && P.cidx_var[aid] >= 0;
+    const int ci0 = SEQ ? 0 : P.cidx_spot[0], ci1 = SEQ ? 1 : P.cidx_var[0];
+    const int fid0 = P.fid_spot[aid], fid1 = P.fid_var[aid];
+    const int nfa = P.stack_factors;
+    float2* stk = reinterpret_cast<float2*>(S.stk);
+    const bool degenerate = P.degenerate[aid] != 0;
+
+    float2 X = f2s(0.f), CP = f2s(0.f), V = f2s(P.v0[aid]), WB = f2s(0.f), Y = f2s(1.f);
+    float2 Wp0 = f2s(0.f), Wp1 = f2s(0.f), T0 = f2s(0.f), T1 = f2s(0.f);
+    int sp = 0;
+    apply_events(0, aid, t, 0.f, 0.f, 0.f, 1.f);
+    apply_events(0, aid, t + TH, 0.f, 0.f, 0.f, 1.f);
+    const bool store = P.path_out && aid == P.path_asset;
+    if (store)
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+            if (valid[p]) P.path_out[n[p] - (uint64_t)P.skip - 1] = P.s0[aid];
+
+    StepRec rec = load_rec(P, 1);
+    for (int i = 1; i <= P.n_steps; ++i) {
+        const StepRec cur = rec;
+        if (i < P.n_steps) rec = load_rec(P, i + 1);
+        // this step's constants, requested before the bridge work that covers their latency
+        float4 c0 = u0, c1 = u1, c2 = u2, c3 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!UNIFORM) {
+            const float4* cs = reinterpret_cast<const float4*>(P.steps[(i - 1) * P.n_assets + aid].c);
+            c0 = __ldg(cs);
+            c1 = __ldg(cs + 1);
+            c2 = __ldg(cs + 2);
+            if (MODEL == M_LSV || (SEQ && model == M_LSV)) c3 = __ldg(cs + 3);
+        }
+        // ---- Brownian bridge: normalised increments nz0 (spot), nz1 (variance) ----
+        float2 nz0, nz1 = f2s(0.f);
+        if (P.use_sobol) {
+            float2 Wi0 = f2s(0.f), Wi1 = f2s(0.f);
+            if (cur.count == 0) {
+                const int base = (sp - 1) * nfa;
+                Wi0 = T0;
+                T0 = stk[(base + ci0) * TH + t];
+                if (act1) {
+                    Wi1 = T1;
+                    T1 = stk[(base + ci1) * TH + t];
+                }
+                --sp;
+            } else if (cur.count == 1) {
+                Wi0 = comb2(cur.lw, cur.rw, cur.sd, Wp0, T0, pair_gauss(P, L, n, cur.dim + fid0));
+                if (act1) Wi1 = comb2(cur.lw, cur.rw, cur.sd, Wp1, T1, pair_gauss(P, L, n, cur.dim + fid1));
+            } else {
+                float lw = cur.lw, rw = cur.rw, sd = cur.sd;
+                int dim = cur.dim;
+                BridgeNode nd = P.nodes[cur.first]; // node 1 of the chain, loaded one node ahead
+                for (int k = 0; k < cur.count; ++k) {
+                    if (k > 0) {
+                        lw = nd.lw;
+                        rw = nd.rw;
+                        sd = nd.sd;
+                        dim = nd.bstep * P.ref_factors;
+                        if (k + 1 < cur.count) nd = P.nodes[cur.first + k];
+                    }
+                    const float2 w0 = comb2(lw, rw, sd, Wp0, T0, pair_gauss(P, L, n, dim + fid0));
+                    float2 w1 = f2s(0.f);
+                    if (act1) w1 = comb2(lw, rw, sd, Wp1, T1, pair_gauss(P, L, n, dim + fid1));
+                    if (k + 1 < cur.count) {
+                        const int base = sp * nfa;
+                        stk[(base + ci0) * TH + t] = T0;
+                        T0 = w0;
+                        if (act1) {
+                            stk[(base + ci1) * TH + t] = T1;
+                            T1 = w1;
+                        }
+                        ++sp;
+                    } else {
+                        Wi0 = w0;
+                        Wi1 = w1;
+                    }
+                }
+            }
+            nz0 = __fmul2_rn(sub2(Wi0, Wp0), f2s(cur.isd));
+            Wp0 = Wi0;
+            if (act1) {
+                nz1 = __fmul2_rn(sub2(Wi1, Wp1), f2s(cur.isd));
+                Wp1 = Wi1;
+            }
+        } else {
+            const uint32_t d0 = (uint32_t)((i - 1) * P.ref_factors + fid0);
+            nz0 = f2(quantile_u32(hash_u32(P.seed, n[0], d0)), quantile_u32(hash_u32(P.seed, n[1], d0)));
+            if (act1) {
+                const uint32_t d1 = (uint32_t)((i - 1) * P.ref_factors + fid1);
+                nz1 = f2(quantile_u32(hash_u32(P.seed, n[0], d1)), quantile_u32(hash_u32(P.seed, n[1], d1)));
+            }
+        }
+        // ---- the model's step of the log-spot (relative to S0) ----------------------
+        float2 step;
+        if (MODEL == M_GBM || (SEQ && model == M_GBM)) {
+            step = __ffma2_rn(f2s(c0.y), nz0, f2s(c0.x));
+            WB = __ffma2_rn(f2s(c0.z), nz0, WB);
+        } else {
+            const float2 vc = qe_step2(V, nz1, c0.x, c0.y, c0.z, c0.w);
+            if ((MODEL == M_HESTON || (SEQ && model == M_HESTON)) && !degenerate) {
+                const float2 s2 = __fadd2_rn(V, vc);
+                const float2 F = __ffma2_rn(f2s(c2.y), sub2(vc, V), __ffma2_rn(f2s(c1.z), s2, f2s(c1.y)));
+                const float2 qr = sqrt2_approx(__fmul2_rn(f2s(c2.x), s2));
+                const float2 B = __ffma2_rn(qr, nz0, F);
+                step = __ffma2_rn(f2s(-c1.w), s2, __fadd2_rn(f2s(c1.x), B));
+            } else {
+                float sl[2];
+                const float vpl[2] = {V.x, V.y}, vcl[2] = {vc.x, vc.y}, xl[2] = {X.x, X.y}, zl[2] = {nz0.x, nz0.y};
+                float yl[2] = {Y.x, Y.y};
+#pragma unroll
+                for (int p = 0; p < 2; ++p) {
+                    const float vp = vpl[p], vcp = vcl[p];
+                    float Lv = 1.f, dL = 0.f;
+                    if (model == M_LSV) leverage(P, aid, c3, xl[p], Lv, dL);
+                    const float s = vp + vcp;
+                    if (!degenerate) {
+                        const float B = fmaf(c2.y, vcp - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * zl[p];
+                        if (model == M_LSV) {
+                            sl[p] = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
+                            yl[p] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
+                        } else {
+                            sl[p] = c1.x + B - c1.w * s;
+                        }
+                    } else {
+                        const float sq = fast_sqrt(vp * c2.z) * zl[p];
+                        sl[p] = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
+                        if (model == M_LSV) yl[p] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
+                    }
+                }
+                step = f2(sl[0], sl[1]);
+                Y = f2(yl[0], yl[1]);
+            }
+            V = vc;
+        }
+        // ---- Kahan-compensated log-spot ------------------------------------------
+        {
+            const float2 yy = sub2(step, CP);
+            const float2 tt = __fadd2_rn(X, yy);
+            CP = sub2(sub2(tt, X), yy);
+            X = tt;
+        }
+        if (cur.ev) {
+            apply_events(i, aid, t, X.x, step.x, WB.x, Y.x);
+            apply_events(i, aid, t + TH, X.y, step.y, WB.y, Y.y);
+        }
+        if (store) {
+            if (valid[0]) P.path_out[(size_t)i * P.path_ld + (n[0] - (uint64_t)P.skip - 1)] = P.s0[aid] * expf(X.x);
+            if (valid[1]) P.path_out[(size_t)i * P.path_ld + (n[1] - (uint64_t)P.skip - 1)] = P.s0[aid] * expf(X.y);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // The book kernel. Template parameters:
 //   TB      log2 paths per tile (= threads per CTA)
 //   NA      compile-time asset slots (1 = single-asset fast path)
@@ -656,6 +839,10 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
         constexpr bool SEQ = (MODEL == M_SEQ);
         const int n_pass = SEQ ? P.n_assets : 1;
         for (int a0 = 0; a0 < n_pass; ++a0) {
+            if constexpr (NA == 1 && PP == 2) {
+                pair_pass<TB, MODEL, UNIFORM>(P, S, L, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
+                continue;
+            }
             // ---- path state -------------------------------------------------
             float x[PP][NA], comp[PP][NA], v[PP][NA], Wb[PP][NA], y[PP][NA];
             float Wprev[PP][FS], top[PP][FS], nz[PP][FS];
