@@ -550,16 +550,64 @@ __device__ __forceinline__ float2 comb2(float lw, float rw, float sd, float2 wp,
     return __ffma2_rn(f2s(lw), wp, __ffma2_rn(f2s(rw), tp, __fmul2_rn(f2s(sd), z)));
 }
 
+// The Sobol lane of a thread with two paths: a running pointer into the tile parts in shared
+// memory (refilled HS_CHUNK entries at a time, uniformly across the CTA as in gauss) and a
+// running pointer into the book's low words, whose table carries two rows of padding so that
+// the load two entries ahead needs no bounds test.
+struct PairLane {
+    const uint2* hs;      // tile part of the next entry
+    const uint2* hs_end;  // end of the chunk in shared memory
+    const uint32_t* lo;   // low word of the entry two ahead (this thread's column)
+    uint32_t cur, nxt;    // low words of the next two entries
+    int jc;               // first entry of the chunk in shared memory
+    int64_t m;            // tile index
+};
+
 template <int T>
-__device__ __forceinline__ float2 pair_gauss(const DevPlan& P, SobolLane<T, 2>& L, const uint64_t (&n)[2], int dim)
+__device__ __forceinline__ PairLane pair_lane(const DevPlan& P, const uint2* hs, int64_t m)
 {
-    float z[2];
-    gauss<T, 2>(P, L, n, dim, z);
-    return f2(z[0], z[1]);
+    PairLane L;
+    L.hs = hs;
+    L.hs_end = hs + HS_CHUNK;
+    L.lo = P.sobol_lo + 2 * T + threadIdx.x;
+    L.cur = __ldg(P.sobol_lo + threadIdx.x);
+    L.nxt = __ldg(P.sobol_lo + T + threadIdx.x);
+    L.jc = 0;
+    L.m = m;
+    return L;
+}
+
+template <int TB>
+__device__ __forceinline__ float2 pair_gauss(const DevPlan& P, uint2* hs_base, PairLane& L, const uint64_t (&n)[2],
+                                             int dim)
+{
+    constexpr int T = 1 << TB;
+    uint32_t x0, x1;
+    if (dim < P.sobol_dims) {
+        if (L.hs == L.hs_end) { // next chunk of tile parts (uniform across the CTA)
+            L.jc += HS_CHUNK;
+            __syncthreads();
+            tile_high_bits<TB>(P, hs_base, L.m, L.jc);
+            __syncthreads();
+            L.hs = hs_base;
+        }
+        const uint2 h = *L.hs++;
+        x0 = h.x ^ L.cur; // columns t and t + T/2 share the low word through the tile-part pair
+        x1 = h.y ^ L.cur;
+        L.cur = L.nxt;
+        L.nxt = __ldg(L.lo);
+        L.lo += T;
+    } else {
+        x0 = hash_u32(P.seed, n[0], (uint32_t)dim);
+        x1 = hash_u32(P.seed, n[1], (uint32_t)dim);
+    }
+    float z0, z1;
+    quantile_pair(x0, x1, z0, z1);
+    return f2(z0, z1);
 }
 
 template <int TB, int MODEL, bool UNIFORM, class Ev>
-__device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, SobolLane<1 << TB, 2>& L,
+__device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairLane& L,
                                           const uint64_t (&n)[2], const bool (&valid)[2], int a0, float4 u0,
                                           float4 u1, float4 u2, Ev& apply_events)
 {
@@ -615,8 +663,8 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, Sobol
                 }
                 --sp;
             } else if (cur.count == 1) {
-                Wi0 = comb2(cur.lw, cur.rw, cur.sd, Wp0, T0, pair_gauss(P, L, n, cur.dim + fid0));
-                if (act1) Wi1 = comb2(cur.lw, cur.rw, cur.sd, Wp1, T1, pair_gauss(P, L, n, cur.dim + fid1));
+                Wi0 = comb2(cur.lw, cur.rw, cur.sd, Wp0, T0, pair_gauss<TB>(P, S.hs, L, n, cur.dim + fid0));
+                if (act1) Wi1 = comb2(cur.lw, cur.rw, cur.sd, Wp1, T1, pair_gauss<TB>(P, S.hs, L, n, cur.dim + fid1));
             } else {
                 float lw = cur.lw, rw = cur.rw, sd = cur.sd;
                 int dim = cur.dim;
@@ -629,9 +677,9 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, Sobol
                         dim = nd.bstep * P.ref_factors;
                         if (k + 1 < cur.count) nd = P.nodes[cur.first + k];
                     }
-                    const float2 w0 = comb2(lw, rw, sd, Wp0, T0, pair_gauss(P, L, n, dim + fid0));
+                    const float2 w0 = comb2(lw, rw, sd, Wp0, T0, pair_gauss<TB>(P, S.hs, L, n, dim + fid0));
                     float2 w1 = f2s(0.f);
-                    if (act1) w1 = comb2(lw, rw, sd, Wp1, T1, pair_gauss(P, L, n, dim + fid1));
+                    if (act1) w1 = comb2(lw, rw, sd, Wp1, T1, pair_gauss<TB>(P, S.hs, L, n, dim + fid1));
                     if (k + 1 < cur.count) {
                         const int base = sp * nfa;
                         stk[(base + ci0) * TH + t] = T0;
@@ -838,9 +886,10 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
         // one pass per asset for M_SEQ (asset a0), one pass for every asset otherwise
         constexpr bool SEQ = (MODEL == M_SEQ);
         const int n_pass = SEQ ? P.n_assets : 1;
+        PairLane PL = pair_lane<T>(P, S.hs, m); // unused (and dropped) unless NA == 1 and PP == 2
         for (int a0 = 0; a0 < n_pass; ++a0) {
             if constexpr (NA == 1 && PP == 2) {
-                pair_pass<TB, MODEL, UNIFORM>(P, S, L, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
+                pair_pass<TB, MODEL, UNIFORM>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
                 continue;
             }
             // ---- path state -------------------------------------------------

@@ -193,15 +193,15 @@ struct DevPlan {
 // formed from the integer (q = min(x, 2^32 - x), 2u - 1 = (x - 2^31) 2^-31),
 // so the tails keep their relative accuracy.
 // ---------------------------------------------------------------------------
-// the pieces of quantile_u32: s = 2u - 1 and lg = log2(4 q (1 - q)) <= 0
+// the pieces of quantile_u32: s = 2u - 1 and lg = log2(4 q (1 - q)) <= 0, with
+// 4 q (1 - q) = qf (2^-30 - qf 2^-62) for qf = q 2^32
 __device__ __forceinline__ void quantile_prep(uint32_t x, float& s, float& lg)
 {
     const uint32_t qi = min(x, 0u - x);                                     // q * 2^32 in [1, 2^31]
     s = __int2float_rn((int)(x ^ 0x80000000u)) * 4.656612873077393e-10f;    // 2u - 1
     const float qf = __uint2float_rn(qi);
-    const float one_m_q = fmaf(qf, -2.3283064365386963e-10f, 1.0f);         // 1 - q
-    // at q = 1/2 the MUFU result is clamped (fminf drops a NaN operand)
-    lg = fminf(__log2f(qf * 9.313225746154785e-10f * one_m_q), 0.0f);
+    // the MUFU result at q = 1/2 (argument 1) is clamped: fminf drops a NaN operand
+    lg = fminf(__log2f(qf * fmaf(qf, -2.168404344971009e-19f, 9.313225746154785e-10f)), 0.0f);
 }
 
 constexpr float QUANTILE_TAIL_LG = -9.016844005556021f; // w = -ln2 lg = 6.25
@@ -300,11 +300,10 @@ __device__ __forceinline__ void quantile_pair(uint32_t x0, uint32_t x1, float& z
     const float2 sv = __fmul2_rn(f2(__int2float_rn((int)(x0 ^ 0x80000000u)), __int2float_rn((int)(x1 ^ 0x80000000u))),
                                  f2s(4.656612873077393e-10f));
     const float2 qf = f2(__uint2float_rn(q0), __uint2float_rn(q1));
-    const float2 one_m_q = __ffma2_rn(qf, f2s(-2.3283064365386963e-10f), f2s(1.0f));
-    const float2 arg = __fmul2_rn(__fmul2_rn(qf, f2s(9.313225746154785e-10f)), one_m_q);
+    const float2 arg = __fmul2_rn(qf, __ffma2_rn(qf, f2s(-2.168404344971009e-19f), f2s(9.313225746154785e-10f)));
     const float lg0 = fminf(__log2f(arg.x), 0.0f), lg1 = fminf(__log2f(arg.y), 0.0f);
     float2 zz = quantile_central2(f2(lg0, lg1));
-    if (!(lg0 > QUANTILE_TAIL_LG) || !(lg1 > QUANTILE_TAIL_LG)) {
+    if (!(fminf(lg0, lg1) > QUANTILE_TAIL_LG)) {
         if (!(lg0 > QUANTILE_TAIL_LG)) zz.x = quantile_tail(lg0);
         if (!(lg1 > QUANTILE_TAIL_LG)) zz.y = quantile_tail(lg1);
     }
@@ -382,37 +381,61 @@ __device__ __forceinline__ float log2f_approx(float x)
 // Phi(-z) = erfc(z / sqrt 2) / 2 with the Chebyshev-fitted erfc of Press et al.
 // (Numerical Recipes in C, 2nd ed., section 6.2, "erfcc"; fractional error
 // below 1.2e-7 everywhere), so the exponential QE branch keeps its accuracy in
-// the upper tail without a library call.
+// the upper tail without a library call. That fit is erfc(a) = t exp(-a^2 + P(t)),
+// t = 1 / (1 + a / 2), a = |z| / sqrt 2; here it is taken in base 2 with the factor 1/2
+// folded into the exponent: h = erfc(a) / 2 = t 2^(Q(t) - z^2 log2(e) / 2), where
+// Q = log2(e) P - 1 (phi_q: Press's coefficients times log2 e, the constant term less 1).
+constexpr float HALF_LOG2E = 0.7213475108146667f;
+
+__device__ __forceinline__ float phi_q(float t)
+{
+    float p = 0.24651730060577393f;
+    p = fmaf(p, t, -1.1861149072647095f);
+    p = fmaf(p, t, 2.147474527359009f);
+    p = fmaf(p, t, -1.6377531290054321f);
+    p = fmaf(p, t, 0.40232157707214355f);
+    p = fmaf(p, t, -0.2687568664550781f);
+    p = fmaf(p, t, 0.1396300494670868f);
+    p = fmaf(p, t, 0.5397006273269653f);
+    p = fmaf(p, t, 1.4427292346954346f);
+    p = fmaf(p, t, -2.8257482051849365f);
+    return p;
+}
+
+__device__ __forceinline__ float2 phi_q2(float2 t)
+{
+    float2 p = f2s(0.24651730060577393f);
+    p = __ffma2_rn(p, t, f2s(-1.1861149072647095f));
+    p = __ffma2_rn(p, t, f2s(2.147474527359009f));
+    p = __ffma2_rn(p, t, f2s(-1.6377531290054321f));
+    p = __ffma2_rn(p, t, f2s(0.40232157707214355f));
+    p = __ffma2_rn(p, t, f2s(-0.2687568664550781f));
+    p = __ffma2_rn(p, t, f2s(0.1396300494670868f));
+    p = __ffma2_rn(p, t, f2s(0.5397006273269653f));
+    p = __ffma2_rn(p, t, f2s(1.4427292346954346f));
+    p = __ffma2_rn(p, t, f2s(-2.8257482051849365f));
+    return p;
+}
+
 __device__ __forceinline__ float phi_neg(float z)
 {
-    const float y = z * 0.7071067811865476f;
-    const float ny = z * -0.7071067811865476f;
-    const float a = fabsf(y);
-    const float t = rcp_approx(fmaf(0.5f, a, 1.0f));
-    float p = 0.17087277f;
-    p = fmaf(p, t, -0.82215223f);
-    p = fmaf(p, t, 1.48851587f);
-    p = fmaf(p, t, -1.13520398f);
-    p = fmaf(p, t, 0.27886807f);
-    p = fmaf(p, t, -0.18628806f);
-    p = fmaf(p, t, 0.09678418f);
-    p = fmaf(p, t, 0.37409196f);
-    p = fmaf(p, t, 1.00002368f);
-    p = fmaf(p, t, -1.26551223f);
-    // h = erfc(|y|) / 2; Phi(-z) = h for y >= 0 (sign bit clear), 1 - h otherwise, as
-    // sg h + off with sg = +-1, off = 0 or 1 (at y = -0, h = 1/2 and both forms give 1/2)
-    const float h = 0.5f * (t * exp2f_approx(fmaf(y, ny, p) * LOG2E));
-    const float sg = copysignf(1.0f, y);
+    const float t = rcp_approx(fmaf(0.3535533845424652f, fabsf(z), 1.0f));
+    const float p = phi_q(t);
+    const float h = t * exp2f_approx(fmaf(z * z, -HALF_LOG2E, p));
+    // Phi(-z) = h for z >= 0 (sign bit clear), 1 - h otherwise, as sg h + off with sg = +-1,
+    // off = 0 or 1 (at z = -0, h = 1/2 and both forms give 1/2)
+    const float sg = copysignf(1.0f, z);
     return fmaf(sg, h, fmaf(sg, -0.5f, 0.5f));
 }
 
 // Andersen QE variance step in FP32 (heston_variance_node.cpp:17-57).
 // c = {e, theta (1 - e), A, B}: m = theta + (v - theta) e, s2 = A v + B.
 // psi = s2 / m^2 <= 1.5 is tested as s2 <= 1.5 m^2; the exponential branch
-// uses 1 - u = Phi(-z) and 1 - p = 2 m^2 / (s2 + m^2). Both branches are
-// evaluated and one is selected: the paths of a warp nearly always take both,
-// so this costs no more issue slots than divergence and schedules as one block.
-// The guards on the quadratic branch only act when it is not selected.
+// uses 1 - u = Phi(-z) and 1 - p = 2 m^2 / (s2 + m^2), and 1/beta = (s2 + m^2) / (2 m).
+// Both branches are evaluated and one is selected: the paths of a warp nearly always take
+// both, so this costs no more issue slots than divergence and schedules as one block. The
+// quadratic branch's square roots need no guard: where c (c - 1) or b^2 is negative (c < 1,
+// psi > 2) the branch is not selected, and its NaN is dropped by the selection.
 __device__ __forceinline__ float qe_step(float v, float z, float e, float th1e, float A, float B)
 {
     const float m = fmaf(v, e, th1e);
@@ -423,15 +446,15 @@ __device__ __forceinline__ float qe_step(float v, float z, float e, float th1e, 
     // below single precision) so that c (c - 1) stays finite for a vanishing vol of vol
     const float c = fminf(tm2 * rcp_approx(s2), 1e18f);
     const float cm1 = c - 1.0f;
-    const float b2 = cm1 + fast_sqrt(fmaxf(c * cm1, 0.0f));
+    const float b2 = cm1 + fast_sqrt(c * cm1);
     const float a = m * rcp_approx(1.0f + b2);
-    const float bz = fast_sqrt(fmaxf(b2, 0.0f)) + z;
+    const float bz = fast_sqrt(b2) + z;
     const float vq = (a * bz) * bz;
     // exponential branch
     const float num = s2 + m2;
     const float one_m_p = tm2 * rcp_approx(num);
     const float uc = phi_neg(z);
-    const float r = (num * rcp_approx(2.0f * m)) * (log2f_approx(one_m_p * rcp_approx(uc)) * LN2);
+    const float r = (num * rcp_approx(m)) * (log2f_approx(one_m_p * rcp_approx(uc)) * (0.5f * LN2));
     const float ve = (uc >= one_m_p) ? 0.0f : r;
     return (s2 <= 1.5f * m2) ? vq : ve;
 }
@@ -439,23 +462,11 @@ __device__ __forceinline__ float qe_step(float v, float z, float e, float th1e, 
 // phi_neg for a thread's two paths (same expressions, paired)
 __device__ __forceinline__ float2 phi_neg2(float2 z)
 {
-    const float2 y = __fmul2_rn(z, f2s(0.7071067811865476f));
-    const float2 ny = __fmul2_rn(z, f2s(-0.7071067811865476f));
-    const float2 a = f2(fabsf(y.x), fabsf(y.y));
-    const float2 t = rcp2_approx(__ffma2_rn(f2s(0.5f), a, f2s(1.0f)));
-    float2 p = f2s(0.17087277f);
-    p = __ffma2_rn(p, t, f2s(-0.82215223f));
-    p = __ffma2_rn(p, t, f2s(1.48851587f));
-    p = __ffma2_rn(p, t, f2s(-1.13520398f));
-    p = __ffma2_rn(p, t, f2s(0.27886807f));
-    p = __ffma2_rn(p, t, f2s(-0.18628806f));
-    p = __ffma2_rn(p, t, f2s(0.09678418f));
-    p = __ffma2_rn(p, t, f2s(0.37409196f));
-    p = __ffma2_rn(p, t, f2s(1.00002368f));
-    p = __ffma2_rn(p, t, f2s(-1.26551223f));
-    const float2 g = __fmul2_rn(__ffma2_rn(y, ny, p), f2s(LOG2E));
-    const float2 h = __fmul2_rn(f2s(0.5f), __fmul2_rn(t, f2(exp2f_approx(g.x), exp2f_approx(g.y))));
-    const float2 sg = f2(copysignf(1.0f, y.x), copysignf(1.0f, y.y));
+    const float2 t = rcp2_approx(__ffma2_rn(f2s(0.3535533845424652f), f2(fabsf(z.x), fabsf(z.y)), f2s(1.0f)));
+    const float2 p = phi_q2(t);
+    const float2 g = __ffma2_rn(__fmul2_rn(z, z), f2s(-HALF_LOG2E), p);
+    const float2 h = __fmul2_rn(t, f2(exp2f_approx(g.x), exp2f_approx(g.y)));
+    const float2 sg = f2(copysignf(1.0f, z.x), copysignf(1.0f, z.y));
     return __ffma2_rn(sg, h, __ffma2_rn(sg, f2s(-0.5f), f2s(0.5f)));
 }
 
@@ -469,17 +480,16 @@ __device__ __forceinline__ float2 qe_step2(float2 v, float2 z, float e, float th
     const float2 cr = __fmul2_rn(tm2, rcp2_approx(s2));
     const float2 c = f2(fminf(cr.x, 1e18f), fminf(cr.y, 1e18f));
     const float2 cm1 = __fadd2_rn(c, f2s(-1.0f));
-    const float2 cc = __fmul2_rn(c, cm1);
-    const float2 b2 = __fadd2_rn(cm1, sqrt2_approx(f2(fmaxf(cc.x, 0.0f), fmaxf(cc.y, 0.0f))));
+    const float2 b2 = __fadd2_rn(cm1, sqrt2_approx(__fmul2_rn(c, cm1)));
     const float2 a = __fmul2_rn(m, rcp2_approx(__fadd2_rn(f2s(1.0f), b2)));
-    const float2 bz = __fadd2_rn(sqrt2_approx(f2(fmaxf(b2.x, 0.0f), fmaxf(b2.y, 0.0f))), z);
+    const float2 bz = __fadd2_rn(sqrt2_approx(b2), z);
     const float2 vq = __fmul2_rn(__fmul2_rn(a, bz), bz);
     const float2 num = __fadd2_rn(s2, m2);
     const float2 one_m_p = __fmul2_rn(tm2, rcp2_approx(num));
     const float2 uc = phi_neg2(z);
     const float2 q = __fmul2_rn(one_m_p, rcp2_approx(uc));
-    const float2 r = __fmul2_rn(__fmul2_rn(num, rcp2_approx(__fmul2_rn(f2s(2.0f), m))),
-                                __fmul2_rn(f2(log2f_approx(q.x), log2f_approx(q.y)), f2s(LN2)));
+    const float2 r = __fmul2_rn(__fmul2_rn(num, rcp2_approx(m)),
+                                __fmul2_rn(f2(log2f_approx(q.x), log2f_approx(q.y)), f2s(0.5f * LN2)));
     const float2 ve = f2(uc.x >= one_m_p.x ? 0.0f : r.x, uc.y >= one_m_p.y ? 0.0f : r.y);
     const float2 lim = __fmul2_rn(f2s(1.5f), m2);
     return f2(s2.x <= lim.x ? vq.x : ve.x, s2.y <= lim.y ? vq.y : ve.y);

@@ -1073,7 +1073,9 @@ double trust_of(double s1, double s2, double n)
 }
 
 // bytes of a book's low Sobol words in consumption order ([n_sobol][T])
-size_t low_bytes(const Plan& P) { return sizeof(uint32_t) * (size_t)P.dp.n_sobol * P.T; }
+// the book's low words in consumption order, and two rows of padding that the kernel's
+// load two entries ahead may read past the last entry
+size_t low_bytes(const Plan& P) { return sizeof(uint32_t) * ((size_t)P.dp.n_sobol + 2) * P.T; }
 
 // the book's low words from the device-wide table (one small gather kernel)
 cudaError_t gather_low(const Plan& P, cudaStream_t st)
