@@ -618,11 +618,14 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
     const int model = SEQ ? P.model[aid] : MODEL;
     // the spot factor, and the variance factor where the model has one: compact stack row and
     // reference factor index (the dimension of a node is its bridge step * F + that index)
-    const bool act1 = MODEL != M_GBM && P.cidx_var[aid] >= 0;
-    const int ci0 = SEQ ? 0 : P.cidx_spot[0], ci1 = SEQ ? 1 : P.cidx_var[0];
-    const int fid0 = P.fid_spot[aid], fid1 = P.fid_var[aid];
-    const int nfa = P.stack_factors;
-    float2* stk = reinterpret_cast<float2*>(S.stk);
+    // A single-asset book's spot factor is reference factor 0 and stack row 0; a Heston or LSV
+    // asset adds its variance factor as factor 1 and row 1. A pass of a multi-asset book uses
+    // rows 0 and 1 of a two-row stack and the asset's own factors.
+    const bool act1 = MODEL == M_GBM ? false : (SEQ ? model != M_GBM : true);
+    constexpr int ci0 = 0, ci1 = 1;
+    const int fid0 = SEQ ? P.fid_spot[aid] : 0, fid1 = SEQ ? P.fid_var[aid] : 1;
+    constexpr int nfa = MODEL == M_GBM ? 1 : 2;
+    float2* const stk = reinterpret_cast<float2*>(S.stk) + t; // this thread's column of the stack
     const bool degenerate = P.degenerate[aid] != 0;
 
     float2 X = f2s(0.f), CP = f2s(0.f), V = f2s(P.v0[aid]), WB = f2s(0.f), Y = f2s(1.f);
@@ -656,10 +659,10 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
             if (cur.count == 0) {
                 const int base = (sp - 1) * nfa;
                 Wi0 = T0;
-                T0 = stk[(base + ci0) * TH + t];
+                T0 = stk[(base + ci0) * TH];
                 if (act1) {
                     Wi1 = T1;
-                    T1 = stk[(base + ci1) * TH + t];
+                    T1 = stk[(base + ci1) * TH];
                 }
                 --sp;
             } else if (cur.count == 1) {
@@ -682,10 +685,10 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
                     if (act1) w1 = comb2(lw, rw, sd, Wp1, T1, pair_gauss<TB>(P, S.hs, L, n, dim + fid1));
                     if (k + 1 < cur.count) {
                         const int base = sp * nfa;
-                        stk[(base + ci0) * TH + t] = T0;
+                        stk[(base + ci0) * TH] = T0;
                         T0 = w0;
                         if (act1) {
-                            stk[(base + ci1) * TH + t] = T1;
+                            stk[(base + ci1) * TH] = T1;
                             T1 = w1;
                         }
                         ++sp;
