@@ -502,6 +502,22 @@ int thoth_gpu_surrogate_set_params(ThothSurrogate* s, const float* params);
  * learning-rate decay over all steps; batch a multiple of 128. */
 int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
                               int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss);
+/* As thoth_gpu_surrogate_train, with tail averaging of the weights: the cosine decay runs
+ * from lr to lr_avg over the first epochs - avg_epochs epochs, lr_avg then holds, and the
+ * weights at the end of each of the last avg_epochs epochs are averaged on the device; the
+ * model keeps that average (one network, whose fit averages out more of the label noise
+ * than the last iterate does). avg_epochs = 0 is thoth_gpu_surrogate_train. */
+int thoth_gpu_surrogate_train_avg(ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
+                                  int32_t epochs, int32_t batch, double lr, uint64_t seed, int32_t avg_epochs,
+                                  double lr_avg, double* final_loss);
+/* An ensemble's k members (1 <= k <= 64, distinct handles on one device) trained side by
+ * side on the same set: member j as by thoth_gpu_surrogate_train_avg with data-order seed
+ * seed + j (its initialisation is its own creation seed); each member replays its own step
+ * on its own stream, so their kernels share the device. final_loss (may be null) holds k
+ * values. */
+int thoth_gpu_surrogate_train_members(ThothSurrogate* const* members, int32_t k, const float* x, const float* y,
+                                      const float* scale, int64_t n, int32_t epochs, int32_t batch, double lr,
+                                      uint64_t seed, int32_t avg_epochs, double lr_avg, double* final_loss);
 /* Gradient of that loss over `rows` rows (multiple of 128) at the current
  * parameters, without updating them; for checks against a CPU oracle. */
 int thoth_gpu_surrogate_gradient(ThothSurrogate* s, const float* x, const float* y, const float* scale, int32_t rows,
@@ -520,6 +536,14 @@ int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, fl
 int thoth_gpu_surrogate_price_lattice(ThothSurrogate* s, const double* params, int32_t n_sets, const double* lms,
                                       int32_t n_lm, const double* Ts, int32_t n_T, const double* box_lo,
                                       const double* box_hi, double floor, float* prices, double* device_ms);
+/* As thoth_gpu_surrogate_price_lattice for an ensemble of k networks (1 <= k <= 64, all on
+ * one device): the features are built once, every member is evaluated on them, and their
+ * normalised outputs are added on the device in member order; the mean is scaled to prices.
+ * Member 0's buffers and stream serve the call. */
+int thoth_gpu_surrogate_price_lattice_mean(ThothSurrogate* const* members, int32_t k, const double* params,
+                                           int32_t n_sets, const double* lms, int32_t n_lm, const double* Ts,
+                                           int32_t n_T, const double* box_lo, const double* box_hi, double floor,
+                                           float* prices, double* device_ms);
 const char* thoth_gpu_surrogate_last_error(void);
 
 /* Cooperative cancellation (reference: helpers/cancellation.hpp:9-15): a

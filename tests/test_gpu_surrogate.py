@@ -52,6 +52,58 @@ def test_inference_matches_cpu_oracle(gpu):
     m.close()
 
 
+def test_weight_averaged_training(gpu):
+    """Training with tail averaging of the weights: the model keeps the average, its bf16
+    operand copies follow (predictions equal the oracle's network on the returned FP32
+    weights), the loss falls, and no averaging is the plain training call bit for bit."""
+    x, y, sc = _batch(11, n=4096)
+    xo = x.astype(np.float64)
+    plain, avg0 = S.Surrogate(seed=9), S.Surrogate(seed=9)
+    la = plain.train(x, y, sc, epochs=6, batch=1024, lr=2e-3, seed=5)
+    lb = avg0.train(x, y, sc, epochs=6, batch=1024, lr=2e-3, seed=5, avg_epochs=0)
+    assert la == lb and np.array_equal(plain.params(), avg0.params())
+    m = S.Surrogate(seed=9)
+    _, l0 = m.gradient(x[:1024], y[:1024], sc[:1024])
+    m.train(x, y, sc, epochs=6, batch=1024, lr=2e-3, seed=5, avg_epochs=3, lr_avg=5e-4)
+    p = m.params().astype(np.float64)
+    assert not np.array_equal(p, plain.params().astype(np.float64))
+    W1 = p[MO.OFF_W1:MO.OFF_B1].reshape(MO.H, MO.KIN)
+    assert np.array_equal(W1[:, :7], W1[:, 7:14])          # the tied hi / lo input columns
+    got, _ = m.predict(x)
+    want, _, _ = MO.forward(p, xo)
+    assert np.abs(got - want).max() <= 1e-3 * max(1.0, np.abs(want).max())
+    _, l1 = m.gradient(x[:1024], y[:1024], sc[:1024])
+    assert l1 < 0.9 * l0                                   # random targets: the fit is partial
+    with pytest.raises(gpu.ThothGpuError):
+        m.train(x, y, sc, epochs=4, batch=1024, lr=2e-3, avg_epochs=4, lr_avg=1e-4)
+    with pytest.raises(gpu.ThothGpuError):
+        m.train(x, y, sc, epochs=4, batch=1024, lr=2e-3, avg_epochs=2, lr_avg=0.0)
+    for s_ in (plain, avg0, m):
+        s_.close()
+
+
+def test_ensemble_trains_members_side_by_side_and_serves_their_mean(gpu):
+    """An ensemble's members trained side by side on their own streams end with exactly the
+    weights each gets trained alone (same initialisation, data-order seed seed + j); the
+    ensemble's lattice prices are the mean of the members' own lattice prices."""
+    x, y, sc = _batch(12, n=4096)
+    ens = S.Ensemble(members=3, seed=20)
+    losses = ens.train(x, y, sc, epochs=3, batch=1024, lr=2e-3, seed=7)
+    assert len(losses) == 3 and all(np.isfinite(losses))
+    for j, m in enumerate(ens.members):
+        alone = S.Surrogate(seed=20 + j)
+        alone.train(x, y, sc, epochs=3, batch=1024, lr=2e-3, seed=7 + j)
+        assert np.array_equal(alone.params(), m.params()), j
+        alone.close()
+    rng = np.random.default_rng(3)
+    sets = rng.uniform(S.BOX_LO[2:], S.BOX_HI[2:], size=(11, 5))
+    got, ms = ens.price_lattice(sets)
+    each = np.stack([m.price_lattice(sets)[0] for m in ens.members]).astype(np.float64)
+    assert ms > 0 and got.shape == each.shape[1:]
+    assert np.abs(got - each.mean(axis=0)).max() <= 1e-6 * max(1.0, np.abs(each).max())
+    ens.close()
+
+
 def test_lattice_serving_matches_host_features(gpu):
     """Features, clipping, normalisation and price scale built on the device give the prices
     of the host path (predict_prices on the clipped lattice features), and the oracle's

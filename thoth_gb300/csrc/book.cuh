@@ -642,7 +642,7 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
     StepRec rec = load_rec(P, 1);
     for (int i = 1; i <= P.n_steps; ++i) {
         const StepRec cur = rec;
-        if (i < P.n_steps) rec = load_rec(P, i + 1);
+        rec = load_rec(P, i + 1); // the record past the last step is padding
         // this step's constants, requested before the bridge work that covers their latency
         float4 c0 = u0, c1 = u1, c2 = u2, c3 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (!UNIFORM) {
@@ -932,7 +932,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
             StepRec rec = load_rec(P, 1);
             for (int i = 1; i <= P.n_steps; ++i) {
                 const StepRec cur = rec;
-                if (i < P.n_steps) rec = load_rec(P, i + 1);
+                rec = load_rec(P, i + 1); // the record past the last step is padding
                 // one asset a pass: its constants for this step are requested before the bridge
                 // work, which covers their latency
                 constexpr bool HOIST = !UNIFORM && (NA == 1 || MODEL == M_SEQ);

@@ -153,7 +153,7 @@ struct DevPlan {
     const AssetStep* steps;      // [n_steps][n_assets]   (index i-1 for step i)
     const float* inv_sqrt_dt;    // [n_steps] path-generator 1/sqrt(t_i - t_{i-1})
     const StepProg* prog;        // [n_steps]
-    const StepRec* recs;         // [n_steps]
+    const StepRec* recs;         // [n_steps + 1] (the last is padding for the load one step ahead)
     int uniform_steps;           // 1: every step's AssetStep equals step 1's
     const BridgeNode* nodes;     // time-ordered program
     const int2* ev_range;        // [(n_steps + 1)][n_assets] (first, count) into events; row 0 = date 0

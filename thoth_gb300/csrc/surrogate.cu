@@ -209,6 +209,8 @@ struct TrainSched {
     double lr0;                // peak learning rate
     float lr_t, bc1, bc2;      // this step's learning rate and bias corrections
     int rows;                  // batch rows
+    long long decay_steps;     // steps of the cosine decay (after them the rate stays at lr_lo)
+    double lr_lo;              // the rate the decay ends at
 };
 
 struct TrainArgs {
@@ -366,14 +368,15 @@ __global__ void __launch_bounds__(128) bwd_layer_kernel(TrainArgs A)
     if (warp == 0) tc::tmem_dealloc(c.tm, 256);
 }
 
-// the cosine learning-rate schedule and Adam's bias corrections of step `count` of a training
-// call, computed where the graph of one step can read them (its kernels' arguments stay
-// the same from step to step)
+// the learning-rate schedule (a cosine decay from lr0 to lr_lo over decay_steps steps, then
+// lr_lo) and Adam's bias corrections of step `count` of a training call, computed where the
+// graph of one step can read them (its kernels' arguments stay the same from step to step)
 __host__ __device__ inline void sched_set(TrainSched& s)
 {
     const double pi = 3.14159265358979323846;
     const double step = (double)(s.step0 + s.count + 1);
-    s.lr_t = (float)(s.lr0 * 0.5 * (1.0 + cos(pi * (double)s.count / (double)s.total)) + 1e-6);
+    const double c = (double)(s.count < s.decay_steps ? s.count : s.decay_steps);
+    s.lr_t = (float)(s.lr_lo + (s.lr0 - s.lr_lo) * 0.5 * (1.0 + cos(pi * c / (double)s.decay_steps)) + 1e-6);
     s.bc1 = (float)(1.0 - pow(0.9, step));
     s.bc2 = (float)(1.0 - pow(0.999, step));
 }
@@ -413,6 +416,33 @@ __global__ void adam_kernel(float* params, float* m, float* v, const float* part
     const float p = params[j] - lr * (mj / bc1) / (sqrtf(vj / bc2) + eps);
     params[j] = p;
     // bf16 copies of W1..W4
+    if (j < OFF_B1) {
+        params[j + 7] = p;
+        wbf[OFF_BF_W1 + j] = __float2bfloat16(p);
+        wbf[OFF_BF_W1 + j + 7] = __float2bfloat16(p);
+    } else if (j >= OFF_W2 && j < OFF_W5) {
+        const int l = (j - OFF_W2) / LAYER, o = (j - OFF_W2) % LAYER;
+        if (o < H * H) wbf[OFF_BF_W2 + l * H * H + o] = __float2bfloat16(p);
+    }
+}
+
+// tail averaging of the weights: avg = params (k == 0), else avg += (params - avg) / (k + 1)
+__global__ void weight_avg_kernel(const float* __restrict__ params, float* __restrict__ avg, int k)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N_PARAMS) return;
+    avg[j] = k == 0 ? params[j] : fmaf(params[j] - avg[j], 1.0f / (float)(k + 1), avg[j]);
+}
+
+// the model takes the averaged weights, and its bf16 operand copies follow (as in adam_kernel)
+__global__ void weight_avg_finish_kernel(float* __restrict__ params, const float* __restrict__ avg,
+                                         __nv_bfloat16* __restrict__ wbf)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N_PARAMS) return;
+    if (j < OFF_B1 && j % KIN >= 7) return; // the tied hi/lo columns are written by their partner
+    const float p = avg[j];
+    params[j] = p;
     if (j < OFF_B1) {
         params[j + 7] = p;
         wbf[OFF_BF_W1 + j] = __float2bfloat16(p);
@@ -623,6 +653,34 @@ cudaError_t mlp_train_step(const mlp::TrainArgs& A, float* params, float* m, flo
 }
 
 void mlp_sched_init(mlp::TrainSched& s) { mlp::sched_set(s); }
+
+// sum = y (j == 0) or sum + y; at the last member (j == k - 1) the sum becomes the mean
+__global__ void mean_add_kernel(float* __restrict__ sum, const float* __restrict__ y, int64_t n, int j, int k)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a = j == 0 ? y[i] : sum[i] + y[i];
+    if (j == k - 1) a *= 1.0f / (float)k;
+    sum[i] = a;
+}
+
+cudaError_t mlp_mean_add(float* sum, const float* y, int64_t n, int j, int k, cudaStream_t st)
+{
+    mean_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(sum, y, n, j, k);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_weight_avg(const float* params, float* avg, int k, cudaStream_t st)
+{
+    mlp::weight_avg_kernel<<<(mlp::N_PARAMS + 255) / 256, 256, 0, st>>>(params, avg, k);
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_weight_avg_finish(float* params, const float* avg, __nv_bfloat16* wbf, cudaStream_t st)
+{
+    mlp::weight_avg_finish_kernel<<<(mlp::N_PARAMS + 255) / 256, 256, 0, st>>>(params, avg, wbf);
+    return cudaGetLastError();
+}
 
 cudaError_t mlp_sched_advance(mlp::TrainSched* s, cudaStream_t st)
 {

@@ -37,6 +37,8 @@ struct TrainSched {
     double lr0;
     float lr_t, bc1, bc2;
     int rows;
+    long long decay_steps;
+    double lr_lo;
 };
 } // namespace mlp
 cudaError_t mlp_train_step(const mlp::TrainArgs& A, float* params, float* m, float* v, __nv_bfloat16* wbf, float lr,
@@ -45,6 +47,9 @@ cudaError_t mlp_train_step(const mlp::TrainArgs& A, float* params, float* m, flo
 cudaError_t mlp_train_prepare();
 void mlp_sched_init(mlp::TrainSched& s);
 cudaError_t mlp_sched_advance(mlp::TrainSched* s, cudaStream_t st);
+cudaError_t mlp_weight_avg(const float* params, float* avg, int k, cudaStream_t st);
+cudaError_t mlp_mean_add(float* sum, const float* y, int64_t n, int j, int k, cudaStream_t st);
+cudaError_t mlp_weight_avg_finish(float* params, const float* avg, __nv_bfloat16* wbf, cudaStream_t st);
 cudaError_t mlp_infer(const __nv_bfloat16* x, int n, const float* params, const __nv_bfloat16* wbf, float* y,
                       int* status, int grid, cudaStream_t st);
 cudaError_t mlp_gather_batch(const __nv_bfloat16* X, const float* Y, const float* W, const int* perm, int64_t first,
@@ -117,6 +122,8 @@ struct ThothSurrogate {
     unsigned char* lb = nullptr;
     // the training schedule the captured step reads (learning rate, bias corrections, batch)
     mlp::TrainSched* sched = nullptr;
+    // the running average of the weights over a training call's last epochs
+    float* avg = nullptr;
     // device copy of a training set and its per-epoch permutation (grown on demand)
     int64_t cap_ds = 0;
     unsigned char* ds = nullptr;
@@ -231,6 +238,139 @@ int check_status(ThothSurrogate* s)
     return THOTH_GPU_OK;
 }
 
+
+// one network's training call in three phases, so that several networks can train side by side
+struct TrainRun {
+    ThothSurrogate* s = nullptr;
+    int64_t n = 0, steps_per_epoch = 0, total = 0;
+    int epochs = 0, avg_epochs = 0;
+    int* dP = nullptr;              // the device permutation of the current epoch
+    std::vector<int> idx;           // the host permutation
+    std::mt19937_64 rng;
+    cudaGraphExec_t exec = nullptr; // one captured step: gather, forward, backward, Adam, loss, schedule
+    TrainRun() = default;
+    TrainRun(const TrainRun&) = delete;
+    TrainRun& operator=(const TrainRun&) = delete;
+    ~TrainRun()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+// the training set up once on the member's device memory (bf16 hi/lo inputs, targets, loss
+// weights), the schedule of this call, and the captured step
+int train_setup(TrainRun& R, ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
+                int epochs, int batch, double lr, uint64_t seed, int avg_epochs, double lr_avg)
+{
+    R.s = s;
+    R.n = n;
+    R.epochs = epochs;
+    R.avg_epochs = avg_epochs;
+    const int B = (int)std::min<int64_t>(batch, n / 128 * 128);
+    int rc = ensure_train(s, B);
+    if (rc) return rc;
+    if (avg_epochs > 0 && !s->avg) STRY(cudaMalloc(&s->avg, sizeof(float) * s->np));
+    // each epoch uploads one permutation and every step gathers its rows on the device
+    if (n > s->cap_ds) {
+        if (s->ds) cudaFree(s->ds);
+        if (s->perm_host) cudaFreeHost(s->perm_host);
+        s->ds = nullptr;
+        s->perm_host = nullptr;
+        s->cap_ds = 0;
+        STRY(cudaMalloc(&s->ds, (size_t)n * (KIN * 2 + 4 + 4 + 4) + 1024));
+        STRY(cudaHostAlloc(&s->perm_host, sizeof(int) * (size_t)n, cudaHostAllocDefault));
+        if (!s->perm_copied) STRY(cudaEventCreateWithFlags(&s->perm_copied, cudaEventDisableTiming));
+        s->cap_ds = n;
+    }
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    __nv_bfloat16* dX = reinterpret_cast<__nv_bfloat16*>(s->ds);
+    float* dY = reinterpret_cast<float*>(s->ds + up((size_t)n * KIN * 2));
+    float* dW = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(dY) + up((size_t)n * 4));
+    R.dP = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(dW) + up((size_t)n * 4));
+    {
+        std::vector<__nv_bfloat16> hx;
+        std::vector<float> hy, hw;
+        pack(x, y, scale, nullptr, 0, (int)n, hx, hy, hw);
+        STRY(cudaMemcpy(dX, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice));
+        STRY(cudaMemcpy(dY, hy.data(), hy.size() * 4, cudaMemcpyHostToDevice));
+        STRY(cudaMemcpy(dW, hw.data(), hw.size() * 4, cudaMemcpyHostToDevice));
+    }
+    R.idx.resize(n);
+    for (int64_t i = 0; i < n; i++) R.idx[i] = (int)i;
+    R.rng.seed(seed);
+    R.steps_per_epoch = n / B;
+    R.total = R.steps_per_epoch * epochs;
+    mlp::TrainArgs& A = s->A;
+    A.a[0] = const_cast<__nv_bfloat16*>(A.x);
+    A.rows = B;
+    // the schedule of this call on the device: the captured step reads its batch offset,
+    // learning rate and bias corrections there and advances it
+    if (!s->sched) STRY(cudaMalloc(&s->sched, sizeof(mlp::TrainSched)));
+    mlp::TrainSched sc{};
+    sc.count = 0;
+    sc.total = R.total;
+    sc.steps_per_epoch = R.steps_per_epoch;
+    sc.step0 = s->step;
+    sc.lr0 = lr;
+    sc.rows = B;
+    // without averaging the decay runs over every step down to zero; with it, over the steps
+    // before the averaged epochs, down to lr_avg, which then holds
+    sc.decay_steps = avg_epochs > 0 ? R.steps_per_epoch * (int64_t)(epochs - avg_epochs) : R.total;
+    sc.lr_lo = avg_epochs > 0 ? lr_avg : 0.0;
+    if (sc.decay_steps < 1) sc.decay_steps = 1;
+    mlp_sched_init(sc);
+    STRY(cudaMemcpyAsync(s->sched, &sc, sizeof sc, cudaMemcpyHostToDevice, s->st));
+    STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
+    STRY(mlp_train_prepare());
+    // one step (gather, forward, backward, Adam, loss, schedule) captured once, replayed
+    // for every step: its launches' arguments do not change from step to step
+    cudaGraph_t graph = nullptr;
+    STRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = mlp_gather_batch(dX, dY, dW, R.dP, 0, B, const_cast<__nv_bfloat16*>(A.x),
+                                      const_cast<float*>(A.y), const_cast<float*>(A.inv_w2), s->st, s->sched);
+    if (ce == cudaSuccess)
+        ce = mlp_train_step(A, s->params, s->m, s->v, s->wbf, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f, s->loss, s->st,
+                            s->sched);
+    if (ce == cudaSuccess) ce = mlp_sched_advance(s->sched, s->st);
+    const cudaError_t ee = cudaStreamEndCapture(s->st, &graph);
+    if (ce == cudaSuccess) ce = ee;
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&R.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return sfail(THOTH_GPU_E_CUDA, std::string("training step graph: ") + cudaGetErrorString(ce));
+    STRY(cudaEventRecord(s->perm_copied, s->st));
+    return THOTH_GPU_OK;
+}
+
+// epoch e: the next permutation is drawn on the host while the device runs the previous
+// epoch; at the averaged epochs the weights at the epoch's end join the running average
+int train_epoch(TrainRun& R, int e)
+{
+    ThothSurrogate* s = R.s;
+    std::shuffle(R.idx.begin(), R.idx.end(), R.rng);
+    STRY(cudaEventSynchronize(s->perm_copied)); // the previous permutation has left the pinned buffer
+    std::memcpy(s->perm_host, R.idx.data(), sizeof(int) * (size_t)R.n);
+    STRY(cudaMemcpyAsync(R.dP, s->perm_host, sizeof(int) * (size_t)R.n, cudaMemcpyHostToDevice, s->st));
+    STRY(cudaEventRecord(s->perm_copied, s->st));
+    for (int64_t b = 0; b < R.steps_per_epoch; b++) STRY(cudaGraphLaunch(R.exec, s->st));
+    if (R.avg_epochs > 0 && e >= R.epochs - R.avg_epochs)
+        STRY(mlp_weight_avg(s->params, s->avg, e - (R.epochs - R.avg_epochs), s->st));
+    return THOTH_GPU_OK;
+}
+
+int train_finish(TrainRun& R, double* final_loss)
+{
+    ThothSurrogate* s = R.s;
+    if (R.avg_epochs > 0) STRY(mlp_weight_avg_finish(s->params, s->avg, s->wbf, s->st));
+    s->step += R.total;
+    float l = 0;
+    STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
+    STRY(cudaStreamSynchronize(s->st));
+    const int rc = check_status(s);
+    if (rc) return rc;
+    if (final_loss) *final_loss = l / s->A.rows;
+    return THOTH_GPU_OK;
+}
+
 } // namespace
 
 extern "C" {
@@ -309,6 +449,7 @@ int thoth_gpu_surrogate_destroy(ThothSurrogate* s)
         if (s->ib) cudaFree(s->ib);
         if (s->lb) cudaFree(s->lb);
         if (s->sched) cudaFree(s->sched);
+        if (s->avg) cudaFree(s->avg);
         if (s->ds) cudaFree(s->ds);
         if (s->perm_host) cudaFreeHost(s->perm_host);
         if (s->perm_copied) cudaEventDestroy(s->perm_copied);
@@ -401,103 +542,53 @@ int thoth_gpu_surrogate_gradient(ThothSurrogate* s, const float* x, const float*
 int thoth_gpu_surrogate_train(ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
                               int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss)
 {
+    return thoth_gpu_surrogate_train_avg(s, x, y, scale, n, epochs, batch, lr, seed, 0, 0.0, final_loss);
+}
+
+int thoth_gpu_surrogate_train_avg(ThothSurrogate* s, const float* x, const float* y, const float* scale, int64_t n,
+                                  int32_t epochs, int32_t batch, double lr, uint64_t seed, int32_t avg_epochs,
+                                  double lr_avg, double* final_loss)
+{
+    return thoth_gpu_surrogate_train_members(&s, 1, x, y, scale, n, epochs, batch, lr, seed, avg_epochs, lr_avg,
+                                             final_loss);
+}
+
+int thoth_gpu_surrogate_train_members(ThothSurrogate* const* members, int32_t k, const float* x, const float* y,
+                                      const float* scale, int64_t n, int32_t epochs, int32_t batch, double lr,
+                                      uint64_t seed, int32_t avg_epochs, double lr_avg, double* final_loss)
+{
     try {
-        if (!s || !x || !y || n < 128 || epochs < 1 || batch < 128 || batch % 128 || !(lr > 0))
+        if (!members || k < 1 || k > 64 || !x || !y || n < 128 || epochs < 1 || batch < 128 || batch % 128 ||
+            !(lr > 0))
             return sfail(THOTH_GPU_E_INVALID, "bad training arguments (batch must be a multiple of 128)");
-        std::lock_guard<std::mutex> lk(s_mu);
-        STRY(cudaSetDevice(s->dev));
-        const int B = (int)std::min<int64_t>(batch, n / 128 * 128);
-        int rc = ensure_train(s, B);
-        if (rc) return rc;
+        if (avg_epochs < 0 || avg_epochs >= epochs || (avg_epochs > 0 && !(lr_avg > 0 && lr_avg <= lr)))
+            return sfail(THOTH_GPU_E_INVALID, "bad weight averaging (0 <= avg_epochs < epochs, 0 < lr_avg <= lr)");
         if (n > ((int64_t)1 << 31) - 1) return sfail(THOTH_GPU_E_TOO_LARGE, "training set beyond 2^31 rows");
-        // the whole training set goes up once, packed (bf16 hi/lo inputs, targets, loss weights);
-        // each epoch uploads one permutation and every step gathers its rows on the device
-        if (n > s->cap_ds) {
-            if (s->ds) cudaFree(s->ds);
-            if (s->perm_host) cudaFreeHost(s->perm_host);
-            s->ds = nullptr;
-            s->perm_host = nullptr;
-            s->cap_ds = 0;
-            STRY(cudaMalloc(&s->ds, (size_t)n * (KIN * 2 + 4 + 4 + 4) + 1024));
-            STRY(cudaHostAlloc(&s->perm_host, sizeof(int) * (size_t)n, cudaHostAllocDefault));
-            if (!s->perm_copied) STRY(cudaEventCreateWithFlags(&s->perm_copied, cudaEventDisableTiming));
-            s->cap_ds = n;
+        for (int j = 0; j < k; j++) {
+            if (!members[j]) return sfail(THOTH_GPU_E_INVALID, "null member");
+            for (int i = 0; i < j; i++)
+                if (members[i] == members[j]) return sfail(THOTH_GPU_E_INVALID, "a member appears twice");
+            if (members[j]->dev != members[0]->dev) return sfail(THOTH_GPU_E_INVALID, "members on different devices");
         }
-        auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
-        __nv_bfloat16* dX = reinterpret_cast<__nv_bfloat16*>(s->ds);
-        float* dY = reinterpret_cast<float*>(s->ds + up((size_t)n * KIN * 2));
-        float* dW = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(dY) + up((size_t)n * 4));
-        int* dP = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(dW) + up((size_t)n * 4));
-        {
-            std::vector<__nv_bfloat16> hx;
-            std::vector<float> hy, hw;
-            pack(x, y, scale, nullptr, 0, (int)n, hx, hy, hw);
-            STRY(cudaMemcpy(dX, hx.data(), hx.size() * 2, cudaMemcpyHostToDevice));
-            STRY(cudaMemcpy(dY, hy.data(), hy.size() * 4, cudaMemcpyHostToDevice));
-            STRY(cudaMemcpy(dW, hw.data(), hw.size() * 4, cudaMemcpyHostToDevice));
+        std::lock_guard<std::mutex> lk(s_mu);
+        STRY(cudaSetDevice(members[0]->dev));
+        std::vector<TrainRun> runs(k);
+        for (int j = 0; j < k; j++) {
+            const int rc = train_setup(runs[j], members[j], x, y, scale, n, epochs, batch, lr, seed + (uint64_t)j,
+                                       avg_epochs, lr_avg);
+            if (rc) return rc;
         }
-        std::vector<int> idx(n);
-        for (int64_t i = 0; i < n; i++) idx[i] = (int)i;
-        std::mt19937_64 rng(seed);
-        const int64_t steps_per_epoch = n / B, total = steps_per_epoch * epochs;
-        mlp::TrainArgs& A = s->A;
-        A.a[0] = const_cast<__nv_bfloat16*>(A.x);
-        A.rows = B;
-        // the schedule of this call on the device: the captured step reads its batch offset,
-        // learning rate and bias corrections there and advances it
-        if (!s->sched) STRY(cudaMalloc(&s->sched, sizeof(mlp::TrainSched)));
-        mlp::TrainSched sc{};
-        sc.count = 0;
-        sc.total = total;
-        sc.steps_per_epoch = steps_per_epoch;
-        sc.step0 = s->step;
-        sc.lr0 = lr;
-        sc.rows = B;
-        mlp_sched_init(sc);
-        STRY(cudaMemcpyAsync(s->sched, &sc, sizeof sc, cudaMemcpyHostToDevice, s->st));
-        STRY(cudaMemsetAsync(s->status, 0, sizeof(int), s->st));
-        STRY(mlp_train_prepare());
-        // one step (gather, forward, backward, Adam, loss, schedule) captured once, replayed
-        // for every step: its launches' arguments do not change from step to step
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        STRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
-        cudaError_t ce = mlp_gather_batch(dX, dY, dW, dP, 0, B, const_cast<__nv_bfloat16*>(A.x), const_cast<float*>(A.y),
-                                          const_cast<float*>(A.inv_w2), s->st, s->sched);
-        if (ce == cudaSuccess)
-            ce = mlp_train_step(A, s->params, s->m, s->v, s->wbf, 0.f, 0.9f, 0.999f, 1e-8f, 1.f, 1.f, s->loss, s->st,
-                                s->sched);
-        if (ce == cudaSuccess) ce = mlp_sched_advance(s->sched, s->st);
-        const cudaError_t ee = cudaStreamEndCapture(s->st, &graph);
-        if (ce == cudaSuccess) ce = ee;
-        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
-        if (graph) cudaGraphDestroy(graph);
-        if (ce != cudaSuccess) {
-            if (exec) cudaGraphExecDestroy(exec);
-            return sfail(THOTH_GPU_E_CUDA, std::string("training step graph: ") + cudaGetErrorString(ce));
+        // the members' epochs interleaved: each member replays its own step graph on its own stream,
+        // so their kernels run side by side on the device
+        for (int e = 0; e < epochs; e++)
+            for (int j = 0; j < k; j++) {
+                const int rc = train_epoch(runs[j], e);
+                if (rc) return rc;
+            }
+        for (int j = 0; j < k; j++) {
+            const int rc = train_finish(runs[j], final_loss ? final_loss + j : nullptr);
+            if (rc) return rc;
         }
-        struct ExecGuard {
-            cudaGraphExec_t e;
-            ~ExecGuard() { cudaGraphExecDestroy(e); }
-        } guard{exec};
-        STRY(cudaEventRecord(s->perm_copied, s->st));
-        for (int e = 0; e < epochs; e++) {
-            // the next permutation is drawn on the host while the device runs the previous epoch
-            std::shuffle(idx.begin(), idx.end(), rng);
-            STRY(cudaEventSynchronize(s->perm_copied)); // the previous permutation has left the pinned buffer
-            std::memcpy(s->perm_host, idx.data(), sizeof(int) * (size_t)n);
-            STRY(cudaMemcpyAsync(dP, s->perm_host, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->st));
-            STRY(cudaEventRecord(s->perm_copied, s->st));
-            for (int64_t b = 0; b < steps_per_epoch; b++) STRY(cudaGraphLaunch(exec, s->st));
-        }
-        s->step += total;
-        float l = 0;
-        STRY(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->st));
-        STRY(cudaStreamSynchronize(s->st));
-        const double last = l / B;
-        rc = check_status(s);
-        if (rc) return rc;
-        if (final_loss) *final_loss = last;
         return THOTH_GPU_OK;
     } catch (const std::bad_alloc&) {
         return sfail(THOTH_GPU_E_NOMEM, "out of host memory");
@@ -517,7 +608,7 @@ int thoth_gpu_surrogate_predict(ThothSurrogate* s, const float* x, int64_t n, fl
             s->ib = nullptr;
             s->cap_inf = 0;
             const int64_t cap = (n + 127) / 128 * 128;
-            STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 4) + 256));
+            STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 8) + 512));
             s->cap_inf = cap;
         }
         __nv_bfloat16* dx = reinterpret_cast<__nv_bfloat16*>(s->ib);
@@ -559,10 +650,24 @@ int thoth_gpu_surrogate_price_lattice(ThothSurrogate* s, const double* params, i
                                       int32_t n_lm, const double* Ts, int32_t n_T, const double* box_lo,
                                       const double* box_hi, double floor, float* prices, double* device_ms)
 {
+    return thoth_gpu_surrogate_price_lattice_mean(&s, 1, params, n_sets, lms, n_lm, Ts, n_T, box_lo, box_hi, floor,
+                                                  prices, device_ms);
+}
+
+int thoth_gpu_surrogate_price_lattice_mean(ThothSurrogate* const* members, int32_t k, const double* params,
+                                           int32_t n_sets, const double* lms, int32_t n_lm, const double* Ts,
+                                           int32_t n_T, const double* box_lo, const double* box_hi, double floor,
+                                           float* prices, double* device_ms)
+{
     try {
-        if (!s || !params || !lms || !Ts || !box_lo || !box_hi || !prices || n_sets < 1 || n_lm < 1 || n_T < 1 ||
-            !(floor > 0))
+        if (!members || k < 1 || k > 64 || !params || !lms || !Ts || !box_lo || !box_hi || !prices || n_sets < 1 ||
+            n_lm < 1 || n_T < 1 || !(floor > 0))
             return sfail(THOTH_GPU_E_INVALID, "bad lattice arguments");
+        for (int j = 0; j < k; j++) {
+            if (!members[j]) return sfail(THOTH_GPU_E_INVALID, "null member");
+            if (members[j]->dev != members[0]->dev) return sfail(THOTH_GPU_E_INVALID, "members on different devices");
+        }
+        ThothSurrogate* s = members[0]; // its buffers and stream serve the call
         const int64_t n = (int64_t)n_sets * n_lm * n_T;
         if (n > ((int64_t)1 << 30)) return sfail(THOTH_GPU_E_TOO_LARGE, "more than 2^30 lattice cells");
         for (int q = 0; q < 7; q++)
@@ -575,7 +680,7 @@ int thoth_gpu_surrogate_price_lattice(ThothSurrogate* s, const double* params, i
             s->ib = nullptr;
             s->cap_inf = 0;
             const int64_t cap = (n + 127) / 128 * 128;
-            STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 4) + 256));
+            STRY(cudaMalloc(&s->ib, (size_t)cap * (KIN * 2 + 8) + 512));
             s->cap_inf = cap;
         }
         const size_t in_bytes = up(sizeof(double) * ((size_t)n_sets * 5 + n_lm + n_T));
@@ -616,8 +721,18 @@ int thoth_gpu_surrogate_price_lattice(ThothSurrogate* s, const double* params, i
         const int grid = std::min(tiles, s->sms);
         STRY(cudaEventRecord(e0, s->st));
         STRY(lattice_features(A, dx, s->st));
-        STRY(mlp_infer(dx, (int)n, s->params, s->wbf, dy, s->status, grid, s->st));
-        STRY(lattice_scale(A, dy, dprice, s->st));
+        if (k == 1) {
+            STRY(mlp_infer(dx, (int)n, s->params, s->wbf, dy, s->status, grid, s->st));
+            STRY(lattice_scale(A, dy, dprice, s->st));
+        } else {
+            // each member's normalised prices, added in member order into the mean
+            float* dsum = reinterpret_cast<float*>(s->ib + ((size_t)s->cap_inf * (KIN * 2 + 4) + 255) / 256 * 256);
+            for (int j = 0; j < k; j++) {
+                STRY(mlp_infer(dx, (int)n, members[j]->params, members[j]->wbf, dy, s->status, grid, s->st));
+                STRY(mlp_mean_add(dsum, dy, n, j, k, s->st));
+            }
+            STRY(lattice_scale(A, dsum, dprice, s->st));
+        }
         STRY(cudaEventRecord(e1, s->st));
         STRY(cudaMemcpyAsync(prices, dprice, sizeof(float) * n, cudaMemcpyDeviceToHost, s->st));
         STRY(cudaStreamSynchronize(s->st));

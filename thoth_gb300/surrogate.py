@@ -154,6 +154,9 @@ class Surrogate:
         L.thoth_gpu_surrogate_train.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                                 C.POINTER(C.c_float), C.c_int64, C.c_int32, C.c_int32, C.c_double,
                                                 C.c_uint64, C.POINTER(C.c_double)]
+        L.thoth_gpu_surrogate_train_avg.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                                    C.POINTER(C.c_float), C.c_int64, C.c_int32, C.c_int32, C.c_double,
+                                                    C.c_uint64, C.c_int32, C.c_double, C.POINTER(C.c_double)]
         L.thoth_gpu_surrogate_gradient.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                                    C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
                                                    C.POINTER(C.c_double)]
@@ -197,13 +200,15 @@ class Surrogate:
                                                         g.ctypes.data_as(C.POINTER(C.c_float)), C.byref(loss)))
         return g, loss.value
 
-    def train(self, xn, y, scale, epochs=20, batch=8192, lr=2e-3, seed=1):
+    def train(self, xn, y, scale, epochs=20, batch=8192, lr=2e-3, seed=1, avg_epochs=0, lr_avg=0.0):
+        """Adam with a cosine learning-rate decay; with avg_epochs > 0 the decay ends at lr_avg
+        before the last avg_epochs epochs, whose end-of-epoch weights are averaged into the model."""
         xn, px = self._f(xn)
         y, py = self._f(y)
         sc, ps = self._f(scale)
         loss = C.c_double()
-        self._check(self.L.thoth_gpu_surrogate_train(self.h, px, py, ps, len(y), epochs, batch, lr, seed,
-                                                     C.byref(loss)))
+        self._check(self.L.thoth_gpu_surrogate_train_avg(self.h, px, py, ps, len(y), epochs, batch, lr, seed,
+                                                         int(avg_epochs), float(lr_avg), C.byref(loss)))
         return loss.value
 
     def predict(self, xn):
@@ -240,6 +245,64 @@ class Surrogate:
             self.close()
         except Exception:
             pass
+
+
+class Ensemble:
+    """k networks of the surrogate's architecture, each from its own initialisation and data
+    order, trained side by side (thoth_gpu_surrogate_train_members) and served as the mean of
+    their outputs (thoth_gpu_surrogate_price_lattice_mean). Trained on MC labels, one network's
+    fit carries part of the labels' noise, differently for each initialisation; the mean keeps
+    the common fit and averages that part out."""
+
+    def __init__(self, members=4, seed=1):
+        if members < 1:
+            raise ValueError("an ensemble needs at least one member")
+        self.members = [Surrogate(seed=seed + j) for j in range(members)]
+        self.seed = seed
+        L = self.L = self.members[0].L
+        L.thoth_gpu_surrogate_train_members.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_float),
+                                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64,
+                                                        C.c_int32, C.c_int32, C.c_double, C.c_uint64, C.c_int32,
+                                                        C.c_double, C.POINTER(C.c_double)]
+        L.thoth_gpu_surrogate_price_lattice_mean.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_double),
+                                                             C.c_int32, C.POINTER(C.c_double), C.c_int32,
+                                                             C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_double),
+                                                             C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_float),
+                                                             C.POINTER(C.c_double)]
+
+    def _handles(self):
+        return (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+
+    def train(self, xn, y, scale, epochs=20, batch=8192, lr=2e-3, seed=None, avg_epochs=0, lr_avg=0.0):
+        """Every member on the same labels, member j with data-order seed seed + j; the final
+        losses, one a member."""
+        seed = self.seed if seed is None else seed
+        xn, px = Surrogate._f(xn)
+        y, py = Surrogate._f(y)
+        sc, ps = Surrogate._f(scale)
+        loss = (C.c_double * len(self.members))()
+        self.members[0]._check(self.L.thoth_gpu_surrogate_train_members(
+            self._handles(), len(self.members), px, py, ps, len(y), epochs, batch, lr, seed, int(avg_epochs),
+            float(lr_avg), loss))
+        return list(loss)
+
+    def price_lattice(self, param_sets, lms=LATTICE_LM, Ts=LATTICE_T):
+        """As Surrogate.price_lattice, for the members' mean."""
+        d = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        P, lm, T, lo, hi = d(param_sets), d(lms), d(Ts), d(BOX_LO), d(BOX_HI)
+        if P.ndim != 2 or P.shape[1] != 5:
+            raise ValueError("param_sets must be [n][5] (kappa, theta, xi, rho, v0)")
+        out = np.zeros(len(P) * len(lm) * len(T), dtype=np.float32)
+        ms = C.c_double()
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self.members[0]._check(self.L.thoth_gpu_surrogate_price_lattice_mean(
+            self._handles(), len(self.members), ptr(P), len(P), ptr(lm), len(lm), ptr(T), len(T), ptr(lo), ptr(hi),
+            FLOOR, out.ctypes.data_as(C.POINTER(C.c_float)), C.byref(ms)))
+        return out, ms.value
+
+    def close(self):
+        for m in self.members:
+            m.close()
 
 
 def _mc_subset(param_sets, paths, lms, Ts):
