@@ -143,6 +143,12 @@ typedef struct ThothBookDesc
     int32_t use_sobol;  /* 1: Sobol + Brownian bridge; 0: counter-based pseudo-random */
     int32_t greeks;     /* THOTH_GREEK_* mask                                       */
     uint64_t seed;      /* pseudo-random stream (use_sobol = 0, and Sobol dims > 4097) */
+    /* 1: the Cholesky factor also drives the spot white noise of Heston and LSV assets
+     * (asset u's spot noise = sum_v L[u][v] n_v, as for a GBM Brownian); their variance
+     * noises stay independent. An extension with no reference counterpart: the reference
+     * correlates only GBM spots (pricer_mcl.cpp:277-283; single.cpp:88). 0: the
+     * reference's behaviour. */
+    int32_t correlate_all_spots;
 } ThothBookDesc;
 
 /* Per-product and book results. Arrays are caller-owned, n_products long;

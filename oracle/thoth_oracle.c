@@ -504,7 +504,18 @@ static void* run_job(void* arg)
                     }
                     V[a * nd + i] = vn;
                     /* heston_spot_node.cpp:32-94 */
-                    const double vp = v, vc = vn, zs = noise[a], rho = A->rho;
+                    const double vp = v, vc = vn, rho = A->rho;
+                    /* the spot's white noise (single.cpp:88); with correlate_all_spots (an extension
+                     * of this project, not the reference's behaviour) correlated through the Cholesky
+                     * factor as a GBM Brownian is */
+                    double zs = noise[a];
+                    if (d->correlate_all_spots && na > 1 && d->cholesky) {
+                        zs = 0;
+                        for (int v2 = 0; v2 < na; v2++) {
+                            const double l = d->cholesky[a * na + v2];
+                            if (l != 0) zs += noise[v2] * l;
+                        }
+                    }
                     const double L = (A->model == THOTH_MODEL_LSV) ? lev_lookup(A, i, S[a * nd + i - 1]) : 1.0;
                     double step;
                     if (xi > 1e-12) {

@@ -178,6 +178,17 @@ def test_heston_calendar_grid_shared_paths(gpu):
 
 
 def test_heston_grid_vs_characteristic_function(gpu):
+    # config 2 at 2^22 paths: every cell within 1e-3 of the FP64 CF (relative, floor 1 unit of
+    # price), the benchmark spec's accuracy bar; at 2^20 paths every cell is within its trust
+    b = W.heston_grid(paths=1 << 22)
+    r = gpu.price_book(b)
+    cf = []
+    for m in W.MONTHS:
+        for K in W.STRIKES:
+            for typ in (abi.CALL, abi.PUT):
+                cf.append(oracle.heston_price(100, K, m / 12.0, 0.03, 0.0, 0.04, 1.5, 0.04, 0.6, -0.7, typ == abi.CALL))
+    cf = np.array(cf)
+    assert np.all(np.abs(r["premium"] - cf) <= 1e-3 * np.maximum(cf, 1.0))
     b = W.heston_grid(paths=1 << 20)
     r = gpu.price_book(b)
     cf = []
@@ -230,6 +241,64 @@ def test_independent_assets_in_turn_shared_paths(gpu):
     assert_shared_path_parity(r, ref["premium"], ref["trust"], "assets in turn")
     assert abs(r["book_premium"] - ref["book_premium"]) <= 0.5 * ref["book_trust"] + 1e-4 * abs(ref["book_premium"])
     assert np.isfinite(r["delta"][[0, 1, 2, 5]]).all()
+
+
+def _correlated_book(paths, xi=(0.5, 0.7, 0.6), lsv=True):
+    days = np.arange(0, 121)
+    b = abi.Book(days=days, paths=paths)
+    h0 = b.add_heston(100.0, 0.05, 2.0, 0.05, xi[0], -0.6, 0.02)
+    h1 = b.add_heston(80.0, 0.04, 1.5, 0.04, xi[1], -0.7, 0.01)
+    lev = None
+    if lsv:
+        ln_step = (np.log(300.0) - np.log(30.0)) / 49
+        offset = int(np.floor(np.log(30.0) / ln_step))
+        vals = 0.8 + 0.4 * np.random.default_rng(4).random((len(days), 50))
+        lev = (np.full(len(days), ln_step), np.full(len(days), offset, dtype=np.int64), vals)
+    h2 = b.add_heston(120.0, 0.06, 1.0, 0.06, xi[2], -0.5, 0.03, leverage=lev)
+    C = np.array([[1.0, 0.6, 0.3], [0.6, 1.0, 0.5], [0.3, 0.5, 1.0]])
+    b.set_cholesky(np.linalg.cholesky(C))
+    b.correlate_all_spots = True
+    return b, (h0, h1, h2)
+
+
+def test_correlated_stochastic_vol_spots_shared_paths(gpu):
+    """Extension (no reference counterpart): the Cholesky factor drives the spot noises of
+    Heston and LSV names too. A basket across three such names, a spread (weights 1, -1) and a
+    vanilla, against the oracle's restatement of the same extension on the same paths; without
+    the flag the book runs its names one by one, as the reference would."""
+    b, (h0, h1, h2) = _correlated_book((1 << 13) + 21)
+    b.add_basket([h0, h1, h2], [0.3, 0.4, 0.3], 100.0, 120, zero_rate=0.02)
+    b.add_basket([h0, h1], [1.0, -1.0], 10.0, 90, zero_rate=0.02)
+    b.add_vanilla(h2, 120.0, 120, abi.PUT, zero_rate=0.02)
+    assert gpu.plan_summary(b)["variant"] == 3
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "correlated spots")
+    b.correlate_all_spots = False
+    assert gpu.plan_summary(b)["variant"] == 6
+    r0 = gpu.price_book(b)
+    ref0 = oracle.price_book(b)
+    assert_shared_path_parity(r0, ref0["premium"], ref0["trust"], "independent spots")
+    assert abs(r["premium"][1] - r0["premium"][1]) > 3 * r["trust"][1]   # the spread feels the correlation
+
+
+def test_correlated_spots_gbm_limit_exchange_option(gpu):
+    """Two Heston names with no vol of vol and v0 = theta are GBMs of volatility sqrt(theta);
+    with their spots correlated, the exchange option max(S0 - S1, 0) (a basket of weights 1, -1
+    and strike 0) has Margrabe's closed form."""
+    from scipy.special import ndtr
+    T, rho, v = 1.0, 0.6, (0.05, 0.04)
+    b = abi.Book(days=np.arange(0, 366), paths=1 << 18)
+    a0 = b.add_heston(100.0, v[0], 1.0, v[0], 0.0, 0.0, 0.0)
+    a1 = b.add_heston(95.0, v[1], 1.0, v[1], 0.0, 0.0, 0.0)
+    b.set_cholesky(np.linalg.cholesky(np.array([[1.0, rho], [rho, 1.0]])))
+    b.correlate_all_spots = True
+    b.add_basket([a0, a1], [1.0, -1.0], 0.0, 365, zero_rate=0.0)
+    r = gpu.price_book(b)
+    s = np.sqrt(v[0] + v[1] - 2 * rho * np.sqrt(v[0] * v[1]))
+    d1 = (np.log(100.0 / 95.0) + 0.5 * s * s * T) / (s * np.sqrt(T))
+    margrabe = 100.0 * ndtr(d1) - 95.0 * ndtr(d1 - s * np.sqrt(T))
+    assert abs(r["premium"][0] - margrabe) < 3 * r["trust"][0] + 1e-3 * margrabe
 
 
 def test_shared_running_groups_shared_paths(gpu):

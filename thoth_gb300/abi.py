@@ -86,7 +86,7 @@ class ThothBookDesc(C.Structure):
         ("sobol_skip", C.c_int64),
         ("use_sobol", C.c_int32),
         ("greeks", C.c_int32),
-        ("seed", C.c_uint64),
+        ("seed", C.c_uint64), ("correlate_all_spots", C.c_int32),
     ]
 
 
@@ -212,6 +212,9 @@ class Book:
         self.assets = []
         self.products = []
         self.cholesky = None
+        # True: the Cholesky factor also drives Heston / LSV spot noises (an extension; the
+        # reference correlates only GBM spots)
+        self.correlate_all_spots = False
         self.paths = int(paths)
         self.sobol_skip = int(sobol_skip)
         self.use_sobol = bool(use_sobol)
@@ -345,6 +348,7 @@ class Book:
         d.use_sobol = int(self.use_sobol)
         d.greeks = self.greeks
         d.seed = self.seed
+        d.correlate_all_spots = int(bool(self.correlate_all_spots))
         keep += [A, P]
         self._keep = keep
         return d

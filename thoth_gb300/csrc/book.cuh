@@ -577,13 +577,14 @@ __device__ __forceinline__ PairLane pair_lane(const DevPlan& P, const uint2* hs,
     return L;
 }
 
-template <int TB>
+// ALL: every dimension of the book is a Sobol dimension (the bound test is dropped)
+template <int TB, bool ALL>
 __device__ __forceinline__ float2 pair_gauss(const DevPlan& P, uint2* hs_base, PairLane& L, const uint64_t (&n)[2],
                                              int dim)
 {
     constexpr int T = 1 << TB;
     uint32_t x0, x1;
-    if (dim < P.sobol_dims) {
+    if (ALL || dim < P.sobol_dims) {
         if (L.hs == L.hs_end) { // next chunk of tile parts (uniform across the CTA)
             L.jc += HS_CHUNK;
             __syncthreads();
@@ -606,7 +607,8 @@ __device__ __forceinline__ float2 pair_gauss(const DevPlan& P, uint2* hs_base, P
     return f2(z0, z1);
 }
 
-template <int TB, int MODEL, bool UNIFORM, class Ev>
+// FAST: the book is in Sobol mode with every dimension a Sobol dimension, and stores no paths
+template <int TB, int MODEL, bool UNIFORM, bool FAST, class Ev>
 __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairLane& L,
                                           const uint64_t (&n)[2], const bool (&valid)[2], int a0, float4 u0,
                                           float4 u1, float4 u2, Ev& apply_events)
@@ -633,7 +635,7 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
     int sp = 0;
     apply_events(0, aid, t, 0.f, 0.f, 0.f, 1.f);
     apply_events(0, aid, t + TH, 0.f, 0.f, 0.f, 1.f);
-    const bool store = P.path_out && aid == P.path_asset;
+    const bool store = !FAST && P.path_out && aid == P.path_asset;
     if (store)
 #pragma unroll
         for (int p = 0; p < 2; ++p)
@@ -652,9 +654,15 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
             c2 = __ldg(cs + 2);
             if (MODEL == M_LSV || (SEQ && model == M_LSV)) c3 = __ldg(cs + 3);
         }
+        // LSV: the leverage at the step's start, requested before the bridge work (see book_kernel)
+        float lvL[2] = {1.f, 1.f}, lvD[2] = {0.f, 0.f};
+        if (MODEL == M_LSV || (SEQ && model == M_LSV)) {
+            leverage(P, aid, c3, X.x, lvL[0], lvD[0]);
+            leverage(P, aid, c3, X.y, lvL[1], lvD[1]);
+        }
         // ---- Brownian bridge: normalised increments nz0 (spot), nz1 (variance) ----
         float2 nz0, nz1 = f2s(0.f);
-        if (P.use_sobol) {
+        if (FAST || P.use_sobol) {
             float2 Wi0 = f2s(0.f), Wi1 = f2s(0.f);
             if (cur.count == 0) {
                 const int base = (sp - 1) * nfa;
@@ -666,8 +674,8 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
                 }
                 --sp;
             } else if (cur.count == 1) {
-                Wi0 = comb2(cur.lw, cur.rw, cur.sd, Wp0, T0, pair_gauss<TB>(P, S.hs, L, n, cur.dim + fid0));
-                if (act1) Wi1 = comb2(cur.lw, cur.rw, cur.sd, Wp1, T1, pair_gauss<TB>(P, S.hs, L, n, cur.dim + fid1));
+                Wi0 = comb2(cur.lw, cur.rw, cur.sd, Wp0, T0, pair_gauss<TB, FAST>(P, S.hs, L, n, cur.dim + fid0));
+                if (act1) Wi1 = comb2(cur.lw, cur.rw, cur.sd, Wp1, T1, pair_gauss<TB, FAST>(P, S.hs, L, n, cur.dim + fid1));
             } else {
                 float lw = cur.lw, rw = cur.rw, sd = cur.sd;
                 int dim = cur.dim;
@@ -680,9 +688,9 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
                         dim = nd.bstep * P.ref_factors;
                         if (k + 1 < cur.count) nd = P.nodes[cur.first + k];
                     }
-                    const float2 w0 = comb2(lw, rw, sd, Wp0, T0, pair_gauss<TB>(P, S.hs, L, n, dim + fid0));
+                    const float2 w0 = comb2(lw, rw, sd, Wp0, T0, pair_gauss<TB, FAST>(P, S.hs, L, n, dim + fid0));
                     float2 w1 = f2s(0.f);
-                    if (act1) w1 = comb2(lw, rw, sd, Wp1, T1, pair_gauss<TB>(P, S.hs, L, n, dim + fid1));
+                    if (act1) w1 = comb2(lw, rw, sd, Wp1, T1, pair_gauss<TB, FAST>(P, S.hs, L, n, dim + fid1));
                     if (k + 1 < cur.count) {
                         const int base = sp * nfa;
                         stk[(base + ci0) * TH] = T0;
@@ -727,13 +735,12 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
                 step = __ffma2_rn(f2s(-c1.w), s2, __fadd2_rn(f2s(c1.x), B));
             } else {
                 float sl[2];
-                const float vpl[2] = {V.x, V.y}, vcl[2] = {vc.x, vc.y}, xl[2] = {X.x, X.y}, zl[2] = {nz0.x, nz0.y};
+                const float vpl[2] = {V.x, V.y}, vcl[2] = {vc.x, vc.y}, zl[2] = {nz0.x, nz0.y};
                 float yl[2] = {Y.x, Y.y};
 #pragma unroll
                 for (int p = 0; p < 2; ++p) {
                     const float vp = vpl[p], vcp = vcl[p];
-                    float Lv = 1.f, dL = 0.f;
-                    if (model == M_LSV) leverage(P, aid, c3, xl[p], Lv, dL);
+                    const float Lv = lvL[p], dL = lvD[p];
                     const float s = vp + vcp;
                     if (!degenerate) {
                         const float B = fmaf(c2.y, vcp - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * zl[p];
@@ -892,7 +899,10 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
         PairLane PL = pair_lane<T>(P, S.hs, m); // unused (and dropped) unless NA == 1 and PP == 2
         for (int a0 = 0; a0 < n_pass; ++a0) {
             if constexpr (NA == 1 && PP == 2) {
-                pair_pass<TB, MODEL, UNIFORM>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
+                if (P.use_sobol && P.sobol_dims >= P.n_steps * P.ref_factors && !P.path_out)
+                    pair_pass<TB, MODEL, UNIFORM, true>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
+                else
+                    pair_pass<TB, MODEL, UNIFORM, false>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
                 continue;
             }
             // ---- path state -------------------------------------------------
@@ -945,6 +955,20 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
                     h2 = __ldg(cs + 2);
                     h3 = (MODEL == M_LSV || (MODEL == M_SEQ && P.model[ha] == M_LSV)) ? __ldg(cs + 3)
                                                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                // LSV: the leverage at the step's start (it depends on the log-spot of the previous
+                // date only), requested before the bridge work, which covers its dependent loads
+                float lvL[PP], lvD[PP];
+#pragma unroll
+                for (int p = 0; p < PP; ++p) {
+                    lvL[p] = 1.f;
+                    lvD[p] = 0.f;
+                }
+                if constexpr (HOIST) {
+                    const int ha = MODEL == M_SEQ ? a0 : 0;
+                    if (MODEL == M_LSV || (MODEL == M_SEQ && P.model[ha] == M_LSV))
+#pragma unroll
+                        for (int p = 0; p < PP; ++p) leverage(P, ha, h3, x[p][0], lvL[p], lvD[p]);
                 }
                 if (P.use_sobol) {
                     bridge_step<NA, T, PP, SEQ>(P, S, cur, sp, L, n, Wprev, top, nz, a0);
@@ -1033,12 +1057,27 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
                         } else {
                             const float vp = v[p][a];
                             const float vc = PAIRED ? vcs[p] : qe_step(vp, nz[p][NA + a], c0.x, c0.y, c0.z, c0.w);
+                            // the spot's noise: its own, or correlated through chol (correlate_all_spots)
+                            float zs = nz[p][a];
+                            if (MODEL == M_MIXED && P.corr_all) {
+                                zs = 0.f;
+#pragma unroll
+                                for (int u = 0; u < NA; ++u)
+                                    if (u < P.n_assets) zs = fmaf(P.chol[a * MAX_ASSETS + u], nz[p][u], zs);
+                            }
                             float Lv = 1.f, dL = 0.f;
-                            if (model == M_LSV) leverage(P, aid, c3, x[p][a], Lv, dL);
+                            if (model == M_LSV) {
+                                if constexpr (HOIST) {
+                                    Lv = lvL[p];
+                                    dL = lvD[p];
+                                } else {
+                                    leverage(P, aid, c3, x[p][a], Lv, dL);
+                                }
+                            }
                             const float s = vp + vc;
                             if (!P.degenerate[aid]) {
                                 const float B =
-                                    fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * nz[p][a];
+                                    fmaf(c2.y, vc - vp, fmaf(c1.z, s, c1.y)) + fast_sqrt(c2.x * s) * zs;
                                 if (model == M_LSV) {
                                     step = fmaf(Lv, B, c1.x) - Lv * Lv * c1.w * s;
                                     y[p][a] *= fmaf(B - 2.f * Lv * c1.w * s, dL, 1.f);
@@ -1046,7 +1085,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
                                     step = c1.x + B - c1.w * s;
                                 }
                             } else {
-                                const float sq = fast_sqrt(vp * c2.z) * nz[p][a];
+                                const float sq = fast_sqrt(vp * c2.z) * zs;
                                 step = c1.x - 0.5f * Lv * Lv * vp * c2.z + Lv * sq;
                                 if (model == M_LSV) y[p][a] *= fmaf(-Lv * vp * c2.z + sq, dL, 1.f);
                             }

@@ -134,6 +134,7 @@ struct DevPlan {
     int n_products;
     int greeks;
     int corr;             // 1: GBM noises correlated with chol
+    int corr_all;         // 1: Heston / LSV spot noises correlated with chol as well
     int64_t skip, paths;  // Sobol index range [skip + 1, skip + paths]
     int64_t tile_first, n_tiles;
     uint64_t seed;

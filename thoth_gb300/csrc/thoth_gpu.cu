@@ -562,16 +562,18 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
                 D.chol[u * MAX_ASSETS + v] = (float)l;
             }
         D.corr = 1;
+        D.corr_all = d->correlate_all_spots ? 1 : 0;
     }
     // variant (tile size fixed by it; uniform-step variants decided below). The
     // reference correlates only GBM spots (correlated_noise_node.cpp:15-27): a
     // multi-asset book without a correlated GBM name has independent assets and
-    // runs them one after the other (variant 6).
+    // runs them one after the other (variant 6), unless the book asks for every
+    // spot noise to be correlated (correlate_all_spots).
     bool any_gbm = false;
     for (int a = 0; a < NA; a++) any_gbm |= d->assets[a].model == THOTH_MODEL_GBM;
     if (NA == 1 && !mixed && !D.corr) {
         P.variant = d->assets[0].model; // 0 GBM, 1 Heston, 2 LSV
-    } else if (D.corr && any_gbm) {
+    } else if (D.corr && (any_gbm || D.corr_all)) {
         P.variant = 3;
     } else {
         P.variant = 6;
