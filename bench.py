@@ -437,8 +437,9 @@ def batch_parity(G, books, check_paths=1 << 16):
 
 def ragged_batch_section(G, steps):
     """256 ragged books (path counts log-uniform in [2^14, 2^22], 12..730 daily steps,
-    40% GBM / 40% Heston / 20% LSV) priced as one CUDA graph: untuned, after the
-    autotuner, and one book at a time for comparison."""
+    40% GBM / 40% Heston / 20% LSV) priced as one CUDA graph: the single-asset books in one
+    persistent launch (the default), the same batch with one launch per book, after the
+    autotuner (which times both), and one book at a time for comparison."""
     import numpy as np
     from thoth_gb300 import workloads as W
     books = W.ragged_books()
@@ -454,16 +455,26 @@ def ragged_batch_section(G, steps):
             ms.append(r[0]["device_ms"])
         return float(np.mean(ms)), float(np.mean(wall)), r
 
-    G.price_batch(books)                       # capture
-    untuned_ms, untuned_wall, _ = timed(max(1, steps // 2))
+    G.price_batch(books)                       # capture: one persistent launch
+    untuned_ms, untuned_wall, pers_res = timed(max(1, steps // 2))
+    pers_launches = G.batch_launches()
+    G.set_batch_persistent(False)
+    G.price_batch(books)                       # capture: one launch per book
+    per_book_ms, _, per_res = timed(max(1, steps // 2))
+    per_book_launches = G.batch_launches()
+    G.set_batch_persistent(True)
+    same = all(np.array_equal(a["premium"], b["premium"]) and a["book_premium"] == b["book_premium"]
+               for a, b in zip(pers_res, per_res))
     t0 = time.perf_counter()
     tune = G.autotune_batch(books, reps=1)
     tune_s = time.perf_counter() - t0
     G.price_batch(books)                       # capture with the tuned configuration
     tuned_ms, tuned_wall, res = timed(max(2, steps // 2))
+    launches = G.batch_launches()
     one_ms = 0.0
     for b in books:
         one_ms += G.price_book(b)["device_ms"]
+    parity = batch_parity(G, books)
     G.autotune_clear()
     return {
         "workload": "256 ragged books: paths log-uniform [2^14, 2^22], steps uniform [12, 730], "
@@ -472,13 +483,20 @@ def ragged_batch_section(G, steps):
         "path_steps_per_sec": work / (tuned_ms * 1e-3),
         "device_ms": tuned_ms, "e2e_ms": 1e3 * tuned_wall,
         "e2e_path_steps_per_sec": work / tuned_wall,
+        "persistent_launch": {"device_ms": untuned_ms, "e2e_ms": 1e3 * untuned_wall,
+                              "path_steps_per_sec": work / (untuned_ms * 1e-3), "gpu_launches": pers_launches,
+                              "note": "every single-asset book's work items in one persistent kernel between one "
+                                      "gather and one reduction"},
+        "one_launch_per_book": {"device_ms": per_book_ms, "gpu_launches": per_book_launches,
+                                "note": "gather, book kernel and reduction per book over 8 streams"},
+        "modes_bit_identical": bool(same),
         "untuned_device_ms": untuned_ms, "one_book_at_a_time_device_ms": one_ms,
         "autotune": dict(tune, seconds=tune_s,
-                         note="stream count, one launch shape for the single-asset books "
-                              "(-1: each book's default) and grid policy, timed on the batch graph"),
-        "gpu_launches_per_batch": 3 * len(books),  # gather, book kernel, reduction per book
+                         note="persistent launch (grid policy) against one launch per book (stream count, one "
+                              "launch shape for the single-asset books, grid policy), timed on the batch graph"),
+        "gpu_launches_per_batch": launches,
         "books_nonfinite": int(sum(not np.all(np.isfinite(r["premium"])) for r in res)),
-        "parity": batch_parity(G, books),
+        "parity": parity,
     }
 
 

@@ -404,11 +404,20 @@ int thoth_gpu_calibrate_leverage(ThothLeverageCalib* c);
 int thoth_gpu_xoshiro_jump(const uint64_t s[4], uint64_t n, uint64_t out[4]);
 
 /* Price n_books independent books (ragged path and step counts) in one CUDA
- * graph launch: all plans in one upload, each book's persistent kernel and
- * reduction on one of several streams (largest first), all sums back in one
- * copy. The graph is captured on the first call and replayed while the batch's
- * shapes repeat. device_ms of every result is the whole batch's device time.
- * No reference counterpart beyond repeated PriceBook calls (pricer_mcl.cpp:197-240). */
+ * graph launch: all plans in one upload, all sums back in one copy. By default
+ * the single-asset books run in ONE persistent kernel launch over a shared work
+ * list (item r of a book = the tiles r, r + grid, ... that CTA r of the book's own
+ * launch takes, so every book's sums are bit for bit those of its own launch at
+ * the same grid; largest items first, taken by resident CTAs from a counter),
+ * between one gather of the books' low Sobol words and one fixed-order
+ * reduction of every book's rows: three kernel launches for the batch. Books
+ * that kernel does not run (several assets, or shared memory beyond what keeps
+ * its CTAs resident) get their own launches on side streams meanwhile. With
+ * thoth_gpu_batch_persistent(0), every book's gather, kernel and reduction go
+ * on one of several streams instead (largest first). The graph is captured on
+ * the first call and replayed while the batch's shapes repeat. device_ms of
+ * every result is the whole batch's device time. No reference counterpart
+ * beyond repeated PriceBook calls (pricer_mcl.cpp:197-240). */
 int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBookResult* out);
 
 /* ---- autotuner (no reference counterpart) ----------------------------------
@@ -419,7 +428,9 @@ int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBook
  *    128, paths per thread 1 or 2, so 64 to 256 threads per CTA), and the
  *    persistent grid (k x SMs for k = 1 .. resident CTAs per SM, and the
  *    "balanced" grid of each: same waves, fewest CTAs);
- *  - per batch: the stream count (1 .. 32), one launch shape for every
+ *  - per batch: the persistent launch or one launch per book; for the
+ *    persistent launch the grid policy of its books' work items; for one launch
+ *    per book the stream count (1 .. 32), one launch shape for every
  *    single-asset book of the batch (or each book's own), and the grid policy
  *    of the batch graph (0 full, 1 balanced, 2 half).
  * Choices can be saved to and loaded from a small text file, which is tied to
@@ -437,6 +448,7 @@ typedef struct ThothTuneResult {
     int32_t tile_paths;    /* paths per tile of the chosen shape */
     double best_ms;        /* mean device time of the chosen configuration */
     double default_ms;     /* the same for the untuned configuration */
+    int32_t persistent;    /* batch: 1 the persistent launch was chosen, 0 one launch per book */
 } ThothTuneResult;
 
 int thoth_gpu_autotune_book(const ThothBookDesc* book, int32_t reps, ThothTuneResult* out);
@@ -446,8 +458,16 @@ int thoth_gpu_autotune_load(const char* path);
 /* forget every tuned choice (back to the untuned defaults) */
 int thoth_gpu_autotune_clear(void);
 
-/* Number of streams a batch graph fans out over (default 8). */
+/* Number of streams a batch graph fans out over (default 8): every book in
+ * the per-book mode, the books outside the persistent launch otherwise. */
 int thoth_gpu_batch_streams(int32_t n);
+
+/* 1 (default): the single-asset books of a batch in one persistent launch;
+ * 0: one launch per book. */
+int thoth_gpu_batch_persistent(int32_t on);
+
+/* Kernel launches recorded into the cached batch graph (0 before the first batch). */
+int thoth_gpu_batch_launches(void);
 
 /* Replays of the cached batch graph since its capture (0 right after a capture). */
 int thoth_gpu_batch_graph_replays(void);

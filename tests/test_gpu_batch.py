@@ -61,14 +61,55 @@ def test_long_books_with_lsv_barriers_vs_oracle(gpu):
                                                                 1e-4 * max(abs(ref["book_premium"]), sc.sum()))
 
 
-def test_batch_equals_one_at_a_time(gpu):
+@pytest.mark.parametrize("persistent", [True, False])
+def test_batch_equals_one_at_a_time(gpu, persistent):
+    """Work item r of a book in the persistent launch is CTA r's share of the book's own
+    launch: every book's sums are bit for bit those of pricing it alone, in either mode."""
     books = small_batch(n=20, seed=3)
-    res = gpu.price_batch(books)
+    gpu.set_batch_persistent(persistent)
+    try:
+        res = gpu.price_batch(books)
+        assert gpu.batch_launches() == (3 if persistent else 3 * len(books))
+    finally:
+        gpu.set_batch_persistent(True)
     for b, r in zip(books, res):
         one = gpu.price_book(b)
         np.testing.assert_array_equal(r["premium"], one["premium"])
         np.testing.assert_array_equal(r["trust"], one["trust"])
         assert r["book_premium"] == one["book_premium"]
+
+
+def test_persistent_launch_with_books_it_does_not_run(gpu):
+    """Multi-asset books (correlated GBM names, LSV and Heston names in turn) beside single-asset
+    books of every model: the single-asset books share the persistent launch, the others
+    get their own launches meanwhile; every book equals its own pricing bit for bit, and
+    long LSV books with daily barriers among them match the oracle on shared paths."""
+    books = small_batch(n=14, seed=17)
+    books += W.ragged_books(n_books=3, seed=41, min_paths=1 << 10, max_paths=1 << 11, min_steps=400,
+                            max_steps=500, model_mix=(0.0, 0.0, 1.0), payoffs=(1,))
+    two = abi.Book(days=np.arange(0, 61), paths=3000)   # two independent Heston names: assets in turn
+    h0 = two.add_heston(100.0, 0.05, 2.0, 0.05, 0.5, -0.6, 0.02)
+    h1 = two.add_heston(80.0, 0.04, 1.5, 0.04, 0.7, -0.7, 0.01)
+    two.add_vanilla(h0, 100.0, 60, abi.CALL, zero_rate=0.02)
+    two.add_vanilla(h1, 80.0, 40, abi.PUT, zero_rate=0.02)
+    pair = abi.Book(days=np.arange(0, 31), paths=2500)  # two correlated GBM names: the mixed kernel
+    g0 = pair.add_gbm(100.0, 0.25, 0.02)
+    g1 = pair.add_gbm(90.0, 0.30, 0.01)
+    pair.set_cholesky(np.linalg.cholesky(np.array([[1.0, 0.5], [0.5, 1.0]])))
+    pair.add_basket([g0, g1], [0.5, 0.5], 95.0, 30, zero_rate=0.02)
+    multi = [W.lsv_book(paths=2000), pair, two]
+    assert [gpu.plan_summary(m)["variant"] for m in multi] == [6, 3, 6]
+    books[3:3] = multi
+    res = gpu.price_batch(books)
+    assert gpu.batch_launches() == 3 + len(multi)
+    for i, (b, r) in enumerate(zip(books, res)):
+        one = gpu.price_book(b)
+        np.testing.assert_array_equal(r["premium"], one["premium"], err_msg="book %d" % i)
+        assert r["book_premium"] == one["book_premium"]
+    for i in range(len(books) - 3, len(books)):
+        ref = oracle.price_book(books[i], threads=THREADS)
+        assert_shared_path_parity(res[i], ref["premium"], ref["trust"], "LSV barrier book %d" % i,
+                                  scale=leg_scale(books[i]))
 
 
 def test_graph_is_replayed_while_shapes_repeat(gpu):
@@ -166,11 +207,14 @@ def test_autotune_batch_save_load(gpu, tmp_path):
     books = small_batch(n=16, seed=21)
     t = gpu.autotune_batch(books, reps=1)
     assert t["streams"] in (1, 2, 4, 8, 16) and t["policy"] in (0, 1, 2) and t["shape"] in (-1, 0, 1, 2, 3, 4)
-    assert t["candidates"] >= 10
+    assert t["persistent"] in (0, 1) and (t["shape"] == -1 or not t["persistent"])
+    assert t["candidates"] >= 13
+    assert t["best_ms"] <= t["default_ms"] * (1 + 1e-9)
     path = tmp_path / "tune.txt"
     gpu.autotune_save(path)
     text = path.read_text().splitlines()
-    assert text[0] == "thoth-autotune 1" and text[2] == "batch %d %d %d" % (t["streams"], t["policy"], t["shape"])
+    assert text[0] == "thoth-autotune 1"
+    assert text[2] == "batch %d %d %d %d" % (t["streams"], t["policy"], t["shape"], t["persistent"])
     tuned = gpu.price_batch(books)
     gpu.autotune_clear()
     gpu.autotune_load(path)

@@ -56,6 +56,8 @@ def lib():
         L.thoth_gpu_measure_mufu_peak.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.thoth_gpu_debug_fail_allocations.argtypes = [C.c_int32]
         L.thoth_gpu_batch_streams.argtypes = [C.c_int32]
+        L.thoth_gpu_batch_persistent.argtypes = [C.c_int32]
+        L.thoth_gpu_batch_launches.argtypes = []
         L.thoth_gpu_bump_greeks.argtypes = [C.POINTER(abi.ThothBookDesc), C.POINTER(abi.ThothBumpGreeks)]
         L.thoth_gpu_bump_greeks_last_error.restype = C.c_char_p
         L.thoth_gpu_calibrate_leverage.argtypes = [C.POINTER(abi.ThothLeverageCalib)]
@@ -241,10 +243,20 @@ def set_batch_streams(n):
     _check(lib().thoth_gpu_batch_streams(int(n)))
 
 
+def set_batch_persistent(on):
+    """True (default): a batch's single-asset books in one persistent launch; False: one launch per book."""
+    _check(lib().thoth_gpu_batch_persistent(1 if on else 0))
+
+
+def batch_launches():
+    """Kernel launches recorded into the cached batch graph."""
+    return lib().thoth_gpu_batch_launches()
+
+
 def _tune_dict(r):
     return dict(grid=r.grid, default_grid=r.default_grid, candidates=r.candidates, streams=r.streams,
                 policy=r.policy, shape=r.shape, threads=r.threads, tile_paths=r.tile_paths, best_ms=r.best_ms,
-                default_ms=r.default_ms)
+                default_ms=r.default_ms, persistent=r.persistent)
 
 
 def autotune_book(book, reps=3):
@@ -256,7 +268,8 @@ def autotune_book(book, reps=3):
 
 
 def autotune_batch(books, reps=1):
-    """Time stream counts and grid policies of the batch graph; later batches use the fastest."""
+    """Time the persistent launch and the per-book launches (stream counts, shapes, grid policies)
+    of the batch graph; later batches use the fastest."""
     n = len(books)
     descs = (abi.ThothBookDesc * max(n, 1))()
     keep = []

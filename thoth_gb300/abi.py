@@ -113,7 +113,8 @@ class ThothGbmResult(C.Structure):
 class ThothTuneResult(C.Structure):
     _fields_ = [("grid", C.c_int32), ("default_grid", C.c_int32), ("candidates", C.c_int32),
                 ("streams", C.c_int32), ("policy", C.c_int32), ("shape", C.c_int32), ("threads", C.c_int32),
-                ("tile_paths", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double)]
+                ("tile_paths", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double),
+                ("persistent", C.c_int32)]
 
 
 BUMP_DELTA, BUMP_GAMMA, BUMP_VEGA, BUMP_RHO, BUMP_THETA, BUMP_PARAMS = 1, 2, 4, 8, 16, 32

@@ -23,12 +23,12 @@ LIB = BUILD / "libthoth_gpu.so"
 # host code of the sanitized build (nvcc splits -Xcompiler values at commas: one flag each)
 SAN_HOST = ["-fsanitize=address", "-fsanitize=undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["book_heston.cu", "book_multi.cu", "book_lsv.cu", "book_gbm.cu", "kernels.cu", "thoth_gpu.cu",
+SOURCES = ["book_batch.cu", "book_heston.cu", "book_multi.cu", "book_lsv.cu", "book_gbm.cu", "kernels.cu", "thoth_gpu.cu",
            "surrogate.cu", "surrogate_host.cu", "greeks.cu", "american.cu", "american_host.cu", "calib.cu"]
 # the path kernels flush FP32 denormals: no value on the path is subnormal, and
 # without it every MUFU approximation (rcp, rsqrt, lg2, ex2) carries a
 # denormal fix-up sequence (11 % of the Heston step's time)
-FLAGS = {"kernels.cu": ["-ftz=true"], "book_gbm.cu": ["-ftz=true"], "book_heston.cu": ["-ftz=true"],
+FLAGS = {"kernels.cu": ["-ftz=true"], "book_batch.cu": ["-ftz=true"], "book_gbm.cu": ["-ftz=true"], "book_heston.cu": ["-ftz=true"],
          "book_lsv.cu": ["-ftz=true"], "book_multi.cu": ["-ftz=true"],
          # the exercise tables and the regression solve are compared bit for bit with the
          # oracle: no contraction of a * b + c into a fused multiply-add on the host

@@ -607,11 +607,73 @@ __device__ __forceinline__ float2 pair_gauss(const DevPlan& P, uint2* hs_base, P
     return f2(z0, z1);
 }
 
-// FAST: the book is in Sobol mode with every dimension a Sobol dimension, and stores no paths
-template <int TB, int MODEL, bool UNIFORM, bool FAST, class Ev>
+// The path events of date i for asset a on both tile columns of a thread (t and t + TH), each
+// event read once and applied to column t, then to column t + TH: per column the operations and
+// their order are those of apply_events in book_body.
+template <int TH>
+__device__ __forceinline__ void pair_events(const DevPlan& P, const Smem& S, int i, int a, float2 x, float2 step,
+                                            float2 w, float2 y)
+{
+    const int stride = 2 * TH + 1;
+    const int t = threadIdx.x;
+    const int2 r = P.ev_range[i * P.n_assets + a];
+    for (int e = r.x; e < r.x + r.y; ++e) {
+        const Event ev = P.events[e];
+        const int k = ev.a * stride + t; // the event's row (slot or group), column t
+        switch (ev.type) {
+        case EV_SNAP_S:
+            S.slots[k] = P.s0[a] * expf(x.x);
+            S.slots[k + TH] = P.s0[a] * expf(x.y);
+            break;
+        case EV_SNAP_W:
+            S.slots[k] = w.x;
+            S.slots[k + TH] = w.y;
+            break;
+        case EV_SNAP_Y:
+            S.slots[k] = y.x;
+            S.slots[k + TH] = y.y;
+            break;
+        case EV_GRP_MIN:
+            S.grp[k] = fminf(S.grp[k], x.x - ev.p);
+            S.grp[k + TH] = fminf(S.grp[k + TH], x.y - ev.p);
+            break;
+        case EV_GRP_MAX:
+            S.grp[k] = fmaxf(S.grp[k], x.x - ev.p);
+            S.grp[k + TH] = fmaxf(S.grp[k + TH], x.y - ev.p);
+            break;
+        case EV_GRP_SQ_STEP: {
+            const float d0 = step.x - ev.p, d1 = step.y - ev.p;
+            S.grp[k] = fmaf(d0, d0, S.grp[k]);
+            S.grp[k + TH] = fmaf(d1, d1, S.grp[k + TH]);
+            break;
+        }
+        case EV_SNAP_G: {
+            const int kg = ev.pad * stride + t;
+            S.slots[k] = S.grp[kg];
+            S.slots[k + TH] = S.grp[kg + TH];
+            break;
+        }
+        default: { // EV_GRP_SQ_OBS
+            const int kl = ev.pad * stride + t; // pad: the group's row of last
+            const float d0 = x.x - S.last[kl] - ev.p;
+            S.grp[k] = fmaf(d0, d0, S.grp[k]);
+            S.last[kl] = x.x;
+            const float d1 = x.y - S.last[kl + TH] - ev.p;
+            S.grp[k + TH] = fmaf(d1, d1, S.grp[k + TH]);
+            S.last[kl + TH] = x.y;
+        }
+        }
+    }
+}
+
+// FAST: the book is in Sobol mode with every dimension a Sobol dimension, and stores no paths.
+// PREFETCH: each step's record is loaded one step ahead (a book's own launch); the batch kernel,
+// whose plan sits in shared memory rather than in the constant bank, loads it at the step and
+// keeps the eight registers.
+template <int TB, int MODEL, bool UNIFORM, bool FAST, bool PREFETCH>
 __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairLane& L,
                                           const uint64_t (&n)[2], const bool (&valid)[2], int a0, float4 u0,
-                                          float4 u1, float4 u2, Ev& apply_events)
+                                          float4 u1, float4 u2)
 {
     constexpr int T = 1 << TB, TH = T / 2;
     constexpr bool SEQ = MODEL == M_SEQ;
@@ -633,8 +695,7 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
     float2 X = f2s(0.f), CP = f2s(0.f), V = f2s(P.v0[aid]), WB = f2s(0.f), Y = f2s(1.f);
     float2 Wp0 = f2s(0.f), Wp1 = f2s(0.f), T0 = f2s(0.f), T1 = f2s(0.f);
     int sp = 0;
-    apply_events(0, aid, t, 0.f, 0.f, 0.f, 1.f);
-    apply_events(0, aid, t + TH, 0.f, 0.f, 0.f, 1.f);
+    pair_events<TH>(P, S, 0, aid, f2s(0.f), f2s(0.f), f2s(0.f), f2s(1.f));
     const bool store = !FAST && P.path_out && aid == P.path_asset;
     if (store)
 #pragma unroll
@@ -643,8 +704,13 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
 
     StepRec rec = load_rec(P, 1);
     for (int i = 1; i <= P.n_steps; ++i) {
-        const StepRec cur = rec;
-        rec = load_rec(P, i + 1); // the record past the last step is padding
+        StepRec cur;
+        if constexpr (PREFETCH) {
+            cur = rec;
+            rec = load_rec(P, i + 1); // the record past the last step is padding
+        } else {
+            cur = load_rec(P, i);
+        }
         // this step's constants, requested before the bridge work that covers their latency
         float4 c0 = u0, c1 = u1, c2 = u2, c3 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (!UNIFORM) {
@@ -768,10 +834,7 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
             CP = sub2(sub2(tt, X), yy);
             X = tt;
         }
-        if (cur.ev) {
-            apply_events(i, aid, t, X.x, step.x, WB.x, Y.x);
-            apply_events(i, aid, t + TH, X.y, step.y, WB.y, Y.y);
-        }
+        if (cur.ev) pair_events<TH>(P, S, i, aid, X, step, WB, Y);
         if (store) {
             if (valid[0]) P.path_out[(size_t)i * P.path_ld + (n[0] - (uint64_t)P.skip - 1)] = P.s0[aid] * expf(X.x);
             if (valid[1]) P.path_out[(size_t)i * P.path_ld + (n[1] - (uint64_t)P.skip - 1)] = P.s0[aid] * expf(X.y);
@@ -794,19 +857,22 @@ struct MinBlocks {
     static constexpr int value = NA != 1 ? 3 : (PP == 4 ? 7 : 768 / ((1 << TB) / PP));
 };
 
-template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
-__global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) book_kernel(const DevPlan P)
+// The work of one CTA of a book: tiles tile0, tile0 + tile_step, ... below P.n_tiles, every
+// product evaluated on each tile's paths, the FP64 sums in the row acc (zeroed here). A book's
+// own launch runs it with tile0 = blockIdx.x and tile_step = gridDim.x; the batch kernel runs
+// the same work items from a shared work list. Returns false when the cancel word stopped it.
+template <int TB, int NA, int MODEL, bool UNIFORM, int PP, bool BATCH = false>
+__device__ __forceinline__ bool book_body(const DevPlan& P, unsigned char* smem_raw, int64_t tile0, int64_t tile_step,
+                                          double* acc)
 {
     constexpr int T = 1 << TB;  // paths per tile
     constexpr int TH = T / PP;  // threads per CTA; path p of thread t is tile column t + p * TH
     constexpr int FS = 2 * NA;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     const Smem S = carve(smem_raw, P, T);
     const int t = threadIdx.x;
     const int stride = T + 1;
     __shared__ int s_cancel;
 
-    double* acc = P.acc + (size_t)blockIdx.x * P.n_acc;
     for (int j = t; j < P.n_acc; j += TH) acc[j] = 0.0;
 
     // uniform step constants (UNIFORM: step 1's for every step)
@@ -827,7 +893,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
     int cancel_ahead = (t == 0 && P.cancel != nullptr) ? *P.cancel : 0;
     int ntile = 0;        // tiles done by this CTA
     int64_t nvalid = 0;   // valid paths of those tiles (few-product mode)
-    for (int64_t tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
+    for (int64_t tile = tile0; tile < P.n_tiles; tile += tile_step) {
         const int64_t m = P.tile_first + tile;
         uint64_t n[PP];
         bool valid[PP];
@@ -845,7 +911,7 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
         __syncthreads();
         if (s_cancel) {
             if (t == 0) atomicExch(P.status, 1);
-            return;
+            return false;
         }
         SobolLane<T, PP> L = sobol_lane<TB, PP>(P, S.hs, m);
 
@@ -900,9 +966,9 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
         for (int a0 = 0; a0 < n_pass; ++a0) {
             if constexpr (NA == 1 && PP == 2) {
                 if (P.use_sobol && P.sobol_dims >= P.n_steps * P.ref_factors && !P.path_out)
-                    pair_pass<TB, MODEL, UNIFORM, true>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
+                    pair_pass<TB, MODEL, UNIFORM, true, !BATCH>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0]);
                 else
-                    pair_pass<TB, MODEL, UNIFORM, false>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0], apply_events);
+                    pair_pass<TB, MODEL, UNIFORM, false, !BATCH>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0]);
                 continue;
             }
             // ---- path state -------------------------------------------------
@@ -1349,6 +1415,76 @@ __global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) 
             acc[idx] = d1 + n * c;
             acc[idx + 1] = d2 + 2.0 * c * d1 + n * c * c;
         }
+    }
+    return true;
+}
+
+template <int TB, int NA, int MODEL, bool UNIFORM, int PP>
+__global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, NA, PP>::value) book_kernel(const DevPlan P)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    book_body<TB, NA, MODEL, UNIFORM, PP>(P, smem_raw, blockIdx.x, gridDim.x, P.acc + (size_t)blockIdx.x * P.n_acc);
+}
+
+// ---------------------------------------------------------------------------
+// Ragged batches in one persistent launch. Work item r of a book is what CTA r of
+// the book's own launch does (its tiles r, r + grid, ..., its row r of FP64 sums),
+// so a batch prices every book bit for bit as its own launch at the same grid
+// would. The items sit in one list: books in decreasing item cost, a book's
+// items consecutive. Resident CTAs take the next item from a counter in global
+// memory, so the largest items go first and the small ones fill the tail; a CTA
+// keeps the current book's plan in shared memory while its items follow on.
+// ---------------------------------------------------------------------------
+template <int TB, int PP>
+__global__ void __launch_bounds__((1 << TB) / PP, MinBlocks<TB, 1, PP>::value)
+    batch_kernel(const DevPlan* __restrict__ plans, const BatchBook* __restrict__ books, int n_books, int n_items,
+                 int* next)
+{
+    constexpr int TH = (1 << TB) / PP;
+    static_assert(sizeof(DevPlan) % 8 == 0, "plans are copied in 8-byte words");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(16) DevPlan sp;
+    __shared__ int s_item, s_book, s_cur; // s_cur: the book whose plan is in sp
+    const int t = threadIdx.x;
+    if (t == 0) s_cur = -1;
+    for (;;) {
+        __syncthreads(); // the previous item is done with shared memory
+        if (t == 0) {
+            const int j = atomicAdd(next, 1);
+            int lo = 0;
+            if (j < n_items) { // the last book whose first item is at or before j
+                int hi = n_books - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (__ldg(&books[mid].first) <= j) lo = mid;
+                    else hi = mid - 1;
+                }
+            }
+            s_item = j;
+            s_book = lo;
+        }
+        __syncthreads();
+        const int j = s_item, k = s_book;
+        if (j >= n_items) break;
+        const BatchBook bk = books[k];
+        if (k != s_cur) { // nothing but shared memory carries over from one item to the next
+            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(plans + bk.plan);
+            unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sp);
+            for (int w = t; w < (int)(sizeof(DevPlan) / 8); w += TH) dst[w] = __ldg(src + w);
+            __syncthreads();
+            if (t == 0) s_cur = k;
+        }
+        const int r = j - bk.first;
+        double* acc = sp.acc + (size_t)r * sp.n_acc;
+        bool ok = true;
+        switch (bk.variant) {
+        case 0: ok = book_body<TB, 1, M_GBM, false, PP, true>(sp, smem_raw, r, bk.grid, acc); break;
+        case 1: ok = book_body<TB, 1, M_HESTON, false, PP, true>(sp, smem_raw, r, bk.grid, acc); break;
+        case 2: ok = book_body<TB, 1, M_LSV, false, PP, true>(sp, smem_raw, r, bk.grid, acc); break;
+        case 4: ok = book_body<TB, 1, M_HESTON, true, PP, true>(sp, smem_raw, r, bk.grid, acc); break;
+        default: ok = book_body<TB, 1, M_GBM, true, PP, true>(sp, smem_raw, r, bk.grid, acc); break;
+        }
+        if (!ok) break; // the book's cancel word is set: this CTA stops
     }
 }
 

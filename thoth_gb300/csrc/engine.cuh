@@ -183,6 +183,30 @@ struct DevPlan {
     int* status;                 // device status word
 };
 
+// ragged batches in one persistent launch (batch_kernel): a book of the work list, its
+// items r = 0 .. grid - 1 being what CTAs r of the book's own launch do
+struct alignas(16) BatchBook {
+    int plan;    // index into the plans
+    int variant; // 0 GBM, 1 Heston, 2 LSV, 4 Heston with uniform steps, 5 GBM with uniform steps
+    int grid;    // the book's own grid: its work items and the stride between an item's tiles
+    int first;   // list index of the book's item 0
+};
+
+// the variants the batch kernel runs (single-asset books in the (8, 2) launch shape)
+__host__ __device__ constexpr bool batch_variant(int v) { return v == 0 || v == 1 || v == 2 || v == 4 || v == 5; }
+
+// one book's fixed-order reduction of its rows, and its gather of low Sobol words, in a batch
+struct alignas(16) BatchReduce {
+    const double* acc;
+    double* out;
+    int rows, n_acc;
+};
+struct alignas(16) BatchGather {
+    const int* order;
+    uint32_t* out;
+    int n, T;
+};
+
 // ---------------------------------------------------------------------------
 // Inverse normal CDF in FP32 for a uniform u = x * 2^-32, x a nonzero uint32.
 // Method: Giles (2010, "Approximating the erfinv function") change of variable

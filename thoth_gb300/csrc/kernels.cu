@@ -30,6 +30,35 @@ __global__ void __launch_bounds__(32 * REDUCE_GROUPS)
     }
 }
 
+// the same reduction for every book of a batch at once: block (x, y) sums columns
+// 32 x .. 32 x + 31 of book y's rows
+__global__ void __launch_bounds__(32 * REDUCE_GROUPS) reduce_rows_batch(const BatchReduce* __restrict__ jobs)
+{
+    __shared__ double part[REDUCE_GROUPS][33];
+    const BatchReduce J = jobs[blockIdx.y];
+    if ((int)blockIdx.x * 32 >= J.n_acc) return; // uniform over the block
+    const int c = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + c;
+    double s = 0.0;
+    if (j < J.n_acc)
+        for (int r = g; r < J.rows; r += REDUCE_GROUPS) s += J.acc[(size_t)r * J.n_acc + j];
+    part[g][c] = s;
+    __syncthreads();
+    if (g == 0 && j < J.n_acc) {
+        double t = 0.0;
+        for (int k = 0; k < REDUCE_GROUPS; ++k) t += part[k][c];
+        J.out[j] = t;
+    }
+}
+
+cudaError_t launch_reduce_batch(const void* jobs, int n_books, int max_acc, cudaStream_t st)
+{
+    if (n_books == 0) return cudaSuccess;
+    const dim3 grid((unsigned)((max_acc + 31) / 32), (unsigned)n_books);
+    reduce_rows_batch<<<grid, 32 * REDUCE_GROUPS, 0, st>>>(reinterpret_cast<const BatchReduce*>(jobs));
+    return cudaGetLastError();
+}
+
 // the book's low Sobol words in consumption order: out[j][t] = lo_all[order[j]][t]
 __global__ void gather_low_kernel(const uint32_t* __restrict__ lo_all, const int* __restrict__ order, int n, int T,
                                   uint32_t* __restrict__ out)
@@ -45,6 +74,29 @@ cudaError_t launch_gather_low(const uint32_t* lo_all, const int* order, int n, i
     const int64_t total = (int64_t)n * T;
     if (total == 0) return cudaSuccess;
     gather_low_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(lo_all, order, n, T, out);
+    return cudaGetLastError();
+}
+
+// the same gather for every book of a batch at once: blocks (., y) stride over book y's words
+constexpr int GATHER_BATCH_BLOCKS = 32;
+
+__global__ void __launch_bounds__(256) gather_low_batch_kernel(const uint32_t* __restrict__ lo_all,
+                                                               const BatchGather* __restrict__ jobs)
+{
+    const BatchGather J = jobs[blockIdx.y];
+    const int64_t total = (int64_t)J.n * J.T;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i / J.T), t = (int)(i % J.T);
+        J.out[i] = __ldg(lo_all + (size_t)__ldg(J.order + j) * SOBOL_LO_ROW + t);
+    }
+}
+
+cudaError_t launch_gather_low_batch(const uint32_t* lo_all, const void* jobs, int n_books, cudaStream_t st)
+{
+    if (n_books == 0) return cudaSuccess;
+    gather_low_batch_kernel<<<dim3(GATHER_BATCH_BLOCKS, (unsigned)n_books), 256, 0, st>>>(
+        lo_all, reinterpret_cast<const BatchGather*>(jobs));
     return cudaGetLastError();
 }
 

@@ -38,6 +38,13 @@ cudaError_t launch_sobol_points(const uint32_t* V, int dims, int64_t skip, int64
 cudaError_t launch_quantile(const uint32_t* x, int64_t n, float* out, cudaStream_t st);
 cudaError_t launch_bridge(const DevPlan& P, int grid, size_t smem, float* out, cudaStream_t st);
 cudaError_t launch_gather_low(const uint32_t* lo_all, const int* order, int n, int T, uint32_t* out, cudaStream_t st);
+cudaError_t launch_gather_low_batch(const uint32_t* lo_all, const void* jobs, int n_books, cudaStream_t st);
+cudaError_t launch_reduce_batch(const void* jobs, int n_books, int max_acc, cudaStream_t st);
+int batch_threads();
+int batch_tile_paths();
+int batch_occupancy(size_t smem);
+cudaError_t launch_batch_kernel(const DevPlan* plans, const BatchBook* books, int n_books, int n_items, int* next,
+                                int grid, size_t smem, cudaStream_t st);
 cudaError_t launch_fma_peak(float* out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_mufu_peak(float* out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_tc_gemm_test(const void* A, const void* B, int N, int K, float* D, int* status, cudaStream_t st);
@@ -1662,15 +1669,22 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
 }
 
 // ---------------------------------------------------------------------------
-// Ragged batches: every book's plan in one upload, each book's kernel and
-// reduction launched on one of several streams, the whole batch captured once
+// Ragged batches: every book's plan in one upload, the whole batch captured once
 // into a CUDA graph and replayed while the batch's shapes repeat, all sums back
-// in one copy.
+// in one copy. By default the single-asset books run in one persistent launch
+// (batch_kernel): one work list of every book's items (item r of a book = what
+// CTA r of the book's own launch does), largest items first, taken by resident
+// CTAs from a counter; one gather of the books' low Sobol words before it and
+// one fixed-order reduction of all books' rows after it. Books that kernel does
+// not run (several assets, or more shared memory than keeps its CTAs resident)
+// get their own launches on side streams meanwhile. The other mode launches each
+// book's gather, kernel and reduction on one of several streams.
 // ---------------------------------------------------------------------------
 struct BatchCache {
     int streams_wanted = 8;
-    int policy = 0; // grid policy of every book in the batch (grid_policy)
-    int shape = -1; // launch shape of every single-asset book (-1: each book's tuned or default shape)
+    int policy = 0;     // grid policy of every book in the batch (grid_policy)
+    int shape = -1;     // per-book mode: launch shape of every single-asset book (-1: each book's own)
+    int persistent = 1; // 1: the single-asset books in one persistent launch
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
     cudaGraphExec_t exec = nullptr;
@@ -1680,6 +1694,7 @@ struct BatchCache {
     unsigned char* host = nullptr; // pinned
     size_t host_size = 0;
     int replays = 0;
+    int launches = 0; // kernel launches recorded into the cached graph
 };
 static BatchCache g_batch;
 
@@ -1696,36 +1711,83 @@ static int ensure_batch_streams()
     return THOTH_GPU_OK;
 }
 
-// the batch's device work as recorded into the graph: zero the status words,
-// fork onto S streams, each book's kernel and reduction on the stream chosen by
-// a longest-processing-time schedule (books by decreasing path-steps, each onto
-// the stream with the least work so far), join
+// the persistent launch of a batch: its books (positions into the plans, decreasing item
+// cost), grid and shared memory, and where its tables sit in the batch's device buffer
+struct BatchLaunch {
+    std::vector<int> books;
+    std::vector<char> member; // [n] 1: the book runs in the persistent launch
+    int items = 0, grid = 0, max_acc = 0;
+    size_t smem = 0;
+    size_t o_plans = 0, o_books = 0, o_gather = 0, o_reduce = 0, o_next = 0;
+};
+
+static double batch_cost(const Plan& P) { return (double)P.paths * P.dp.n_steps * std::max(1, P.dp.n_assets); }
+
+// the cost of one work item of a book in the persistent launch: its tiles x steps, weighted
+// by the model's arithmetic per path-step (GBM one normal, Heston two and the QE step, LSV
+// those and the leverage lookup)
+static double item_cost(const Plan& P, int grid)
+{
+    const double w = (P.variant == 0 || P.variant == 5) ? 1.0 : P.variant == 2 ? 4.0 : 3.0;
+    const double tiles = (double)((P.dp.n_tiles + grid - 1) / std::max(grid, 1));
+    return tiles * P.T * P.dp.n_steps * w;
+}
+
+// the batch's device work as recorded into the graph: zero the status words (and the work
+// counter), then either the persistent launch with the other books on side streams, or each
+// book's gather, kernel and reduction on the stream chosen by a longest-processing-time
+// schedule (books by decreasing path-steps, each onto the stream with the least work so far)
 static int record_batch(std::vector<Plan>& plans, const std::vector<int>& grid, const std::vector<size_t>& o_out,
-                        size_t o_sts, int S, cudaStream_t st)
+                        size_t o_sts, int S, cudaStream_t st, const BatchLaunch* BL)
 {
     const int n = (int)plans.size();
-    CUDA_TRY(cudaMemsetAsync(g_batch.dev + o_sts, 0, sizeof(int) * (size_t)n, st));
-    CUDA_TRY(cudaEventRecord(g_batch.events[0], st));
-    for (int k = 0; k < S; k++) CUDA_TRY(cudaStreamWaitEvent(g_batch.streams[k], g_batch.events[0], 0));
-    std::vector<int> order(n);
-    for (int b = 0; b < n; b++) order[b] = b;
-    auto cost = [&](int b) { return (double)plans[b].paths * plans[b].dp.n_steps * std::max(1, plans[b].dp.n_assets); };
-    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return cost(a) > cost(c); });
-    std::vector<double> load(S, 0.0);
-    for (int j = 0; j < n; j++) {
-        const int b = order[j];
-        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[k] += cost(b);
-        cudaStream_t s = g_batch.streams[k];
-        CUDA_TRY(gather_low(plans[b], s));
-        CUDA_TRY(launch_book(plans[b].dp, plans[b].variant, plans[b].shape, grid[b], plans[b].smem, s));
-        CUDA_TRY(launch_reduce(plans[b].dp.acc, grid[b], plans[b].dp.n_acc,
-                               reinterpret_cast<double*>(g_batch.dev + o_out[b]), s));
+    int launches = 0;
+    CUDA_TRY(cudaMemsetAsync(g_batch.dev + o_sts, 0, sizeof(int) * (size_t)(n + 1), st));
+    std::vector<int> order;
+    for (int b = 0; b < n; b++)
+        if (!BL || !BL->member[b]) order.push_back(b);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int c) { return batch_cost(plans[a]) > batch_cost(plans[c]); });
+    if (BL) {
+        CUDA_TRY(launch_gather_low_batch(g_dev.sobol_lo, g_batch.dev + BL->o_gather, n, st));
+        launches++;
     }
-    for (int k = 0; k < S; k++) {
+    const int side = BL ? (int)std::min<size_t>(order.size(), (size_t)S) : S;
+    CUDA_TRY(cudaEventRecord(g_batch.events[0], st));
+    for (int k = 0; k < side; k++) CUDA_TRY(cudaStreamWaitEvent(g_batch.streams[k], g_batch.events[0], 0));
+    std::vector<double> load(std::max(side, 1), 0.0);
+    for (int b : order) {
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += batch_cost(plans[b]);
+        cudaStream_t s = g_batch.streams[k];
+        if (!BL) {
+            CUDA_TRY(gather_low(plans[b], s));
+            launches++;
+        }
+        CUDA_TRY(launch_book(plans[b].dp, plans[b].variant, plans[b].shape, grid[b], plans[b].smem, s));
+        launches++;
+        if (!BL) {
+            CUDA_TRY(launch_reduce(plans[b].dp.acc, grid[b], plans[b].dp.n_acc,
+                                   reinterpret_cast<double*>(g_batch.dev + o_out[b]), s));
+            launches++;
+        }
+    }
+    if (BL && !BL->books.empty()) {
+        CUDA_TRY(launch_batch_kernel(reinterpret_cast<const DevPlan*>(g_batch.dev + BL->o_plans),
+                                     reinterpret_cast<const BatchBook*>(g_batch.dev + BL->o_books),
+                                     (int)BL->books.size(), BL->items, reinterpret_cast<int*>(g_batch.dev + BL->o_next),
+                                     BL->grid, BL->smem, st));
+        launches++;
+    }
+    for (int k = 0; k < side; k++) {
         CUDA_TRY(cudaEventRecord(g_batch.events[k], g_batch.streams[k]));
         CUDA_TRY(cudaStreamWaitEvent(st, g_batch.events[k], 0));
     }
+    if (BL) {
+        CUDA_TRY(launch_reduce_batch(g_batch.dev + BL->o_reduce, n, BL->max_acc, st));
+        launches++;
+    }
+    g_batch.launches = launches;
     return THOTH_GPU_OK;
 }
 
@@ -1736,6 +1798,7 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
     if (n == 0) return THOTH_GPU_OK;
     rc = ensure_batch_streams();
     if (rc) return rc;
+    const bool pers = g_batch.persistent != 0 && n <= 65535; // the batched gather / reduction grids
     const int S = std::min(g_batch.streams_wanted, n);
     std::vector<Plan> plans(n);
     std::vector<int> grid(n);
@@ -1743,10 +1806,25 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
     size_t off = 0;
     auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
     std::string sig = std::to_string(n) + ":" + std::to_string(S) + ":" + std::to_string(g_batch.policy) + ":" +
-                      std::to_string(g_batch.shape);
+                      std::to_string(g_batch.shape) + ":" + std::to_string(pers ? 1 : 0);
+    // the persistent launch: the books it runs, those whose (8, 2) plan keeps its CTAs resident at
+    // their register-bound count; the others keep their own (tuned or default) shape and launch
+    const int full = pers ? batch_occupancy(0) : 0;
+    std::vector<char> member(n, 0);
+    auto joins = [&](const Plan& P) {
+        return full > 0 && batch_variant(P.variant) && P.shape == 0 && P.T == batch_tile_paths() &&
+               batch_occupancy(P.smem) >= full;
+    };
     for (int b = 0; b < n; b++) {
-        rc = build_plan(&books[b], plans[b], g_batch.shape);
+        rc = build_plan(&books[b], plans[b], pers ? -1 : g_batch.shape);
         if (rc) return fail(rc, "book " + std::to_string(b) + ": " + g_err);
+        if (pers && batch_variant(plans[b].variant) && plans[b].shape != 0) {
+            Plan q;
+            rc = build_plan(&books[b], q, 0);
+            if (rc) return fail(rc, "book " + std::to_string(b) + ": " + g_err);
+            if (joins(q)) plans[b] = std::move(q);
+        }
+        member[b] = pers && joins(plans[b]);
         grid[b] = grid_for(plans[b], g_batch.policy);
         o_blob[b] = off;
         off += up(plans[b].blob.bytes.size());
@@ -1759,7 +1837,34 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
                std::to_string(plans[b].smem) + "," + std::to_string(plans[b].blob.bytes.size()) + "," +
                std::to_string(plans[b].dp.n_acc) + "," + std::to_string(plans[b].dp.n_tiles);
     }
-    // outputs and status words contiguous at the end: one device->host copy
+    // the persistent launch: its books' work-list order, its grid and its tables
+    BatchLaunch BL;
+    if (pers) {
+        BL.member = member;
+        for (int b = 0; b < n; b++)
+            if (member[b]) {
+                BL.books.push_back(b);
+                BL.smem = std::max(BL.smem, plans[b].smem);
+            }
+        std::stable_sort(BL.books.begin(), BL.books.end(), [&](int a, int c) {
+            return item_cost(plans[a], grid[a]) > item_cost(plans[c], grid[c]);
+        });
+        for (int b : BL.books) BL.items += grid[b];
+        BL.grid = std::max(1, std::min(full * g_dev.sms, BL.items));
+        for (int b = 0; b < n; b++) BL.max_acc = std::max(BL.max_acc, plans[b].dp.n_acc);
+        BL.o_plans = off;
+        off += up(sizeof(DevPlan) * BL.books.size());
+        BL.o_books = off;
+        off += up(sizeof(BatchBook) * BL.books.size());
+        BL.o_gather = off;
+        off += up(sizeof(BatchGather) * (size_t)n);
+        BL.o_reduce = off;
+        off += up(sizeof(BatchReduce) * (size_t)n);
+        sig += "|persistent " + std::to_string(BL.grid) + "," + std::to_string(BL.smem) + "," +
+               std::to_string(BL.items);
+        for (int b : BL.books) sig += "," + std::to_string(b);
+    }
+    // outputs and status words (then the work counter) contiguous at the end: one device->host copy
     const size_t o_outs = off;
     size_t cur = o_outs;
     for (int b = 0; b < n; b++) {
@@ -1769,7 +1874,8 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
     cur = up(cur);
     const size_t o_sts = cur;
     for (int b = 0; b < n; b++) o_st[b] = o_sts + sizeof(int) * (size_t)b;
-    const size_t total = o_sts + up(sizeof(int) * (size_t)n);
+    BL.o_next = o_sts + sizeof(int) * (size_t)n;
+    const size_t total = o_sts + up(sizeof(int) * (size_t)(n + 1));
     const size_t back = total - o_outs;
     // device and pinned buffers (a new size invalidates the cached graph)
     if (total > g_batch.dev_size) {
@@ -1789,11 +1895,8 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
         CUDA_TRY(host_alloc(&g_batch.host, std::max(o_outs, back)));
         g_batch.host_size = std::max(o_outs, back);
     }
-    for (int b = 0; b < n; b++)
-        std::memcpy(g_batch.host + o_blob[b], plans[b].blob.bytes.data(), plans[b].blob.bytes.size());
-    cudaStream_t st = g_dev.stream;
-    CUDA_TRY(cudaMemcpyAsync(g_batch.dev, g_batch.host, o_outs, cudaMemcpyHostToDevice, st));
     for (int b = 0; b < n; b++) {
+        std::memcpy(g_batch.host + o_blob[b], plans[b].blob.bytes.data(), plans[b].blob.bytes.size());
         bind(plans[b], g_batch.dev + o_blob[b]);
         plans[b].dp.sobol_lo = reinterpret_cast<const uint32_t*>(g_batch.dev + o_lo[b]);
         plans[b].dp.acc = reinterpret_cast<double*>(g_batch.dev + o_acc[b]);
@@ -1801,6 +1904,26 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
         // the kernel parameters are baked into the graph: a replay needs them byte-equal
         sig.append(reinterpret_cast<const char*>(&plans[b].dp), sizeof(DevPlan));
     }
+    if (pers) {
+        // the persistent launch's tables, uploaded with the plans
+        int first = 0;
+        for (size_t k = 0; k < BL.books.size(); k++) {
+            const int b = BL.books[k];
+            std::memcpy(g_batch.host + BL.o_plans + sizeof(DevPlan) * k, &plans[b].dp, sizeof(DevPlan));
+            BatchBook bb{(int)k, plans[b].variant, grid[b], first};
+            std::memcpy(g_batch.host + BL.o_books + sizeof(BatchBook) * k, &bb, sizeof bb);
+            first += grid[b];
+        }
+        for (int b = 0; b < n; b++) {
+            const Plan& P = plans[b];
+            BatchGather g{P.dp.sobol_order, const_cast<uint32_t*>(P.dp.sobol_lo), P.dp.n_sobol, P.T};
+            std::memcpy(g_batch.host + BL.o_gather + sizeof(BatchGather) * (size_t)b, &g, sizeof g);
+            BatchReduce r{P.dp.acc, reinterpret_cast<double*>(g_batch.dev + o_out[b]), grid[b], P.dp.n_acc};
+            std::memcpy(g_batch.host + BL.o_reduce + sizeof(BatchReduce) * (size_t)b, &r, sizeof r);
+        }
+    }
+    cudaStream_t st = g_dev.stream;
+    CUDA_TRY(cudaMemcpyAsync(g_batch.dev, g_batch.host, o_outs, cudaMemcpyHostToDevice, st));
     if (g_batch.signature != sig || !g_batch.exec) {
         if (g_batch.exec) cudaGraphExecDestroy(g_batch.exec);
         g_batch.exec = nullptr;
@@ -1808,7 +1931,7 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
         // kernel attributes are set outside the capture
         for (int b = 0; b < n; b++) occupancy_of(plans[b]);
         CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        rc = record_batch(plans, grid, o_out, o_sts, S, st);
+        rc = record_batch(plans, grid, o_out, o_sts, S, st, pers ? &BL : nullptr);
         cudaGraph_t graph = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(st, &graph); // always leave capture mode
         if (rc) {
@@ -1952,6 +2075,7 @@ static int autotune_book_locked(const ThothBookDesc* book, int reps, ThothTuneRe
         out->tile_paths = best_plan.T;
         out->best_ms = best;
         out->default_ms = def_ms;
+        out->persistent = 0;
     }
     return THOTH_GPU_OK;
 }
@@ -1960,8 +2084,10 @@ static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, Th
 {
     std::vector<ThothBookResult> res(std::max(n, 1));
     std::memset(res.data(), 0, sizeof(ThothBookResult) * res.size());
-    const int keep_s = g_batch.streams_wanted, keep_p = g_batch.policy, keep_h = g_batch.shape;
-    auto time_one = [&](int S, int pol, int shape, double* ms) {
+    const int keep_s = g_batch.streams_wanted, keep_p = g_batch.policy, keep_h = g_batch.shape,
+              keep_x = g_batch.persistent;
+    auto time_one = [&](int X, int S, int pol, int shape, double* ms) {
+        g_batch.persistent = X;
         g_batch.streams_wanted = S;
         g_batch.policy = pol;
         g_batch.shape = shape;
@@ -1977,48 +2103,65 @@ static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, Th
         return THOTH_GPU_OK;
     };
     double best = 1e300, def_ms = 0;
-    int best_s = keep_s, best_p = 0, best_h = -1, count = 0;
+    int best_s = keep_s, best_p = 0, best_h = -1, best_x = 1, count = 0;
     auto restore = [&](int rc) {
+        g_batch.persistent = keep_x;
         g_batch.streams_wanted = keep_s;
         g_batch.policy = keep_p;
         g_batch.shape = keep_h;
         return rc;
     };
-    // 1. stream count, with each book's own shape and the full grid
+    auto consider = [&](double ms, int X, int S, int pol, int shape) {
+        count++;
+        if (ms < best) {
+            best = ms;
+            best_x = X;
+            best_s = S;
+            best_p = pol;
+            best_h = shape;
+        }
+    };
+    // 1. the persistent launch (the default) under each grid policy of its books
+    for (int pol : {0, 1, 2}) {
+        double ms;
+        const int rc = time_one(1, keep_s, pol, -1, &ms);
+        if (rc) return restore(rc);
+        if (pol == 0) def_ms = ms;
+        consider(ms, 1, keep_s, pol, -1);
+    }
+    // 2. one launch per book: stream count, with each book's own shape and the full grid
+    int per_s = keep_s;
+    double per_best = 1e300;
     for (int S : {1, 2, 4, 8, 16, 32}) {
         if (S > std::max(n, 1) && S != 1) break;
         double ms;
-        const int rc = time_one(S, 0, -1, &ms);
+        const int rc = time_one(0, S, 0, -1, &ms);
         if (rc) return restore(rc);
-        count++;
-        if (S == 8 || (n < 8 && S == 1)) def_ms = ms;
-        if (ms < best) {
-            best = ms;
-            best_s = S;
+        consider(ms, 0, S, 0, -1);
+        if (ms < per_best) {
+            per_best = ms;
+            per_s = S;
         }
     }
-    // 2. one launch shape for every single-asset book
+    // 3. one launch shape for every single-asset book, then the grid policy
+    int per_h = -1;
     for (int h = 0; h < 4; h++) {
         double ms;
-        const int rc = time_one(best_s, 0, h, &ms);
+        const int rc = time_one(0, per_s, 0, h, &ms);
         if (rc) return restore(rc);
-        count++;
-        if (ms < best) {
-            best = ms;
-            best_h = h;
+        consider(ms, 0, per_s, 0, h);
+        if (ms < per_best) {
+            per_best = ms;
+            per_h = h;
         }
     }
-    // 3. grid policy
     for (int pol : {1, 2}) {
         double ms;
-        const int rc = time_one(best_s, pol, best_h, &ms);
+        const int rc = time_one(0, per_s, pol, per_h, &ms);
         if (rc) return restore(rc);
-        count++;
-        if (ms < best) {
-            best = ms;
-            best_p = pol;
-        }
+        consider(ms, 0, per_s, pol, per_h);
     }
+    g_batch.persistent = best_x;
     g_batch.streams_wanted = best_s;
     g_batch.policy = best_p;
     g_batch.shape = best_h;
@@ -2033,6 +2176,7 @@ static int autotune_batch_locked(const ThothBookDesc* books, int n, int reps, Th
         out->tile_paths = 0;
         out->best_ms = best;
         out->default_ms = def_ms;
+        out->persistent = best_x;
     }
     return THOTH_GPU_OK;
 }
@@ -2045,7 +2189,8 @@ static int autotune_save_locked(const char* path)
     FILE* f = std::fopen(path, "w");
     if (!f) return fail(THOTH_GPU_E_INVALID, std::string("cannot write ") + path);
     std::fprintf(f, "thoth-autotune 1\ndevice %d %s\n", g_dev.sms, g_dev.name.c_str());
-    std::fprintf(f, "batch %d %d %d\n", g_batch.streams_wanted, g_batch.policy, g_batch.shape);
+    std::fprintf(f, "batch %d %d %d %d\n", g_batch.streams_wanted, g_batch.policy, g_batch.shape,
+                 g_batch.persistent);
     for (const auto& kv : g_tuned)
         std::fprintf(f, "book %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
                      kv.second.shape, kv.second.per_sm, kv.second.policy);
@@ -2063,14 +2208,19 @@ static int autotune_load_locked(const char* path)
     int version = 0, sms = -1;
     std::string name;
     std::map<TuneKey, TuneChoice> books;
-    int streams = g_batch.streams_wanted, policy = g_batch.policy, bshape = g_batch.shape;
+    int streams = g_batch.streams_wanted, policy = g_batch.policy, bshape = g_batch.shape, pers = g_batch.persistent;
     bool bad = false;
     while (std::fgets(line, sizeof line, f)) {
         int a, b, c, e, g, h;
         char nm[400];
         if (std::sscanf(line, "thoth-autotune %d", &a) == 1) version = a;
         else if (std::sscanf(line, "device %d %399[^\n]", &a, nm) == 2) { sms = a; name = nm; }
-        else if (std::sscanf(line, "batch %d %d %d", &a, &b, &c) == 3) { streams = a; policy = b; bshape = c; }
+        else if (std::sscanf(line, "batch %d %d %d %d", &a, &b, &c, &e) == 4) {
+            streams = a;
+            policy = b;
+            bshape = c;
+            pers = e;
+        } else if (std::sscanf(line, "batch %d %d %d", &a, &b, &c) == 3) { streams = a; policy = b; bshape = c; }
         else if (std::sscanf(line, "batch %d %d", &a, &b) == 2) { streams = a; policy = b; bshape = -1; }
         else if (std::sscanf(line, "book %d %d %d %d %d %d", &a, &b, &c, &e, &g, &h) == 6) {
             if (a < 0 || a > 6 || e < 0 || e >= book_shape_count(a) || g < 0 || h < 0 || h > 1) bad = true;
@@ -2083,7 +2233,7 @@ static int autotune_load_locked(const char* path)
     }
     std::fclose(f);
     if (version != 1 || bad || streams < 1 || streams > 64 || policy < 0 || policy > 2 || bshape < -1 ||
-        bshape >= book_shape_count(0))
+        bshape >= book_shape_count(0) || pers < 0 || pers > 1)
         return fail(THOTH_GPU_E_INVALID, std::string("malformed autotune file ") + path);
     if (sms != g_dev.sms || name != g_dev.name)
         return fail(THOTH_GPU_E_UNSUPPORTED, "autotune file was measured on another device (" + name + ")");
@@ -2091,6 +2241,7 @@ static int autotune_load_locked(const char* path)
     g_batch.streams_wanted = streams;
     g_batch.policy = policy;
     g_batch.shape = bshape;
+    g_batch.persistent = pers;
     return THOTH_GPU_OK;
 }
 
@@ -2334,6 +2485,7 @@ int thoth_gpu_autotune_clear(void)
         g_batch.streams_wanted = 8;
         g_batch.policy = 0;
         g_batch.shape = -1;
+        g_batch.persistent = 1;
         return THOTH_GPU_OK;
     } catch (const std::bad_alloc&) {
         return fail(THOTH_GPU_E_NOMEM, "out of host memory");
@@ -2834,6 +2986,32 @@ int thoth_gpu_price_batch(const ThothBookDesc* books, int32_t n_books, ThothBook
         if (!books || !out || n_books < 0) return fail(THOTH_GPU_E_INVALID, "bad batch");
         std::lock_guard<std::mutex> lk(g_mu);
         return price_batch_locked(books, n_books, out);
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_batch_persistent(int32_t on)
+{
+    try {
+        if (on < 0 || on > 1) return fail(THOTH_GPU_E_INVALID, "persistent must be 0 or 1");
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_batch.persistent = on;
+        return THOTH_GPU_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(THOTH_GPU_E_NOMEM, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(THOTH_GPU_E_INVALID, std::string("host error: ") + e.what());
+    }
+}
+
+int thoth_gpu_batch_launches(void)
+{
+    try {
+        std::lock_guard<std::mutex> lk(g_mu);
+        return g_batch.exec ? g_batch.launches : 0;
     } catch (const std::bad_alloc&) {
         return fail(THOTH_GPU_E_NOMEM, "out of host memory");
     } catch (const std::exception& e) {
