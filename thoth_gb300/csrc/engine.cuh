@@ -61,7 +61,7 @@ struct StepProg {
     int first, count;
 };
 
-// per-step record read once per step (prefetched one step ahead): the first
+// per-step record read at the start of each step: the first
 // bridge node inline, the node count (0 = pop), the remaining nodes' start,
 // 1/sqrt(dt) of the path generator, and whether any asset has events this date
 struct alignas(16) StepRec {
@@ -154,7 +154,7 @@ struct DevPlan {
     const AssetStep* steps;      // [n_steps][n_assets]   (index i-1 for step i)
     const float* inv_sqrt_dt;    // [n_steps] path-generator 1/sqrt(t_i - t_{i-1})
     const StepProg* prog;        // [n_steps]
-    const StepRec* recs;         // [n_steps + 1] (the last is padding for the load one step ahead)
+    const StepRec* recs;         // [n_steps]
     int uniform_steps;           // 1: every step's AssetStep equals step 1's
     const BridgeNode* nodes;     // time-ordered program
     const int2* ev_range;        // [(n_steps + 1)][n_assets] (first, count) into events; row 0 = date 0
