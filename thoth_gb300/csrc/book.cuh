@@ -667,8 +667,10 @@ __device__ __forceinline__ void pair_events(const DevPlan& P, const Smem& S, int
 }
 
 // FAST: the book is in Sobol mode with every dimension a Sobol dimension, and stores no paths.
-// Each step's record is loaded at the step: loading it one step ahead holds eight more registers
-// across the step and measured slower (2.75 against 2.93 ms for the 2^20-path Heston grid).
+// There each step's record is loaded at the step: loading it one step ahead holds eight more
+// registers across the step and measured slower (2.93 against 2.75 ms for the 2^20-path Heston
+// grid). The other pass loads it one step ahead, which measured faster where the paths are
+// stored (GBM, 2^20 paths x 252 steps: 1.11 against 1.23 ms).
 template <int TB, int MODEL, bool UNIFORM, bool FAST>
 __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairLane& L,
                                           const uint64_t (&n)[2], const bool (&valid)[2], int a0, float4 u0,
@@ -701,8 +703,16 @@ __device__ __forceinline__ void pair_pass(const DevPlan& P, const Smem& S, PairL
         for (int p = 0; p < 2; ++p)
             if (valid[p]) P.path_out[n[p] - (uint64_t)P.skip - 1] = P.s0[aid];
 
+    StepRec rec;
+    if constexpr (!FAST) rec = load_rec(P, 1);
     for (int i = 1; i <= P.n_steps; ++i) {
-        const StepRec cur = load_rec(P, i);
+        StepRec cur;
+        if constexpr (FAST) {
+            cur = load_rec(P, i);
+        } else {
+            cur = rec;
+            rec = load_rec(P, i + 1); // the record past the last step is padding
+        }
         // this step's constants, requested before the bridge work that covers their latency
         float4 c0 = u0, c1 = u1, c2 = u2, c3 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (!UNIFORM) {
@@ -957,7 +967,9 @@ __device__ __forceinline__ bool book_body(const DevPlan& P, unsigned char* smem_
         PairLane PL = pair_lane<T>(P, S.hs, m); // unused (and dropped) unless NA == 1 and PP == 2
         for (int a0 = 0; a0 < n_pass; ++a0) {
             if constexpr (NA == 1 && PP == 2) {
-                if (P.use_sobol && P.sobol_dims >= P.n_steps * P.ref_factors && !P.path_out)
+                // both passes in one kernel: the fast pass's own instantiation measured slower
+                // (Heston grid 2.91 against 2.75 ms, same box)
+                if (fast_pass(P))
                     pair_pass<TB, MODEL, UNIFORM, true>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0]);
                 else
                     pair_pass<TB, MODEL, UNIFORM, false>(P, S, PL, n, valid, a0, u0[0], u1[0], u2[0]);

@@ -61,7 +61,7 @@ struct StepProg {
     int first, count;
 };
 
-// per-step record read at the start of each step: the first
+// per-step record read once per step (at the step, or one step ahead): the first
 // bridge node inline, the node count (0 = pop), the remaining nodes' start,
 // 1/sqrt(dt) of the path generator, and whether any asset has events this date
 struct alignas(16) StepRec {
@@ -154,7 +154,7 @@ struct DevPlan {
     const AssetStep* steps;      // [n_steps][n_assets]   (index i-1 for step i)
     const float* inv_sqrt_dt;    // [n_steps] path-generator 1/sqrt(t_i - t_{i-1})
     const StepProg* prog;        // [n_steps]
-    const StepRec* recs;         // [n_steps]
+    const StepRec* recs;         // [n_steps + 1] (the last is padding for a load one step ahead)
     int uniform_steps;           // 1: every step's AssetStep equals step 1's
     const BridgeNode* nodes;     // time-ordered program
     const int2* ev_range;        // [(n_steps + 1)][n_assets] (first, count) into events; row 0 = date 0
@@ -194,6 +194,13 @@ struct alignas(16) BatchBook {
 
 // the variants the batch kernel runs (single-asset books in the (8, 2) launch shape)
 __host__ __device__ constexpr bool batch_variant(int v) { return v == 0 || v == 1 || v == 2 || v == 4 || v == 5; }
+
+// a plan whose single-asset passes run the fast pair pass: Sobol mode with every dimension a
+// Sobol dimension, no stored paths
+__host__ __device__ inline bool fast_pass(const DevPlan& P)
+{
+    return P.use_sobol && P.sobol_dims >= P.n_steps * P.ref_factors && !P.path_out;
+}
 
 // one book's fixed-order reduction of its rows, and its gather of low Sobol words, in a batch
 struct alignas(16) BatchReduce {

@@ -369,12 +369,14 @@ bool build_bridge(const std::vector<double>& t, BridgeProgram& out, std::string&
     return true;
 }
 
-// per-step records: first node inline, node count, 1/sqrt(dt), event flag
+// per-step records: first node inline, node count, 1/sqrt(dt), event flag; one zero record
+// past the last step, which a load one step ahead reads at the last step
 std::vector<StepRec> make_recs(const BridgeProgram& bp, const std::vector<float>& isd, const std::vector<char>& ev_flag,
                                int ref_factors)
 {
     const size_t N = isd.size();
-    std::vector<StepRec> recs(N);
+    std::vector<StepRec> recs(N + 1);
+    std::memset(&recs[N], 0, sizeof(StepRec));
     for (size_t i = 0; i < N; i++) {
         StepRec& r = recs[i];
         std::memset(&r, 0, sizeof r);
