@@ -467,13 +467,17 @@ __global__ void sum_kernel(const float* x, int n, float* out)
     if (threadIdx.x == 0) *out = s[0];
 }
 
-// fused inference: persistent CTAs of two warpgroups. The weights are resident
-// in shared memory and shared by both; each warpgroup walks its own 128-cell
-// tiles with its own TMEM accumulator (128 columns each), mbarrier and named
-// barrier, so one warpgroup's bias + SiLU epilogue overlaps the other's MMAs.
-// The epilogue streams 16 accumulator columns at a time straight into the next
-// layer's A operand (K-major core-matrix layout); the last layer folds the head.
-constexpr int INFER_THREADS = 256;
+// fused inference: persistent CTAs of three warpgroups, one CTA per SM. The weights
+// are resident in shared memory and shared by all; each warpgroup walks its own
+// 128-cell tiles with its own TMEM accumulator (128 columns each), mbarrier and
+// named barrier, so the warpgroups' bias + SiLU epilogues overlap one another's
+// MMAs. The epilogue streams 16 accumulator columns at a time straight into the
+// next layer's A operand (K-major core-matrix layout); the last layer folds the head.
+// Three warpgroups: 208 KB of shared memory (the weights and three tiles of
+// activations) and 384 of the 512 TMEM columns.
+constexpr int INFER_WG = 3;
+constexpr int INFER_THREADS = 128 * INFER_WG;
+constexpr uint32_t INFER_TMEM_COLS = 512; // a power of two >= 128 x INFER_WG
 
 __device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
 
@@ -495,7 +499,7 @@ __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat1
                                                               float* __restrict__ y, int* status)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ uint64_t mbar[2];
+    __shared__ uint64_t mbar[INFER_WG];
     __shared__ uint32_t tm_s;
     __shared__ __align__(16) float sb[4 * H + H + 1]; // biases of layers 1..4, head weights, head bias (pairs read as float2)
     unsigned char* sW1 = sm;                         // 128 x 16
@@ -503,11 +507,9 @@ __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat1
     const int t = threadIdx.x, warp = t >> 5, wg = t >> 7, r = t & 127;
     unsigned char* sX = sW + 3 * H * H * 2 + wg * (ROWS * KIN * 2 + ROWS * H * 2); // this warpgroup's 128 x 16
     unsigned char* sAct = sX + ROWS * KIN * 2;                                    // and 128 x 128
-    if (warp == 0) tc::tmem_alloc(&tm_s, 256);
-    if (t == 0) {
-        tc::mbar_init(&mbar[0], 1);
-        tc::mbar_init(&mbar[1], 1);
-    }
+    if (warp == 0) tc::tmem_alloc(&tm_s, INFER_TMEM_COLS);
+    if (t == 0)
+        for (int w = 0; w < INFER_WG; ++w) tc::mbar_init(&mbar[w], 1);
     stage<H>(sW1, wbf + OFF_BF_W1, KIN, KIN, H);
     for (int l = 0; l < 3; ++l) stage<H>(sW + l * H * H * 2, wbf + OFF_BF_W2 + l * H * H, H, H, H);
     for (int i = t; i < 4 * H; i += INFER_THREADS) sb[i] = params[b_off(1 + i / H) + i % H];
@@ -519,7 +521,7 @@ __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat1
     Ctx c{&mbar[wg], tm_s + (uint32_t)(wg * 128), 0, status};
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16; // TMEM lanes of this warp
     const int tiles = (n + ROWS - 1) / ROWS;
-    for (int tile = 2 * blockIdx.x + wg; tile < tiles; tile += 2 * gridDim.x) {
+    for (int tile = INFER_WG * blockIdx.x + wg; tile < tiles; tile += INFER_WG * gridDim.x) {
         const int r0 = tile * ROWS;
         const int valid = min(ROWS, n - r0);
         // this warpgroup stages its input tile (row r by thread r: two 16-byte chunks)
@@ -590,7 +592,7 @@ __global__ void __launch_bounds__(INFER_THREADS) infer_kernel(const __nv_bfloat1
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tm_s, 256);
+    if (warp == 0) tc::tmem_dealloc(tm_s, INFER_TMEM_COLS);
 }
 
 } // namespace mlp
@@ -692,7 +694,7 @@ cudaError_t mlp_infer(const __nv_bfloat16* x, int n, const float* params, const 
                       int* status, int grid, cudaStream_t st)
 {
     using namespace mlp;
-    const size_t smem = (size_t)(H * KIN + 3 * H * H + 2 * (ROWS * KIN + ROWS * H)) * 2;
+    const size_t smem = (size_t)(H * KIN + 3 * H * H + INFER_WG * (ROWS * KIN + ROWS * H)) * 2;
     cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     infer_kernel<<<grid, INFER_THREADS, smem, st>>>(x, n, params, wbf, y, status);
