@@ -56,6 +56,31 @@ int main(void){
     assert got == want
 
 
+def test_every_abi_struct_matches_header_field_by_field():
+    """Every ctypes mirror in thoth_gb300/abi.py of a struct the header declares: its size and the
+    offset of each of its fields, as gcc lays the header's struct out."""
+    header = open(HEADER).read()
+    structs = [v for v in vars(abi).values() if isinstance(v, type) and issubclass(v, C.Structure)
+               and re.search(r"}\s*%s\s*;" % v.__name__, header)]
+    assert len(structs) >= 8
+    lines, want = [], []
+    for st in structs:
+        lines.append('printf("%%zu\\n", sizeof(%s));' % st.__name__)
+        want.append(C.sizeof(st))
+        for f in st._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (st.__name__, f[0]))
+            want.append(getattr(st, f[0]).offset)
+    src = "#include <stdio.h>\n#include <stddef.h>\n#include \"thoth_gpu.h\"\nint main(void){\n%s\nreturn 0;}\n" % \
+        "\n".join(lines)
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "b.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "b")
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want
+
+
 def _emulate(t, F, skip, npaths):
     """Run the kernel's time-ordered bridge program in FP64 on the oracle's normals."""
     fc, nodes, depth = G.bridge_program(t)
