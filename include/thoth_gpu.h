@@ -405,7 +405,8 @@ int thoth_gpu_xoshiro_jump(const uint64_t s[4], uint64_t n, uint64_t out[4]);
 
 /* Price n_books independent books (ragged path and step counts) in one CUDA
  * graph launch: all plans in one upload, all sums back in one copy. By default
- * the single-asset books run in ONE persistent kernel launch over a shared work
+ * (batches of up to 65535 books; larger ones launch per book) the
+ * single-asset books run in ONE persistent kernel launch over a shared work
  * list (item r of a book = the tiles r, r + grid, ... that CTA r of the book's own
  * launch takes, so every book's sums are bit for bit those of its own launch at
  * the same grid; largest items first, taken by resident CTAs from a counter),
