@@ -140,9 +140,11 @@ typedef struct ThothBookDesc
     const ThothProduct* products;
     int64_t paths;      /* number of Monte-Carlo paths (> 1)                       */
     int64_t sobol_skip; /* leading Sobol points skipped (mcl_configuration sobol_skip) */
-    int32_t use_sobol;  /* 1: Sobol + Brownian bridge; 0: counter-based pseudo-random */
+    int32_t use_sobol;  /* 1: Sobol + Brownian bridge (dimensions beyond 4097: the
+                           reference Rng's stream); 0: counter-based pseudo-random */
     int32_t greeks;     /* THOTH_GREEK_* mask                                       */
-    uint64_t seed;      /* pseudo-random stream (use_sobol = 0, and Sobol dims > 4097) */
+    uint64_t seed;      /* the Rng seed: dimensions beyond 4097 (the reference's
+                           xoshiro256++ stream), and the counter-based use_sobol = 0 */
     /* 1: the Cholesky factor also drives the spot white noise of Heston and LSV assets
      * (asset u's spot noise = sum_v L[u][v] n_v, as for a GBM Brownian); their variance
      * noises stay independent. An extension with no reference counterpart: the reference

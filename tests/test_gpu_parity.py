@@ -369,9 +369,32 @@ def test_maturity_zero_and_single_step(gpu):
     assert_shared_path_parity(r, ref["premium"], ref["trust"], "single step")
 
 
+@pytest.mark.parametrize("model", ["gbm", "heston"])
+def test_beyond_sobol_budget_reference_stream_shared_paths(gpu, model):
+    """Reference dimensions beyond the 4097 Sobol dimensions are the reference Rng's Gaussians,
+    drawn path after path in dimension order from one stream seeded with the book's seed
+    (path_generator.cpp:139-157): prices match the single-threaded oracle, which draws them
+    as one reference pricing does, on the same paths. 4200 dates of GBM (one factor) or 2100
+    of Heston (two): 103 tail dimensions a path."""
+    if model == "gbm":
+        b = abi.Book(days=np.arange(0, 4201), paths=(1 << 11) + 3)
+        a = b.add_gbm(100.0, 0.25, 0.02)
+        b.add_vanilla(a, 100.0, 4200, abi.CALL, zero_rate=0.02)
+        b.add_vanilla(a, 95.0, 3000, abi.PUT, zero_rate=0.02)
+    else:
+        b = W.heston_grid(paths=(1 << 11) + 5, calendar=True, months=(69,), strikes=(90, 100, 110))
+    b.seed = 12345
+    assert gpu.plan_summary(b)["sobol_dims"] == 4097
+    r = gpu.price_book(b)
+    ref = oracle.price_book(b, threads=1)
+    assert_shared_path_parity(r, ref["premium"], ref["trust"], "tail stream " + model)
+    b.seed = 12346                                  # another stream: other tail Gaussians
+    assert not np.array_equal(gpu.price_book(b)["premium"], r["premium"])
+
+
 def test_beyond_sobol_budget_is_statistically_consistent(gpu):
-    # 2100 daily steps x 2 factors: tail dims from the counter-based generator, not the
-    # reference's serial xoshiro stream, so only statistical agreement is expected
+    # 2100 daily steps x 2 factors: the tail dimensions from the reference Rng's stream; at
+    # 2^14 paths the prices agree with the characteristic-function price statistically
     b = W.heston_grid(paths=1 << 14, calendar=True, months=(69,), strikes=(100,))
     r = gpu.price_book(b)
     cf = [oracle.heston_price(100, 100, 2099 / 365.0, 0.03, 0, 0.04, 1.5, 0.04, 0.6, -0.7, t == abi.CALL)

@@ -165,6 +165,14 @@ __device__ __forceinline__ SobolLane<1 << TB, PP> sobol_lane(const DevPlan& P, u
     return L;
 }
 
+// the Gaussian of tail dimension dim (>= sobol_dims) of the path with Sobol index n, from the
+// book's tail table (0 for a column outside the book's paths)
+__device__ __forceinline__ float tail_gauss(const DevPlan& P, uint64_t n, int dim)
+{
+    const uint64_t k = n - (uint64_t)P.skip - 1; // the path's place in the book
+    return k < (uint64_t)P.paths ? __ldg(P.tail + (size_t)(dim - P.sobol_dims) * (size_t)P.tail_ld + k) : 0.f;
+}
+
 // Gaussians of reference dimension `dim` for the thread's PP paths (Sobol
 // indices n[p]); a Sobol dimension is the lane's next entry
 template <int T, int PP>
@@ -200,6 +208,11 @@ __device__ __forceinline__ void gauss(const DevPlan& P, SobolLane<T, PP>& L, con
             L.nxt[p] = more ? __ldg(L.lo + jn * T + p * TH) : 0u;
         }
         ++L.j;
+    } else if (P.tail) {
+        // beyond the Sobol budget: the reference Rng's Gaussians of this path (tail_normals)
+#pragma unroll
+        for (int p = 0; p < PP; ++p) z[p] = tail_gauss(P, n[p], dim);
+        return;
     } else {
 #pragma unroll
         for (int p = 0; p < PP; ++p) x[p] = hash_u32(P.seed, n[p], (uint32_t)dim);
@@ -598,6 +611,8 @@ __device__ __forceinline__ float2 pair_gauss(const DevPlan& P, uint2* hs_base, P
         L.cur = L.nxt;
         L.nxt = __ldg(L.lo);
         L.lo += T;
+    } else if (P.tail) {
+        return f2(tail_gauss(P, n[0], dim), tail_gauss(P, n[1], dim));
     } else {
         x0 = hash_u32(P.seed, n[0], (uint32_t)dim);
         x1 = hash_u32(P.seed, n[1], (uint32_t)dim);

@@ -583,6 +583,33 @@ bool find_chi()
     return true;
 }
 
+// ---- the reference Rng's stream for the book kernel's tail dimensions -------------------
+__constant__ uint64_t c_xo_pow2[64 * 4]; // x^(2^i) mod chi for i < 64
+
+struct TailSeed {
+    uint64_t s[4];
+};
+
+constexpr int TAIL_THREADS = 128;
+constexpr int TAIL_PATHS_PER_THREAD = 16;
+
+// thread k draws the tail Gaussians of paths [16 k, 16 k + 16): one jump to its first path's
+// place in the stream (p dt draws in: the binary powers of x), then its paths' draws in stream
+// order, as the reference's NextPath draws them
+__global__ void __launch_bounds__(TAIL_THREADS) tail_normals_kernel(const TailSeed s0, int dt, int64_t paths,
+                                                                    float* __restrict__ out)
+{
+    const int64_t p0 = ((int64_t)blockIdx.x * TAIL_THREADS + threadIdx.x) * TAIL_PATHS_PER_THREAD;
+    if (p0 >= paths) return;
+    uint64_t s[4] = {s0.s[0], s0.s[1], s0.s[2], s0.s[3]};
+    const uint64_t pos = (uint64_t)p0 * (uint64_t)dt;
+    for (int i = 0; i < 64; i++)
+        if ((pos >> i) & 1u) xo_jump(c_xo_pow2 + 4 * i, s);
+    const int64_t pend = p0 + TAIL_PATHS_PER_THREAD < paths ? p0 + TAIL_PATHS_PER_THREAD : paths;
+    for (int64_t p = p0; p < pend; p++)
+        for (int d = 0; d < dt; d++) out[(size_t)d * (size_t)paths + (size_t)p] = (float)gaussian(s);
+}
+
 } // namespace
 
 void xo_seed_state(uint64_t seed, uint64_t s[4])
@@ -654,4 +681,32 @@ cudaError_t launch_calib(const CalibArgs& A, int grid, size_t smem, cudaStream_t
     void* args[] = {&a};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(lsv_calib_kernel), dim3(grid),
                                        dim3(CALIB_THREADS), args, smem, st);
+}
+
+cudaError_t tail_normals_prepare()
+{
+    static std::mutex mu;
+    static bool ready[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && ready[dev]) return cudaSuccess;
+    std::vector<uint64_t> pw(64 * 4);
+    for (int i = 0; i < 64; i++)
+        if (!xo_jump_poly(1ull << i, pw.data() + 4 * i)) return cudaErrorUnknown;
+    e = cudaMemcpyToSymbol(c_xo_pow2, pw.data(), sizeof(uint64_t) * pw.size());
+    if (e == cudaSuccess && dev >= 0 && dev < 64) ready[dev] = true;
+    return e;
+}
+
+cudaError_t launch_tail_normals(uint64_t seed, int dt, int64_t paths, float* out, cudaStream_t st)
+{
+    if (dt <= 0 || paths <= 0) return cudaSuccess;
+    TailSeed s0;
+    xo_seed_state(seed, s0.s);
+    const int64_t threads = (paths + TAIL_PATHS_PER_THREAD - 1) / TAIL_PATHS_PER_THREAD;
+    const unsigned blocks = (unsigned)((threads + TAIL_THREADS - 1) / TAIL_THREADS);
+    tail_normals_kernel<<<blocks, TAIL_THREADS, 0, st>>>(s0, dt, paths, out);
+    return cudaGetLastError();
 }

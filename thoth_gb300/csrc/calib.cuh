@@ -54,3 +54,11 @@ bool xo_jump_poly(uint64_t d, uint64_t out[4]);
 void xo_apply_jump(const uint64_t poly[4], uint64_t s[4]);
 // the nibble table of the jump poly (CALIB_JTAB_WORDS words, layout of CalibArgs::jtab)
 void xo_jump_table(const uint64_t poly[4], uint64_t* tab);
+
+// The book kernel's Gaussians beyond the Sobol budget: the reference's PathGenerator::NextPath
+// (path_generator.cpp:139-157) draws them from one Rng seeded with the pricing's seed, path
+// after path, dt of them a path in dimension order. out[d][p] (d < dt, p < paths) is the
+// d-th of path p, rounded to float. tail_normals_prepare uploads the jump polynomials to the
+// current device once (call it before any stream capture).
+cudaError_t tail_normals_prepare();
+cudaError_t launch_tail_normals(uint64_t seed, int dt, int64_t paths, float* out, cudaStream_t st);

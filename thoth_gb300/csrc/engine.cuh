@@ -173,6 +173,9 @@ struct DevPlan {
     const int* sobol_order;      // [n_sobol] Sobol dimensions in the order the step loop consumes them
     const uint32_t* sobol_lo;    // [n_sobol][T] low-bit words of those dimensions, in that order
     int n_sobol;
+    int n_tail;                  // reference dimensions beyond the Sobol budget (Sobol mode): n_steps F - sobol_dims
+    const float* tail;           // [n_tail][tail_ld] their Gaussians, the reference Rng's stream (path-major)
+    int64_t tail_ld;             // paths per tail dimension (the book's path count)
     double* acc;                 // [gridDim][n_acc] per-CTA FP64 sums
     int n_acc;
     int few_m;                   // > 0: few-product accumulation over few_m moments (see book_kernel)
@@ -358,7 +361,8 @@ __device__ __forceinline__ void quantile_n<4>(const uint32_t (&x)[4], float (&z)
     quantile_pair(x[2], x[3], z[2], z[3]);
 }
 
-// counter-based uint32 for dimensions beyond the Sobol budget and use_sobol = 0
+// counter-based uint32 for use_sobol = 0 (and beyond the Sobol budget where a plan has no tail
+// table: the bridge test hook)
 // (splitmix64 finaliser of a Weyl combination of seed, point index and dimension)
 __device__ __forceinline__ uint32_t hash_u32(uint64_t seed, uint64_t n, uint32_t dim)
 {

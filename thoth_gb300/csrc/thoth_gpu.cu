@@ -104,6 +104,9 @@ Device g_dev;
 
 int max_dims() { return 4097; }
 
+// the largest tail table of one book (dimensions beyond the Sobol budget x paths, floats)
+constexpr size_t TAIL_MAX_BYTES = size_t(8) << 30;
+
 // direction numbers V[d][32] from the embedded Joe-Kuo table (sobol_generator.cpp:22-76)
 bool build_direction_numbers(std::vector<uint32_t>& V)
 {
@@ -560,6 +563,16 @@ int build_plan(const ThothBookDesc* d, Plan& P, int shape = -1)
     D.ref_factors = F;
     D.n_factors_active = F;
     D.sobol_dims = d->use_sobol ? (int)std::min<long>((long)N * F, max_dims()) : 0;
+    // dimensions beyond the Sobol budget: the reference Rng's stream, drawn into the book's
+    // tail table before its kernel (tail_normals)
+    D.n_tail = d->use_sobol ? (int)((long)N * F - D.sobol_dims) : 0;
+    D.tail_ld = d->paths;
+    if (D.n_tail > 0) {
+        if ((double)D.n_tail * (double)d->paths * sizeof(float) > (double)TAIL_MAX_BYTES)
+            return fail(THOTH_GPU_E_TOO_LARGE, "Gaussians beyond the Sobol budget exceed 8 GiB: fewer paths or dates");
+        tail_normals_prepare(); // before any capture; retried (and its error reported) at the launch
+        cudaGetLastError();
+    }
     D.corr = 0;
     if (NA > 1 && d->cholesky) {
         for (int u = 0; u < NA; u++)
@@ -1086,12 +1099,39 @@ double trust_of(double s1, double s2, double n)
 // bytes of a book's low Sobol words in consumption order ([n_sobol][T])
 // the book's low words in consumption order, and two rows of padding that the kernel's
 // load two entries ahead may read past the last entry
-size_t low_bytes(const Plan& P) { return sizeof(uint32_t) * ((size_t)P.dp.n_sobol + 2) * P.T; }
+// a book's own device tables after its plan blob: its low Sobol words in consumption order, then
+// (aligned) its tail Gaussians
+size_t low_words_bytes(const Plan& P) { return sizeof(uint32_t) * ((size_t)P.dp.n_sobol + 2) * P.T; }
+size_t low_bytes(const Plan& P)
+{
+    const size_t lo = low_words_bytes(P);
+    if (P.dp.n_tail <= 0) return lo;
+    return ((lo + 255) & ~size_t(255)) + sizeof(float) * (size_t)P.dp.n_tail * (size_t)P.dp.tail_ld;
+}
+
+// places those tables at lo (a region of low_bytes(P) bytes)
+void bind_low(Plan& P, unsigned char* lo)
+{
+    P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(lo);
+    P.dp.tail = P.dp.n_tail > 0 ? reinterpret_cast<const float*>(lo + ((low_words_bytes(P) + 255) & ~size_t(255)))
+                                : nullptr;
+}
+
+// the book's tail Gaussians (dimensions beyond the Sobol budget) into its tail table
+cudaError_t tail_normals(const Plan& P, cudaStream_t st)
+{
+    cudaError_t e = tail_normals_prepare();
+    if (e != cudaSuccess) return e;
+    return launch_tail_normals(P.dp.seed, P.dp.n_tail, P.dp.tail_ld, const_cast<float*>(P.dp.tail), st);
+}
 
 // the book's low words from the device-wide table (one small gather kernel)
 cudaError_t gather_low(const Plan& P, cudaStream_t st)
 {
-    return launch_gather_low(g_dev.sobol_lo, P.dp.sobol_order, P.dp.n_sobol, P.T, const_cast<uint32_t*>(P.dp.sobol_lo), st);
+    cudaError_t e = launch_gather_low(g_dev.sobol_lo, P.dp.sobol_order, P.dp.n_sobol, P.T,
+                                      const_cast<uint32_t*>(P.dp.sobol_lo), st);
+    if (e == cudaSuccess && P.dp.n_tail > 0) e = tail_normals(P, st);
+    return e;
 }
 
 // device layout of one priced book: [plan blob][low Sobol words][acc rows][out][status]
@@ -1119,7 +1159,7 @@ int run_bound(Plan& P, unsigned char* base, const Layout& L, int grid, ThothBook
     cudaStream_t st = g_dev.stream;
     int rc = ensure_pinned(sizeof(double) * n_acc + sizeof(int));
     if (rc) return rc;
-    P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(base + L.o_lo);
+    bind_low(P, base + L.o_lo);
     P.dp.acc = reinterpret_cast<double*>(base + L.o_acc);
     P.dp.status = reinterpret_cast<int*>(base + L.o_st);
     CUDA_TRY(cudaMemsetAsync(base + L.o_st, 0, sizeof(int), st));
@@ -1635,7 +1675,7 @@ static int price_noalloc_locked(const ThothBookDesc* book, ThothBookResult* out)
     CUDA_TRY(cudaMemset(base + o_st, 0, sizeof(int))); // status must start at zero; the sums are zeroed by the kernel
     bind(P, base);
     P.dp.sobol_v = reinterpret_cast<const uint32_t*>(base + o_v);
-    P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(base + o_lo);
+    bind_low(P, base + o_lo);
     // the engine's host-mapped cancel word, where the engine set it up (it needs no allocation
     // here); the kernel reads it at every tile
     P.dp.cancel = g_dev.ready ? g_dev.cancel_dev : nullptr;
@@ -1751,6 +1791,11 @@ static int record_batch(std::vector<Plan>& plans, const std::vector<int>& grid, 
     if (BL) {
         CUDA_TRY(launch_gather_low_batch(g_dev.sobol_lo, g_batch.dev + BL->o_gather, n, st));
         launches++;
+        for (int b = 0; b < n; b++)
+            if (plans[b].dp.n_tail > 0) {
+                CUDA_TRY(tail_normals(plans[b], st));
+                launches++;
+            }
     }
     const int side = BL ? (int)std::min<size_t>(order.size(), (size_t)S) : S;
     CUDA_TRY(cudaEventRecord(g_batch.events[0], st));
@@ -1762,7 +1807,7 @@ static int record_batch(std::vector<Plan>& plans, const std::vector<int>& grid, 
         cudaStream_t s = g_batch.streams[k];
         if (!BL) {
             CUDA_TRY(gather_low(plans[b], s));
-            launches++;
+            launches += plans[b].dp.n_tail > 0 ? 2 : 1;
         }
         CUDA_TRY(launch_book(plans[b].dp, plans[b].variant, plans[b].shape, grid[b], plans[b].smem, s));
         launches++;
@@ -1898,7 +1943,7 @@ static int price_batch_locked(const ThothBookDesc* books, int n, ThothBookResult
     for (int b = 0; b < n; b++) {
         std::memcpy(g_batch.host + o_blob[b], plans[b].blob.bytes.data(), plans[b].blob.bytes.size());
         bind(plans[b], g_batch.dev + o_blob[b]);
-        plans[b].dp.sobol_lo = reinterpret_cast<const uint32_t*>(g_batch.dev + o_lo[b]);
+        bind_low(plans[b], g_batch.dev + o_lo[b]);
         plans[b].dp.acc = reinterpret_cast<double*>(g_batch.dev + o_acc[b]);
         plans[b].dp.status = reinterpret_cast<int*>(g_batch.dev + o_st[b]);
         // the kernel parameters are baked into the graph: a replay needs them byte-equal
@@ -2025,7 +2070,7 @@ static int autotune_book_locked(const ThothBookDesc* book, int reps, ThothTuneRe
         if (rc) return rc;
         CUDA_TRY(cudaMemcpy(g_dev.arena, P.blob.bytes.data(), P.blob.bytes.size(), cudaMemcpyHostToDevice));
         bind(P, g_dev.arena);
-        P.dp.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + L.o_lo);
+        bind_low(P, g_dev.arena + L.o_lo);
         CUDA_TRY(gather_low(P, st));
         P.dp.acc = reinterpret_cast<double*>(g_dev.arena + L.o_acc);
         P.dp.status = reinterpret_cast<int*>(g_dev.arena + L.o_st);
@@ -2533,7 +2578,7 @@ int thoth_gpu_book_create(const ThothBookDesc* book, ThothBookHandle** out)
             return fail(THOTH_GPU_E_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
         }
         bind(h->plan, h->dev);
-        h->plan.dp.sobol_lo = reinterpret_cast<const uint32_t*>(h->dev + h->layout.o_lo);
+        bind_low(h->plan, h->dev + h->layout.o_lo);
         e = gather_low(h->plan, g_dev.stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g_dev.stream);
         if (e != cudaSuccess) {
@@ -2927,7 +2972,7 @@ int thoth_gpu_bridge_increments(const double* t, int32_t n_dates, int32_t factor
         D.recs = reinterpret_cast<const StepRec*>(g_dev.arena + P.o_recs);
         D.sobol_v = g_dev.sobol_v;
         D.sobol_order = reinterpret_cast<const int*>(g_dev.arena + P.o_sord);
-        D.sobol_lo = reinterpret_cast<const uint32_t*>(g_dev.arena + o_lo);
+        bind_low(P, g_dev.arena + o_lo);
         float* d_out = reinterpret_cast<float*>(g_dev.arena + o_out);
         CUDA_TRY(gather_low(P, g_dev.stream));
         const int grid = (int)std::min<int64_t>(D.n_tiles, (int64_t)g_dev.sms * 2);
