@@ -159,6 +159,12 @@ def test_descriptor_validation():
         b.add_gbm(100, 0.2, 0.0)
     b.add_vanilla(0, 100, 1)
     assert _code(b) == abi.THOTH_GPU_E_TOO_LARGE             # more than THOTH_MAX_ASSETS
+    b = abi.Book(days=np.arange(0, 6001), paths=1 << 20)     # 1903 dims beyond the Sobol budget
+    b.add_gbm(100, 0.2, 0.0)
+    b.add_vanilla(0, 100, 6000)
+    assert _code(b) == 0                                      # tail table 7.98 GB
+    b.paths = (1 << 20) + (1 << 17)
+    assert _code(b) == abi.THOTH_GPU_E_TOO_LARGE             # tail table above 8 GiB
 
 
 def test_kernel_selection_and_sizes():
