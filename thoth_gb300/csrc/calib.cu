@@ -591,23 +591,102 @@ struct TailSeed {
 };
 
 constexpr int TAIL_THREADS = 128;
+constexpr int TAIL_WARPS = TAIL_THREADS / 32;
 constexpr int TAIL_PATHS_PER_THREAD = 16;
+constexpr double ACKLAM_P_LOW = 0.02425;
+
+// normal_cdf_inv's two branches apart, each the same expression the reference evaluates there
+__device__ __forceinline__ double acklam_central(double P) // P in [p_low, 1 - p_low]
+{
+    const double a0 = -3.969683028665376e+01, a1 = 2.209460984245205e+02, a2 = -2.759285104469687e+02,
+                 a3 = 1.383577518672690e+02, a4 = -3.066479806614716e+01, a5 = 2.506628277459239e+00;
+    const double b0 = -5.447609879822406e+01, b1 = 1.615858368580409e+02, b2 = -1.556989798598866e+02,
+                 b3 = 6.680131188771972e+01, b4 = -1.328068155288572e+01;
+    const double q = P - 0.5;
+    const double r = q * q;
+    const double cn = (((((a0 * r + a1) * r + a2) * r + a3) * r + a4) * r + a5) * q;
+    const double cd = ((((b0 * r + b1) * r + b2) * r + b3) * r + b4) * r + 1.0;
+    return cn / cd;
+}
+
+__device__ __forceinline__ double acklam_tail(double P) // P < p_low or P > 1 - p_low
+{
+    const double c0 = -7.784894002430293e-03, c1 = -3.223964580411365e-01, c2 = -2.400758277161838e+00,
+                 c3 = -2.549732539343734e+00, c4 = 4.374664141464968e+00, c5 = 2.938163982698783e+00;
+    const double d0 = 7.784695709041462e-03, d1 = 3.224671290700398e-01, d2 = 2.445134137142996e+00,
+                 d3 = 3.754408661907416e+00;
+    const bool lower = P < ACKLAM_P_LOW;
+    const double qt = sqrt(-2.0 * log(lower ? P : 1.0 - P));
+    const double tn = ((((c0 * qt + c1) * qt + c2) * qt + c3) * qt + c4) * qt + c5;
+    const double td = (((d0 * qt + d1) * qt + d2) * qt + d3) * qt + 1.0;
+    return (lower ? tn : -tn) / td;
+}
 
 // thread k draws the tail Gaussians of paths [16 k, 16 k + 16): one jump to its first path's
 // place in the stream (p dt draws in: the binary powers of x), then its paths' draws in stream
-// order, as the reference's NextPath draws them
+// order, as the reference's NextPath draws them. A draw in the central region is inverted at
+// once; one in a tail (4.85 % of them) waits in its warp's queue in shared memory, and 32
+// queued draws are inverted at once on the warp's 32 lanes, so the logarithm runs on full
+// warps instead of on most warps' iterations.
 __global__ void __launch_bounds__(TAIL_THREADS) tail_normals_kernel(const TailSeed s0, int dt, int64_t paths,
                                                                     float* __restrict__ out)
 {
+    __shared__ double q_u[TAIL_WARPS][64];
+    __shared__ uint32_t q_i[TAIL_WARPS][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t p0 = ((int64_t)blockIdx.x * TAIL_THREADS + threadIdx.x) * TAIL_PATHS_PER_THREAD;
-    if (p0 >= paths) return;
+    const bool live = p0 < paths;
+    if (__all_sync(0xffffffffu, !live)) return; // warp-uniform
+    const int np = live ? (int)(paths - p0 < TAIL_PATHS_PER_THREAD ? paths - p0 : TAIL_PATHS_PER_THREAD) : 0;
     uint64_t s[4] = {s0.s[0], s0.s[1], s0.s[2], s0.s[3]};
-    const uint64_t pos = (uint64_t)p0 * (uint64_t)dt;
-    for (int i = 0; i < 64; i++)
-        if ((pos >> i) & 1u) xo_jump(c_xo_pow2 + 4 * i, s);
-    const int64_t pend = p0 + TAIL_PATHS_PER_THREAD < paths ? p0 + TAIL_PATHS_PER_THREAD : paths;
-    for (int64_t p = p0; p < pend; p++)
-        for (int d = 0; d < dt; d++) out[(size_t)d * (size_t)paths + (size_t)p] = (float)gaussian(s);
+    if (live) {
+        const uint64_t pos = (uint64_t)p0 * (uint64_t)dt;
+        for (int i = 0; i < 64; i++)
+            if ((pos >> i) & 1u) xo_jump(c_xo_pow2 + 4 * i, s);
+    }
+    int qn = 0; // the warp's queue length (the same on every lane)
+    for (int pl = 0; pl < TAIL_PATHS_PER_THREAD; pl++) {
+        const bool act = pl < np;
+        for (int d = 0; d < dt; d++) {
+            double u = 0.0;
+            uint32_t idx = 0;
+            bool tail = false;
+            if (act) {
+                const double u0 = (double)(xo_next(s) >> 11) * (1.0 / 9007199254740992.0);
+                u = u0 > 0.0 ? u0 : (1.0 / 9007199254740992.0);
+                idx = (uint32_t)((size_t)d * (size_t)paths + (size_t)(p0 + pl)); // < 2^31: the table's size limit
+                tail = u < ACKLAM_P_LOW || !(u <= 1.0 - ACKLAM_P_LOW);
+                if (!tail) out[idx] = (float)acklam_central(u);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, tail);
+            if (tail) {
+                const int slot = qn + __popc(m & ((1u << lane) - 1u)); // < 63
+                q_u[w][slot] = u;
+                q_i[w][slot] = idx;
+            }
+            qn += __popc(m);
+            if (qn >= 32) { // 32 to 63 entries: invert the first 32, keep the rest
+                __syncwarp();
+                out[q_i[w][lane]] = (float)acklam_tail(q_u[w][lane]);
+                const int rest = qn - 32;
+                double mu = 0.0;
+                uint32_t mi = 0;
+                if (lane < rest) {
+                    mu = q_u[w][32 + lane];
+                    mi = q_i[w][32 + lane];
+                }
+                __syncwarp();
+                if (lane < rest) {
+                    q_u[w][lane] = mu;
+                    q_i[w][lane] = mi;
+                }
+                __syncwarp();
+                qn = rest;
+            }
+        }
+    }
+    __syncwarp();
+    if (lane < qn) out[q_i[w][lane]] = (float)acklam_tail(q_u[w][lane]);
 }
 
 } // namespace
